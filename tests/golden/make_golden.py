@@ -1,0 +1,56 @@
+"""Generate the golden fixtures from the reference implementation itself.
+
+Run in a checkout that has the reference next to it (not needed anywhere else):
+
+    python tests/golden/make_golden.py /root/reference
+
+For every problem in ``cases.CASES`` it builds the model from the reference's own classes,
+compiles it with the reference's ``compile_model`` and steps the reference's ``NumpyEngine`` in
+float32 and float64. It stores fingerprints (digests of every compiled array and of the float32
+fields, the probe DFTs, the energy) under ``tests/golden/<case>.npz``. The tests compare
+``open_analysis_gb300.model.compile_model`` and the oracle in ``oracle/`` against them, and the
+GPU tests compare the CUDA engine against the oracle and these fingerprints.
+"""
+
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+
+
+def main(reference_root: str) -> None:
+    root = Path(reference_root)
+    sys.path.insert(0, str(root / "packages" / "oa-fdtd" / "src"))
+    sys.path.insert(0, str(root / "packages" / "oa-accel" / "src"))
+    sys.path.insert(0, str(HERE))
+    sys.path.insert(0, str(HERE.parent.parent))
+    import numpy as np
+    from cases import CASES, namespace  # type: ignore[import-not-found]
+    from fingerprint import compiled_fingerprint, save, state_fingerprint  # type: ignore[import-not-found]
+    from oa_fdtd.model import compile_model  # type: ignore[import-not-found]
+    from oa_fdtd.reference import NumpyEngine  # type: ignore[import-not-found]
+
+    ns = namespace("ref")
+    for name, (builder, steps) in CASES.items():
+        model = builder(ns)
+        c = compile_model(model, "float32")
+        data = compiled_fingerprint(c)
+        data["steps"] = steps
+        for dtype in ("float32", "float64"):
+            eng = NumpyEngine(c, dtype)
+            eng.step(steps)
+            for k, v in state_fingerprint(eng).items():
+                data[f"{dtype}.{k}"] = v
+        if name == "mixed_walls":
+            eng = NumpyEngine(c, "float32")
+            eng.step(steps)
+            for comp, arr in zip(("Ex", "Ey", "Ez", "Hx", "Hy", "Hz"), (*eng.E, *eng.H), strict=True):
+                data[f"full.{comp}"] = np.ascontiguousarray(arr)
+        save(str(HERE / f"{name}.npz"), data)
+        print(name, "steps", steps, "batch", c.batch, "keys", len(data))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
