@@ -1,0 +1,430 @@
+#!/usr/bin/env python
+"""FDTD time-stepping throughput on GB300: Gcell-updates/s and the HBM roofline.
+
+``python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]``
+
+Workload (default): the via-transition problem, 400 x 400 x 120 cells of 25 um (19.2 M cells),
+single-pole Debye dielectric, surface-impedance copper, 10-cell CPML, two lumped ports (batch of
+two excitations), 256 DFT frequencies (``open_analysis_gb300.structures.via_transition``),
+synthetic geometry. One bench step = one 64-time-step chunk, the unit the reference run loop
+advances between energy checks. Gcell-updates/s = interior cells x batch x time steps / time.
+
+* ``value``: device time (CUDA events on the engine's stream) of K chunks, fields resident in HBM
+  (the fields, 0.98 GB, are far larger than the 129 MB L2, so no flush is needed).
+* ``e2e``: the same metric through the public API from host buffers: engine creation (the host
+  ``Compiled`` arrays copied to the device), K chunks each followed by the energy check (a device
+  to host read, as the run loop does), the probe DFTs read back at the end; host wall clock.
+* ``roofline``: the dominant kernel's algorithmic bytes per launch (traffic model below) over its
+  average launch time measured with CUDA events inside the timed region.
+* ``cpu_baseline``: the CPU oracle (the reference's NumPy engine restated) in float32 on the same
+  compiled problem, a bounded sample of time steps, one host thread.
+
+``--impl reference`` times the reference's CPU path (the oracle port; the reference is a Python
+package and is not installed on the GPU host) on the same workload, one time step per bench step.
+For N > 1 (torchrun) every rank runs its own replica (independent instances: weak scaling, no
+collective on the data path); rank 0 prints the line with the max time over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+from typing import Any
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+CHUNK = 64
+WORKLOAD = "via_transition_400x400x120"
+
+
+# ---------------------------------------------------------------------------- distributed plumbing
+class Ranks:
+    """Rank bookkeeping; torch.distributed (gloo, host-side only) for barrier and max."""
+
+    def __init__(self, gpus: int) -> None:
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.gpus = gpus
+        self.dist = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self) -> None:
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max(self, v: float) -> float:
+        if self.dist is None:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self) -> None:
+        if self.dist is not None:
+            self.dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi SM clock and throttle-reason samples every 200 ms during the timed region."""
+
+    QUERY = (
+        "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+        "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, gpu: int) -> None:
+        self.gpu = gpu
+        self.proc: subprocess.Popen[bytes] | None = None
+        self.path = Path(tempfile.mkstemp(prefix="clocks_", suffix=".csv")[1])
+
+    def start(self) -> None:
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)],
+                stdout=open(self.path, "wb"),
+                stderr=subprocess.DEVNULL,
+            )
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict[str, Any] | None:
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = [r.split(",") for r in self.path.read_text().strip().splitlines() if r.strip()]
+        self.path.unlink(missing_ok=True)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for name, flag in zip(names, r[5:9], strict=False):
+                if flag.strip().lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {
+            "sm_mhz": statistics.median(sm),
+            "sm_max_mhz": max(smax),
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+        }
+
+
+# ---------------------------------------------------------------------------- traffic model
+def kernel_bytes(c: Any, real: int = 4) -> dict[str, float]:
+    """Algorithmic DRAM bytes per launch of each kernel (all batch members).
+
+    h_sweep: read 3 E, read-modify-write 3 H per interior cell and member (36 B in float32) plus
+    psi read+write (8 B) per cell of every H correction box. e_sweep: read 3 H, read-modify-write
+    3 E (36 B) per cell and member, the three uint16 indices once per cell (6 B), psi (8 B) per
+    cell of every E correction box, the Debye current J read+write (8 B per pole) per dispersive
+    edge. edges: per surface-impedance edge J_prev and v_p read+write (8 B (1 + P)), two H samples
+    (8 B) and the E write (4 B), per member.
+    """
+    nx, ny, nz = c.grid.n
+    cells = float(nx * ny * nz)
+    b = c.batch
+    psi = {"E": 0.0, "H": 0.0}
+    for k in c.pml.corrections:
+        psi[k.kind] += float(np.prod(k.shape))
+    h = cells * b * 9 * real + psi["H"] * b * 2 * real
+    e = cells * b * 9 * real + cells * 6 + psi["E"] * b * 2 * real
+    if c.ade is not None:
+        e += sum(f.size for f in c.ade.flat) * b * c.ade.tau.size * 2 * real
+    edges = 0.0
+    if c.sibc is not None:
+        edges = c.sibc.flat.size * b * (2 * real * (1 + c.sibc.cp.size) + 2 * real + real)
+    return {"h_sweep": h, "e_sweep": e, "edges": edges}
+
+
+def launches_per_step(c: Any) -> int:
+    n = 2  # h_sweep, e_sweep
+    n += sum(1 for w in c.walls if w == "pmc")
+    kinds = {p["kind"] for p in c.probes}
+    n += 1 if "E" in kinds else 0
+    has_h = "H" in kinds
+    deferred = False
+    if c.ade is not None and c.channels:
+        for comp, fl in zip(c.ade.comp, c.ade.flat, strict=True):
+            targets = [
+                np.asarray(ch["flat"])[np.broadcast_to(np.asarray(ch["comp"]), np.asarray(ch["flat"]).shape) == comp]
+                for ch in c.channels
+            ]
+            if np.isin(fl, np.concatenate(targets)).any():
+                deferred = True
+    n += 1 if (has_h or deferred) else 0
+    n += 1 if (c.sibc is not None or c.channels) else 0
+    return n
+
+
+def measured_peak() -> tuple[float, str]:
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        try:
+            return float(json.loads(path.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel: str) -> float | None:
+    """DRAM bytes per launch of ``kernel`` from the committed ncu summary, scaled to this
+    workload, or None when no capture exists."""
+    path = ROOT / "profiles" / f"{kernel}_via_transition_traffic.txt"
+    if not path.exists():
+        return None
+    vals: dict[str, float] = {}
+    for line in path.read_text().splitlines():
+        if "=" in line and not line.lstrip().startswith("#"):
+            k, v = line.split("=", 1)
+            try:
+                vals[k.strip()] = float(v.split()[0])
+            except (ValueError, IndexError):
+                continue
+    if "bytes_per_launch_full_workload" in vals:
+        return vals["bytes_per_launch_full_workload"]
+    return None
+
+
+# ---------------------------------------------------------------------------- arms
+def build_problem(args: argparse.Namespace) -> tuple[Any, Any]:
+    from open_analysis_gb300.model import compile_model
+    from open_analysis_gb300.structures import microstrip, via_transition
+
+    if args.workload == "microstrip":
+        m = microstrip()
+    else:
+        m = via_transition()
+    return m, compile_model(m, "float32")
+
+
+def cpu_sample(c: Any, target_s: float) -> dict[str, Any]:
+    """The oracle in float32 on the same problem: one untimed step, then as many steps as fit
+    about ``target_s`` seconds (at least two)."""
+    from oracle.numpy_engine import OracleEngine
+
+    eng = OracleEngine(c, "float32")
+    t0 = time.perf_counter()
+    eng.step(1)
+    one = time.perf_counter() - t0
+    n = max(2, int(target_s / max(one, 1e-6)))
+    t0 = time.perf_counter()
+    eng.step(n)
+    dt = time.perf_counter() - t0
+    nx, ny, nz = c.grid.n
+    rate = nx * ny * nz * c.batch * n / dt / 1e9
+    return {
+        "value": rate,
+        "unit": "Gcell-updates/s",
+        "cores": 1,
+        "kind": "port",
+        "sample": f"{n} time steps of the full {nx}x{ny}x{nz} grid, batch {c.batch}, float32, "
+        f"after 1 untimed step ({dt:.1f} s); NumPy elementwise runs on one thread",
+    }
+
+
+def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
+    from open_analysis_gb300 import native
+    from open_analysis_gb300.engine import Gb300Engine
+
+    native.set_device(ranks.local)
+    model, c = build_problem(args)
+    nx, ny, nz = c.grid.n
+    cells = nx * ny * nz
+    max_steps = (args.warmup + args.steps + 2) * CHUNK
+    eng = Gb300Engine(c, "float32", max_steps=max_steps)
+    eng.set_profiling(True)  # CUDA events around every kernel, captured inside the graph
+    for _ in range(args.warmup):
+        eng.step(CHUNK)
+    sampler = ClockSampler(ranks.local)
+    ranks.barrier()
+    sampler.start()
+    times = []
+    ksum: dict[str, float] = {}
+    for _ in range(args.steps):
+        times.append(eng.step_timed(CHUNK))
+        for k, v in eng.kernel_times().items():  # per-step averages over this chunk
+            ksum[k] = ksum.get(k, 0.0) + v
+    ktimes = {k: v / args.steps for k, v in ksum.items()}
+    clocks = sampler.stop()
+    ranks.barrier()
+    total_ms = ranks.max(float(sum(times)))
+    updates = float(cells) * c.batch * CHUNK * args.steps * ranks.world
+    value = updates / (total_ms / 1e3) / 1e9
+    kb = kernel_bytes(c)
+    dominant = max(("h_sweep", "e_sweep", "edges"), key=lambda k: ktimes.get(k, 0.0))
+    peak, peak_kind = measured_peak()
+    achieved = kb[dominant] / (ktimes[dominant] / 1e3) / 1e9
+    step_bytes = sum(kb.values())
+    eng.close()
+
+    # e2e through the public API with host buffers
+    ranks.barrier()
+    t0 = time.perf_counter()
+    eng2 = Gb300Engine(c, "float32", max_steps=max_steps)
+    h2d = eng2.h2d_bytes
+    for _ in range(args.steps):
+        eng2.step(CHUNK)
+        eng2.energy()
+    res = eng2.results()
+    eng2.close()
+    e2e_s = ranks.max(time.perf_counter() - t0)
+    d2h = args.steps * 6 * 8 + sum(v.nbytes for v in res.values())
+    e2e_value = float(cells) * c.batch * CHUNK * args.steps * ranks.world / e2e_s / 1e9
+
+    cpu = None
+    if ranks.rank == 0 and ranks.world == 1 and not args.no_cpu:
+        cpu = cpu_sample(c, args.cpu_seconds)
+
+    if ranks.rank == 0:
+        line = {
+            "metric": "Gcell-updates/s",
+            "value": value,
+            "unit": "Gcell-updates/s",
+            "n_gpus": ranks.world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic",
+            "config": {
+                "workload": WORKLOAD if args.workload != "microstrip" else "microstrip_120x60x40",
+                "cells": [nx, ny, nz],
+                "batch": c.batch,
+                "time_steps_per_step": CHUNK,
+                "dft_frequencies": int(c.frequencies.size),
+                "ade_poles": 0 if c.ade is None else int(c.ade.tau.size),
+                "sibc_edges": 0 if c.sibc is None else int(c.sibc.flat.size),
+                "l2": "inputs larger than L2 (fields 6 x batch x 4 B per storage cell), no flush",
+                "parallelism": f"replicas{ranks.world}",
+            },
+            "roofline": {
+                "bound": "hbm",
+                "kernel": dominant,
+                "achieved": achieved,
+                "peak": peak,
+                "peak_source": peak_kind,
+                "unit": "GB/s",
+                "frac": achieved / peak,
+                "traffic": profiled_traffic(dominant),
+                "kernel_ms": ktimes,
+                "algorithmic_bytes_per_launch": kb,
+                "step_frac": step_bytes / (ktimes["step"] / 1e3) / 1e9 / peak,
+            },
+            "e2e": {
+                "value": e2e_value,
+                "unit": "Gcell-updates/s",
+                "h2d_bytes_per_step": h2d / args.steps,
+                "d2h_bytes_per_step": d2h / args.steps,
+                "seconds": e2e_s,
+            },
+            "gpu_launches": (launches_per_step(c) * CHUNK + 1) * args.steps,
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def run_reference(args: argparse.Namespace, ranks: Ranks) -> None:
+    if ranks.rank != 0:
+        return
+    from oracle.numpy_engine import OracleEngine
+
+    _, c = build_problem(args)
+    nx, ny, nz = c.grid.n
+    eng = OracleEngine(c, "float32")
+    for _ in range(args.warmup):
+        eng.step(1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.step(1)
+    dt = time.perf_counter() - t0
+    value = nx * ny * nz * c.batch * args.steps / dt / 1e9
+    sample = (
+        f"one time step of the full {nx}x{ny}x{nz} grid (batch {c.batch}, float32) per bench step; "
+        "the reference's NumPy engine restated (the reference is a Python package, not installable "
+        "on the GPU host); NumPy elementwise runs on one thread"
+    )
+    print(
+        json.dumps(
+            {
+                "impl": "reference",
+                "metric": "Gcell-updates/s",
+                "value": value,
+                "unit": "Gcell-updates/s",
+                "n_gpus": ranks.world,
+                "steps": args.steps,
+                "warmup": args.warmup,
+                "ms_per_step": dt * 1e3 / args.steps,
+                "higher_is_better": True,
+                "scaling": "weak",
+                "vs_baseline": None,
+                "dtype": "f32",
+                "data": "synthetic",
+                "config": {"workload": WORKLOAD if args.workload != "microstrip" else "microstrip_120x60x40",
+                           "cells": [nx, ny, nz], "batch": c.batch},
+                "cpu_baseline": {"value": value, "unit": "Gcell-updates/s", "cores": 1, "kind": "port",
+                                 "sample": sample},
+                "e2e": {"value": value, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0},
+            }
+        ),
+        flush=True,
+    )
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="via_transition", choices=["via_transition", "microstrip"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    ranks = Ranks(args.gpus)
+    try:
+        if args.impl == "reference":
+            run_reference(args, ranks)
+        else:
+            run_gb300(args, ranks)
+    finally:
+        ranks.close()
+
+
+if __name__ == "__main__":
+    main()

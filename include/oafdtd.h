@@ -1,0 +1,204 @@
+/*
+ * oafdtd — GB300 (sm_103a) FDTD time-stepping engine, C ABI.
+ *
+ * This is the drop-in boundary for the engine layer of the oa-fdtd solver. The reference engine
+ * is a Python class driven by the run loop (packages/oa-fdtd/src/oa_fdtd/run.py:46-137):
+ * CupyEngine (packages/oa-fdtd/src/oa_fdtd/engine.py:67-506) and NumpyEngine
+ * (packages/oa-fdtd/src/oa_fdtd/reference.py:41-331). Both consume a compiled problem
+ * (`Compiled`, packages/oa-fdtd/src/oa_fdtd/model.py:246-269) and expose
+ * step / energy / results / series / get_fields / peak_bytes. Each function below replaces one
+ * of those methods; the comment on each names the reference method.
+ *
+ * Conventions
+ *  - Plain C types and host pointers only. The caller owns every host buffer for the duration of
+ *    a call; the library copies what it needs and owns all device memory of a handle.
+ *  - Every function returns an int status: OAFDTD_OK (0) or a negative OAFDTD_E_* code.
+ *    oafdtd_last_error() returns a message for the last failure on the calling thread.
+ *  - One handle = one CUDA stream on the device that was current at creation. Calls on one handle
+ *    are not re-entrant; different handles may be used from different threads.
+ *  - oafdtd_step() returns after the stream has synchronised, as the reference engine's step()
+ *    does (engine.py:437).
+ *  - Storage layout of every field component: (batch, nz + 2, ny + 2, pitch), x fastest,
+ *    storage index = cell/node index + 1, ghost planes at 0 and n + 1 (oa_fdtd/grid.py:1-10).
+ */
+#ifndef OAFDTD_H
+#define OAFDTD_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OAFDTD_ABI_VERSION 1
+
+enum {
+  OAFDTD_OK = 0,
+  OAFDTD_E_INVALID = -1,      /* bad descriptor or argument (ModelError analogue) */
+  OAFDTD_E_OOM = -2,          /* device allocation failed (ACCEL_OUT_OF_MEMORY analogue) */
+  OAFDTD_E_CUDA = -3,         /* a CUDA runtime call failed */
+  OAFDTD_E_RANGE = -4,        /* step past max_steps (the wave table length) */
+  OAFDTD_E_TABLE = -5,        /* more than 65535 combined material entries */
+  OAFDTD_E_NODEVICE = -6,     /* no CUDA device */
+  OAFDTD_E_TIMEOUT = -7       /* a bounded device-side wait gave up */
+};
+
+/* One CPML curl-term correction (oa_fdtd/pml.py:56-70): kind 0 = E, 1 = H; corrected component
+ * c, derivative (slab) axis a, source component b, sign, storage box [lo, hi) per x, y, z. */
+typedef struct oafdtd_correction {
+  int32_t kind, c, a, b;
+  double sign;
+  int32_t lo[3], hi[3];
+} oafdtd_correction;
+
+/* A compiled problem (oa_fdtd/model.py:246-269), flattened to plain arrays. */
+typedef struct oafdtd_problem {
+  int32_t abi_version;   /* OAFDTD_ABI_VERSION */
+  int32_t real_bytes;    /* 4: float32 fields (the production mode), 8: float64 */
+  int32_t nx, ny, nz;    /* cells per axis */
+  int32_t pitch;         /* padded storage x extent */
+  int32_t batch;         /* excitations advanced together */
+  double dt;             /* time step [s] */
+  double dtmu;           /* dt / mu0 */
+  /* materials: per-E-component uint16 index into the averaged-material table (0 = PEC) */
+  const uint16_t* idx[3];          /* each (nz+2)*(ny+2)*pitch */
+  int32_t n_mat;
+  const double* ca_tab;            /* n_mat */
+  const double* cb_tab;            /* n_mat */
+  const double* eps_tab;           /* n_mat, relative permittivity (energy only) */
+  /* 1-D metrics over the storage index of each axis (length pitch, ny+2, nz+2) */
+  const double* inv_primal[3];
+  const double* inv_dual[3];
+  const double* node_w[3];
+  const double* cell_w[3];
+  int32_t pmc_mask;                /* bit (2*axis + side) set for a PMC wall */
+  /* CPML */
+  int32_t n_corr;
+  const oafdtd_correction* corr;   /* n_corr, in application order */
+  const double* pml[3][6];         /* per axis: eb, ec, ek, hb, hc, hk (NULL: no CPML on axis) */
+  /* sources: every (channel, edge) contribution in channel order */
+  int32_t n_chan;
+  int32_t max_steps;
+  const double* wave;              /* (n_chan, max_steps): s((n + 1/2) dt) */
+  const double* drive;             /* (batch, n_chan) */
+  int64_t n_inj;
+  const int32_t* inj_comp;
+  const int64_t* inj_flat;
+  const double* inj_amp;
+  const int32_t* inj_chan;
+  /* probes: kind 0 = E, 1 = H */
+  int32_t n_probe;
+  const int32_t* probe_kind;
+  const int32_t* probe_comp;
+  const int64_t* probe_off;        /* n_probe + 1 */
+  const int64_t* probe_flat;
+  const double* probe_w;
+  int32_t n_freq;
+  const double* omega;             /* 2 pi f */
+  int32_t record_series;
+  /* Debye ADE (oa_fdtd/model.py:218-226) */
+  int32_t ade_poles;
+  const double* ade_kp;            /* ade_poles */
+  int64_t ade_n[3];                /* dispersive edges per component (0: none) */
+  const int64_t* ade_flat[3];
+  const double* ade_beta[3];       /* (ade_poles, ade_n[c]) */
+  const double* ade_cbe[3];        /* ade_n[c] */
+  /* surface impedance (oa_fdtd/model.py:230-242) */
+  int64_t sibc_n;
+  int32_t sibc_poles;
+  int32_t sibc_nmat;
+  const int32_t* sibc_comp;
+  const int64_t* sibc_flat;
+  const int32_t* sibc_hcomp;       /* (sibc_n, 2) */
+  const int64_t* sibc_hflat;       /* (sibc_n, 2) */
+  const double* sibc_hsign;        /* (sibc_n, 2) */
+  const int32_t* sibc_mat;
+  const double* sibc_r0;           /* sibc_nmat */
+  const double* sibc_rp;           /* (sibc_nmat, sibc_poles) */
+  const double* sibc_cp;           /* sibc_poles */
+  const double* sibc_gp;           /* sibc_poles */
+} oafdtd_problem;
+
+typedef struct oafdtd_engine oafdtd_engine;
+
+/* Library ABI version (OAFDTD_ABI_VERSION). */
+int32_t oafdtd_abi_version(void);
+
+/* Message of the last failure on this thread ("" when none). */
+const char* oafdtd_last_error(void);
+
+/* Number of CUDA devices visible (0 when none); never fails. */
+int32_t oafdtd_device_count(void);
+
+/* Make `device` the current CUDA device of the calling thread for this library (the device
+ * oafdtd_create builds on). One process per GPU calls it with its local rank. */
+int oafdtd_set_device(int32_t device);
+
+/* Name, compute capability and memory of the current device (the oa_accel AccelReport fields
+ * that CupyEngine's backend fills, packages/oa-accel/src/oa_accel/report.py:13-34, and the free
+ * memory that MemoryBudget.require checks against, packages/oa-accel/src/oa_accel/memory.py:82). */
+int oafdtd_device_info(char* name, int32_t name_len, int32_t* cc_major, int32_t* cc_minor,
+                       int64_t* free_bytes, int64_t* total_bytes, int32_t* runtime_version);
+
+/* Build an engine on the current device: replaces CupyEngine.__init__ (engine.py:73-119), which
+ * copies the Compiled arrays to the device, builds the edge lists and allocates psi/J/v state. */
+int oafdtd_create(const oafdtd_problem* problem, oafdtd_engine** out);
+
+/* Release every device resource of the handle. Replaces dropping the CupyEngine object. */
+int oafdtd_destroy(oafdtd_engine* engine);
+
+/* Advance n time steps: replaces CupyEngine.step (engine.py:418-437). Full 64-step chunks replay
+ * a captured CUDA graph (use_graph != 0, set by oafdtd_set_graph). OAFDTD_E_RANGE when the total
+ * would pass max_steps (the reference raises ValueError there). */
+int oafdtd_step(oafdtd_engine* engine, int64_t n);
+
+/* oafdtd_step with the elapsed device time of its launches (CUDA events recorded on the
+ * handle's stream before the first and after the last launch) written to *device_ms. */
+int oafdtd_step_timed(oafdtd_engine* engine, int64_t n, double* device_ms);
+
+/* Steps taken so far. */
+int oafdtd_step_count(const oafdtd_engine* engine, int64_t* out);
+
+/* Field energy 1/2 sum eps E^2 V + 1/2 mu0 sum H^2 V in float64: replaces CupyEngine.energy
+ * (engine.py:440-468). */
+int oafdtd_energy(oafdtd_engine* engine, double* out);
+
+/* Probe DFT accumulators: replaces CupyEngine.results (engine.py:486-494). Writes
+ * n_probe * batch * n_freq complex values as interleaved (re, im) doubles, probe-major, in the
+ * order of the problem's probe list. */
+int oafdtd_dft(oafdtd_engine* engine, double* out_re_im);
+
+/* Recorded probe samples (record_series != 0): replaces CupyEngine.series (engine.py:496-503).
+ * Writes n_probe * batch * steps doubles, probe-major, step fastest. */
+int oafdtd_series(oafdtd_engine* engine, double* out);
+
+/* One field component as float64, shape (batch, nz+2, ny+2, pitch): comp 0..2 = Ex..Ez,
+ * 3..5 = Hx..Hz. Replaces CupyEngine.get_fields (engine.py:478-484). */
+int oafdtd_fields(oafdtd_engine* engine, int32_t comp, double* out);
+
+/* Device bytes held by the handle: replaces CupyEngine.peak_bytes (engine.py:505-506). */
+int oafdtd_peak_bytes(const oafdtd_engine* engine, int64_t* out);
+
+/* 0: eager launches only; 1 (default): capture the first full 64-step chunk into a CUDA graph
+ * and replay it (the reference's use_graph flag, engine.py:80,425-429). */
+int oafdtd_set_graph(oafdtd_engine* engine, int32_t use_graph);
+
+/* Kernel launch shape: block rows (y extent of a sweep tile) and z planes marched per tile.
+ * 0 keeps the current value. The tile shapes of the autotuner are set through this. */
+int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_y, int32_t tile_z);
+
+/* Average device time per step of each kernel class over the last oafdtd_step call, measured
+ * with CUDA events when profiling is on (oafdtd_set_profiling). Writes up to n values in the
+ * order: h_sweep, ghosts, pre_e, e_sweep, edges, probe_e, whole step. */
+int oafdtd_set_profiling(oafdtd_engine* engine, int32_t on);
+int oafdtd_kernel_times(oafdtd_engine* engine, double* out_ms, int32_t n);
+
+/* Algorithmic DRAM bytes of one time step (all batch members) under the traffic model of the
+ * engine: fields, index, CPML psi, ADE J, SIBC state. Used for the roofline report. */
+int oafdtd_model_bytes(const oafdtd_engine* engine, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OAFDTD_H */

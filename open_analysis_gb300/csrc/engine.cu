@@ -1,0 +1,1027 @@
+// C ABI of the GB300 FDTD engine: device state, host-side preparation of the edge lists and the
+// combined material table, the step driver (eager launches or a captured 64-step CUDA graph) and
+// the observables. The public contract is include/oafdtd.h.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <new>
+#include <string>
+#include <tuple>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/oafdtd.h"
+#include "oafdtd_internal.cuh"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define OA_CUDA(call)                                                                             \
+  do {                                                                                            \
+    cudaError_t err_ = (call);                                                                    \
+    if (err_ != cudaSuccess)                                                                      \
+      return fail(err_ == cudaErrorMemoryAllocation ? OAFDTD_E_OOM : OAFDTD_E_CUDA,               \
+                  std::string(#call) + ": " + cudaGetErrorString(err_));                          \
+  } while (0)
+
+constexpr double kEps0 = 1.0 / (4e-7 * 3.14159265358979323846 * 299792458.0 * 299792458.0);
+constexpr double kMu0 = 4e-7 * 3.14159265358979323846;
+
+// E_TERMS of oa_fdtd/pml.py:26-33: (c, a, b, sign); H_TERMS have the opposite signs.
+constexpr int kTerms[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 2, 0}, {1, 0, 2}, {2, 0, 1}, {2, 1, 0}};
+constexpr double kTermSign[6] = {1.0, -1.0, 1.0, -1.0, 1.0, -1.0};
+
+struct EngineBase {
+  virtual ~EngineBase() = default;
+  virtual int step(int64_t n) = 0;
+  virtual int energy(double* out) = 0;
+  virtual int dft(double* out) = 0;
+  virtual int series(double* out) = 0;
+  virtual int fields(int comp, double* out) = 0;
+  virtual int kernel_times(double* out, int n) = 0;
+  virtual int step_timed(int64_t n, double* ms) = 0;
+  int64_t steps = 0;
+  int64_t bytes = 0;
+  int use_graph = 1;
+  int profiling = 0;
+  int tile_y = 8;
+  int tile_z = 16;
+  bool graph_dirty = false;  // launch shape or profiling changed: the graph is re-captured
+  double model_bytes = 0.0;
+};
+
+template <typename real>
+struct Engine final : EngineBase {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<void*> allocs;
+  int nx = 0, ny = 0, nz = 0, X = 0, Y = 0, Z = 0, B = 0;
+  long long bs = 0;
+  int pmc_mask = 0;
+  int max_steps = 0;
+  int n_probe = 0, n_freq = 0, record_series = 0;
+  oafdtd::SweepArgs<real> sw{};
+  oafdtd::EdgeArgs<real> ed{};
+  oafdtd::ProbeArgs<real> pr{};
+  oafdtd::EnergyArgs<real> en{};
+  long long* step_base = nullptr;
+  double* energy_partial = nullptr;
+  double* energy_out = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  bool graph_ready = false;
+  static constexpr int kClasses = 6;  // h_sweep, ghosts, pre_e, e_sweep, edges, probe_e
+  std::vector<cudaEvent_t> events;    // (kChunk, kClasses + 1) in profiling mode
+  double prof_ms[kClasses + 1] = {};
+  int64_t prof_steps = 0;
+
+  ~Engine() override {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    for (cudaEvent_t e : events) cudaEventDestroy(e);
+    if (t_start) cudaEventDestroy(t_start);
+    if (t_stop) cudaEventDestroy(t_stop);
+    for (void* p : allocs) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  template <typename T>
+  int alloc(T** out, size_t count) {
+    *out = nullptr;
+    if (count == 0) count = 1;
+    void* p = nullptr;
+    cudaError_t err = cudaMalloc(&p, count * sizeof(T));
+    if (err != cudaSuccess)
+      return fail(err == cudaErrorMemoryAllocation ? OAFDTD_E_OOM : OAFDTD_E_CUDA,
+                  "cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes: " + cudaGetErrorString(err));
+    allocs.push_back(p);
+    bytes += (int64_t)(count * sizeof(T));
+    err = cudaMemsetAsync(p, 0, count * sizeof(T), stream);
+    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, cudaGetErrorString(err));
+    *out = static_cast<T*>(p);
+    return OAFDTD_OK;
+  }
+
+  template <typename T>
+  int upload(T** out, const T* host, size_t count) {
+    int rc = alloc(out, count);
+    if (rc) return rc;
+    if (count) OA_CUDA(cudaMemcpyAsync(*out, host, count * sizeof(T), cudaMemcpyHostToDevice, stream));
+    return OAFDTD_OK;
+  }
+
+  template <typename T>
+  int upload_vec(T** out, const std::vector<T>& v) {
+    return upload(out, v.data(), v.size());
+  }
+
+  int upload_real(const real** out, const double* host, size_t count) {
+    std::vector<real> tmp(count);
+    for (size_t k = 0; k < count; ++k) tmp[k] = (real)host[k];
+    real* d = nullptr;
+    int rc = upload_vec(&d, tmp);
+    *out = d;
+    return rc;
+  }
+
+  int build(const oafdtd_problem& p);
+  int launch_step(int off, cudaEvent_t* ev);
+  int capture();
+
+  int step(int64_t n) override;
+  int energy(double* out) override;
+  int dft(double* out) override;
+  int series(double* out) override;
+  int fields(int comp, double* out) override;
+  int kernel_times(double* out, int n) override;
+  int step_timed(int64_t n, double* ms) override;
+  cudaEvent_t t_start = nullptr, t_stop = nullptr;
+};
+
+// ---------------------------------------------------------------------------- build
+template <typename real>
+int Engine<real>::build(const oafdtd_problem& p) {
+  nx = p.nx;
+  ny = p.ny;
+  nz = p.nz;
+  X = p.pitch;
+  Y = ny + 2;
+  Z = nz + 2;
+  B = p.batch;
+  bs = (long long)X * Y * Z;
+  pmc_mask = p.pmc_mask;
+  max_steps = p.max_steps;
+  if (nx < 1 || ny < 1 || nz < 1 || B < 1 || X < nx + 2 || X % 32 != 0)
+    return fail(OAFDTD_E_INVALID, "bad grid or batch size");
+  if (p.n_mat < 1 || p.n_mat > 65535) return fail(OAFDTD_E_INVALID, "n_mat out of range");
+  if (p.ade_poles < 0 || p.ade_poles > oafdtd::kMaxAdePoles)
+    return fail(OAFDTD_E_INVALID, "at most 16 Debye poles are supported");
+  OA_CUDA(cudaGetDevice(&device));
+  OA_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+
+  auto in_range = [&](long long f) { return f >= 0 && f < bs; };
+
+  // fields
+  for (int c = 0; c < 3; ++c) {
+    real* e = nullptr;
+    real* h = nullptr;
+    int rc = alloc(&e, (size_t)bs * B);
+    if (rc) return rc;
+    rc = alloc(&h, (size_t)bs * B);
+    if (rc) return rc;
+    sw.E[c] = e;
+    sw.H[c] = h;
+  }
+
+  // ---- Debye ADE: per-edge coefficient rows and the set of dispersive edges
+  const int P = p.ade_poles;
+  // injection targets (component, flat)
+  std::vector<std::pair<int, long long>> inj_keys;
+  inj_keys.reserve((size_t)p.n_inj);
+  for (int64_t t = 0; t < p.n_inj; ++t) {
+    if (p.inj_comp[t] < 0 || p.inj_comp[t] > 2 || !in_range(p.inj_flat[t]) || p.inj_chan[t] < 0 ||
+        p.inj_chan[t] >= p.n_chan)
+      return fail(OAFDTD_E_INVALID, "injection entry out of range");
+    inj_keys.emplace_back(p.inj_comp[t], p.inj_flat[t]);
+  }
+  std::vector<std::pair<int, long long>> inj_sorted = inj_keys;
+  std::sort(inj_sorted.begin(), inj_sorted.end());
+  auto injected = [&](int c, long long f) {
+    return std::binary_search(inj_sorted.begin(), inj_sorted.end(), std::make_pair(c, f));
+  };
+
+  // combined table: key (material index, ADE row or -1, deferred)
+  std::vector<real> t_ca, t_cb, t_cbe, t_beta;
+  std::vector<double> t_eps;
+  std::vector<uint8_t> t_flag;
+  std::unordered_map<uint64_t, int> comb_id;
+  std::map<std::vector<uint64_t>, int> ade_row_id;  // (cbe bits, beta bits...) -> row
+  std::vector<std::vector<real>> ade_rows;          // cbe, beta_0..P-1
+  auto comb = [&](int v, int ade_row, int defer) -> int {
+    const uint64_t key = (uint64_t)v | ((uint64_t)(ade_row + 1) << 16) | ((uint64_t)defer << 48);
+    auto it = comb_id.find(key);
+    if (it != comb_id.end()) return it->second;
+    const int id = (int)t_ca.size();
+    t_ca.push_back((real)p.ca_tab[v]);
+    t_cb.push_back((real)p.cb_tab[v]);
+    t_eps.push_back(p.eps_tab[v] * kEps0);
+    uint8_t flag = 0;
+    if (ade_row >= 0) flag = defer ? (oafdtd::kFlagAde | oafdtd::kFlagDefer) : oafdtd::kFlagAde;
+    t_flag.push_back(flag);
+    t_cbe.push_back(ade_row >= 0 ? ade_rows[ade_row][0] : (real)0);
+    for (int q = 0; q < P; ++q) t_beta.push_back(ade_row >= 0 ? ade_rows[ade_row][1 + q] : (real)0);
+    comb_id.emplace(key, id);
+    return id;
+  };
+
+  std::vector<int> plain(p.n_mat, -1);
+  std::vector<std::pair<int, long long>> deferred;  // (comp, flat) in component order
+  int kmin[3] = {0, 0, 0}, kmax[3] = {-1, -1, -1};
+  for (int c = 0; c < 3; ++c) {
+    std::vector<uint16_t> m((size_t)bs);
+    const uint16_t* idx = p.idx[c];
+    for (long long q = 0; q < bs; ++q) {
+      const int v = idx[q];
+      if (v >= p.n_mat) return fail(OAFDTD_E_INVALID, "material index beyond the table");
+      int id = plain[v];
+      if (id < 0) id = plain[v] = comb(v, -1, 0);
+      if (id > 65535) return fail(OAFDTD_E_TABLE, "more than 65535 combined material entries");
+      m[q] = (uint16_t)id;
+    }
+    const int64_t ne = P > 0 ? p.ade_n[c] : 0;
+    for (int64_t e = 0; e < ne; ++e) {
+      const long long f = p.ade_flat[c][e];
+      if (!in_range(f)) return fail(OAFDTD_E_INVALID, "ADE edge out of range");
+      std::vector<uint64_t> key(1 + P);
+      std::vector<real> row(1 + P);
+      row[0] = (real)p.ade_cbe[c][e];
+      for (int q = 0; q < P; ++q) row[1 + q] = (real)p.ade_beta[c][(size_t)q * ne + e];
+      for (int q = 0; q <= P; ++q) {
+        uint64_t bits = 0;
+        std::memcpy(&bits, &row[q], sizeof(real));
+        key[q] = bits;
+      }
+      auto it = ade_row_id.find(key);
+      int rid;
+      if (it == ade_row_id.end()) {
+        rid = (int)ade_rows.size();
+        ade_rows.push_back(row);
+        ade_row_id.emplace(key, rid);
+      } else {
+        rid = it->second;
+      }
+      const int defer = injected(c, f) ? 1 : 0;
+      const int id = comb(idx[f], rid, defer);
+      if (id > 65535) return fail(OAFDTD_E_TABLE, "more than 65535 combined material entries");
+      m[f] = (uint16_t)id;
+      if (defer) deferred.emplace_back(c, f);
+      const int k = (int)(f / ((long long)X * Y));
+      if (kmax[c] < kmin[c]) {
+        kmin[c] = kmax[c] = k;
+      } else {
+        kmin[c] = std::min(kmin[c], k);
+        kmax[c] = std::max(kmax[c], k);
+      }
+    }
+    uint16_t* dm = nullptr;
+    int rc = upload_vec(&dm, m);
+    if (rc) return rc;
+    sw.mat[c] = dm;
+    ed.mat[c] = dm;
+    en.mat[c] = dm;
+  }
+  {
+    real* d = nullptr;
+    int rc = upload_vec(&d, t_ca);
+    if (rc) return rc;
+    sw.ca = d;
+    rc = upload_vec(&d, t_cb);
+    if (rc) return rc;
+    sw.cb = d;
+    rc = upload_vec(&d, t_cbe);
+    if (rc) return rc;
+    sw.ade_cbe = ed.ade_cbe = d;
+    if (t_beta.empty()) t_beta.push_back((real)0);
+    rc = upload_vec(&d, t_beta);
+    if (rc) return rc;
+    sw.ade_beta = ed.ade_beta = d;
+    uint8_t* fl = nullptr;
+    rc = upload_vec(&fl, t_flag);
+    if (rc) return rc;
+    sw.flag = ed.flag = fl;
+    double* eps = nullptr;
+    rc = upload_vec(&eps, t_eps);
+    if (rc) return rc;
+    en.eps = eps;
+    std::vector<real> kp(std::max(P, 1), (real)0), onekp(std::max(P, 1), (real)0);
+    for (int q = 0; q < P; ++q) {
+      kp[q] = (real)p.ade_kp[q];
+      onekp[q] = (real)1 + kp[q];
+    }
+    rc = upload_vec(&d, kp);
+    if (rc) return rc;
+    sw.ade_kp = ed.ade_kp = d;
+    rc = upload_vec(&d, onekp);
+    if (rc) return rc;
+    sw.ade_onekp = ed.ade_onekp = d;
+    sw.ade_P = ed.ade_P = P;
+  }
+  for (int c = 0; c < 3; ++c) {
+    const int nk = kmax[c] >= kmin[c] ? kmax[c] - kmin[c] + 1 : 0;
+    sw.jk0[c] = ed.jk0[c] = kmin[c];
+    sw.jnk[c] = ed.jnk[c] = nk;
+    real* J = nullptr;
+    if (nk > 0) {
+      int rc = alloc(&J, (size_t)P * B * nk * Y * X);
+      if (rc) return rc;
+    }
+    sw.J[c] = ed.J[c] = J;
+  }
+
+  // ---- 1-D metrics
+  const int len[3] = {X, Y, Z};
+  for (int a = 0; a < 3; ++a) {
+    int rc = upload_real(&sw.ip[a], p.inv_primal[a], len[a]);
+    if (rc) return rc;
+    rc = upload_real(&sw.idd[a], p.inv_dual[a], len[a]);
+    if (rc) return rc;
+  }
+
+  // ---- CPML
+  sw.has_cpml = p.n_corr > 0;
+  for (int a = 0; a < 3; ++a) {
+    for (int t = 0; t < 3; ++t) sw.pe[a][t] = sw.ph[a][t] = nullptr;
+    if (p.pml[a][0] == nullptr) continue;
+    for (int t = 0; t < 3; ++t) {
+      int rc = upload_real(&sw.pe[a][t], p.pml[a][t], len[a]);
+      if (rc) return rc;
+      rc = upload_real(&sw.ph[a][t], p.pml[a][3 + t], len[a]);
+      if (rc) return rc;
+    }
+  }
+  for (int c = 0; c < 3; ++c)
+    for (int s = 0; s < 2; ++s) {
+      sw.ecorr[c][s] = oafdtd::CpmlTerm<real>{};
+      sw.hcorr[c][s] = oafdtd::CpmlTerm<real>{};
+    }
+  int last_slot[2][3] = {{-1, -1, -1}, {-1, -1, -1}};
+  for (int n = 0; n < p.n_corr; ++n) {
+    const oafdtd_correction& k = p.corr[n];
+    if (k.kind < 0 || k.kind > 1 || k.c < 0 || k.c > 2 || k.a < 0 || k.a > 2 || k.b < 0 || k.b > 2)
+      return fail(OAFDTD_E_INVALID, "bad CPML correction");
+    int term = -1;
+    for (int t = 0; t < 6; ++t)
+      if (kTerms[t][0] == k.c && kTerms[t][1] == k.a && kTerms[t][2] == k.b) term = t;
+    const double want = k.kind == 0 ? kTermSign[term < 0 ? 0 : term] : -kTermSign[term < 0 ? 0 : term];
+    if (term < 0 || k.sign != want) return fail(OAFDTD_E_INVALID, "CPML correction is not a curl term");
+    if (p.pml[k.a][0] == nullptr) return fail(OAFDTD_E_INVALID, "CPML correction on an axis without coefficients");
+    const int first_axis = k.c == 0 ? 1 : 0;
+    const int slot = k.a == first_axis ? 0 : 1;
+    if (slot < last_slot[k.kind][k.c])
+      return fail(OAFDTD_E_INVALID, "CPML corrections of a component must come in ascending axis order");
+    last_slot[k.kind][k.c] = slot;
+    oafdtd::CpmlTerm<real>& term_ref = k.kind == 0 ? sw.ecorr[k.c][slot] : sw.hcorr[k.c][slot];
+    int side = term_ref.side[0].psi == nullptr ? 0 : (term_ref.side[1].psi == nullptr ? 1 : 2);
+    if (side == 2) return fail(OAFDTD_E_INVALID, "more than two CPML sides on one axis");
+    long long vol = B;
+    for (int ax = 0; ax < 3; ++ax) {
+      if (k.lo[ax] < 0 || k.hi[ax] <= k.lo[ax] || k.hi[ax] > len[ax])
+        return fail(OAFDTD_E_INVALID, "CPML box out of range");
+      vol *= (k.hi[ax] - k.lo[ax]);
+    }
+    // the update ranges of the sweeps bound every box: E boxes lie in [1, n + 1], H boxes too
+    real* psi = nullptr;
+    int rc = alloc(&psi, (size_t)vol);
+    if (rc) return rc;
+    term_ref.axis = k.a;
+    term_ref.sign = (real)k.sign;
+    term_ref.side[side].psi = psi;
+    for (int ax = 0; ax < 3; ++ax) {
+      term_ref.side[side].lo[ax] = k.lo[ax];
+      term_ref.side[side].hi[ax] = k.hi[ax];
+    }
+  }
+  sw.dtmu = (real)p.dtmu;
+  sw.nx = nx;
+  sw.ny = ny;
+  sw.nz = nz;
+  sw.X = X;
+  sw.Y = Y;
+  sw.bs = bs;
+  sw.B = B;
+  sw.tile_z = tile_z;
+
+  // ---- edge list: surface impedance, injection targets, deferred ADE edges
+  struct EdgeRec {
+    int comp;
+    long long flat;
+    int sibc = -1;
+    int def = -1;
+    std::vector<int> inj;
+  };
+  std::map<std::pair<int, long long>, EdgeRec> edges;
+  for (int64_t s = 0; s < p.sibc_n; ++s) {
+    const int c = p.sibc_comp[s];
+    const long long f = p.sibc_flat[s];
+    if (c < 0 || c > 2 || !in_range(f) || p.sibc_mat[s] < 0 || p.sibc_mat[s] >= p.sibc_nmat)
+      return fail(OAFDTD_E_INVALID, "SIBC edge out of range");
+    for (int k = 0; k < 2; ++k)
+      if (p.sibc_hsign[2 * s + k] != 0.0 && (p.sibc_hcomp[2 * s + k] < 0 || p.sibc_hcomp[2 * s + k] > 2 ||
+                                             !in_range(p.sibc_hflat[2 * s + k])))
+        return fail(OAFDTD_E_INVALID, "SIBC sample out of range");
+    EdgeRec& r = edges[{c, f}];
+    r.comp = c;
+    r.flat = f;
+    if (r.sibc >= 0) return fail(OAFDTD_E_INVALID, "duplicate SIBC edge");
+    r.sibc = (int)s;
+  }
+  {
+    // within one channel a repeated edge keeps only its last entry (NumPy fancy-index +=)
+    std::map<std::tuple<int, int, long long>, int64_t> last_in_chan;
+    for (int64_t t = 0; t < p.n_inj; ++t) last_in_chan[{p.inj_chan[t], p.inj_comp[t], p.inj_flat[t]}] = t;
+    for (int64_t t = 0; t < p.n_inj; ++t) {
+      if (last_in_chan[{p.inj_chan[t], p.inj_comp[t], p.inj_flat[t]}] != t) continue;
+      EdgeRec& r = edges[{p.inj_comp[t], p.inj_flat[t]}];
+      r.comp = p.inj_comp[t];
+      r.flat = p.inj_flat[t];
+      r.inj.push_back((int)t);
+    }
+  }
+  for (auto& cf : deferred) {
+    EdgeRec& r = edges[cf];
+    if (r.sibc >= 0) return fail(OAFDTD_E_INVALID, "an edge is both dispersive and surface-impedance");
+  }
+  {
+    std::vector<int8_t> comp;
+    std::vector<long long> flat, dflat;
+    std::vector<int8_t> dcomp;
+    std::vector<int> sslot, ibeg, iend, dslot, ichan;
+    std::vector<double> iamp;
+    std::vector<std::pair<int, long long>> def_sorted = deferred;
+    std::sort(def_sorted.begin(), def_sorted.end());
+    for (auto& kv : edges) {
+      EdgeRec& r = kv.second;
+      comp.push_back((int8_t)r.comp);
+      flat.push_back(r.flat);
+      sslot.push_back(r.sibc);
+      ibeg.push_back((int)ichan.size());
+      for (int t : r.inj) {
+        ichan.push_back(p.inj_chan[t]);
+        iamp.push_back(p.inj_amp[t]);
+      }
+      iend.push_back((int)ichan.size());
+      const bool is_def = std::binary_search(def_sorted.begin(), def_sorted.end(), kv.first);
+      if (is_def) {
+        dslot.push_back((int)dflat.size());
+        dflat.push_back(r.flat);
+        dcomp.push_back((int8_t)r.comp);
+      } else {
+        dslot.push_back(-1);
+      }
+    }
+    ed.n = (int)comp.size();
+    int rc;
+    int8_t* d8 = nullptr;
+    long long* dll = nullptr;
+    int* di = nullptr;
+    double* dd = nullptr;
+    if ((rc = upload_vec(&d8, comp))) return rc;
+    ed.comp = d8;
+    if ((rc = upload_vec(&dll, flat))) return rc;
+    ed.flat = dll;
+    if ((rc = upload_vec(&di, sslot))) return rc;
+    ed.sibc_slot = di;
+    if ((rc = upload_vec(&di, ibeg))) return rc;
+    ed.inj_beg = di;
+    if ((rc = upload_vec(&di, iend))) return rc;
+    ed.inj_end = di;
+    if ((rc = upload_vec(&di, dslot))) return rc;
+    ed.def_slot = di;
+    if ((rc = upload_vec(&di, ichan))) return rc;
+    ed.i_chan = di;
+    if ((rc = upload_vec(&dd, iamp))) return rc;
+    ed.i_amp = dd;
+    ed.n_def = pr.n_def = (int)dflat.size();
+    if ((rc = upload_vec(&dll, dflat))) return rc;
+    ed.def_flat = pr.def_flat = dll;
+    if ((rc = upload_vec(&d8, dcomp))) return rc;
+    ed.def_comp = pr.def_comp = d8;
+    real* eold = nullptr;
+    if ((rc = alloc(&eold, (size_t)B * std::max<size_t>(dflat.size(), 1)))) return rc;
+    ed.eold = pr.eold = eold;
+  }
+  // surface impedance tables
+  {
+    const int ns = (int)p.sibc_n, SP = p.sibc_poles;
+    ed.sibc_n = ns;
+    ed.sibc_P = SP;
+    std::vector<int> hc(2 * (size_t)ns);
+    std::vector<long long> hf(2 * (size_t)ns);
+    std::vector<real> hs(2 * (size_t)ns);
+    for (int64_t k = 0; k < 2 * p.sibc_n; ++k) {
+      hc[k] = p.sibc_hcomp[k];
+      hf[k] = p.sibc_hflat[k];
+      hs[k] = (real)p.sibc_hsign[k];
+    }
+    std::vector<real> r0(std::max(p.sibc_nmat, 1)), alpha(std::max(p.sibc_nmat * SP, 1)), gp(std::max(SP, 1));
+    for (int m = 0; m < p.sibc_nmat; ++m) {
+      r0[m] = (real)p.sibc_r0[m];
+      for (int q = 0; q < SP; ++q) alpha[m * SP + q] = (real)(p.sibc_rp[m * SP + q] * p.sibc_cp[q]);
+    }
+    for (int q = 0; q < SP; ++q) gp[q] = (real)p.sibc_gp[q];
+    std::vector<int> smat(p.sibc_mat, p.sibc_mat + p.sibc_n);
+    int rc;
+    int* di = nullptr;
+    long long* dll = nullptr;
+    real* dr = nullptr;
+    if ((rc = upload_vec(&di, hc))) return rc;
+    ed.s_hcomp = di;
+    if ((rc = upload_vec(&dll, hf))) return rc;
+    ed.s_hflat = dll;
+    if ((rc = upload_vec(&dr, hs))) return rc;
+    ed.s_hsign = dr;
+    if ((rc = upload_vec(&di, smat))) return rc;
+    ed.s_mat = di;
+    if ((rc = upload_vec(&dr, r0))) return rc;
+    ed.s_r0 = dr;
+    if ((rc = upload_vec(&dr, alpha))) return rc;
+    ed.s_alpha = dr;
+    if ((rc = upload_vec(&dr, gp))) return rc;
+    ed.s_gp = dr;
+    if ((rc = alloc(&dr, (size_t)B * std::max(ns, 1)))) return rc;
+    ed.s_jprev = dr;
+    if ((rc = alloc(&dr, (size_t)SP * B * std::max(ns, 1)))) return rc;
+    ed.s_v = dr;
+  }
+  // sources
+  {
+    int rc;
+    double* dd = nullptr;
+    const size_t nw = (size_t)p.n_chan * (size_t)p.max_steps;
+    if ((rc = upload(&dd, p.wave, p.n_chan > 0 ? nw : 0))) return rc;
+    ed.wave = dd;
+    if ((rc = upload(&dd, p.drive, (size_t)B * p.n_chan))) return rc;
+    ed.drive = dd;
+    ed.n_chan = p.n_chan;
+    ed.max_steps = p.max_steps;
+  }
+  for (int c = 0; c < 3; ++c) {
+    ed.E[c] = sw.E[c];
+    ed.H[c] = sw.H[c];
+    pr.E[c] = sw.E[c];
+    pr.F[c] = sw.E[c];
+    pr.F[3 + c] = sw.H[c];
+    en.F[c] = sw.E[c];
+    en.F[3 + c] = sw.H[c];
+  }
+  ed.bs = pr.bs = bs;
+  ed.X = X;
+  ed.Y = Y;
+  ed.B = pr.B = en.B = B;
+  if (int rc = alloc(&step_base, 1)) return rc;
+  ed.step_base = pr.step_base = step_base;
+
+  // ---- probes
+  {
+    n_probe = p.n_probe;
+    n_freq = p.n_freq;
+    record_series = p.record_series;
+    std::vector<int> kinds(p.probe_kind, p.probe_kind + p.n_probe);
+    std::vector<int> comps(p.probe_comp, p.probe_comp + p.n_probe);
+    std::vector<long long> off(p.probe_off, p.probe_off + p.n_probe + 1);
+    std::vector<int> lists[2];
+    for (int q = 0; q < p.n_probe; ++q) {
+      if (kinds[q] < 0 || kinds[q] > 1 || comps[q] < 0 || comps[q] > 2 || off[q + 1] < off[q])
+        return fail(OAFDTD_E_INVALID, "bad probe");
+      lists[kinds[q]].push_back(q);
+    }
+    const long long total = p.n_probe > 0 ? off[p.n_probe] : 0;
+    for (long long e = 0; e < total; ++e)
+      if (!in_range(p.probe_flat[e])) return fail(OAFDTD_E_INVALID, "probe point out of range");
+    int rc;
+    int* di = nullptr;
+    long long* dll = nullptr;
+    double* dd = nullptr;
+    if ((rc = upload_vec(&di, kinds))) return rc;
+    pr.kind = di;
+    if ((rc = upload_vec(&di, comps))) return rc;
+    pr.comp = di;
+    if ((rc = upload_vec(&dll, off))) return rc;
+    pr.off = dll;
+    if ((rc = upload(&dll, reinterpret_cast<const long long*>(p.probe_flat), (size_t)total))) return rc;
+    pr.flat = dll;
+    if ((rc = upload(&dd, p.probe_w, (size_t)total))) return rc;
+    pr.w = dd;
+    for (int k = 0; k < 2; ++k) {
+      if ((rc = upload_vec(&di, lists[k]))) return rc;
+      pr.list[k] = di;
+      pr.n_kind[k] = (int)lists[k].size();
+    }
+    pr.n_probe = p.n_probe;
+    pr.n_freq = p.n_freq;
+    if ((rc = upload(&dd, p.omega, (size_t)p.n_freq))) return rc;
+    pr.omega = dd;
+    pr.dt = p.dt;
+    double2* acc = nullptr;
+    if ((rc = alloc(&acc, (size_t)std::max(p.n_probe, 1) * B * std::max(p.n_freq, 1)))) return rc;
+    pr.acc = acc;
+    pr.max_steps = p.max_steps;
+    pr.series = nullptr;
+    if (p.record_series && p.n_probe > 0) {
+      double* ser = nullptr;
+      if ((rc = alloc(&ser, (size_t)p.n_probe * B * p.max_steps))) return rc;
+      pr.series = ser;
+    }
+  }
+  // ---- energy
+  {
+    en.X = X;
+    en.Y = Y;
+    en.Z = Z;
+    const double* nodew[3];
+    const double* cellw[3];
+    for (int a = 0; a < 3; ++a) {
+      double* d = nullptr;
+      int rc = upload(&d, p.node_w[a], (size_t)len[a]);
+      if (rc) return rc;
+      nodew[a] = d;
+      rc = upload(&d, p.cell_w[a], (size_t)len[a]);
+      if (rc) return rc;
+      cellw[a] = d;
+    }
+    for (int cc = 0; cc < 6; ++cc) {
+      const int c = cc % 3;
+      const bool is_e = cc < 3;
+      for (int a = 0; a < 3; ++a) {
+        const bool node = is_e ? (a != c) : (a == c);
+        en.w[cc][a] = node ? nodew[a] : cellw[a];
+      }
+    }
+    if (int rc = alloc(&energy_partial, (size_t)6 * oafdtd::kEnergyBlocks)) return rc;
+    if (int rc = alloc(&energy_out, 6)) return rc;
+  }
+  // ---- traffic model (bytes per time step, all batch members)
+  {
+    // H sweep: read 3 E, read-modify-write 3 H; E sweep: read 3 H, read-modify-write 3 E:
+    // 18 values per interior cell and batch member, plus the three uint16 indices per cell.
+    const double cells = (double)nx * ny * nz;
+    const double rb = sizeof(real);
+    double mb = cells * B * 18.0 * rb + cells * 6.0;
+    double psi_cells = 0.0;
+    for (int n = 0; n < p.n_corr; ++n) {
+      const oafdtd_correction& k = p.corr[n];
+      psi_cells += (double)(k.hi[0] - k.lo[0]) * (k.hi[1] - k.lo[1]) * (k.hi[2] - k.lo[2]);
+    }
+    mb += psi_cells * B * 2.0 * rb;  // psi read + write
+    double ade_edges = 0.0;
+    for (int c = 0; c < 3; ++c) ade_edges += (double)(P > 0 ? p.ade_n[c] : 0);
+    mb += ade_edges * B * P * 2.0 * rb;  // J read + write
+    mb += (double)p.sibc_n * B * (2.0 * rb * (1 + p.sibc_poles) + 2.0 * rb);  // v, Jprev RMW; 2 H samples
+    model_bytes = mb;
+  }
+  OA_CUDA(cudaStreamSynchronize(stream));
+  return OAFDTD_OK;
+}
+
+// ---------------------------------------------------------------------------- step
+template <typename real>
+int Engine<real>::launch_step(int off, cudaEvent_t* ev) {
+  cudaError_t err;
+  if (ev) OA_CUDA(cudaEventRecord(ev[0], stream));
+  err = oafdtd::launch_h_sweep<real>(sw, tile_y, stream);
+  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("h_sweep: ") + cudaGetErrorString(err));
+  if (ev) OA_CUDA(cudaEventRecord(ev[1], stream));
+  if (pmc_mask) {
+    err = oafdtd::launch_ghosts<real>(sw.H, pmc_mask, nx, ny, nz, X, Y, B, stream);
+    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("ghosts: ") + cudaGetErrorString(err));
+  }
+  if (ev) OA_CUDA(cudaEventRecord(ev[2], stream));
+  err = oafdtd::launch_pre_e<real>(pr, off, stream);
+  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("pre_e: ") + cudaGetErrorString(err));
+  if (ev) OA_CUDA(cudaEventRecord(ev[3], stream));
+  err = oafdtd::launch_e_sweep<real>(sw, tile_y, stream);
+  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("e_sweep: ") + cudaGetErrorString(err));
+  if (ev) OA_CUDA(cudaEventRecord(ev[4], stream));
+  err = oafdtd::launch_edges<real>(ed, off, stream);
+  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("edges: ") + cudaGetErrorString(err));
+  if (ev) OA_CUDA(cudaEventRecord(ev[5], stream));
+  err = oafdtd::launch_probe_e<real>(pr, off, stream);
+  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("probe_e: ") + cudaGetErrorString(err));
+  if (ev) OA_CUDA(cudaEventRecord(ev[6], stream));
+  return OAFDTD_OK;
+}
+
+template <typename real>
+int Engine<real>::capture() {
+  if (graph_exec) {
+    cudaGraphExecDestroy(graph_exec);
+    graph_exec = nullptr;
+  }
+  graph_ready = false;
+  cudaGraph_t graph = nullptr;
+  OA_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+  int rc = OAFDTD_OK;
+  for (int o = 0; o < oafdtd::kChunk && rc == OAFDTD_OK; ++o)
+    rc = launch_step(o, profiling ? &events[(size_t)o * (kClasses + 1)] : nullptr);
+  if (rc == OAFDTD_OK) {
+    cudaError_t err = oafdtd::launch_bump(step_base, oafdtd::kChunk, stream);
+    if (err != cudaSuccess) rc = fail(OAFDTD_E_CUDA, cudaGetErrorString(err));
+  }
+  cudaError_t err = cudaStreamEndCapture(stream, &graph);
+  if (rc != OAFDTD_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(err));
+  err = cudaGraphInstantiate(&graph_exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(err));
+  graph_ready = true;
+  return OAFDTD_OK;
+}
+
+template <typename real>
+int Engine<real>::step(int64_t n) {
+  if (n < 0) return fail(OAFDTD_E_INVALID, "negative step count");
+  if (steps + n > max_steps) return fail(OAFDTD_E_RANGE, "step count exceeds max_steps (wave table length)");
+  OA_CUDA(cudaSetDevice(device));
+  if (graph_dirty) {
+    graph_ready = false;
+    graph_dirty = false;
+  }
+  if (profiling && events.empty()) {
+    events.resize((size_t)oafdtd::kChunk * (kClasses + 1));
+    for (auto& e : events) OA_CUDA(cudaEventCreate(&e));
+    graph_ready = false;
+  }
+  sw.tile_z = tile_z;
+  if (profiling) {
+    for (double& v : prof_ms) v = 0.0;
+    prof_steps = 0;
+  }
+  int64_t done = 0;
+  while (done < n) {
+    const int64_t start = steps;
+    const int take = (int)std::min<int64_t>(n - done, oafdtd::kChunk - start % oafdtd::kChunk);
+    if (use_graph && take == oafdtd::kChunk) {
+      if (!graph_ready) {
+        int rc = capture();
+        if (rc) return rc;
+      }
+      OA_CUDA(cudaGraphLaunch(graph_exec, stream));
+    } else {
+      for (int o = 0; o < take; ++o) {
+        int rc = launch_step(o, profiling ? &events[(size_t)o * (kClasses + 1)] : nullptr);
+        if (rc) return rc;
+      }
+      cudaError_t err = oafdtd::launch_bump(step_base, take, stream);
+      if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, cudaGetErrorString(err));
+    }
+    if (profiling) {
+      OA_CUDA(cudaStreamSynchronize(stream));
+      for (int o = 0; o < take; ++o) {
+        cudaEvent_t* ev = &events[(size_t)o * (kClasses + 1)];
+        for (int k = 0; k < kClasses; ++k) {
+          float ms = 0.f;
+          OA_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+          prof_ms[k] += ms;
+        }
+        float ms = 0.f;
+        OA_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[kClasses]));
+        prof_ms[kClasses] += ms;
+      }
+      prof_steps += take;
+    }
+    steps += take;
+    done += take;
+  }
+  OA_CUDA(cudaStreamSynchronize(stream));
+  OA_CUDA(cudaGetLastError());
+  return OAFDTD_OK;
+}
+
+template <typename real>
+int Engine<real>::step_timed(int64_t n, double* ms) {
+  OA_CUDA(cudaSetDevice(device));
+  if (!t_start) OA_CUDA(cudaEventCreate(&t_start));
+  if (!t_stop) OA_CUDA(cudaEventCreate(&t_stop));
+  OA_CUDA(cudaEventRecord(t_start, stream));
+  int rc = step(n);
+  if (rc) return rc;
+  OA_CUDA(cudaEventRecord(t_stop, stream));
+  OA_CUDA(cudaEventSynchronize(t_stop));
+  float f = 0.f;
+  OA_CUDA(cudaEventElapsedTime(&f, t_start, t_stop));
+  *ms = f;
+  return OAFDTD_OK;
+}
+
+template <typename real>
+int Engine<real>::kernel_times(double* out, int n) {
+  for (int k = 0; k < std::min(n, kClasses + 1); ++k) out[k] = prof_steps ? prof_ms[k] / prof_steps : 0.0;
+  return OAFDTD_OK;
+}
+
+template <typename real>
+int Engine<real>::energy(double* out) {
+  OA_CUDA(cudaSetDevice(device));
+  cudaError_t err = oafdtd::launch_energy<real>(en, energy_partial, oafdtd::kEnergyBlocks, energy_out, stream);
+  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, cudaGetErrorString(err));
+  double parts[6];
+  OA_CUDA(cudaMemcpyAsync(parts, energy_out, sizeof(parts), cudaMemcpyDeviceToHost, stream));
+  OA_CUDA(cudaStreamSynchronize(stream));
+  double total = 0.0;
+  for (int c = 0; c < 3; ++c) {
+    total += 0.5 * parts[c];
+    total += 0.5 * kMu0 * parts[3 + c];
+  }
+  *out = total;
+  return OAFDTD_OK;
+}
+
+template <typename real>
+int Engine<real>::dft(double* out) {
+  OA_CUDA(cudaSetDevice(device));
+  const size_t count = (size_t)n_probe * B * n_freq;
+  if (count)
+    OA_CUDA(cudaMemcpyAsync(out, pr.acc, count * sizeof(double2), cudaMemcpyDeviceToHost, stream));
+  OA_CUDA(cudaStreamSynchronize(stream));
+  return OAFDTD_OK;
+}
+
+template <typename real>
+int Engine<real>::series(double* out) {
+  if (!record_series) return fail(OAFDTD_E_INVALID, "the engine was created without record_series");
+  OA_CUDA(cudaSetDevice(device));
+  for (int q = 0; q < n_probe; ++q)
+    for (int b = 0; b < B; ++b)
+      if (steps)
+        OA_CUDA(cudaMemcpyAsync(out + ((size_t)q * B + b) * steps,
+                                pr.series + ((size_t)q * B + b) * max_steps, steps * sizeof(double),
+                                cudaMemcpyDeviceToHost, stream));
+  OA_CUDA(cudaStreamSynchronize(stream));
+  return OAFDTD_OK;
+}
+
+template <typename real>
+int Engine<real>::fields(int comp, double* out) {
+  if (comp < 0 || comp > 5) return fail(OAFDTD_E_INVALID, "component must be 0..5");
+  OA_CUDA(cudaSetDevice(device));
+  const real* src = comp < 3 ? sw.E[comp] : sw.H[comp - 3];
+  const size_t count = (size_t)bs * B;
+  std::vector<real> tmp(count);
+  OA_CUDA(cudaMemcpyAsync(tmp.data(), src, count * sizeof(real), cudaMemcpyDeviceToHost, stream));
+  OA_CUDA(cudaStreamSynchronize(stream));
+  for (size_t k = 0; k < count; ++k) out[k] = (double)tmp[k];
+  return OAFDTD_OK;
+}
+
+}  // namespace
+
+struct oafdtd_engine {
+  std::unique_ptr<EngineBase> impl;
+};
+
+extern "C" {
+
+int32_t oafdtd_abi_version(void) { return OAFDTD_ABI_VERSION; }
+
+const char* oafdtd_last_error(void) { return g_last_error.c_str(); }
+
+int32_t oafdtd_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int oafdtd_set_device(int32_t device) {
+  const int n = oafdtd_device_count();
+  if (device < 0 || device >= n) return fail(OAFDTD_E_NODEVICE, "device index out of range");
+  OA_CUDA(cudaSetDevice(device));
+  return OAFDTD_OK;
+}
+
+int oafdtd_device_info(char* name, int32_t name_len, int32_t* cc_major, int32_t* cc_minor,
+                       int64_t* free_bytes, int64_t* total_bytes, int32_t* runtime_version) {
+  if (oafdtd_device_count() == 0) return fail(OAFDTD_E_NODEVICE, "no CUDA device is visible");
+  int dev = 0;
+  OA_CUDA(cudaGetDevice(&dev));
+  cudaDeviceProp prop;
+  OA_CUDA(cudaGetDeviceProperties(&prop, dev));
+  if (name && name_len > 0) {
+    std::strncpy(name, prop.name, (size_t)name_len - 1);
+    name[name_len - 1] = 0;
+  }
+  if (cc_major) *cc_major = prop.major;
+  if (cc_minor) *cc_minor = prop.minor;
+  size_t fr = 0, tot = 0;
+  OA_CUDA(cudaMemGetInfo(&fr, &tot));
+  if (free_bytes) *free_bytes = (int64_t)fr;
+  if (total_bytes) *total_bytes = (int64_t)tot;
+  int rv = 0;
+  OA_CUDA(cudaRuntimeGetVersion(&rv));
+  if (runtime_version) *runtime_version = rv;
+  return OAFDTD_OK;
+}
+
+int oafdtd_create(const oafdtd_problem* problem, oafdtd_engine** out) {
+  if (out == nullptr || problem == nullptr) return fail(OAFDTD_E_INVALID, "null argument");
+  *out = nullptr;
+  if (problem->abi_version != OAFDTD_ABI_VERSION) return fail(OAFDTD_E_INVALID, "ABI version mismatch");
+  if (oafdtd_device_count() == 0) return fail(OAFDTD_E_NODEVICE, "no CUDA device is visible");
+  std::unique_ptr<oafdtd_engine> h(new (std::nothrow) oafdtd_engine);
+  if (!h) return fail(OAFDTD_E_OOM, "host allocation failed");
+  int rc;
+  try {
+    if (problem->real_bytes == 4) {
+      auto* e = new Engine<float>();
+      h->impl.reset(e);
+      rc = e->build(*problem);
+    } else if (problem->real_bytes == 8) {
+      auto* e = new Engine<double>();
+      h->impl.reset(e);
+      rc = e->build(*problem);
+    } else {
+      return fail(OAFDTD_E_INVALID, "real_bytes must be 4 or 8");
+    }
+  } catch (const std::bad_alloc&) {
+    return fail(OAFDTD_E_OOM, "host allocation failed while preparing the problem");
+  }
+  if (rc != OAFDTD_OK) return rc;
+  *out = h.release();
+  return OAFDTD_OK;
+}
+
+int oafdtd_destroy(oafdtd_engine* engine) {
+  delete engine;
+  return OAFDTD_OK;
+}
+
+int oafdtd_step(oafdtd_engine* engine, int64_t n) {
+  if (!engine) return fail(OAFDTD_E_INVALID, "null engine");
+  return engine->impl->step(n);
+}
+
+int oafdtd_step_timed(oafdtd_engine* engine, int64_t n, double* device_ms) {
+  if (!engine || !device_ms) return fail(OAFDTD_E_INVALID, "null argument");
+  return engine->impl->step_timed(n, device_ms);
+}
+
+int oafdtd_step_count(const oafdtd_engine* engine, int64_t* out) {
+  if (!engine || !out) return fail(OAFDTD_E_INVALID, "null argument");
+  *out = engine->impl->steps;
+  return OAFDTD_OK;
+}
+
+int oafdtd_energy(oafdtd_engine* engine, double* out) {
+  if (!engine || !out) return fail(OAFDTD_E_INVALID, "null argument");
+  return engine->impl->energy(out);
+}
+
+int oafdtd_dft(oafdtd_engine* engine, double* out) {
+  if (!engine || !out) return fail(OAFDTD_E_INVALID, "null argument");
+  return engine->impl->dft(out);
+}
+
+int oafdtd_series(oafdtd_engine* engine, double* out) {
+  if (!engine || !out) return fail(OAFDTD_E_INVALID, "null argument");
+  return engine->impl->series(out);
+}
+
+int oafdtd_fields(oafdtd_engine* engine, int32_t comp, double* out) {
+  if (!engine || !out) return fail(OAFDTD_E_INVALID, "null argument");
+  return engine->impl->fields(comp, out);
+}
+
+int oafdtd_peak_bytes(const oafdtd_engine* engine, int64_t* out) {
+  if (!engine || !out) return fail(OAFDTD_E_INVALID, "null argument");
+  *out = engine->impl->bytes;
+  return OAFDTD_OK;
+}
+
+int oafdtd_set_graph(oafdtd_engine* engine, int32_t use_graph) {
+  if (!engine) return fail(OAFDTD_E_INVALID, "null engine");
+  engine->impl->use_graph = use_graph ? 1 : 0;
+  return OAFDTD_OK;
+}
+
+int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_y, int32_t tile_z) {
+  if (!engine) return fail(OAFDTD_E_INVALID, "null engine");
+  if (tile_y < 0 || tile_z < 0) return fail(OAFDTD_E_INVALID, "negative tile size");
+  if (tile_y && (tile_y > 32 || 32 * tile_y > 256)) return fail(OAFDTD_E_INVALID, "tile_y must be 1..8");
+  if (tile_y) engine->impl->tile_y = tile_y;
+  if (tile_z) engine->impl->tile_z = tile_z;
+  engine->impl->graph_dirty = true;  // a new launch shape needs a new graph
+  return OAFDTD_OK;
+}
+
+int oafdtd_set_profiling(oafdtd_engine* engine, int32_t on) {
+  if (!engine) return fail(OAFDTD_E_INVALID, "null engine");
+  engine->impl->profiling = on ? 1 : 0;
+  engine->impl->graph_dirty = true;  // event records live inside the captured graph
+  return OAFDTD_OK;
+}
+
+int oafdtd_kernel_times(oafdtd_engine* engine, double* out_ms, int32_t n) {
+  if (!engine || !out_ms) return fail(OAFDTD_E_INVALID, "null argument");
+  return engine->impl->kernel_times(out_ms, n);
+}
+
+int oafdtd_model_bytes(const oafdtd_engine* engine, double* out) {
+  if (!engine || !out) return fail(OAFDTD_E_INVALID, "null argument");
+  *out = engine->impl->model_bytes;
+  return OAFDTD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,176 @@
+// Internal types shared by the engine's host code and its kernels.
+//
+// Device data layout (HBM):
+//  * fields: six arrays E0..E2, H0..H2, each (B, Z, Y, X) with Z = nz + 2, Y = ny + 2, X = pitch;
+//    x rows are 128-byte aligned (pitch is a multiple of 32 elements).
+//  * mat[c]: uint16 per E edge (Z, Y, X), index into the combined table. The combined table
+//    holds, per entry, the update coefficients ca/cb of the averaged material, its permittivity
+//    (energy) and, for dispersive edges, the Debye ADE coefficients (cbe, beta_p) and flags. It
+//    replaces both the reference's material index and its per-edge ADE arrays, so the E sweep
+//    reads one 2-byte index per edge, shared by every batch member.
+//  * psi: one dense array per CPML correction, (B, nk, nj, ni) over its box.
+//  * J[c]: dense Debye currents (P, B, nzA, Y, X) over the z range that holds dispersive edges.
+//  * edge list (surface impedance, injection, dispersive edges with injection), sorted by
+//    (component, flat index), one thread per edge.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace oafdtd {
+
+constexpr int kChunk = 64;        // steps per captured graph (the reference's CHUNK)
+constexpr int kMaxAdePoles = 16;  // Debye poles handled by the fused sweep
+constexpr uint8_t kFlagAde = 1;   // entry is dispersive
+constexpr uint8_t kFlagDefer = 2; // dispersive edge with injection: ADE applied by the edge pass
+
+template <typename real>
+struct CpmlSide {
+  real* psi;         // nullptr: side absent
+  int lo[3], hi[3];  // storage box [lo, hi) per x, y, z
+};
+
+template <typename real>
+struct CpmlTerm {    // the correction of one (kind, component, derivative axis)
+  int axis;
+  real sign;
+  CpmlSide<real> side[2];
+};
+
+template <typename real>
+struct SweepArgs {
+  real* E[3];
+  real* H[3];
+  const uint16_t* mat[3];
+  const real* ca;
+  const real* cb;
+  const uint8_t* flag;
+  const real* ade_cbe;      // [entry]
+  const real* ade_beta;     // [entry * P + p]
+  const real* ade_kp;       // [p]
+  const real* ade_onekp;    // [p]: 1 + kp in the field precision
+  int ade_P;
+  real* J[3];
+  int jk0[3];
+  int jnk[3];
+  const real* ip[3];        // inverse primal lengths
+  const real* idd[3];       // inverse dual lengths
+  const real* pe[3][3];     // per axis: eb, ec, ek
+  const real* ph[3][3];     // per axis: hb, hc, hk
+  CpmlTerm<real> ecorr[3][2];  // [component][ascending derivative axis]
+  CpmlTerm<real> hcorr[3][2];
+  int has_cpml;
+  real dtmu;
+  int nx, ny, nz, X, Y;
+  long long bs;             // Z * Y * X
+  int B;
+  int tile_z;
+};
+
+template <typename real>
+struct EdgeArgs {
+  real* E[3];
+  const real* H[3];
+  int n;                     // union edges
+  const int8_t* comp;
+  const long long* flat;
+  const int* sibc_slot;      // -1: none
+  const int* inj_beg;
+  const int* inj_end;
+  const int* def_slot;       // -1: none
+  // surface impedance
+  int sibc_n, sibc_P;
+  const int* s_hcomp;        // (ns, 2)
+  const long long* s_hflat;  // (ns, 2)
+  const real* s_hsign;       // (ns, 2)
+  const int* s_mat;
+  const real* s_r0;          // [m]
+  const real* s_alpha;       // [m * P + p] = rp * cp (rounded once to the field precision)
+  const real* s_gp;          // [p]
+  real* s_jprev;             // (B, ns)
+  real* s_v;                 // (P, B, ns)
+  // injection contributions, ordered by edge then channel
+  const int* i_chan;
+  const double* i_amp;
+  const double* wave;        // (n_chan, max_steps)
+  const double* drive;       // (B, n_chan)
+  int n_chan, max_steps;
+  // deferred ADE
+  int n_def;
+  real* eold;                // (B, n_def)
+  const uint16_t* mat[3];
+  const uint8_t* flag;
+  const real* ade_cbe;
+  const real* ade_beta;
+  const real* ade_kp;
+  const real* ade_onekp;
+  int ade_P;
+  real* J[3];
+  int jk0[3];
+  int jnk[3];
+  const long long* def_flat; // (n_def)
+  const int8_t* def_comp;
+  long long bs;
+  int X, Y, B;
+  const long long* step_base;
+};
+
+template <typename real>
+struct ProbeArgs {
+  const real* F[6];          // E0..E2, H0..H2
+  int n_probe;
+  const int* kind;
+  const int* comp;
+  const long long* off;
+  const long long* flat;
+  const double* w;
+  const int* list[2];        // probe ids of kind E / H
+  int n_kind[2];
+  int n_freq;
+  const double* omega;
+  double dt;
+  double2* acc;              // (n_probe, B, F)
+  double* series;            // (n_probe, B, max_steps) or nullptr
+  int max_steps;
+  long long bs;
+  int B;
+  const long long* step_base;
+  // deferred-ADE save (in the pre-E launch)
+  int n_def;
+  real* eold;
+  const long long* def_flat;
+  const int8_t* def_comp;
+  const real* E[3];
+};
+
+template <typename real>
+struct EnergyArgs {
+  const real* F[6];
+  const uint16_t* mat[3];
+  const double* eps;         // [entry] eps_r * eps0
+  const double* w[6][3];     // per component, per axis: node or cell weights
+  int X, Y, Z, B;
+};
+
+// kernel launchers (kernels.cu)
+template <typename real>
+cudaError_t launch_h_sweep(const SweepArgs<real>& a, int tile_y, cudaStream_t s);
+template <typename real>
+cudaError_t launch_e_sweep(const SweepArgs<real>& a, int tile_y, cudaStream_t s);
+template <typename real>
+cudaError_t launch_ghosts(real* const H[3], int pmc_mask, int nx, int ny, int nz, int X, int Y, int B,
+                          cudaStream_t s);
+template <typename real>
+cudaError_t launch_pre_e(const ProbeArgs<real>& a, int off, cudaStream_t s);
+template <typename real>
+cudaError_t launch_edges(const EdgeArgs<real>& a, int off, cudaStream_t s);
+template <typename real>
+cudaError_t launch_probe_e(const ProbeArgs<real>& a, int off, cudaStream_t s);
+template <typename real>
+cudaError_t launch_energy(const EnergyArgs<real>& a, double* partial, int nblocks, double* out,
+                          cudaStream_t s);
+cudaError_t launch_bump(long long* step_base, int n, cudaStream_t s);
+
+constexpr int kEnergyBlocks = 1216;  // 8 per SM on a 152-SM GB300; fixed for a deterministic sum
+
+}  // namespace oafdtd

@@ -1,0 +1,292 @@
+"""``Gb300Engine``: the engine protocol over the sm_103a CUDA library.
+
+Drop-in for the reference's ``CupyEngine`` (``packages/oa-fdtd/src/oa_fdtd/engine.py:67-506``):
+same constructor arguments, same methods (``step, energy, results, series, get_fields,
+peak_bytes``), same shapes, units and time stamps (H probes at (n+1/2) dt, E probes at (n+1) dt,
+sources at (n+1/2) dt), same ``ValueError`` past ``max_steps``. It consumes a ``Compiled``
+problem as-is; the library copies it to the device once and owns all device state.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from typing import Any
+
+import numpy as np
+import numpy.typing as npt
+
+from open_analysis_gb300 import native
+from open_analysis_gb300.grid import MU0
+
+FloatArray = npt.NDArray[np.float64]
+CHUNK = 64
+
+
+def estimate_bytes(c: Any, itemsize: int) -> int:
+    """Device bytes of a problem: fields, the index, CPML psi, ADE and SIBC state, plus 5 %
+    (the reference's estimate, ``engine.py:29-40``, which the run driver checks before creating
+    the engine)."""
+    cells = int(np.prod(c.grid.shape))
+    psi = sum(int(np.prod(k.shape)) for k in c.pml.corrections) * c.batch * itemsize
+    extra = 0
+    if c.ade is not None:
+        ne = sum(f.size for f in c.ade.flat)
+        extra += ne * (c.ade.tau.size * (c.batch + 1) + c.batch + 2) * itemsize
+    if c.sibc is not None:
+        ne = c.sibc.flat.size
+        extra += ne * (c.batch * (1 + c.sibc.cp.size) * itemsize + 2 * (4 + 8 + itemsize))
+    return int((cells * (6 * itemsize * c.batch + 6) + psi + extra) * 1.05)
+
+
+def wave_table(c: Any, max_steps: int) -> FloatArray:
+    """``s_c((n + 1/2) dt)`` for every channel and step (float64), evaluated as the reference's
+    injection does; a vectorised evaluation is used only when it equals the per-step one."""
+    t = (np.arange(max_steps) + 0.5) * c.dt
+    out = np.zeros((len(c.channels), max_steps))
+    for ci, ch in enumerate(c.channels):
+        wf = ch["waveform"]
+        vec = np.asarray(wf(t), dtype=np.float64)
+        probe = np.unique(np.linspace(0, max_steps - 1, min(max_steps, 97)).astype(np.int64))
+        scalar = np.array([float(wf(np.array([(int(n) + 0.5) * c.dt]))[0]) for n in probe])
+        if not np.array_equal(vec[probe], scalar):
+            vec = np.array([float(wf(np.array([(n + 0.5) * c.dt]))[0]) for n in range(max_steps)])
+        out[ci] = vec
+    return out
+
+
+def _ptr(a: np.ndarray, ctype: Any) -> Any:
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+class Gb300Engine:
+    """Leapfrog Yee engine on one GB300 (the current CUDA device)."""
+
+    name = "gb300"
+
+    def __init__(
+        self,
+        c: Any,
+        dtype: str = "float32",
+        record_series: bool = False,
+        max_steps: int = 200_000,
+        use_graph: bool = True,
+        **_: Any,
+    ) -> None:
+        self.c = c
+        self.dtype = str(np.dtype(dtype))
+        if self.dtype not in ("float32", "float64"):
+            raise ValueError("dtype must be float32 or float64")
+        self.record_series = bool(record_series)
+        self.max_steps = int(max_steps)
+        self._lib = native.load()
+        self._h = C.c_void_p()
+        self._keep: list[np.ndarray] = []
+        g = c.grid
+        self.B = c.batch
+        self.shape = (self.B, *g.shape)
+        prob = self._problem()
+        self.h2d_bytes = int(sum(a.nbytes for a in self._keep))  # host buffers the library copies
+        native.check(self._lib.oafdtd_create(C.byref(prob), C.byref(self._h)), "create")
+        self._keep.clear()
+        self.set_graph(use_graph)
+        self._probes = list(c.probes)
+
+    # ------------------------------------------------------------------ descriptor
+    def _arr(self, a: Any, dtype: Any) -> np.ndarray:
+        out = np.ascontiguousarray(np.asarray(a, dtype=dtype))
+        self._keep.append(out)
+        return out
+
+    def _problem(self) -> native.Problem:
+        c, g = self.c, self.c.grid
+        p = native.Problem()
+        p.abi_version = native.ABI_VERSION
+        p.real_bytes = 4 if self.dtype == "float32" else 8
+        p.nx, p.ny, p.nz = g.n
+        p.pitch = g.pitch
+        p.batch = self.B
+        p.dt = float(c.dt)
+        p.dtmu = float(c.dt / MU0)
+        for ci in range(3):
+            p.idx[ci] = _ptr(self._arr(c.idx[ci], np.uint16), C.c_uint16)
+        p.n_mat = int(c.eps_tab.size)
+        p.ca_tab = _ptr(self._arr(c.ca_tab, np.float64), C.c_double)
+        p.cb_tab = _ptr(self._arr(c.cb_tab, np.float64), C.c_double)
+        p.eps_tab = _ptr(self._arr(c.eps_tab, np.float64), C.c_double)
+        for a in range(3):
+            p.inv_primal[a] = _ptr(self._arr(g.inv_primal(a), np.float64), C.c_double)
+            p.inv_dual[a] = _ptr(self._arr(g.inv_dual(a), np.float64), C.c_double)
+            p.node_w[a] = _ptr(self._arr(g.node_weights(a), np.float64), C.c_double)
+            p.cell_w[a] = _ptr(self._arr(g.cell_weights(a), np.float64), C.c_double)
+        p.pmc_mask = sum(1 << k for k in range(6) if c.walls[k] == "pmc")
+        corr = c.pml.corrections
+        p.n_corr = len(corr)
+        if corr:
+            arr = (native.Correction * len(corr))()
+            for n, k in enumerate(corr):
+                arr[n].kind = 0 if k.kind == "E" else 1
+                arr[n].c, arr[n].a, arr[n].b = k.c, k.a, k.b
+                arr[n].sign = float(k.sign)
+                for ax in range(3):
+                    arr[n].lo[ax], arr[n].hi[ax] = k.box[ax]
+            self._corr = arr
+            p.corr = C.cast(arr, C.POINTER(native.Correction))
+        for a, co in c.pml.coeffs.items():
+            for t, name in enumerate(("eb", "ec", "ek", "hb", "hc", "hk")):
+                p.pml[a][t] = _ptr(self._arr(getattr(co, name), np.float64), C.c_double)
+        # sources
+        chans = c.channels
+        p.n_chan = len(chans)
+        p.max_steps = self.max_steps
+        p.wave = _ptr(self._arr(wave_table(c, self.max_steps) if chans else np.zeros(1), np.float64), C.c_double)
+        p.drive = _ptr(self._arr(c.drive, np.float64), C.c_double)
+        comp, flat, amp, chan = [], [], [], []
+        for ci, ch in enumerate(chans):
+            fl = np.asarray(ch["flat"], dtype=np.int64)
+            comp.append(np.broadcast_to(np.asarray(ch["comp"], np.int32), fl.shape))
+            flat.append(fl)
+            amp.append(np.asarray(ch["amps"], np.float64))
+            chan.append(np.full(fl.size, ci, np.int32))
+        cat = (lambda v, dt: np.concatenate(v).astype(dt) if v else np.zeros(0, dt))
+        inj_comp, inj_flat = cat(comp, np.int32), cat(flat, np.int64)
+        p.n_inj = int(inj_flat.size)
+        p.inj_comp = _ptr(self._arr(inj_comp, np.int32), C.c_int32)
+        p.inj_flat = _ptr(self._arr(inj_flat, np.int64), C.c_int64)
+        p.inj_amp = _ptr(self._arr(cat(amp, np.float64), np.float64), C.c_double)
+        p.inj_chan = _ptr(self._arr(cat(chan, np.int32), np.int32), C.c_int32)
+        # probes
+        probes = c.probes
+        p.n_probe = len(probes)
+        sizes = [np.asarray(q["flat"]).size for q in probes]
+        p.probe_kind = _ptr(self._arr([0 if q["kind"] == "E" else 1 for q in probes] or [0], np.int32), C.c_int32)
+        p.probe_comp = _ptr(self._arr([int(q["comp"]) for q in probes] or [0], np.int32), C.c_int32)
+        p.probe_off = _ptr(self._arr(np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64), np.int64), C.c_int64)
+        p.probe_flat = _ptr(
+            self._arr(cat([np.asarray(q["flat"], np.int64) for q in probes], np.int64), np.int64), C.c_int64
+        )
+        p.probe_w = _ptr(
+            self._arr(cat([np.asarray(q["weights"], np.float64) for q in probes], np.float64), np.float64),
+            C.c_double,
+        )
+        p.n_freq = int(c.frequencies.size)
+        p.omega = _ptr(self._arr(2.0 * np.pi * c.frequencies, np.float64), C.c_double)
+        p.record_series = int(self.record_series)
+        # Debye ADE
+        if c.ade is not None:
+            a = c.ade
+            p.ade_poles = int(a.tau.size)
+            p.ade_kp = _ptr(self._arr(a.kp, np.float64), C.c_double)
+            for comp_, fl, be, cbe in zip(a.comp, a.flat, a.beta, a.cbe, strict=True):
+                p.ade_n[comp_] = int(np.asarray(fl).size)
+                p.ade_flat[comp_] = _ptr(self._arr(fl, np.int64), C.c_int64)
+                p.ade_beta[comp_] = _ptr(self._arr(be, np.float64), C.c_double)
+                p.ade_cbe[comp_] = _ptr(self._arr(cbe, np.float64), C.c_double)
+        # surface impedance
+        if c.sibc is not None:
+            s = c.sibc
+            p.sibc_n = int(s.flat.size)
+            p.sibc_poles = int(s.cp.size)
+            p.sibc_nmat = int(s.r0.size)
+            p.sibc_comp = _ptr(self._arr(s.comp, np.int32), C.c_int32)
+            p.sibc_flat = _ptr(self._arr(s.flat, np.int64), C.c_int64)
+            p.sibc_hcomp = _ptr(self._arr(s.hcomp, np.int32), C.c_int32)
+            p.sibc_hflat = _ptr(self._arr(s.hflat, np.int64), C.c_int64)
+            p.sibc_hsign = _ptr(self._arr(s.hsign, np.float64), C.c_double)
+            p.sibc_mat = _ptr(self._arr(s.mat, np.int32), C.c_int32)
+            p.sibc_r0 = _ptr(self._arr(s.r0, np.float64), C.c_double)
+            p.sibc_rp = _ptr(self._arr(s.rp, np.float64), C.c_double)
+            p.sibc_cp = _ptr(self._arr(s.cp, np.float64), C.c_double)
+            p.sibc_gp = _ptr(self._arr(s.gp, np.float64), C.c_double)
+        return p
+
+    # ------------------------------------------------------------------ protocol
+    @property
+    def step_count(self) -> int:
+        n = C.c_int64()
+        native.check(self._lib.oafdtd_step_count(self._h, C.byref(n)), "step_count")
+        return int(n.value)
+
+    def step(self, n: int = 1) -> None:
+        if self.step_count + n > self.max_steps:
+            raise ValueError("step count exceeds max_steps (wave table length)")
+        native.check(self._lib.oafdtd_step(self._h, int(n)), "step")
+
+    def step_timed(self, n: int) -> float:
+        """``step(n)``; returns the device time of its launches [ms] (CUDA events on the engine's
+        own stream)."""
+        if self.step_count + n > self.max_steps:
+            raise ValueError("step count exceeds max_steps (wave table length)")
+        ms = C.c_double()
+        native.check(self._lib.oafdtd_step_timed(self._h, int(n), C.byref(ms)), "step_timed")
+        return float(ms.value)
+
+    def energy(self) -> float:
+        out = C.c_double()
+        native.check(self._lib.oafdtd_energy(self._h, C.byref(out)), "energy")
+        return float(out.value)
+
+    def results(self) -> dict[str, npt.NDArray[np.complex128]]:
+        nf = self.c.frequencies.size
+        buf = np.zeros((max(len(self._probes), 1), self.B, max(nf, 1), 2))
+        native.check(self._lib.oafdtd_dft(self._h, _ptr(buf, C.c_double)), "dft")
+        acc = buf[..., 0] + 1j * buf[..., 1]
+        return {q["name"]: acc[pi, :, :nf].copy() for pi, q in enumerate(self._probes)}
+
+    def series(self) -> dict[str, FloatArray]:
+        if not self.record_series:
+            return {}
+        steps = self.step_count
+        if steps == 0 or not self._probes:
+            return {}
+        buf = np.zeros((len(self._probes), self.B, steps))
+        native.check(self._lib.oafdtd_series(self._h, _ptr(buf, C.c_double)), "series")
+        return {q["name"]: buf[pi].copy() for pi, q in enumerate(self._probes)}
+
+    def field(self, comp: int) -> FloatArray:
+        out = np.zeros(self.shape)
+        native.check(self._lib.oafdtd_fields(self._h, int(comp), _ptr(out, C.c_double)), "fields")
+        return out
+
+    def get_fields(self) -> dict[str, FloatArray]:
+        names = ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")
+        return {n: self.field(k) for k, n in enumerate(names)}
+
+    def peak_bytes(self) -> int:
+        out = C.c_int64()
+        native.check(self._lib.oafdtd_peak_bytes(self._h, C.byref(out)), "peak_bytes")
+        return int(out.value)
+
+    # ------------------------------------------------------------------ tuning and profiling
+    def set_graph(self, on: bool) -> None:
+        native.check(self._lib.oafdtd_set_graph(self._h, int(bool(on))), "set_graph")
+
+    def set_tuning(self, tile_y: int = 0, tile_z: int = 0) -> None:
+        native.check(self._lib.oafdtd_set_tuning(self._h, int(tile_y), int(tile_z)), "set_tuning")
+
+    def set_profiling(self, on: bool) -> None:
+        native.check(self._lib.oafdtd_set_profiling(self._h, int(bool(on))), "set_profiling")
+
+    KERNELS = ("h_sweep", "ghosts", "pre_e", "e_sweep", "edges", "probe_e", "step")
+
+    def kernel_times(self) -> dict[str, float]:
+        """Average device ms per time step of each kernel class over the last ``step`` call."""
+        out = np.zeros(len(self.KERNELS))
+        native.check(self._lib.oafdtd_kernel_times(self._h, _ptr(out, C.c_double), len(out)), "kernel_times")
+        return dict(zip(self.KERNELS, out.tolist(), strict=True))
+
+    def model_bytes(self) -> float:
+        """Algorithmic DRAM bytes of one time step under the engine's traffic model."""
+        out = C.c_double()
+        native.check(self._lib.oafdtd_model_bytes(self._h, C.byref(out)), "model_bytes")
+        return float(out.value)
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.oafdtd_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass

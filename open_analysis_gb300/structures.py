@@ -1,0 +1,146 @@
+"""Synthetic engine-level problems with the shapes of the benchmark workloads.
+
+No board files or meshers are needed (the reference's EMProblem front end is not part of this
+package): each builder returns a :class:`~open_analysis_gb300.model.Model` directly, with seeded
+geometry where the workload calls for randomness.
+
+* :func:`microstrip` — 50-ohm-class microstrip, 120 x 60 x 40 cells of 50 um, FR-4 (4.3)
+  substrate 0.2 mm, zero-thickness PEC strip 0.36 mm wide, PEC ground, 8-cell CPML (m = 3,
+  kappa_max = 5), Gaussian-derivative source 0-20 GHz, 0.99 Courant, two lumped ports, 64 DFT
+  frequencies.
+* :func:`via_transition` — 400 x 400 x 120 cells of 25 um: a four-layer stack with a single-pole
+  Debye dielectric (eps_inf 4.0, delta_eps 0.35, tau 8 ps), three copper planes and two trace
+  layers as surface-impedance copper (sigma 5.8e7 S/m), a via (0.3 mm drill as the 1.694 r
+  square barrel, 0.5 mm pads, 0.8 mm antipads), 10-cell CPML, two lumped ports, 256 DFT
+  frequencies 0.1-20 GHz.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+import numpy.typing as npt
+
+from open_analysis_gb300.grid import Grid, uniform_lines
+from open_analysis_gb300.model import Conductor, LumpedPort, Model, Region, Waveform
+from open_analysis_gb300.pml import CpmlSpec
+
+FloatArray = npt.NDArray[np.float64]
+
+
+@dataclass(frozen=True)
+class GaussDerivative:
+    """First derivative of a Gaussian, normalised to a unit peak: no DC content, spectrum
+    proportional to ``f exp(-(pi f tau)^2)``. ``tau = sqrt(ln 10) / (pi bandwidth)`` as for the
+    reference's Gaussian, so the envelope factor is -20 dB at ``bandwidth``. Same interface as
+    :class:`~open_analysis_gb300.model.Waveform` (``kind``, ``tau``, ``delay_tau``, call).
+    """
+
+    bandwidth: float
+    delay_tau: float = 5.0
+    kind: str = "gauss_deriv"
+    f0: float = 0.0
+
+    @property
+    def tau(self) -> float:
+        return math.sqrt(math.log(10.0)) / (math.pi * self.bandwidth)
+
+    def __call__(self, t: FloatArray) -> FloatArray:
+        tau = self.tau
+        x = (t - self.delay_tau * tau) / tau
+        return -math.sqrt(2.0 * math.e) * x * np.exp(-(x**2))  # type: ignore[no-any-return]
+
+
+def microstrip(nx: int = 120, ny: int = 60, nz: int = 40, h: float = 50e-6, batch_both: bool = True) -> Model:
+    """The plain 50-ohm microstrip workload (defaults: 120 x 60 x 40 cells of 50 um)."""
+    g = Grid(uniform_lines(nx, h), uniform_lines(ny, h), uniform_lines(nz, h))
+    freqs = np.linspace(20e9 / 64, 20e9, 64)
+    m = Model(
+        g,
+        GaussDerivative(bandwidth=20e9),  # type: ignore[arg-type]
+        freqs,
+        walls=("cpml", "cpml", "cpml", "cpml", "pec", "cpml"),
+        cpml=CpmlSpec(cells=8, m=3.0, kappa_max=5.0),
+        courant=0.99,
+    )
+    sub = 0.2e-3
+    m.regions.append(Region((-1.0, -1.0, 0.0), (1.0, 1.0, sub), 4.3))
+    yc = (ny // 2) * h
+    x0, x1 = 14 * h, (nx - 14) * h
+    m.regions.append(Region((x0, yc - 0.18e-3, sub), (x1, yc + 0.18e-3, sub), pec=True))
+    m.ports.append(LumpedPort("p1", 2, (x0, yc, 0.0), (x0, yc, sub), 50.0))
+    m.ports.append(LumpedPort("p2", 2, (x1, yc, 0.0), (x1, yc, sub), 50.0))
+    if not batch_both:
+        m.excite = ("p1",)
+    return m
+
+
+def via_transition(
+    nx: int = 400,
+    ny: int = 400,
+    nz: int = 120,
+    h: float = 25e-6,
+    n_freq: int = 256,
+    cpml_cells: int = 10,
+    drill: float = 0.3e-3,
+    pad: float = 0.5e-3,
+    antipad: float = 0.8e-3,
+    eps_inf: float = 4.0,
+    delta_eps: float = 0.35,
+    tau: float = 8e-12,
+) -> Model:
+    """Top trace -> via -> bottom trace through three planes (four dielectric layers).
+
+    Layer positions scale with ``nz``: the stack spans z cells ``[0.13 nz, 0.87 nz]``; the planes
+    sit at the quarter points of the stack. Lateral features are given in metres and snapped by
+    the compiler to the mesh.
+    """
+    g = Grid(uniform_lines(nx, h), uniform_lines(ny, h), uniform_lines(nz, h))
+    freqs = np.linspace(0.1e9, 20e9, n_freq)
+    m = Model(
+        g,
+        Waveform("gauss_mod", 10.05e9, 19.9e9),
+        freqs,
+        walls=("cpml",) * 6,
+        cpml=CpmlSpec(cells=cpml_cells),
+        courant=0.95,
+    )
+    kb = int(round(0.13 * nz))  # bottom trace layer (one cell of copper)
+    kt = int(round(0.87 * nz))  # top trace layer
+    span = kt - (kb + 1)
+    planes = [kb + 1 + (span * q) // 4 for q in (1, 2, 3)]
+    z = lambda k: k * h  # noqa: E731
+    big = 1.0
+    m.regions.append(Region((-big, -big, z(kb)), (big, big, z(kt + 1)), eps_inf, poles=((delta_eps, tau),)))
+    cx, cy = (nx // 2) * h, (ny // 2) * h
+    half_ap = 0.5 * antipad
+    cu = dict(sigma=5.8e7, thickness=35e-6)
+    for k in planes:
+        lo_z, hi_z = z(k), z(k + 1)
+        for lo, hi in (
+            ((-big, -big, lo_z), (cx - half_ap, big, hi_z)),
+            ((cx + half_ap, -big, lo_z), (big, big, hi_z)),
+            ((cx - half_ap, -big, lo_z), (cx + half_ap, cy - half_ap, hi_z)),
+            ((cx - half_ap, cy + half_ap, lo_z), (cx + half_ap, big, hi_z)),
+        ):
+            m.conductors.append(Conductor(lo, hi, **cu))
+    side = 0.5 * drill / 0.5902  # square barrel with the conformal radius of the drill
+    m.conductors.append(Conductor((cx - side / 2, cy - side / 2, z(kb)), (cx + side / 2, cy + side / 2, z(kt + 1)), **cu))
+    for k in (kb, kt):
+        m.conductors.append(Conductor((cx - pad / 2, cy - pad / 2, z(k)), (cx + pad / 2, cy + pad / 2, z(k + 1)), **cu))
+    w = 0.4e-3
+    x_p1, x_p2 = round(0.1 * nx) * h, round(0.9 * nx) * h
+    m.conductors.append(Conductor((x_p1, cy - w / 2, z(kt)), (cx, cy + w / 2, z(kt + 1)), **cu))
+    m.conductors.append(Conductor((cx, cy - w / 2, z(kb)), (x_p2, cy + w / 2, z(kb + 1)), **cu))
+    # ports: top trace to the plane below it; bottom trace to the plane above it
+    m.ports.append(LumpedPort("p1", 2, (x_p1, cy, z(planes[2] + 1)), (x_p1, cy, z(kt)), 50.0))
+    m.ports.append(LumpedPort("p2", 2, (x_p2, cy, z(kb + 1)), (x_p2, cy, z(planes[0])), 50.0))
+    return m
+
+
+WORKLOADS = {
+    "microstrip_120x60x40": microstrip,
+    "via_transition_400x400x120": via_transition,
+}

@@ -1,0 +1,157 @@
+"""GPU engine against the CPU oracle: bit-exact float32 fields, DFTs, energy, S-parameters.
+
+The oracle (``oracle/numpy_engine.py``) is pinned against the reference itself by
+``test_golden_compile.py``; here the CUDA engine runs the same compiled problems through the
+C ABI and must reproduce the oracle's float32 fields bit for bit (the library is built without
+FMA contraction and keeps the reference's operation order, including the fused CPML order).
+"""
+
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+from cases import CASES, namespace
+from fingerprint import digest, load
+
+from open_analysis_gb300.model import compile_model
+from oracle.numpy_engine import OracleEngine
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
+NAMES = ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")
+
+
+def _engine(c, dtype="float32", **kw):  # type: ignore[no-untyped-def]
+    from open_analysis_gb300.engine import Gb300Engine
+
+    return Gb300Engine(c, dtype, max_steps=kw.pop("max_steps", 2000), **kw)
+
+
+def test_report_numpy_pole_sum_order() -> None:
+    """Not a check: records whether this host's NumPy sums Debye poles in the kernel's order
+    (it decides whether multi-pole cases compare bit for bit or by rel-L2)."""
+    print("einsum sequential:", _einsum_is_sequential())
+
+
+def _einsum_is_sequential() -> bool:
+    """Whether this host's NumPy sums Debye poles as a plain float32 loop (the kernel's order)."""
+    rng = np.random.default_rng(0)
+    a = rng.random(3).astype(np.float32)
+    j = rng.standard_normal((3, 4, 257)).astype(np.float32)
+    seq = np.zeros((4, 257), np.float32)
+    for p in range(3):
+        seq = seq + a[p] * j[p]
+    return bool(np.array_equal(np.einsum("p,pbe->be", a, j), seq))
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+def test_fields_match_oracle(case: str, dtype: str) -> None:
+    builder, steps = CASES[case]
+    c = compile_model(builder(namespace("gb300")), "float32")
+    gpu = _engine(c, dtype)
+    ref = OracleEngine(c, dtype)
+    gpu.step(steps)
+    ref.step(steps)
+    exact = case != "dispersive_copper" or _einsum_is_sequential()
+    for k, name in enumerate(NAMES):
+        got = gpu.field(k)
+        want = (ref.E + ref.H)[k].astype(np.float64)
+        if exact:
+            assert np.array_equal(got, want), f"{name}: max |d| = {np.abs(got - want).max()}"
+        else:
+            rel = np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-300)
+            assert rel <= 1e-5, f"{name}: rel-L2 {rel}"
+    r_gpu, r_ref = gpu.results(), ref.results()
+    assert set(r_gpu) == set(r_ref)
+    # identical fields: the DFTs differ only by float64 summation order; otherwise by the ulps
+    # of the pole sum propagated through the fields
+    tol = 1e-9 if exact else 1e-6
+    for name, v in r_ref.items():
+        assert r_gpu[name].shape == v.shape
+        scale = max(np.abs(v).max(), 1e-300)
+        assert np.abs(r_gpu[name] - v).max() <= tol * scale, name
+    e_gpu, e_ref = gpu.energy(), ref.energy()
+    assert abs(e_gpu - e_ref) <= 1e-10 * abs(e_ref)
+
+
+@pytest.mark.parametrize("case", ["mixed_walls", "microstrip"])
+def test_fields_match_reference_fixture(case: str) -> None:
+    """The float32 fields' digests equal those of the reference's own NumPy engine."""
+    ref = load(str(GOLDEN / f"{case}.npz"))
+    builder, steps = CASES[case]
+    c = compile_model(builder(namespace("gb300")), "float32")
+    gpu = _engine(c)
+    gpu.step(steps)
+    for k, name in enumerate(NAMES):
+        assert digest(gpu.field(k).astype(np.float32)) == ref[f"float32.field.{name}.sha"], name
+
+
+def test_graph_equals_eager_and_runs_repeat() -> None:
+    c = compile_model(CASES["mixed_walls"][0](namespace("gb300")), "float32")
+    a = _engine(c, use_graph=True, max_steps=700)
+    b = _engine(c, use_graph=False, max_steps=700)
+    a.step(256)
+    b.step(100)
+    b.step(156)
+    for k, v in a.results().items():
+        assert np.array_equal(v, b.results()[k])
+    for k in range(6):
+        assert np.array_equal(a.field(k), b.field(k))
+    d = _engine(c, use_graph=True, max_steps=700)
+    d.step(256)
+    assert np.array_equal(a.energy(), d.energy())
+
+
+def test_step_past_max_steps_raises() -> None:
+    c = compile_model(CASES["microstrip"][0](namespace("gb300")), "float32")
+    eng = _engine(c, max_steps=10)
+    eng.step(10)
+    with pytest.raises(ValueError):
+        eng.step(1)
+
+
+def test_series_recording_matches_oracle() -> None:
+    c = compile_model(CASES["mixed_walls"][0](namespace("gb300")), "float32")
+    gpu = _engine(c, record_series=True, max_steps=200)
+    ref = OracleEngine(c, "float32", record_series=True)
+    gpu.step(70)
+    ref.step(70)
+    sg, sr = gpu.series(), ref.series()
+    assert set(sg) == set(sr)
+    for k, v in sr.items():
+        assert sg[k].shape == v.shape
+        assert np.abs(sg[k] - v).max() <= 1e-12 * max(np.abs(v).max(), 1e-300)
+
+
+def test_run_sparams_match_oracle() -> None:
+    """run() + sparams() through the engine against the same driver over the oracle."""
+    from open_analysis_gb300.run import run, sparams
+
+    m = CASES["microstrip"][0](namespace("gb300"))
+    gpu = run(m, engine="gb300", dtype="float32", end_db=None, max_steps=300)
+    ref = run(m, engine=OracleEngine, dtype="float32", end_db=None, max_steps=300)
+    s_gpu, s_ref = sparams(m, gpu), sparams(m, ref)
+    assert np.abs(s_gpu - s_ref).max() <= 1e-3
+    assert np.abs(s_gpu - s_ref).max() <= 1e-9  # same float32 fields: only DFT rounding differs
+    assert gpu.engine == "gb300" and gpu.peak_bytes > 0 and gpu.report["backend"] == "cuda"
+
+
+def test_energy_end_criterion_runs() -> None:
+    from open_analysis_gb300.run import run
+
+    m = CASES["microstrip"][0](namespace("gb300"))
+    res = run(m, engine="gb300", end_db=-30.0, max_steps=20000)
+    assert res.stopped_by == "end_criterion" and res.energy_db <= -30.0
+
+
+def test_kernel_profile_and_model_bytes() -> None:
+    c = compile_model(CASES["dispersive_copper"][0](namespace("gb300")), "float32")
+    eng = _engine(c)
+    eng.set_profiling(True)
+    eng.step(64)
+    t = eng.kernel_times()
+    assert t["step"] > 0 and t["h_sweep"] > 0 and t["e_sweep"] > 0
+    assert eng.model_bytes() > 0
