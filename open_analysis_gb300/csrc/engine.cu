@@ -133,7 +133,7 @@ struct Engine final : EngineBase {
   }
 
   int build(const oafdtd_problem& p);
-  int launch_step(int off, cudaEvent_t* ev);
+  int launch_step(int off, cudaEvent_t* ev, bool capturing = false);
   int capture();
 
   int step(int64_t n) override;
@@ -673,29 +673,31 @@ int Engine<real>::build(const oafdtd_problem& p) {
 
 // ---------------------------------------------------------------------------- step
 template <typename real>
-int Engine<real>::launch_step(int off, cudaEvent_t* ev) {
+int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing) {
   cudaError_t err;
-  if (ev) OA_CUDA(cudaEventRecord(ev[0], stream));
+  // inside a stream capture an event record becomes a graph node only with the external flag
+  const unsigned rec = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[0], stream, rec));
   err = oafdtd::launch_h_sweep<real>(sw, tile_y, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("h_sweep: ") + cudaGetErrorString(err));
-  if (ev) OA_CUDA(cudaEventRecord(ev[1], stream));
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[1], stream, rec));
   if (pmc_mask) {
     err = oafdtd::launch_ghosts<real>(sw.H, pmc_mask, nx, ny, nz, X, Y, B, stream);
     if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("ghosts: ") + cudaGetErrorString(err));
   }
-  if (ev) OA_CUDA(cudaEventRecord(ev[2], stream));
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[2], stream, rec));
   err = oafdtd::launch_pre_e<real>(pr, off, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("pre_e: ") + cudaGetErrorString(err));
-  if (ev) OA_CUDA(cudaEventRecord(ev[3], stream));
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[3], stream, rec));
   err = oafdtd::launch_e_sweep<real>(sw, tile_y, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("e_sweep: ") + cudaGetErrorString(err));
-  if (ev) OA_CUDA(cudaEventRecord(ev[4], stream));
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[4], stream, rec));
   err = oafdtd::launch_edges<real>(ed, off, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("edges: ") + cudaGetErrorString(err));
-  if (ev) OA_CUDA(cudaEventRecord(ev[5], stream));
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[5], stream, rec));
   err = oafdtd::launch_probe_e<real>(pr, off, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("probe_e: ") + cudaGetErrorString(err));
-  if (ev) OA_CUDA(cudaEventRecord(ev[6], stream));
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[6], stream, rec));
   return OAFDTD_OK;
 }
 
@@ -710,7 +712,7 @@ int Engine<real>::capture() {
   OA_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
   int rc = OAFDTD_OK;
   for (int o = 0; o < oafdtd::kChunk && rc == OAFDTD_OK; ++o)
-    rc = launch_step(o, profiling ? &events[(size_t)o * (kClasses + 1)] : nullptr);
+    rc = launch_step(o, profiling ? &events[(size_t)o * (kClasses + 1)] : nullptr, true);
   if (rc == OAFDTD_OK) {
     cudaError_t err = oafdtd::launch_bump(step_base, oafdtd::kChunk, stream);
     if (err != cudaSuccess) rc = fail(OAFDTD_E_CUDA, cudaGetErrorString(err));

@@ -74,7 +74,7 @@ def test_fields_match_oracle(case: str, dtype: str) -> None:
         scale = max(np.abs(v).max(), 1e-300)
         assert np.abs(r_gpu[name] - v).max() <= tol * scale, name
     e_gpu, e_ref = gpu.energy(), ref.energy()
-    assert abs(e_gpu - e_ref) <= 1e-10 * abs(e_ref)
+    assert abs(e_gpu - e_ref) <= (1e-10 if exact else 1e-6) * abs(e_ref)
 
 
 @pytest.mark.parametrize("case", ["mixed_walls", "microstrip"])
