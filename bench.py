@@ -221,6 +221,9 @@ def build_problem(args: argparse.Namespace) -> tuple[Any, Any]:
 
     if args.workload == "microstrip":
         m = microstrip()
+    elif args.cells:
+        nx, ny, nz = (int(v) for v in args.cells.split(","))
+        m = via_transition(nx=nx, ny=ny, nz=nz)
     else:
         m = via_transition()
     return m, compile_model(m, "float32")
@@ -287,18 +290,26 @@ def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
     eng.close()
 
     # e2e through the public API with host buffers
-    ranks.barrier()
-    t0 = time.perf_counter()
-    eng2 = Gb300Engine(c, "float32", max_steps=max_steps)
-    h2d = eng2.h2d_bytes
-    for _ in range(args.steps):
-        eng2.step(CHUNK)
-        eng2.energy()
-    res = eng2.results()
-    eng2.close()
-    e2e_s = ranks.max(time.perf_counter() - t0)
-    d2h = args.steps * 6 * 8 + sum(v.nbytes for v in res.values())
-    e2e_value = float(cells) * c.batch * CHUNK * args.steps * ranks.world / e2e_s / 1e9
+    e2e = None
+    if not args.no_e2e:
+        ranks.barrier()
+        t0 = time.perf_counter()
+        eng2 = Gb300Engine(c, "float32", max_steps=max_steps)
+        h2d = eng2.h2d_bytes
+        for _ in range(args.steps):
+            eng2.step(CHUNK)
+            eng2.energy()
+        res = eng2.results()
+        eng2.close()
+        e2e_s = ranks.max(time.perf_counter() - t0)
+        d2h = args.steps * 6 * 8 + sum(v.nbytes for v in res.values())
+        e2e = {
+            "value": float(cells) * c.batch * CHUNK * args.steps * ranks.world / e2e_s / 1e9,
+            "unit": "Gcell-updates/s",
+            "h2d_bytes_per_step": h2d / args.steps,
+            "d2h_bytes_per_step": d2h / args.steps,
+            "seconds": e2e_s,
+        }
 
     cpu = None
     if ranks.rank == 0 and ranks.world == 1 and not args.no_cpu:
@@ -319,7 +330,7 @@ def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
             "dtype": "f32",
             "data": "synthetic",
             "config": {
-                "workload": WORKLOAD if args.workload != "microstrip" else "microstrip_120x60x40",
+                "workload": "microstrip_120x60x40" if args.workload == "microstrip" else f"via_transition_{nx}x{ny}x{nz}",
                 "cells": [nx, ny, nz],
                 "batch": c.batch,
                 "time_steps_per_step": CHUNK,
@@ -342,13 +353,7 @@ def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
                 "algorithmic_bytes_per_launch": kb,
                 "step_frac": step_bytes / (ktimes["step"] / 1e3) / 1e9 / peak,
             },
-            "e2e": {
-                "value": e2e_value,
-                "unit": "Gcell-updates/s",
-                "h2d_bytes_per_step": h2d / args.steps,
-                "d2h_bytes_per_step": d2h / args.steps,
-                "seconds": e2e_s,
-            },
+            "e2e": e2e,
             "gpu_launches": (launches_per_step(c) * CHUNK + 1) * args.steps,
             "clocks": clocks,
             "cpu_baseline": cpu,
@@ -413,6 +418,8 @@ def main() -> None:
     ap.add_argument("--workload", default="via_transition", choices=["via_transition", "microstrip"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--cells", default="", help="via-transition grid 'nx,ny,nz' (smaller profiling cases)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
