@@ -198,45 +198,29 @@ int Engine<real>::build(const oafdtd_problem& p) {
     return std::binary_search(inj_sorted.begin(), inj_sorted.end(), std::make_pair(c, f));
   };
 
-  // combined table: key (material index, ADE row or -1, deferred)
-  std::vector<real> t_ca, t_cb, t_cbe, t_beta;
-  std::vector<double> t_eps;
-  std::vector<uint8_t> t_flag;
-  std::unordered_map<uint64_t, int> comb_id;
+  // ---- combined table. Entry key: (category, material index, ADE row); categories 0 plain,
+  // 1 dispersive, 2 dispersive with injection (deferred). The map orders entries by category, so
+  // the kernels tell dispersive entries by an index range.
   std::map<std::vector<uint64_t>, int> ade_row_id;  // (cbe bits, beta bits...) -> row
   std::vector<std::vector<real>> ade_rows;          // cbe, beta_0..P-1
-  auto comb = [&](int v, int ade_row, int defer) -> int {
-    const uint64_t key = (uint64_t)v | ((uint64_t)(ade_row + 1) << 16) | ((uint64_t)defer << 48);
-    auto it = comb_id.find(key);
-    if (it != comb_id.end()) return it->second;
-    const int id = (int)t_ca.size();
-    t_ca.push_back((real)p.ca_tab[v]);
-    t_cb.push_back((real)p.cb_tab[v]);
-    t_eps.push_back(p.eps_tab[v] * kEps0);
-    uint8_t flag = 0;
-    if (ade_row >= 0) flag = defer ? (oafdtd::kFlagAde | oafdtd::kFlagDefer) : oafdtd::kFlagAde;
-    t_flag.push_back(flag);
-    t_cbe.push_back(ade_row >= 0 ? ade_rows[ade_row][0] : (real)0);
-    for (int q = 0; q < P; ++q) t_beta.push_back(ade_row >= 0 ? ade_rows[ade_row][1 + q] : (real)0);
-    comb_id.emplace(key, id);
-    return id;
+  std::vector<uint8_t> present(p.n_mat, 0);
+  struct AdeEdge {
+    long long f;
+    int rid;
+    int defer;
   };
-
-  std::vector<int> plain(p.n_mat, -1);
+  std::vector<AdeEdge> ade_edges[3];
   std::vector<std::pair<int, long long>> deferred;  // (comp, flat) in component order
   int kmin[3] = {0, 0, 0}, kmax[3] = {-1, -1, -1};
+  std::map<std::tuple<int, int, int>, int> entry;   // (category, v, rid) -> id
   for (int c = 0; c < 3; ++c) {
-    std::vector<uint16_t> m((size_t)bs);
     const uint16_t* idx = p.idx[c];
     for (long long q = 0; q < bs; ++q) {
-      const int v = idx[q];
-      if (v >= p.n_mat) return fail(OAFDTD_E_INVALID, "material index beyond the table");
-      int id = plain[v];
-      if (id < 0) id = plain[v] = comb(v, -1, 0);
-      if (id > 65535) return fail(OAFDTD_E_TABLE, "more than 65535 combined material entries");
-      m[q] = (uint16_t)id;
+      if (idx[q] >= p.n_mat) return fail(OAFDTD_E_INVALID, "material index beyond the table");
+      present[idx[q]] = 1;
     }
     const int64_t ne = P > 0 ? p.ade_n[c] : 0;
+    ade_edges[c].reserve((size_t)ne);
     for (int64_t e = 0; e < ne; ++e) {
       const long long f = p.ade_flat[c][e];
       if (!in_range(f)) return fail(OAFDTD_E_INVALID, "ADE edge out of range");
@@ -259,9 +243,8 @@ int Engine<real>::build(const oafdtd_problem& p) {
         rid = it->second;
       }
       const int defer = injected(c, f) ? 1 : 0;
-      const int id = comb(idx[f], rid, defer);
-      if (id > 65535) return fail(OAFDTD_E_TABLE, "more than 65535 combined material entries");
-      m[f] = (uint16_t)id;
+      ade_edges[c].push_back({f, rid, defer});
+      entry[{1 + defer, idx[f], rid}] = 0;
       if (defer) deferred.emplace_back(c, f);
       const int k = (int)(f / ((long long)X * Y));
       if (kmax[c] < kmin[c]) {
@@ -271,6 +254,37 @@ int Engine<real>::build(const oafdtd_problem& p) {
         kmax[c] = std::max(kmax[c], k);
       }
     }
+  }
+  for (int v = 0; v < p.n_mat; ++v)
+    if (present[v]) entry[{0, v, -1}] = 0;
+  if (entry.size() > 65536) return fail(OAFDTD_E_TABLE, "more than 65536 combined material entries");
+  std::vector<oafdtd::Coef<real>> t_coef;
+  std::vector<real> t_beta;
+  std::vector<double> t_eps;
+  std::vector<int> plain(p.n_mat, 0);
+  int ade_lo = -1, ade_hi = -1;
+  for (auto& kv : entry) {
+    const int cat = std::get<0>(kv.first), v = std::get<1>(kv.first), rid = std::get<2>(kv.first);
+    const int id = (int)t_coef.size();
+    kv.second = id;
+    if (cat == 1 && ade_lo < 0) ade_lo = id;
+    if (cat == 1) ade_hi = id + 1;
+    if (cat == 0) plain[v] = id;
+    oafdtd::Coef<real> cf;
+    cf.ca = (real)p.ca_tab[v];
+    cf.cb = (real)p.cb_tab[v];
+    cf.cbe = rid >= 0 ? ade_rows[rid][0] : (real)0;
+    cf.beta0 = (rid >= 0 && P > 0) ? ade_rows[rid][1] : (real)0;
+    t_coef.push_back(cf);
+    for (int q = 0; q < P; ++q) t_beta.push_back(rid >= 0 ? ade_rows[rid][1 + q] : (real)0);
+    t_eps.push_back(p.eps_tab[v] * kEps0);
+  }
+  if (ade_lo < 0) ade_lo = ade_hi = 0;
+  for (int c = 0; c < 3; ++c) {
+    std::vector<uint16_t> m((size_t)bs);
+    const uint16_t* idx = p.idx[c];
+    for (long long q = 0; q < bs; ++q) m[q] = (uint16_t)plain[idx[q]];
+    for (const AdeEdge& ae : ade_edges[c]) m[ae.f] = (uint16_t)entry[{1 + ae.defer, idx[ae.f], ae.rid}];
     uint16_t* dm = nullptr;
     int rc = upload_vec(&dm, m);
     if (rc) return rc;
@@ -279,24 +293,17 @@ int Engine<real>::build(const oafdtd_problem& p) {
     en.mat[c] = dm;
   }
   {
+    oafdtd::Coef<real>* dc = nullptr;
+    int rc = upload_vec(&dc, t_coef);
+    if (rc) return rc;
+    sw.coef = ed.coef = dc;
+    sw.ade_lo = ade_lo;
+    sw.ade_hi = ade_hi;
     real* d = nullptr;
-    int rc = upload_vec(&d, t_ca);
-    if (rc) return rc;
-    sw.ca = d;
-    rc = upload_vec(&d, t_cb);
-    if (rc) return rc;
-    sw.cb = d;
-    rc = upload_vec(&d, t_cbe);
-    if (rc) return rc;
-    sw.ade_cbe = ed.ade_cbe = d;
     if (t_beta.empty()) t_beta.push_back((real)0);
     rc = upload_vec(&d, t_beta);
     if (rc) return rc;
     sw.ade_beta = ed.ade_beta = d;
-    uint8_t* fl = nullptr;
-    rc = upload_vec(&fl, t_flag);
-    if (rc) return rc;
-    sw.flag = ed.flag = fl;
     double* eps = nullptr;
     rc = upload_vec(&eps, t_eps);
     if (rc) return rc;
@@ -353,6 +360,8 @@ int Engine<real>::build(const oafdtd_problem& p) {
       sw.hcorr[c][s] = oafdtd::CpmlTerm<real>{};
     }
   int last_slot[2][3] = {{-1, -1, -1}, {-1, -1, -1}};
+  std::vector<uint8_t> slab[3] = {std::vector<uint8_t>(X, 0), std::vector<uint8_t>(Y, 0),
+                                  std::vector<uint8_t>(Z, 0)};
   for (int n = 0; n < p.n_corr; ++n) {
     const oafdtd_correction& k = p.corr[n];
     if (k.kind < 0 || k.kind > 1 || k.c < 0 || k.c > 2 || k.a < 0 || k.a > 2 || k.b < 0 || k.b > 2)
@@ -371,13 +380,13 @@ int Engine<real>::build(const oafdtd_problem& p) {
     oafdtd::CpmlTerm<real>& term_ref = k.kind == 0 ? sw.ecorr[k.c][slot] : sw.hcorr[k.c][slot];
     int side = term_ref.side[0].psi == nullptr ? 0 : (term_ref.side[1].psi == nullptr ? 1 : 2);
     if (side == 2) return fail(OAFDTD_E_INVALID, "more than two CPML sides on one axis");
-    long long vol = B;
-    for (int ax = 0; ax < 3; ++ax) {
-      if (k.lo[ax] < 0 || k.hi[ax] <= k.lo[ax] || k.hi[ax] > len[ax])
+    for (int ax = 0; ax < 3; ++ax)
+      if (k.lo[ax] < 1 || k.hi[ax] <= k.lo[ax] || k.hi[ax] > len[ax])
         return fail(OAFDTD_E_INVALID, "CPML box out of range");
-      vol *= (k.hi[ax] - k.lo[ax]);
-    }
-    // the update ranges of the sweeps bound every box: E boxes lie in [1, n + 1], H boxes too
+    // psi spans the slab along the derivative axis and the full storage extent on the others
+    long long vol = B;
+    for (int ax = 0; ax < 3; ++ax) vol *= (ax == k.a) ? (k.hi[ax] - k.lo[ax]) : len[ax];
+    for (int q = k.lo[k.a]; q < k.hi[k.a]; ++q) slab[k.a][q] = 1;
     real* psi = nullptr;
     int rc = alloc(&psi, (size_t)vol);
     if (rc) return rc;
@@ -388,6 +397,16 @@ int Engine<real>::build(const oafdtd_problem& p) {
       term_ref.side[side].lo[ax] = k.lo[ax];
       term_ref.side[side].hi[ax] = k.hi[ax];
     }
+  }
+  {
+    uint8_t* d = nullptr;
+    int rc = upload_vec(&d, slab[0]);
+    if (rc) return rc;
+    sw.slab_x = d;
+    if ((rc = upload_vec(&d, slab[1]))) return rc;
+    sw.slab_y = d;
+    if ((rc = upload_vec(&d, slab[2]))) return rc;
+    sw.slab_z = d;
   }
   sw.dtmu = (real)p.dtmu;
   sw.nx = nx;

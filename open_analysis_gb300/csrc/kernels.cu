@@ -1,10 +1,7 @@
 // FDTD time-step kernels for sm_103a.
 //
 // One time step is: h_sweep -> [ghosts] -> [pre_e] -> e_sweep -> [edges] -> [probe_e].
-//  * h_sweep: H update with every CPML-H correction fused, one thread per (i, j) column marching
-//    up a z chunk; E at k + 1 is carried in registers to the next plane.
-//  * e_sweep: E update from the combined material index, CPML-E corrections and the Debye ADE
-//    update fused (E^n stays in a register); H at k - 1 is carried.
+//  * h_sweep, e_sweep: the Yee sweeps with CPML, and Debye ADE fused (sweeps.cu).
 //  * ghosts: PMC mirror planes, one launch per wall in wall order.
 //  * pre_e: H probe sums + running DFT at (n + 1/2) dt; saves E^n of dispersive edges that also
 //    receive injection (their ADE update runs after the injection, in the edge pass).
@@ -20,199 +17,6 @@
 #include "oafdtd_internal.cuh"
 
 namespace oafdtd {
-
-template <typename real>
-__device__ __forceinline__ void apply_cpml(real& f, const CpmlTerm<real>& t, int i, int j, int k, int b,
-                                           real d, real kfac, const real* cb_, const real* cc_,
-                                           const real* ck_) {
-#pragma unroll
-  for (int s = 0; s < 2; ++s) {
-    const CpmlSide<real>& sd = t.side[s];
-    if (sd.psi == nullptr) continue;
-    if (i < sd.lo[0] || i >= sd.hi[0] || j < sd.lo[1] || j >= sd.hi[1] || k < sd.lo[2] ||
-        k >= sd.hi[2])
-      continue;
-    const int ia = t.axis == 0 ? i : (t.axis == 1 ? j : k);
-    const int ni = sd.hi[0] - sd.lo[0], nj = sd.hi[1] - sd.lo[1], nk = sd.hi[2] - sd.lo[2];
-    const long long q =
-        (((long long)b * nk + (k - sd.lo[2])) * nj + (j - sd.lo[1])) * (long long)ni + (i - sd.lo[0]);
-    real ps = sd.psi[q];
-    ps = ps * cb_[ia];
-    ps = ps + cc_[ia] * d;
-    sd.psi[q] = ps;
-    const real upd = ck_[ia] * d + ps;
-    f = f + (t.sign * kfac) * upd;
-  }
-}
-
-// ----------------------------------------------------------------------------- H sweep
-template <typename real>
-__global__ void __launch_bounds__(256) h_sweep_kernel(const __grid_constant__ SweepArgs<real> a) {
-  const int i = blockIdx.x * 32 + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int b = blockIdx.z % a.B;
-  const int kc = blockIdx.z / a.B;
-  const int nx = a.nx, ny = a.ny, nz = a.nz;
-  if (i < 1 || i > nx + 1 || j > ny + 1) return;
-  const int k0 = 1 + kc * a.tile_z;
-  const int k1 = min(k0 + a.tile_z, nz + 2);
-  const long long sy = a.X, sz = (long long)a.X * a.Y;
-  const long long base = (long long)b * a.bs;
-  const real* __restrict__ Ex = a.E[0] + base;
-  const real* __restrict__ Ey = a.E[1] + base;
-  const real* __restrict__ Ez = a.E[2] + base;
-  real* __restrict__ Hx = a.H[0] + base;
-  real* __restrict__ Hy = a.H[1] + base;
-  real* __restrict__ Hz = a.H[2] + base;
-  const real ipx = a.ip[0][i], ipy = a.ip[1][j];
-  const real dtmu = a.dtmu;
-  long long p = (long long)k0 * sz + (long long)j * sy + i;
-  real ex_c = Ex[p], ey_c = Ey[p];
-  for (int k = k0; k < k1; ++k, p += sz) {
-    const bool kin = k <= nz;
-    const real ex_n = kin ? Ex[p + sz] : (real)0;
-    const real ey_n = kin ? Ey[p + sz] : (real)0;
-    const real ez = Ez[p];
-    const real ipz = a.ip[2][k];
-    if (j <= ny && kin) {  // Hx: node along x, cell along y and z
-      const real dy = (Ez[p + sy] - ez) * ipy;
-      const real dz = (ey_n - ey_c) * ipz;
-      const real acc = (-dy) + dz;
-      real h = Hx[p] + dtmu * acc;
-      if (a.has_cpml) {
-        apply_cpml(h, a.hcorr[0][0], i, j, k, b, dy, dtmu, a.ph[1][0], a.ph[1][1], a.ph[1][2]);
-        apply_cpml(h, a.hcorr[0][1], i, j, k, b, dz, dtmu, a.ph[2][0], a.ph[2][1], a.ph[2][2]);
-      }
-      Hx[p] = h;
-    }
-    if (i <= nx && kin) {  // Hy
-      const real dz = (ex_n - ex_c) * ipz;
-      const real dx = (Ez[p + 1] - ez) * ipx;
-      const real acc = (-dz) + dx;
-      real h = Hy[p] + dtmu * acc;
-      if (a.has_cpml) {
-        apply_cpml(h, a.hcorr[1][0], i, j, k, b, dx, dtmu, a.ph[0][0], a.ph[0][1], a.ph[0][2]);
-        apply_cpml(h, a.hcorr[1][1], i, j, k, b, dz, dtmu, a.ph[2][0], a.ph[2][1], a.ph[2][2]);
-      }
-      Hy[p] = h;
-    }
-    if (i <= nx && j <= ny) {  // Hz: node along z (k up to nz + 1)
-      const real dx = (Ey[p + 1] - ey_c) * ipx;
-      const real dy = (Ex[p + sy] - ex_c) * ipy;
-      const real acc = (-dx) + dy;
-      real h = Hz[p] + dtmu * acc;
-      if (a.has_cpml) {
-        apply_cpml(h, a.hcorr[2][0], i, j, k, b, dx, dtmu, a.ph[0][0], a.ph[0][1], a.ph[0][2]);
-        apply_cpml(h, a.hcorr[2][1], i, j, k, b, dy, dtmu, a.ph[1][0], a.ph[1][1], a.ph[1][2]);
-      }
-      Hz[p] = h;
-    }
-    ex_c = ex_n;
-    ey_c = ey_n;
-  }
-}
-
-// ----------------------------------------------------------------------------- E sweep
-template <typename real>
-__device__ __forceinline__ real ade_update(real e, real e0, const SweepArgs<real>& a, int c, int m,
-                                           long long jq, long long jstride) {
-  // jt = 1/2 sum_p (1 + k_p) J_p ; E^{n+1} = e - cbe jt ; J_p = k_p J_p + beta_p (E^{n+1} - E^n)
-  real* J = a.J[c];
-  const int P = a.ade_P;
-  real jt = (real)0;
-  for (int p = 0; p < P; ++p) jt = jt + a.ade_onekp[p] * J[jq + p * jstride];
-  jt = (real)0.5 * jt;
-  const real en = e - a.ade_cbe[m] * jt;
-  const real de = en - e0;
-  for (int p = 0; p < P; ++p) {
-    const long long q = jq + p * jstride;
-    J[q] = a.ade_kp[p] * J[q] + a.ade_beta[m * P + p] * de;
-  }
-  return en;
-}
-
-template <typename real>
-__global__ void __launch_bounds__(256) e_sweep_kernel(const __grid_constant__ SweepArgs<real> a) {
-  const int i = blockIdx.x * 32 + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int b = blockIdx.z % a.B;
-  const int kc = blockIdx.z / a.B;
-  const int nx = a.nx, ny = a.ny, nz = a.nz;
-  if (i < 1 || i > nx + 1 || j > ny + 1) return;
-  const int k0 = 1 + kc * a.tile_z;
-  const int k1 = min(k0 + a.tile_z, nz + 2);
-  const long long sy = a.X, sz = (long long)a.X * a.Y;
-  const long long base = (long long)b * a.bs;
-  real* __restrict__ Ex = a.E[0] + base;
-  real* __restrict__ Ey = a.E[1] + base;
-  real* __restrict__ Ez = a.E[2] + base;
-  const real* __restrict__ Hx = a.H[0] + base;
-  const real* __restrict__ Hy = a.H[1] + base;
-  const real* __restrict__ Hz = a.H[2] + base;
-  const real idx_ = a.idd[0][i], idy = a.idd[1][j];
-  long long q = (long long)k0 * sz + (long long)j * sy + i;  // in-plane (batch-free) index
-  real hx_m = Hx[q - sz], hy_m = Hy[q - sz];
-  for (int k = k0; k < k1; ++k, q += sz) {
-    const real hx = Hx[q], hy = Hy[q], hz = Hz[q];
-    const real idz = a.idd[2][k];
-    {  // Ex
-      const real dy = (hz - Hz[q - sy]) * idy;
-      const real dz = (hy - hy_m) * idz;
-      const real acc = dy + (-dz);
-      const int m = a.mat[0][q];
-      const real e0 = Ex[q];
-      const real cbm = a.cb[m];
-      real e = a.ca[m] * e0 + cbm * acc;
-      if (a.has_cpml) {
-        apply_cpml(e, a.ecorr[0][0], i, j, k, b, dy, cbm, a.pe[1][0], a.pe[1][1], a.pe[1][2]);
-        apply_cpml(e, a.ecorr[0][1], i, j, k, b, dz, cbm, a.pe[2][0], a.pe[2][1], a.pe[2][2]);
-      }
-      if (a.flag[m] == kFlagAde)
-        e = ade_update(e, e0, a, 0, m,
-                       (((long long)b * a.jnk[0] + (k - a.jk0[0])) * a.Y + j) * a.X + i,
-                       (long long)a.B * a.jnk[0] * a.Y * a.X);
-      Ex[q] = e;
-    }
-    {  // Ey
-      const real dz = (hx - hx_m) * idz;
-      const real dx = (hz - Hz[q - 1]) * idx_;
-      const real acc = dz + (-dx);
-      const int m = a.mat[1][q];
-      const real e0 = Ey[q];
-      const real cbm = a.cb[m];
-      real e = a.ca[m] * e0 + cbm * acc;
-      if (a.has_cpml) {
-        apply_cpml(e, a.ecorr[1][0], i, j, k, b, dx, cbm, a.pe[0][0], a.pe[0][1], a.pe[0][2]);
-        apply_cpml(e, a.ecorr[1][1], i, j, k, b, dz, cbm, a.pe[2][0], a.pe[2][1], a.pe[2][2]);
-      }
-      if (a.flag[m] == kFlagAde)
-        e = ade_update(e, e0, a, 1, m,
-                       (((long long)b * a.jnk[1] + (k - a.jk0[1])) * a.Y + j) * a.X + i,
-                       (long long)a.B * a.jnk[1] * a.Y * a.X);
-      Ey[q] = e;
-    }
-    {  // Ez
-      const real dx = (hy - Hy[q - 1]) * idx_;
-      const real dy = (hx - Hx[q - sy]) * idy;
-      const real acc = dx + (-dy);
-      const int m = a.mat[2][q];
-      const real e0 = Ez[q];
-      const real cbm = a.cb[m];
-      real e = a.ca[m] * e0 + cbm * acc;
-      if (a.has_cpml) {
-        apply_cpml(e, a.ecorr[2][0], i, j, k, b, dx, cbm, a.pe[0][0], a.pe[0][1], a.pe[0][2]);
-        apply_cpml(e, a.ecorr[2][1], i, j, k, b, dy, cbm, a.pe[1][0], a.pe[1][1], a.pe[1][2]);
-      }
-      if (a.flag[m] == kFlagAde)
-        e = ade_update(e, e0, a, 2, m,
-                       (((long long)b * a.jnk[2] + (k - a.jk0[2])) * a.Y + j) * a.X + i,
-                       (long long)a.B * a.jnk[2] * a.Y * a.X);
-      Ez[q] = e;
-    }
-    hx_m = hx;
-    hy_m = hy;
-  }
-}
 
 // ----------------------------------------------------------------------------- PMC ghosts
 // h[dst plane] = -h[src plane] over the whole plane (every storage index of the other axes).
@@ -352,11 +156,12 @@ __global__ void __launch_bounds__(128) edge_kernel(const __grid_constant__ EdgeA
       real jt = (real)0;
       for (int p = 0; p < AP; ++p) jt = jt + a.ade_onekp[p] * J[jq + p * jstride];
       jt = (real)0.5 * jt;
-      const real en = val - a.ade_cbe[m] * jt;
+      const real en = val - a.coef[m].cbe * jt;
       const real de = en - a.eold[(long long)b * a.n_def + ds];
       for (int p = 0; p < AP; ++p) {
         const long long qq = jq + p * jstride;
-        J[qq] = a.ade_kp[p] * J[qq] + a.ade_beta[m * AP + p] * de;
+        const real beta = p == 0 ? a.coef[m].beta0 : a.ade_beta[(long long)m * AP + p];
+        J[qq] = a.ade_kp[p] * J[qq] + beta * de;
       }
       val = en;
     }
@@ -414,24 +219,6 @@ __global__ void bump_kernel(long long* step_base, int n) { *step_base += n; }
 
 // ----------------------------------------------------------------------------- launchers
 static inline unsigned ceil_div(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
-
-template <typename real>
-cudaError_t launch_h_sweep(const SweepArgs<real>& a, int tile_y, cudaStream_t s) {
-  const int nkc = (a.nz + 1 + a.tile_z - 1) / a.tile_z;
-  dim3 block(32, tile_y);
-  dim3 grid(ceil_div(a.nx + 2, 32), ceil_div(a.ny + 1, tile_y), nkc * a.B);
-  h_sweep_kernel<real><<<grid, block, 0, s>>>(a);
-  return cudaGetLastError();
-}
-
-template <typename real>
-cudaError_t launch_e_sweep(const SweepArgs<real>& a, int tile_y, cudaStream_t s) {
-  const int nkc = (a.nz + 1 + a.tile_z - 1) / a.tile_z;
-  dim3 block(32, tile_y);
-  dim3 grid(ceil_div(a.nx + 2, 32), ceil_div(a.ny + 1, tile_y), nkc * a.B);
-  e_sweep_kernel<real><<<grid, block, 0, s>>>(a);
-  return cudaGetLastError();
-}
 
 template <typename real>
 cudaError_t launch_ghosts(real* const H[3], int pmc_mask, int nx, int ny, int nz, int X, int Y, int B,
@@ -492,8 +279,6 @@ cudaError_t launch_bump(long long* step_base, int n, cudaStream_t s) {
 }
 
 #define OAFDTD_INSTANTIATE(real)                                                                   \
-  template cudaError_t launch_h_sweep<real>(const SweepArgs<real>&, int, cudaStream_t);            \
-  template cudaError_t launch_e_sweep<real>(const SweepArgs<real>&, int, cudaStream_t);            \
   template cudaError_t launch_ghosts<real>(real* const[3], int, int, int, int, int, int, int,      \
                                            cudaStream_t);                                           \
   template cudaError_t launch_pre_e<real>(const ProbeArgs<real>&, int, cudaStream_t);              \

@@ -5,10 +5,12 @@
 //    x rows are 128-byte aligned (pitch is a multiple of 32 elements).
 //  * mat[c]: uint16 per E edge (Z, Y, X), index into the combined table. The combined table
 //    holds, per entry, the update coefficients ca/cb of the averaged material, its permittivity
-//    (energy) and, for dispersive edges, the Debye ADE coefficients (cbe, beta_p) and flags. It
-//    replaces both the reference's material index and its per-edge ADE arrays, so the E sweep
-//    reads one 2-byte index per edge, shared by every batch member.
-//  * psi: one dense array per CPML correction, (B, nk, nj, ni) over its box.
+//    (energy) and, for dispersive edges, the Debye ADE coefficients (cbe, beta_p). Entries are
+//    ordered plain, dispersive, dispersive-with-injection, so the kind of an edge follows from
+//    its index. It replaces both the reference's material index and its per-edge ADE arrays:
+//    the E sweep reads one 2-byte index per edge, shared by every batch member.
+//  * psi: one array per CPML correction, (B, Z', Y', X') with the slab width along the
+//    derivative axis and the full storage extent along the other two axes.
 //  * J[c]: dense Debye currents (P, B, nzA, Y, X) over the z range that holds dispersive edges.
 //  * edge list (surface impedance, injection, dispersive edges with injection), sorted by
 //    (component, flat index), one thread per edge.
@@ -21,8 +23,6 @@ namespace oafdtd {
 
 constexpr int kChunk = 64;        // steps per captured graph (the reference's CHUNK)
 constexpr int kMaxAdePoles = 16;  // Debye poles handled by the fused sweep
-constexpr uint8_t kFlagAde = 1;   // entry is dispersive
-constexpr uint8_t kFlagDefer = 2; // dispersive edge with injection: ADE applied by the edge pass
 
 template <typename real>
 struct CpmlSide {
@@ -37,19 +37,27 @@ struct CpmlTerm {    // the correction of one (kind, component, derivative axis)
   CpmlSide<real> side[2];
 };
 
+// One entry of the combined material table: update coefficients of the averaged material and,
+// for dispersive entries, the Debye coefficients (cbe, beta of the first pole).
+template <typename real>
+struct __align__(4 * sizeof(real)) Coef {
+  real ca, cb, cbe, beta0;
+};
+
 template <typename real>
 struct SweepArgs {
   real* E[3];
   real* H[3];
   const uint16_t* mat[3];
-  const real* ca;
-  const real* cb;
-  const uint8_t* flag;
-  const real* ade_cbe;      // [entry]
+  const Coef<real>* coef;   // [entry]; entries [ade_lo, ade_hi) are dispersive, then deferred ones
+  int ade_lo, ade_hi;
   const real* ade_beta;     // [entry * P + p]
   const real* ade_kp;       // [p]
   const real* ade_onekp;    // [p]: 1 + kp in the field precision
   int ade_P;
+  const uint8_t* slab_x;    // [storage x]: inside some CPML slab along x
+  const uint8_t* slab_y;
+  const uint8_t* slab_z;
   real* J[3];
   int jk0[3];
   int jnk[3];
@@ -99,8 +107,7 @@ struct EdgeArgs {
   int n_def;
   real* eold;                // (B, n_def)
   const uint16_t* mat[3];
-  const uint8_t* flag;
-  const real* ade_cbe;
+  const Coef<real>* coef;
   const real* ade_beta;
   const real* ade_kp;
   const real* ade_onekp;
