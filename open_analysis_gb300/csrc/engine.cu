@@ -362,6 +362,9 @@ int Engine<real>::build(const oafdtd_problem& p) {
   int last_slot[2][3] = {{-1, -1, -1}, {-1, -1, -1}};
   std::vector<uint8_t> slab[3] = {std::vector<uint8_t>(X, 0), std::vector<uint8_t>(Y, 0),
                                   std::vector<uint8_t>(Z, 0)};
+  std::vector<int8_t> side_map[2][3];
+  for (int kind = 0; kind < 2; ++kind)
+    for (int ax = 0; ax < 3; ++ax) side_map[kind][ax].assign((size_t)len[ax], (int8_t)-1);
   for (int n = 0; n < p.n_corr; ++n) {
     const oafdtd_correction& k = p.corr[n];
     if (k.kind < 0 || k.kind > 1 || k.c < 0 || k.c > 2 || k.a < 0 || k.a > 2 || k.b < 0 || k.b > 2)
@@ -386,7 +389,13 @@ int Engine<real>::build(const oafdtd_problem& p) {
     // psi spans the slab along the derivative axis and the full storage extent on the others
     long long vol = B;
     for (int ax = 0; ax < 3; ++ax) vol *= (ax == k.a) ? (k.hi[ax] - k.lo[ax]) : len[ax];
-    for (int q = k.lo[k.a]; q < k.hi[k.a]; ++q) slab[k.a][q] = 1;
+    for (int q = k.lo[k.a]; q < k.hi[k.a]; ++q) {
+      slab[k.a][q] = 1;
+      int8_t& sm = side_map[k.kind][k.a][q];
+      if (sm >= 0 && sm != side)
+        return fail(OAFDTD_E_INVALID, "CPML sides of one kind disagree on their slab ranges");
+      sm = (int8_t)side;
+    }
     real* psi = nullptr;
     int rc = alloc(&psi, (size_t)vol);
     if (rc) return rc;
@@ -407,6 +416,35 @@ int Engine<real>::build(const oafdtd_problem& p) {
     sw.slab_y = d;
     if ((rc = upload_vec(&d, slab[2]))) return rc;
     sw.slab_z = d;
+    for (int kind = 0; kind < 2; ++kind)
+      for (int ax = 0; ax < 3; ++ax) {
+        int8_t* dsm = nullptr;
+        if ((rc = upload_vec(&dsm, side_map[kind][ax]))) return rc;
+        sw.side[kind][ax] = dsm;
+      }
+    // planes [zi0, zi1) hold no z-slab cell; the z slabs sit at the two ends
+    int zi0 = 1, zi1 = nz + 2;
+    while (zi0 < nz + 2 && slab[2][zi0]) ++zi0;
+    while (zi1 > zi0 && slab[2][zi1 - 1]) --zi1;
+    for (int k = zi0; k < zi1; ++k)
+      if (slab[2][k]) return fail(OAFDTD_E_INVALID, "a z CPML slab lies inside the domain");
+    sw.zi0 = zi0;
+    sw.zi1 = zi1;
+    // quads whose column meets an x or y slab
+    std::vector<int> quads;
+    const int X4 = X / 4;
+    for (int j = 1; j <= ny + 1; ++j)
+      for (int q = 0; q < X4; ++q) {
+        const int i0 = 4 * q;
+        if (i0 > nx + 1) break;
+        bool col = slab[1][j] != 0;
+        for (int e = 0; e < 4; ++e) col = col || slab[0][i0 + e] != 0;
+        if (col) quads.push_back(j * X4 + q);
+      }
+    sw.n_slab_quads = (int)quads.size();
+    int* dq = nullptr;
+    if ((rc = upload_vec(&dq, quads))) return rc;
+    sw.slab_quads = dq;
   }
   sw.dtmu = (real)p.dtmu;
   sw.nx = nx;

@@ -58,6 +58,10 @@ struct SweepArgs {
   const uint8_t* slab_x;    // [storage x]: inside some CPML slab along x
   const uint8_t* slab_y;
   const uint8_t* slab_z;
+  const int8_t* side[2][3]; // [kind 0 E / 1 H][axis][storage index]: CPML side slot or -1
+  int zi0, zi1;             // planes [zi0, zi1) meet no z slab; [1, zi0) and [zi1, nz + 2) do
+  const int* slab_quads;    // quads (flattened y, x/4 index) whose column meets an x or y slab
+  int n_slab_quads;
   real* J[3];
   int jk0[3];
   int jnk[3];

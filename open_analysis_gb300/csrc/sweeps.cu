@@ -1,20 +1,22 @@
 // The two Yee sweeps of a time step, fused with every per-cell correction.
 //
-// Thread mapping: each thread owns four consecutive x cells of one storage row (a 16-byte
-// float4 for float32); the threads of a block cover a contiguous stretch of the flattened
-// (y, x/4) plane, and every thread marches up a chunk of z planes, carrying the neighbouring
-// plane in registers. The x neighbour in the next (H sweep) or previous (E sweep) thread's quad
-// comes from a warp shuffle; a lane whose neighbour lane did not load that plane reads it itself.
+// Thread mapping: each thread owns a "quad", four consecutive x cells of one storage row (a
+// 16-byte float4 for float32), and marches up a chunk of z planes, carrying the neighbouring
+// plane in registers. Quads are numbered over the flattened (y, x/4) plane. The x neighbour in
+// the next (H sweep) or previous (E sweep) quad comes from a warp shuffle when the neighbouring
+// lane holds that quad and loaded the plane; otherwise the lane reads it itself.
 //
-// Every sweep is two launches over the same grid that split the cells between them:
-//  * the bulk launch (SLAB = false) updates the cells outside every CPML slab; it carries no CPML
-//    code, so it runs with few registers and high occupancy;
-//  * the slab launch (SLAB = true) updates the cells whose quad column or plane meets a slab and
-//    applies the corrections cell by cell, in the reference's order (bulk update, then the
-//    corrections by ascending derivative axis, each rounded to the field precision).
+// Every sweep is three launches that split the cells between them, each cell exactly once:
+//  * bulk: planes [zi0, zi1) outside every z slab, quads whose column meets no x or y slab; no
+//    CPML code, few registers, high occupancy;
+//  * slab planes: every quad of the z-slab planes, CPML applied;
+//  * slab columns: the quads whose column meets an x or y slab (a short list), planes
+//    [zi0, zi1), CPML applied.
 // Cells are independent within a sweep (H reads only E, E reads only H), so the split changes no
-// value. Material coefficients come from a packed table (ca, cb, cbe, beta_0) indexed by the
-// 16-bit combined index; entries [ade_lo, ade_hi) are dispersive, so no flag lookup is needed.
+// value. The CPML corrections follow the reference's order: bulk update, then the corrections
+// by ascending derivative axis, each rounded to the field precision. Material coefficients come
+// from a packed table (ca, cb, cbe, beta_0) indexed by the 16-bit combined index; entries
+// [ade_lo, ade_hi) are dispersive, so no flag lookup is needed.
 //
 // The library is compiled with -fmad=false: every product and sum is rounded separately, as in
 // the NumPy reference (packages/oa-fdtd/src/oa_fdtd/reference.py:152-207, :119-127).
@@ -54,36 +56,69 @@ __device__ __forceinline__ Quad<real> zero4() {
   return Quad<real>{{(real)0, (real)0, (real)0, (real)0}};
 }
 
-// One CPML correction on one cell: psi <- b psi + c d; f += (sign k) (ek d + psi).
-template <typename real>
-__device__ __noinline__ void cpml_cell(real& f, const CpmlTerm<real>& t, int i, int j, int k, int b,
-                                       real d, real kfac, const real* cb_, const real* cc_,
-                                       const real* ck_, int X, int Y, int Z) {
+enum : int { kBulk = 0, kSlabPlanes = 1, kSlabColumns = 2 };
+
+// The CPML corrections of one component on one quad: for each derivative axis (ascending) whose
+// slab holds the cell, psi <- b psi + c d; f += (sign k) (ek d + psi). Slabs along y and z hold
+// whole quads, so their psi moves as one vector; x slabs are handled cell by cell.
+template <typename real, int KIND>
+__device__ __forceinline__ void cpml_quad(const SweepArgs<real>& a, const CpmlTerm<real> (&terms)[2],
+                                          const real* const (&co)[3][3], Quad<real>& f, const real (&d0)[4],
+                                          const real (&d1)[4], const real (&kfac)[4], const bool (&valid)[4],
+                                          int i0, int j, int k, int b) {
+  const int X = a.X, Y = a.Y, Z = a.nz + 2;
 #pragma unroll
-  for (int s = 0; s < 2; ++s) {
-    const CpmlSide<real>& sd = t.side[s];
-    if (sd.psi == nullptr) continue;
-    if (i < sd.lo[0] || i >= sd.hi[0] || j < sd.lo[1] || j >= sd.hi[1] || k < sd.lo[2] || k >= sd.hi[2])
-      continue;
-    // psi covers the slab along the derivative axis and the full storage extent on the others
-    long long q;
-    if (t.axis == 0) {
-      const int w = sd.hi[0] - sd.lo[0];
-      q = (((long long)b * Z + k) * Y + j) * w + (i - sd.lo[0]);
-    } else if (t.axis == 1) {
-      const int w = sd.hi[1] - sd.lo[1];
-      q = (((long long)b * Z + k) * w + (j - sd.lo[1])) * X + i;
+  for (int t = 0; t < 2; ++t) {
+    const CpmlTerm<real>& T = terms[t];
+    if (T.side[0].psi == nullptr) continue;
+    const int ax = T.axis;
+    const real* cb_ = co[ax][0];
+    const real* cc_ = co[ax][1];
+    const real* ck_ = co[ax][2];
+    if (ax == 0) {
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int i = i0 + e;
+        const int s = a.side[KIND][0][i];
+        if (!valid[e] || s < 0) continue;
+        const CpmlSide<real>& S = T.side[s];
+        if (j < S.lo[1] || j >= S.hi[1] || k < S.lo[2] || k >= S.hi[2] || i < S.lo[0] || i >= S.hi[0]) continue;
+        const int w = S.hi[0] - S.lo[0];
+        const long long q = (((long long)b * Z + k) * Y + j) * w + (i - S.lo[0]);
+        const real d = t == 0 ? d0[e] : d1[e];
+        real ps = S.psi[q];
+        ps = ps * cb_[i];
+        ps = ps + cc_[i] * d;
+        S.psi[q] = ps;
+        const real upd = ck_[i] * d + ps;
+        f.v[e] = f.v[e] + (T.sign * kfac[e]) * upd;
+      }
     } else {
-      const int w = sd.hi[2] - sd.lo[2];
-      q = (((long long)b * w + (k - sd.lo[2])) * Y + j) * X + i;
+      const int ia = ax == 1 ? j : k;
+      const int s = a.side[KIND][ax][ia];
+      if (s < 0) continue;
+      const CpmlSide<real>& S = T.side[s];
+      const int other = ax == 1 ? k : j;
+      const int oax = ax == 1 ? 2 : 1;
+      if (other < S.lo[oax] || other >= S.hi[oax] || ia < S.lo[ax] || ia >= S.hi[ax]) continue;
+      const int w = S.hi[ax] - S.lo[ax];
+      const long long q0 = ax == 1 ? (((long long)b * Z + k) * w + (j - S.lo[1])) * X + i0
+                                   : (((long long)b * w + (k - S.lo[2])) * Y + j) * X + i0;
+      Quad<real> ps4 = ld4(S.psi + q0);
+      const real pb = cb_[ia], pc = cc_[ia], pk = ck_[ia];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int i = i0 + e;
+        if (!valid[e] || i < S.lo[0] || i >= S.hi[0]) continue;
+        const real d = t == 0 ? d0[e] : d1[e];
+        real ps = ps4.v[e] * pb;
+        ps = ps + pc * d;
+        ps4.v[e] = ps;
+        const real upd = pk * d + ps;
+        f.v[e] = f.v[e] + (T.sign * kfac[e]) * upd;
+      }
+      st4(S.psi + q0, ps4);
     }
-    const int ia = t.axis == 0 ? i : (t.axis == 1 ? j : k);
-    real ps = sd.psi[q];
-    ps = ps * cb_[ia];
-    ps = ps + cc_[ia] * d;
-    sd.psi[q] = ps;
-    const real upd = ck_[ia] * d + ps;
-    f = f + (t.sign * kfac) * upd;
   }
 }
 
@@ -106,51 +141,66 @@ __device__ __noinline__ real ade_cell(real e, real e0, real cbe, real beta0, int
   return en;
 }
 
-struct QuadPos {
+// Where a launch's thread works: its quad and its plane range.
+struct Work {
+  int t;        // quad index in the flattened (y, x/4) plane
   int j, i0;
-  bool live, row_end;
+  bool live;    // the quad holds real edges and belongs to this launch
+  bool row_end;
+  int k0, k1;
 };
 
-__device__ __forceinline__ QuadPos quad_pos(int X, int Y, int nx, int ny) {
-  const int X4 = X >> 2;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int tt = min(t, Y * X4 - 1);
-  QuadPos q;
-  q.j = tt / X4;
-  q.i0 = (tt - q.j * X4) * 4;
-  q.live = t < Y * X4 && q.j >= 1 && q.j <= ny + 1 && q.i0 <= nx + 1;
-  q.row_end = q.i0 + 4 >= X;
-  return q;
-}
-
-template <typename real>
-__device__ __forceinline__ bool column_in_slab(const SweepArgs<real>& a, const QuadPos& q) {
-  if (!a.has_cpml) return false;
-  bool s = a.slab_y[q.j] != 0;
+template <typename real, int MODE>
+__device__ __forceinline__ Work work_of(const SweepArgs<real>& a) {
+  const int X = a.X, Y = a.Y, X4 = X >> 2, nx = a.nx, ny = a.ny, nz = a.nz;
+  const int tz = a.tile_z;
+  Work w;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  bool in_launch;
+  if (MODE == kSlabColumns) {
+    in_launch = g < a.n_slab_quads;
+    w.t = a.slab_quads[min(g, a.n_slab_quads - 1)];
+  } else {
+    in_launch = g < Y * X4;
+    w.t = min(g, Y * X4 - 1);
+  }
+  w.j = w.t / X4;
+  w.i0 = (w.t - w.j * X4) * 4;
+  w.row_end = w.i0 + 4 >= X;
+  bool live = in_launch && w.j >= 1 && w.j <= ny + 1 && w.i0 <= nx + 1;
+  if (MODE == kBulk && live && a.has_cpml) {
+    bool col = a.slab_y[w.j] != 0;
 #pragma unroll
-  for (int e = 0; e < 4; ++e) s |= a.slab_x[q.i0 + e] != 0;
-  return s;
+    for (int e = 0; e < 4; ++e) col |= a.slab_x[w.i0 + e] != 0;
+    live = !col;
+  }
+  w.live = live;
+  if (MODE == kSlabPlanes) {
+    const int na = (a.zi0 - 1 + tz - 1) / tz;  // chunks of [1, zi0)
+    const int c = blockIdx.y;
+    if (c < na) {
+      w.k0 = 1 + c * tz;
+      w.k1 = min(w.k0 + tz, a.zi0);
+    } else {
+      w.k0 = a.zi1 + (c - na) * tz;
+      w.k1 = min(w.k0 + tz, nz + 2);
+    }
+  } else {
+    w.k0 = a.zi0 + blockIdx.y * tz;
+    w.k1 = min(w.k0 + tz, a.zi1);
+  }
+  return w;
 }
 
 // ------------------------------------------------------------------------------------- H sweep
-// Minimum resident blocks per SM of the bulk launches: caps their registers so that enough warps
-// are resident to keep HBM busy; the slab launches are left unconstrained.
-template <typename real, bool SLAB>
-struct Occupancy {
-  static constexpr int h = SLAB ? 1 : 4;
-  static constexpr int e = SLAB ? 1 : 3;
-};
-
-template <typename real, bool SLAB>
-__global__ void __launch_bounds__(256, Occupancy<real, SLAB>::h) h_sweep_kernel(const __grid_constant__ SweepArgs<real> a) {
-  const int X = a.X, Y = a.Y, Z = a.nz + 2;
-  const int nx = a.nx, ny = a.ny, nz = a.nz;
-  const QuadPos qp = quad_pos(X, Y, nx, ny);
-  const int j = qp.j, i0 = qp.i0;
+template <typename real, int MODE>
+__global__ void __launch_bounds__(256, MODE == kBulk ? 4 : 2) h_sweep_kernel(const __grid_constant__ SweepArgs<real> a) {
+  constexpr bool SLAB = MODE != kBulk;
+  const Work w = work_of<real, MODE>(a);
+  const int X = a.X, Y = a.Y, nx = a.nx, ny = a.ny, nz = a.nz;
+  const int j = w.j, i0 = w.i0;
   const int b = blockIdx.z;
   const int lane = threadIdx.x & 31;
-  const int k0 = 1 + blockIdx.y * a.tile_z;
-  const int k1 = min(k0 + a.tile_z, nz + 2);
   const long long bs = a.bs;
   const real* __restrict__ Ex = a.E[0] + b * bs;
   const real* __restrict__ Ey = a.E[1] + b * bs;
@@ -162,22 +212,21 @@ __global__ void __launch_bounds__(256, Occupancy<real, SLAB>::h) h_sweep_kernel(
   const Quad<real> ipx = ld4(a.ip[0] + i0);
   const real ipy = a.ip[1][j];
   const real dtmu = a.dtmu;
-  const bool col = column_in_slab(a, qp);
   const long long sz = (long long)X * Y;
-  long long p = (long long)k0 * sz + (long long)j * X + i0;
+  const bool nb_quad = __shfl_down_sync(0xffffffffu, w.t, 1) == w.t + 1 && lane < 31;
+  const unsigned who = __ballot_sync(0xffffffffu, w.live);
+  const bool nb = nb_quad && ((who >> (lane + 1)) & 1u);
+  long long p = (long long)w.k0 * sz + (long long)j * X + i0;
   Quad<real> ex = zero4<real>(), ey = zero4<real>();
-  bool carried = false;
-  for (int k = k0; k < k1; ++k, p += sz) {
-    const bool in_slab = col || (a.has_cpml && a.slab_z[k] != 0);
-    const bool proc = qp.live && (in_slab == SLAB);
-    const unsigned who = __ballot_sync(0xffffffffu, proc);
+  if (w.live && w.k0 < w.k1) {
+    ex = ld4(Ex + p);
+    ey = ld4(Ey + p);
+  }
+  const real kd[4] = {dtmu, dtmu, dtmu, dtmu};
+  for (int k = w.k0; k < w.k1; ++k, p += sz) {
     const bool kin = k <= nz;
     Quad<real> ex1 = zero4<real>(), ey1 = zero4<real>(), ez = zero4<real>();
-    if (proc) {
-      if (!carried) {
-        ex = ld4(Ex + p);
-        ey = ld4(Ey + p);
-      }
+    if (w.live) {
       if (kin) {
         ex1 = ld4(Ex + p + sz);
         ey1 = ld4(Ey + p + sz);
@@ -187,12 +236,8 @@ __global__ void __launch_bounds__(256, Occupancy<real, SLAB>::h) h_sweep_kernel(
     // x + 1 neighbours of element 3 (every lane takes part in the shuffles)
     real ez_r = __shfl_down_sync(0xffffffffu, ez.v[0], 1);
     real ey_r = __shfl_down_sync(0xffffffffu, ey.v[0], 1);
-    if (!proc) {
-      carried = false;
-      continue;
-    }
-    const bool nb = lane < 31 && ((who >> (lane + 1)) & 1u);
-    if (!nb && !qp.row_end) {
+    if (!w.live) continue;
+    if (!nb && !w.row_end) {
       ez_r = Ez[p + 4];
       ey_r = Ey[p + 4];
     }
@@ -200,98 +245,87 @@ __global__ void __launch_bounds__(256, Occupancy<real, SLAB>::h) h_sweep_kernel(
     if (j <= ny && kin) {  // Hx: node along x (1..nx+1), cell along y and z
       const Quad<real> ezy = ld4(Ez + p + sy1);
       Quad<real> h = ld4(Hx + p);
+      real d0[4], d1[4];
+      bool valid[4];
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const int i = i0 + e;
-        if (i < 1 || i > nx + 1) continue;
-        const real dy = (ezy.v[e] - ez.v[e]) * ipy;
-        const real dz = (ey1.v[e] - ey.v[e]) * ipz;
-        const real acc = (-dy) + dz;
-        real hv = h.v[e] + dtmu * acc;
-        if (SLAB) {
-          cpml_cell(hv, a.hcorr[0][0], i, j, k, b, dy, dtmu, a.ph[1][0], a.ph[1][1], a.ph[1][2], X, Y, Z);
-          cpml_cell(hv, a.hcorr[0][1], i, j, k, b, dz, dtmu, a.ph[2][0], a.ph[2][1], a.ph[2][2], X, Y, Z);
-        }
-        h.v[e] = hv;
+        valid[e] = i >= 1 && i <= nx + 1;
+        d0[e] = (ezy.v[e] - ez.v[e]) * ipy;   // axis y
+        d1[e] = (ey1.v[e] - ey.v[e]) * ipz;   // axis z
+        const real acc = (-d0[e]) + d1[e];
+        if (valid[e]) h.v[e] = h.v[e] + dtmu * acc;
       }
+      if (SLAB) cpml_quad<real, 1>(a, a.hcorr[0], a.ph, h, d0, d1, kd, valid, i0, j, k, b);
       st4(Hx + p, h);
     }
     if (kin) {  // Hy: cell along x (1..nx), node along y (1..ny+1), cell along z
       Quad<real> h = ld4(Hy + p);
+      real d0[4], d1[4];
+      bool valid[4];
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const int i = i0 + e;
-        if (i < 1 || i > nx) continue;
+        valid[e] = i >= 1 && i <= nx;
         const real ezr = e < 3 ? ez.v[e + 1] : ez_r;
-        const real dz = (ex1.v[e] - ex.v[e]) * ipz;
-        const real dx = (ezr - ez.v[e]) * ipx.v[e];
-        const real acc = (-dz) + dx;
-        real hv = h.v[e] + dtmu * acc;
-        if (SLAB) {
-          cpml_cell(hv, a.hcorr[1][0], i, j, k, b, dx, dtmu, a.ph[0][0], a.ph[0][1], a.ph[0][2], X, Y, Z);
-          cpml_cell(hv, a.hcorr[1][1], i, j, k, b, dz, dtmu, a.ph[2][0], a.ph[2][1], a.ph[2][2], X, Y, Z);
-        }
-        h.v[e] = hv;
+        d0[e] = (ezr - ez.v[e]) * ipx.v[e];   // axis x
+        d1[e] = (ex1.v[e] - ex.v[e]) * ipz;   // axis z
+        const real acc = (-d1[e]) + d0[e];
+        if (valid[e]) h.v[e] = h.v[e] + dtmu * acc;
       }
+      if (SLAB) cpml_quad<real, 1>(a, a.hcorr[1], a.ph, h, d0, d1, kd, valid, i0, j, k, b);
       st4(Hy + p, h);
     }
     if (j <= ny) {  // Hz: cell along x and y, node along z (1..nz+1)
       const Quad<real> exy = ld4(Ex + p + sy1);
       Quad<real> h = ld4(Hz + p);
+      real d0[4], d1[4];
+      bool valid[4];
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const int i = i0 + e;
-        if (i < 1 || i > nx) continue;
+        valid[e] = i >= 1 && i <= nx;
         const real eyr = e < 3 ? ey.v[e + 1] : ey_r;
-        const real dx = (eyr - ey.v[e]) * ipx.v[e];
-        const real dy = (exy.v[e] - ex.v[e]) * ipy;
-        const real acc = (-dx) + dy;
-        real hv = h.v[e] + dtmu * acc;
-        if (SLAB) {
-          cpml_cell(hv, a.hcorr[2][0], i, j, k, b, dx, dtmu, a.ph[0][0], a.ph[0][1], a.ph[0][2], X, Y, Z);
-          cpml_cell(hv, a.hcorr[2][1], i, j, k, b, dy, dtmu, a.ph[1][0], a.ph[1][1], a.ph[1][2], X, Y, Z);
-        }
-        h.v[e] = hv;
+        d0[e] = (eyr - ey.v[e]) * ipx.v[e];   // axis x
+        d1[e] = (exy.v[e] - ex.v[e]) * ipy;   // axis y
+        const real acc = (-d0[e]) + d1[e];
+        if (valid[e]) h.v[e] = h.v[e] + dtmu * acc;
       }
+      if (SLAB) cpml_quad<real, 1>(a, a.hcorr[2], a.ph, h, d0, d1, kd, valid, i0, j, k, b);
       st4(Hz + p, h);
     }
     ex = ex1;
     ey = ey1;
-    carried = kin;
   }
 }
 
 // ------------------------------------------------------------------------------------- E sweep
-// Bulk update, CPML (slab launch) and the Debye update of one E component on one quad.
+// Bulk update, CPML (slab launches) and the Debye update of one E component on one quad.
+// d0/d1 are the derivatives along the component's two axes in ascending order; the bulk term
+// order of the reference is (d0, -d1) when first_plus, else (d1, -d0).
 template <typename real, bool SLAB>
 __device__ __forceinline__ void e_quad(const SweepArgs<real>& a, int c, real* __restrict__ E, long long p,
                                        const Quad<uint16_t>& m, const real (&d0)[4], const real (&d1)[4],
                                        bool first_plus, int i0, int j, int k, int b) {
-  const int X = a.X, Y = a.Y, Z = a.nz + 2, nx = a.nx;
+  const int X = a.X, Y = a.Y, nx = a.nx;
   const Coef<real>* __restrict__ tab = a.coef;
   Quad<real> e4 = ld4(E + p);
   const Quad<real> e0 = e4;
   Coef<real> cf[4];
+  real kf[4];
+  bool valid[4];
   bool disp = false;
 #pragma unroll
   for (int e = 0; e < 4; ++e) {
     const int i = i0 + e;
     cf[e] = tab[m.v[e]];
-    if (i < 1 || i > nx + 1) continue;
-    // acc = d0 + (-d1) with the terms in the reference's table order for this component
+    kf[e] = cf[e].cb;
+    valid[e] = i >= 1 && i <= nx + 1;
     const real acc = first_plus ? d0[e] + (-d1[e]) : d1[e] + (-d0[e]);
-    real ev = cf[e].ca * e4.v[e] + cf[e].cb * acc;
-    if (SLAB) {
-      const CpmlTerm<real>& t0 = a.ecorr[c][0];
-      const CpmlTerm<real>& t1 = a.ecorr[c][1];
-      cpml_cell(ev, t0, i, j, k, b, d0[e], cf[e].cb, a.pe[t0.axis][0], a.pe[t0.axis][1], a.pe[t0.axis][2], X,
-                Y, Z);
-      cpml_cell(ev, t1, i, j, k, b, d1[e], cf[e].cb, a.pe[t1.axis][0], a.pe[t1.axis][1], a.pe[t1.axis][2], X,
-                Y, Z);
-    }
-    e4.v[e] = ev;
-    disp |= m.v[e] >= a.ade_lo && m.v[e] < a.ade_hi;
+    if (valid[e]) e4.v[e] = cf[e].ca * e4.v[e] + cf[e].cb * acc;
+    disp |= valid[e] && m.v[e] >= a.ade_lo && m.v[e] < a.ade_hi;
   }
+  if (SLAB) cpml_quad<real, 0>(a, a.ecorr[c], a.pe, e4, d0, d1, kf, valid, i0, j, k, b);
   if (disp) {
     const long long jstride = (long long)a.B * a.jnk[c] * Y * X;
     const long long jq = (((long long)b * a.jnk[c] + (k - a.jk0[c])) * Y + j) * X + i0;
@@ -301,7 +335,7 @@ __device__ __forceinline__ void e_quad(const SweepArgs<real>& a, int c, real* __
       const real onekp = a.ade_onekp[0], kp = a.ade_kp[0];
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
-        if (!(m.v[e] >= a.ade_lo && m.v[e] < a.ade_hi)) continue;
+        if (!(valid[e] && m.v[e] >= a.ade_lo && m.v[e] < a.ade_hi)) continue;
         const real jt = (real)0.5 * (onekp * j4.v[e]);
         const real en = e4.v[e] - cf[e].cbe * jt;
         const real de = en - e0.v[e];
@@ -312,7 +346,7 @@ __device__ __forceinline__ void e_quad(const SweepArgs<real>& a, int c, real* __
     } else {
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
-        if (!(m.v[e] >= a.ade_lo && m.v[e] < a.ade_hi)) continue;
+        if (!(valid[e] && m.v[e] >= a.ade_lo && m.v[e] < a.ade_hi)) continue;
         e4.v[e] = ade_cell(e4.v[e], e0.v[e], cf[e].cbe, cf[e].beta0, m.v[e], J, jq + e, jstride, a.ade_kp,
                            a.ade_onekp, a.ade_beta, a.ade_P);
       }
@@ -321,37 +355,33 @@ __device__ __forceinline__ void e_quad(const SweepArgs<real>& a, int c, real* __
   st4(E + p, e4);
 }
 
-template <typename real, bool SLAB>
-__global__ void __launch_bounds__(256, Occupancy<real, SLAB>::e) e_sweep_kernel(const __grid_constant__ SweepArgs<real> a) {
+template <typename real, int MODE>
+__global__ void __launch_bounds__(256, MODE == kBulk ? 3 : 2) e_sweep_kernel(const __grid_constant__ SweepArgs<real> a) {
+  constexpr bool SLAB = MODE != kBulk;
+  const Work w = work_of<real, MODE>(a);
   const int X = a.X, Y = a.Y;
-  const int nx = a.nx, ny = a.ny, nz = a.nz;
-  const QuadPos qp = quad_pos(X, Y, nx, ny);
-  const int j = qp.j, i0 = qp.i0;
+  const int j = w.j, i0 = w.i0;
   const int b = blockIdx.z;
   const int lane = threadIdx.x & 31;
-  const int k0 = 1 + blockIdx.y * a.tile_z;
-  const int k1 = min(k0 + a.tile_z, nz + 2);
   const long long bs = a.bs;
   const real* __restrict__ Hx = a.H[0] + b * bs;
   const real* __restrict__ Hy = a.H[1] + b * bs;
   const real* __restrict__ Hz = a.H[2] + b * bs;
   const Quad<real> idx4 = ld4(a.idd[0] + i0);
   const real idy = a.idd[1][j];
-  const bool col = column_in_slab(a, qp);
   const long long sz = (long long)X * Y;
-  long long p = (long long)k0 * sz + (long long)j * X + i0;  // batch-free index of the quad
+  const bool nb_quad = __shfl_up_sync(0xffffffffu, w.t, 1) == w.t - 1 && lane > 0;
+  const unsigned who = __ballot_sync(0xffffffffu, w.live);
+  const bool nb = nb_quad && ((who >> (lane - 1)) & 1u);
+  long long p = (long long)w.k0 * sz + (long long)j * X + i0;  // batch-free index of the quad
   Quad<real> hx_m = zero4<real>(), hy_m = zero4<real>();
-  bool carried = false;
-  for (int k = k0; k < k1; ++k, p += sz) {
-    const bool in_slab = col || (a.has_cpml && a.slab_z[k] != 0);
-    const bool proc = qp.live && (in_slab == SLAB);
-    const unsigned who = __ballot_sync(0xffffffffu, proc);
+  if (w.live && w.k0 < w.k1) {
+    hx_m = ld4(Hx + p - sz);
+    hy_m = ld4(Hy + p - sz);
+  }
+  for (int k = w.k0; k < w.k1; ++k, p += sz) {
     Quad<real> hx = zero4<real>(), hy = zero4<real>(), hz = zero4<real>();
-    if (proc) {
-      if (!carried) {
-        hx_m = ld4(Hx + p - sz);
-        hy_m = ld4(Hy + p - sz);
-      }
+    if (w.live) {
       hx = ld4(Hx + p);
       hy = ld4(Hy + p);
       hz = ld4(Hz + p);
@@ -359,11 +389,7 @@ __global__ void __launch_bounds__(256, Occupancy<real, SLAB>::e) e_sweep_kernel(
     // x - 1 neighbours of element 0
     real hz_l = __shfl_up_sync(0xffffffffu, hz.v[3], 1);
     real hy_l = __shfl_up_sync(0xffffffffu, hy.v[3], 1);
-    if (!proc) {
-      carried = false;
-      continue;
-    }
-    const bool nb = lane > 0 && ((who >> (lane - 1)) & 1u);
+    if (!w.live) continue;
     if (!nb && i0 > 0) {
       hz_l = Hz[p - 1];
       hy_l = Hy[p - 1];
@@ -378,7 +404,7 @@ __global__ void __launch_bounds__(256, Occupancy<real, SLAB>::e) e_sweep_kernel(
       d1[e] = (hy.v[e] - hy_m.v[e]) * idz;
     }
     e_quad<real, SLAB>(a, 0, a.E[0] + b * bs, p, ld4(a.mat[0] + p), d0, d1, true, i0, j, k, b);
-    // Ey: terms (a = z, +Hx) then (a = x, -Hz); ascending axes: d0 = x term, d1 = z term
+    // Ey: terms (a = z, +Hx) then (a = x, -Hz); d0 is the x term, d1 the z term
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       const real hzl = e > 0 ? hz.v[e - 1] : hz_l;
@@ -396,35 +422,58 @@ __global__ void __launch_bounds__(256, Occupancy<real, SLAB>::e) e_sweep_kernel(
     e_quad<real, SLAB>(a, 2, a.E[2] + b * bs, p, ld4(a.mat[2] + p), d0, d1, true, i0, j, k, b);
     hx_m = hx;
     hy_m = hy;
-    carried = true;
   }
 }
 
 // ------------------------------------------------------------------------------------- launchers
 template <typename real>
+static cudaError_t launch_modes(const SweepArgs<real>& a, cudaStream_t s, bool h) {
+  const int tz = a.tile_z;
+  const long long quads = (long long)a.Y * (a.X / 4);
+  const int inner = a.zi1 - a.zi0;
+  const int bx = (int)((quads + 255) / 256);
+  if (inner > 0) {
+    dim3 grid(bx, (inner + tz - 1) / tz, a.B);
+    if (h)
+      h_sweep_kernel<real, kBulk><<<grid, 256, 0, s>>>(a);
+    else
+      e_sweep_kernel<real, kBulk><<<grid, 256, 0, s>>>(a);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+  }
+  if (!a.has_cpml) return cudaSuccess;
+  const int na = (a.zi0 - 1 + tz - 1) / tz, nb = (a.nz + 2 - a.zi1 + tz - 1) / tz;
+  if (na + nb > 0) {
+    dim3 grid(bx, na + nb, a.B);
+    if (h)
+      h_sweep_kernel<real, kSlabPlanes><<<grid, 256, 0, s>>>(a);
+    else
+      e_sweep_kernel<real, kSlabPlanes><<<grid, 256, 0, s>>>(a);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+  }
+  if (a.n_slab_quads > 0 && inner > 0) {
+    dim3 grid((a.n_slab_quads + 255) / 256, (inner + tz - 1) / tz, a.B);
+    if (h)
+      h_sweep_kernel<real, kSlabColumns><<<grid, 256, 0, s>>>(a);
+    else
+      e_sweep_kernel<real, kSlabColumns><<<grid, 256, 0, s>>>(a);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+  }
+  return cudaSuccess;
+}
+
+template <typename real>
 cudaError_t launch_h_sweep(const SweepArgs<real>& a, int tile_y, cudaStream_t s) {
   (void)tile_y;
-  const int nkc = (a.nz + 1 + a.tile_z - 1) / a.tile_z;
-  const long long quads = (long long)a.Y * (a.X / 4);
-  dim3 grid((unsigned)((quads + 255) / 256), nkc, a.B);
-  h_sweep_kernel<real, false><<<grid, 256, 0, s>>>(a);
-  cudaError_t err = cudaGetLastError();
-  if (err != cudaSuccess || !a.has_cpml) return err;
-  h_sweep_kernel<real, true><<<grid, 256, 0, s>>>(a);
-  return cudaGetLastError();
+  return launch_modes<real>(a, s, true);
 }
 
 template <typename real>
 cudaError_t launch_e_sweep(const SweepArgs<real>& a, int tile_y, cudaStream_t s) {
   (void)tile_y;
-  const int nkc = (a.nz + 1 + a.tile_z - 1) / a.tile_z;
-  const long long quads = (long long)a.Y * (a.X / 4);
-  dim3 grid((unsigned)((quads + 255) / 256), nkc, a.B);
-  e_sweep_kernel<real, false><<<grid, 256, 0, s>>>(a);
-  cudaError_t err = cudaGetLastError();
-  if (err != cudaSuccess || !a.has_cpml) return err;
-  e_sweep_kernel<real, true><<<grid, 256, 0, s>>>(a);
-  return cudaGetLastError();
+  return launch_modes<real>(a, s, false);
 }
 
 template cudaError_t launch_h_sweep<float>(const SweepArgs<float>&, int, cudaStream_t);
