@@ -183,9 +183,9 @@ int oafdtd_peak_bytes(const oafdtd_engine* engine, int64_t* out);
  * and replay it (the reference's use_graph flag, engine.py:80,425-429). */
 int oafdtd_set_graph(oafdtd_engine* engine, int32_t use_graph);
 
-/* Kernel launch shape: block rows (y extent of a sweep tile) and z planes marched per tile.
- * 0 keeps the current value. The tile shapes of the autotuner are set through this. */
-int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_y, int32_t tile_z);
+/* Launch shape of the sweeps: z planes marched per thread in the bulk launch (tile_z) and in the
+ * CPML slab launches (tile_z_slab); 0 keeps the current value. The autotuner sets these. */
+int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_z, int32_t tile_z_slab);
 
 /* Average device time per step of each kernel class over the last oafdtd_step call, measured
  * with CUDA events when profiling is on (oafdtd_set_profiling). Writes up to n values in the

@@ -54,8 +54,8 @@ struct EngineBase {
   int64_t bytes = 0;
   int use_graph = 1;
   int profiling = 0;
-  int tile_y = 8;
   int tile_z = 16;
+  int tile_z_slab = 4;
   bool graph_dirty = false;  // launch shape or profiling changed: the graph is re-captured
   double model_bytes = 0.0;
 };
@@ -64,6 +64,7 @@ template <typename real>
 struct Engine final : EngineBase {
   int device = 0;
   cudaStream_t stream = nullptr;
+  oafdtd::SweepStreams streams{};
   std::vector<void*> allocs;
   int nx = 0, ny = 0, nz = 0, X = 0, Y = 0, Z = 0, B = 0;
   long long bs = 0;
@@ -90,6 +91,9 @@ struct Engine final : EngineBase {
     if (t_start) cudaEventDestroy(t_start);
     if (t_stop) cudaEventDestroy(t_stop);
     for (void* p : allocs) cudaFree(p);
+    if (streams.fork) cudaEventDestroy(streams.fork);
+    if (streams.join) cudaEventDestroy(streams.join);
+    if (streams.side) cudaStreamDestroy(streams.side);
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -166,6 +170,10 @@ int Engine<real>::build(const oafdtd_problem& p) {
     return fail(OAFDTD_E_INVALID, "at most 16 Debye poles are supported");
   OA_CUDA(cudaGetDevice(&device));
   OA_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  OA_CUDA(cudaStreamCreateWithFlags(&streams.side, cudaStreamNonBlocking));
+  OA_CUDA(cudaEventCreateWithFlags(&streams.fork, cudaEventDisableTiming));
+  OA_CUDA(cudaEventCreateWithFlags(&streams.join, cudaEventDisableTiming));
+  streams.main = stream;
 
   auto in_range = [&](long long f) { return f >= 0 && f < bs; };
 
@@ -455,6 +463,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
   sw.bs = bs;
   sw.B = B;
   sw.tile_z = tile_z;
+  sw.tile_z_slab = tile_z_slab;
 
   // ---- edge list: surface impedance, injection targets, deferred ADE edges
   struct EdgeRec {
@@ -735,7 +744,7 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing) {
   // inside a stream capture an event record becomes a graph node only with the external flag
   const unsigned rec = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[0], stream, rec));
-  err = oafdtd::launch_h_sweep<real>(sw, tile_y, stream);
+  err = oafdtd::launch_h_sweep<real>(sw, streams);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("h_sweep: ") + cudaGetErrorString(err));
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[1], stream, rec));
   if (pmc_mask) {
@@ -746,7 +755,7 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing) {
   err = oafdtd::launch_pre_e<real>(pr, off, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("pre_e: ") + cudaGetErrorString(err));
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[3], stream, rec));
-  err = oafdtd::launch_e_sweep<real>(sw, tile_y, stream);
+  err = oafdtd::launch_e_sweep<real>(sw, streams);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("e_sweep: ") + cudaGetErrorString(err));
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[4], stream, rec));
   err = oafdtd::launch_edges<real>(ed, off, stream);
@@ -802,6 +811,7 @@ int Engine<real>::step(int64_t n) {
     graph_ready = false;
   }
   sw.tile_z = tile_z;
+  sw.tile_z_slab = tile_z_slab;
   if (profiling) {
     for (double& v : prof_ms) v = 0.0;
     prof_steps = 0;
@@ -1055,12 +1065,12 @@ int oafdtd_set_graph(oafdtd_engine* engine, int32_t use_graph) {
   return OAFDTD_OK;
 }
 
-int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_y, int32_t tile_z) {
+int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_z, int32_t tile_z_slab) {
   if (!engine) return fail(OAFDTD_E_INVALID, "null engine");
-  if (tile_y < 0 || tile_z < 0) return fail(OAFDTD_E_INVALID, "negative tile size");
-  if (tile_y && (tile_y > 32 || 32 * tile_y > 256)) return fail(OAFDTD_E_INVALID, "tile_y must be 1..8");
-  if (tile_y) engine->impl->tile_y = tile_y;
+  if (tile_z < 0 || tile_z_slab < 0 || tile_z > 4096 || tile_z_slab > 4096)
+    return fail(OAFDTD_E_INVALID, "tile sizes must be 0..4096 planes");
   if (tile_z) engine->impl->tile_z = tile_z;
+  if (tile_z_slab) engine->impl->tile_z_slab = tile_z_slab;
   engine->impl->graph_dirty = true;  // a new launch shape needs a new graph
   return OAFDTD_OK;
 }

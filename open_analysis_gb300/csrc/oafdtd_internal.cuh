@@ -76,7 +76,17 @@ struct SweepArgs {
   int nx, ny, nz, X, Y;
   long long bs;             // Z * Y * X
   int B;
-  int tile_z;
+  int tile_z;       // planes per thread in the bulk launch
+  int tile_z_slab;  // planes per thread in the slab launches (fewer: more blocks)
+};
+
+// Streams of one sweep: the bulk launch runs on `main`, the slab launches on `side`, forked and
+// joined with the two events (inside a captured graph this becomes two parallel branches).
+struct SweepStreams {
+  cudaStream_t main;
+  cudaStream_t side;
+  cudaEvent_t fork;
+  cudaEvent_t join;
 };
 
 template <typename real>
@@ -165,9 +175,9 @@ struct EnergyArgs {
 
 // kernel launchers (kernels.cu)
 template <typename real>
-cudaError_t launch_h_sweep(const SweepArgs<real>& a, int tile_y, cudaStream_t s);
+cudaError_t launch_h_sweep(const SweepArgs<real>& a, const SweepStreams& s);
 template <typename real>
-cudaError_t launch_e_sweep(const SweepArgs<real>& a, int tile_y, cudaStream_t s);
+cudaError_t launch_e_sweep(const SweepArgs<real>& a, const SweepStreams& s);
 template <typename real>
 cudaError_t launch_ghosts(real* const H[3], int pmc_mask, int nx, int ny, int nz, int X, int Y, int B,
                           cudaStream_t s);

@@ -427,58 +427,64 @@ __global__ void __launch_bounds__(256, MODE == kBulk ? 3 : 2) e_sweep_kernel(con
 
 // ------------------------------------------------------------------------------------- launchers
 template <typename real>
-static cudaError_t launch_modes(const SweepArgs<real>& a, cudaStream_t s, bool h) {
-  const int tz = a.tile_z;
+static cudaError_t launch_modes(const SweepArgs<real>& a, const SweepStreams& st, bool h) {
   const long long quads = (long long)a.Y * (a.X / 4);
   const int inner = a.zi1 - a.zi0;
   const int bx = (int)((quads + 255) / 256);
+  cudaError_t err;
+  // slab launches on the side stream, concurrent with the bulk launch
+  const bool slabs = a.has_cpml != 0;
+  if (slabs) {
+    if ((err = cudaEventRecord(st.fork, st.main)) != cudaSuccess) return err;
+    if ((err = cudaStreamWaitEvent(st.side, st.fork, 0)) != cudaSuccess) return err;
+    SweepArgs<real> s = a;
+    s.tile_z = a.tile_z_slab;
+    const int tz = s.tile_z;
+    const int na = (a.zi0 - 1 + tz - 1) / tz, nb = (a.nz + 2 - a.zi1 + tz - 1) / tz;
+    if (na + nb > 0) {
+      dim3 grid(bx, na + nb, a.B);
+      if (h)
+        h_sweep_kernel<real, kSlabPlanes><<<grid, 256, 0, st.side>>>(s);
+      else
+        e_sweep_kernel<real, kSlabPlanes><<<grid, 256, 0, st.side>>>(s);
+      if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    }
+    if (a.n_slab_quads > 0 && inner > 0) {
+      dim3 grid((a.n_slab_quads + 255) / 256, (inner + tz - 1) / tz, a.B);
+      if (h)
+        h_sweep_kernel<real, kSlabColumns><<<grid, 256, 0, st.side>>>(s);
+      else
+        e_sweep_kernel<real, kSlabColumns><<<grid, 256, 0, st.side>>>(s);
+      if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    }
+    if ((err = cudaEventRecord(st.join, st.side)) != cudaSuccess) return err;
+  }
   if (inner > 0) {
+    const int tz = a.tile_z;
     dim3 grid(bx, (inner + tz - 1) / tz, a.B);
     if (h)
-      h_sweep_kernel<real, kBulk><<<grid, 256, 0, s>>>(a);
+      h_sweep_kernel<real, kBulk><<<grid, 256, 0, st.main>>>(a);
     else
-      e_sweep_kernel<real, kBulk><<<grid, 256, 0, s>>>(a);
-    cudaError_t err = cudaGetLastError();
-    if (err != cudaSuccess) return err;
+      e_sweep_kernel<real, kBulk><<<grid, 256, 0, st.main>>>(a);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
   }
-  if (!a.has_cpml) return cudaSuccess;
-  const int na = (a.zi0 - 1 + tz - 1) / tz, nb = (a.nz + 2 - a.zi1 + tz - 1) / tz;
-  if (na + nb > 0) {
-    dim3 grid(bx, na + nb, a.B);
-    if (h)
-      h_sweep_kernel<real, kSlabPlanes><<<grid, 256, 0, s>>>(a);
-    else
-      e_sweep_kernel<real, kSlabPlanes><<<grid, 256, 0, s>>>(a);
-    cudaError_t err = cudaGetLastError();
-    if (err != cudaSuccess) return err;
-  }
-  if (a.n_slab_quads > 0 && inner > 0) {
-    dim3 grid((a.n_slab_quads + 255) / 256, (inner + tz - 1) / tz, a.B);
-    if (h)
-      h_sweep_kernel<real, kSlabColumns><<<grid, 256, 0, s>>>(a);
-    else
-      e_sweep_kernel<real, kSlabColumns><<<grid, 256, 0, s>>>(a);
-    cudaError_t err = cudaGetLastError();
-    if (err != cudaSuccess) return err;
-  }
+  if (slabs && (err = cudaStreamWaitEvent(st.main, st.join, 0)) != cudaSuccess) return err;
   return cudaSuccess;
 }
 
 template <typename real>
-cudaError_t launch_h_sweep(const SweepArgs<real>& a, int tile_y, cudaStream_t s) {
-  (void)tile_y;
+cudaError_t launch_h_sweep(const SweepArgs<real>& a, const SweepStreams& s) {
   return launch_modes<real>(a, s, true);
 }
 
 template <typename real>
-cudaError_t launch_e_sweep(const SweepArgs<real>& a, int tile_y, cudaStream_t s) {
-  (void)tile_y;
+cudaError_t launch_e_sweep(const SweepArgs<real>& a, const SweepStreams& s) {
   return launch_modes<real>(a, s, false);
 }
 
-template cudaError_t launch_h_sweep<float>(const SweepArgs<float>&, int, cudaStream_t);
-template cudaError_t launch_e_sweep<float>(const SweepArgs<float>&, int, cudaStream_t);
-template cudaError_t launch_h_sweep<double>(const SweepArgs<double>&, int, cudaStream_t);
-template cudaError_t launch_e_sweep<double>(const SweepArgs<double>&, int, cudaStream_t);
+template cudaError_t launch_h_sweep<float>(const SweepArgs<float>&, const SweepStreams&);
+template cudaError_t launch_e_sweep<float>(const SweepArgs<float>&, const SweepStreams&);
+template cudaError_t launch_h_sweep<double>(const SweepArgs<double>&, const SweepStreams&);
+template cudaError_t launch_e_sweep<double>(const SweepArgs<double>&, const SweepStreams&);
 
 }  // namespace oafdtd
