@@ -272,12 +272,12 @@ def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
         scratch = Gb300Engine(c, "float32", max_steps=steps_needed() + CHUNK)
         tr = tune(scratch)
         scratch.close()
-        tiles = {"tile_z": tr.tile_z, "tile_z_slab": tr.tile_z_slab, "source": "autotune",
-                 "tuned_ms_per_time_step": tr.ms_per_step,
-                 "table": {f"{k[0]}/{k[1]}": round(v, 5) for k, v in tr.table.items()}}
+        tiles = {"tile_z": tr.tile_z, "tile_z_slab": tr.tile_z_slab, "variant": tr.variant,
+                 "source": "autotune", "tuned_ms_per_time_step": tr.ms_per_step,
+                 "table": {f"{k[0]}/{k[1]}/{k[2]}": round(v, 5) for k, v in tr.table.items()}}
     eng = Gb300Engine(c, "float32", max_steps=max_steps)
     if tiles:
-        eng.set_tuning(tiles["tile_z"], tiles["tile_z_slab"])
+        eng.set_tuning(tiles["tile_z"], tiles["tile_z_slab"], tiles.get("variant", -1))
     eng.set_profiling(True)  # CUDA events around every kernel, captured inside the graph
     for _ in range(args.warmup):
         eng.step(CHUNK)

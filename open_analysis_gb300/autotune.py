@@ -13,31 +13,44 @@ from __future__ import annotations
 from dataclasses import dataclass
 from typing import Any
 
-BULK = (8, 12, 16, 24, 32, 48)
+BULK = (8, 16, 24, 32, 48)
 SLAB = (2, 4, 8)
+VARIANTS = (1, 0)  # shared-memory staged bulk sweeps, register marching
 
 
 @dataclass(frozen=True)
 class TuneResult:
     tile_z: int
     tile_z_slab: int
+    variant: int
     ms_per_step: float
-    table: dict[tuple[int, int], float]
+    table: dict[tuple[int, int, int], float]
 
 
-def tune(engine: Any, chunks: int = 2, bulk: tuple[int, ...] = BULK, slab: tuple[int, ...] = SLAB) -> TuneResult:
-    """Time every (bulk, slab) pair; needs ``(1 + chunks) * 64`` free steps per pair."""
-    table: dict[tuple[int, int], float] = {}
-    for tz in bulk:
-        for ts in slab:
-            engine.set_tuning(tz, ts)
-            engine.step_timed(64)  # capture the graph of this shape
-            ms = sum(engine.step_timed(64) for _ in range(chunks))
-            table[(tz, ts)] = ms / (64 * chunks)
+def _candidates(bulk: tuple[int, ...], slab: tuple[int, ...], variants: tuple[int, ...]) -> list[tuple[int, int, int]]:
+    return [(tz, ts, v) for v in variants for tz in bulk for ts in slab]
+
+
+def tune(
+    engine: Any,
+    chunks: int = 2,
+    bulk: tuple[int, ...] = BULK,
+    slab: tuple[int, ...] = SLAB,
+    variants: tuple[int, ...] = VARIANTS,
+) -> TuneResult:
+    """Time every (bulk tile, slab tile, variant); needs ``(1 + chunks) * 64`` steps each."""
+    table: dict[tuple[int, int, int], float] = {}
+    for cand in _candidates(bulk, slab, variants):
+        engine.set_tuning(*cand)
+        engine.step_timed(64)  # capture the graph of this shape
+        ms = sum(engine.step_timed(64) for _ in range(chunks))
+        table[cand] = ms / (64 * chunks)
     best = min(table, key=table.__getitem__)
     engine.set_tuning(*best)
-    return TuneResult(best[0], best[1], table[best], table)
+    return TuneResult(best[0], best[1], best[2], table[best], table)
 
 
-def steps_needed(chunks: int = 2, bulk: tuple[int, ...] = BULK, slab: tuple[int, ...] = SLAB) -> int:
-    return len(bulk) * len(slab) * (1 + chunks) * 64
+def steps_needed(
+    chunks: int = 2, bulk: tuple[int, ...] = BULK, slab: tuple[int, ...] = SLAB, variants: tuple[int, ...] = VARIANTS
+) -> int:
+    return len(_candidates(bulk, slab, variants)) * (1 + chunks) * 64

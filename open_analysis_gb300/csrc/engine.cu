@@ -56,6 +56,7 @@ struct EngineBase {
   int profiling = 0;
   int tile_z = 16;
   int tile_z_slab = 4;
+  int staged = 1;  // bulk sweeps staged through shared memory (0: register marching)
   bool graph_dirty = false;  // launch shape or profiling changed: the graph is re-captured
   double model_bytes = 0.0;
 };
@@ -464,6 +465,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
   sw.B = B;
   sw.tile_z = tile_z;
   sw.tile_z_slab = tile_z_slab;
+  sw.staged = staged;
 
   // ---- edge list: surface impedance, injection targets, deferred ADE edges
   struct EdgeRec {
@@ -812,6 +814,7 @@ int Engine<real>::step(int64_t n) {
   }
   sw.tile_z = tile_z;
   sw.tile_z_slab = tile_z_slab;
+  sw.staged = staged;
   if (profiling) {
     for (double& v : prof_ms) v = 0.0;
     prof_steps = 0;
@@ -1065,12 +1068,14 @@ int oafdtd_set_graph(oafdtd_engine* engine, int32_t use_graph) {
   return OAFDTD_OK;
 }
 
-int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_z, int32_t tile_z_slab) {
+int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_z, int32_t tile_z_slab, int32_t variant) {
   if (!engine) return fail(OAFDTD_E_INVALID, "null engine");
   if (tile_z < 0 || tile_z_slab < 0 || tile_z > 4096 || tile_z_slab > 4096)
     return fail(OAFDTD_E_INVALID, "tile sizes must be 0..4096 planes");
+  if (variant < -1 || variant > 1) return fail(OAFDTD_E_INVALID, "variant must be -1, 0 or 1");
   if (tile_z) engine->impl->tile_z = tile_z;
   if (tile_z_slab) engine->impl->tile_z_slab = tile_z_slab;
+  if (variant >= 0) engine->impl->staged = variant;
   engine->impl->graph_dirty = true;  // a new launch shape needs a new graph
   return OAFDTD_OK;
 }

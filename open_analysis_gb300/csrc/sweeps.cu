@@ -460,13 +460,17 @@ static cudaError_t launch_modes(const SweepArgs<real>& a, const SweepStreams& st
     if ((err = cudaEventRecord(st.join, st.side)) != cudaSuccess) return err;
   }
   if (inner > 0) {
-    const int tz = a.tile_z;
-    dim3 grid(bx, (inner + tz - 1) / tz, a.B);
-    if (h)
-      h_sweep_kernel<real, kBulk><<<grid, 256, 0, st.main>>>(a);
-    else
-      e_sweep_kernel<real, kBulk><<<grid, 256, 0, st.main>>>(a);
-    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    if (a.staged) {
+      if ((err = launch_staged_bulk<real>(a, st.main, h)) != cudaSuccess) return err;
+    } else {
+      const int tz = a.tile_z;
+      dim3 grid(bx, (inner + tz - 1) / tz, a.B);
+      if (h)
+        h_sweep_kernel<real, kBulk><<<grid, 256, 0, st.main>>>(a);
+      else
+        e_sweep_kernel<real, kBulk><<<grid, 256, 0, st.main>>>(a);
+      if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    }
   }
   if (slabs && (err = cudaStreamWaitEvent(st.main, st.join, 0)) != cudaSuccess) return err;
   return cudaSuccess;

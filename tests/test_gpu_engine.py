@@ -155,3 +155,32 @@ def test_kernel_profile_and_model_bytes() -> None:
     t = eng.kernel_times()
     assert t["step"] > 0 and t["h_sweep"] > 0 and t["e_sweep"] > 0
     assert eng.model_bytes() > 0
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("tiles", [(4, 2), (32, 8)])
+def test_launch_shapes_match_oracle(variant: int, tiles: tuple[int, int]) -> None:
+    """Every bulk variant and z tiling gives the oracle's float32 fields bit for bit."""
+    c = compile_model(CASES["microstrip"][0](namespace("gb300")), "float32")
+    gpu = _engine(c)
+    gpu.set_tuning(tiles[0], tiles[1], variant)
+    ref = OracleEngine(c, "float32")
+    gpu.step(70)
+    ref.step(70)
+    for k in range(6):
+        assert np.array_equal(gpu.field(k), (ref.E + ref.H)[k].astype(np.float64)), NAMES[k]
+
+
+def test_via_transition_small_matches_oracle() -> None:
+    """The benchmark structure (Debye stack, SIBC copper, via, CPML on all walls) at 48x40x32."""
+    from open_analysis_gb300.structures import via_transition
+
+    c = compile_model(via_transition(nx=48, ny=40, nz=32, n_freq=16, cpml_cells=6), "float32")
+    gpu = _engine(c)
+    ref = OracleEngine(c, "float32")
+    gpu.step(50)
+    ref.step(50)
+    for k in range(6):
+        assert np.array_equal(gpu.field(k), (ref.E + ref.H)[k].astype(np.float64)), NAMES[k]
+    for name, v in ref.results().items():
+        assert np.abs(gpu.results()[name] - v).max() <= 1e-9 * max(np.abs(v).max(), 1e-300), name
