@@ -78,7 +78,7 @@ struct SweepArgs {
   int B;
   int tile_z;       // planes per thread in the bulk launch
   int tile_z_slab;  // planes per thread in the slab launches (fewer: more blocks)
-  int staged;       // bulk launch: shared-memory staged pipeline (1) or register marching (0)
+  int staged;       // 1: one shared-memory staged launch per sweep; 0: register-marching launches
 };
 
 // Streams of one sweep: the bulk launch runs on `main`, the slab launches on `side`, forked and
@@ -193,7 +193,7 @@ cudaError_t launch_energy(const EnergyArgs<real>& a, double* partial, int nblock
                           cudaStream_t s);
 cudaError_t launch_bump(long long* step_base, int n, cudaStream_t s);
 template <typename real>
-cudaError_t launch_staged_bulk(const SweepArgs<real>& a, cudaStream_t s, bool h);
+cudaError_t launch_staged_sweep(const SweepArgs<real>& a, cudaStream_t s, bool h);
 
 constexpr int kEnergyBlocks = 1216;  // 8 per SM on a 152-SM GB300; fixed for a deterministic sum
 
