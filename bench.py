@@ -264,20 +264,20 @@ def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
     cells = nx * ny * nz
     max_steps = (args.warmup + args.steps + 2) * CHUNK
     tiles: dict[str, Any] = {}
-    if args.tile_z or args.tile_z_slab:
-        tiles = {"tile_z": args.tile_z, "tile_z_slab": args.tile_z_slab, "source": "flags"}
+    if args.tile_z or args.variant >= 0:
+        tiles = {"tile_z": args.tile_z, "variant": args.variant, "source": "flags"}
     elif not args.no_tune:
         from open_analysis_gb300.autotune import steps_needed, tune
 
         scratch = Gb300Engine(c, "float32", max_steps=steps_needed() + CHUNK)
         tr = tune(scratch)
         scratch.close()
-        tiles = {"tile_z": tr.tile_z, "tile_z_slab": tr.tile_z_slab, "variant": tr.variant,
-                 "source": "autotune", "tuned_ms_per_time_step": tr.ms_per_step,
-                 "table": {f"{k[0]}/{k[1]}/{k[2]}": round(v, 5) for k, v in tr.table.items()}}
+        tiles = {"tile_z": tr.tile_z, "variant": tr.variant, "source": "autotune",
+                 "tuned_ms_per_time_step": tr.ms_per_step,
+                 "table": {f"{k[0]}/{k[1]}": round(v, 5) for k, v in tr.table.items()}}
     eng = Gb300Engine(c, "float32", max_steps=max_steps)
     if tiles:
-        eng.set_tuning(tiles["tile_z"], tiles["tile_z_slab"], tiles.get("variant", -1))
+        eng.set_tuning(tiles["tile_z"], tiles["variant"])
     eng.set_profiling(True)  # CUDA events around every kernel, captured inside the graph
     for _ in range(args.warmup):
         eng.step(CHUNK)
@@ -435,8 +435,8 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape")
-    ap.add_argument("--tile-z", type=int, default=0, help="planes per thread, bulk launch")
-    ap.add_argument("--tile-z-slab", type=int, default=0, help="planes per thread, slab launches")
+    ap.add_argument("--tile-z", type=int, default=0, help="planes per block")
+    ap.add_argument("--variant", type=int, default=-1, help="1 staged sweeps, 0 register marching")
     ap.add_argument("--cells", default="", help="via-transition grid 'nx,ny,nz' (smaller profiling cases)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":

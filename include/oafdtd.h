@@ -183,11 +183,10 @@ int oafdtd_peak_bytes(const oafdtd_engine* engine, int64_t* out);
  * and replay it (the reference's use_graph flag, engine.py:80,425-429). */
 int oafdtd_set_graph(oafdtd_engine* engine, int32_t use_graph);
 
-/* Launch shape of the sweeps: z planes marched per thread in the bulk launch (tile_z) and in the
- * CPML slab launches (tile_z_slab), 0 keeps the current value; bulk variant: 1 stages the planes
- * through shared memory (default), 0 marches them in registers, -1 keeps it. The autotuner sets
- * these. */
-int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_z, int32_t tile_z_slab, int32_t variant);
+/* Launch shape of the sweeps: z planes marched per block (tile_z, 0 keeps the current value) and
+ * the sweep variant (1 stages the planes through shared memory, the default; 0 marches them in
+ * registers; -1 keeps it). The autotuner sets these. */
+int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_z, int32_t variant);
 
 /* Average device time per step of each kernel class over the last oafdtd_step call, measured
  * with CUDA events when profiling is on (oafdtd_set_profiling). Writes up to n values in the

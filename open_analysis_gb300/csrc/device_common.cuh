@@ -1,5 +1,5 @@
-// Device helpers shared by the sweep kernels: 4-cell vectors ("quads"), async copies, the CPML
-// correction of a quad and the general-pole Debye update.
+// Device helpers shared by the sweep kernels: 4-cell vectors ("quads"), async copies and the
+// general-pole Debye update.
 #pragma once
 
 #include "oafdtd_internal.cuh"
@@ -45,72 +45,6 @@ __device__ __forceinline__ Quad<uint16_t> ld4(const uint16_t* p) {
 template <typename real>
 __device__ __forceinline__ Quad<real> zero4() {
   return Quad<real>{{(real)0, (real)0, (real)0, (real)0}};
-}
-
-enum : int { kBulk = 0, kSlabPlanes = 1, kSlabColumns = 2 };
-
-// The CPML corrections of one component on one quad: for each derivative axis (ascending) whose
-// slab holds the cell, psi <- b psi + c d; f += (sign k) (ek d + psi). Slabs along y and z hold
-// whole quads, so their psi moves as one vector; x slabs are handled cell by cell.
-template <typename real, int KIND>
-__device__ __forceinline__ void cpml_quad(const SweepArgs<real>& a, const CpmlTerm<real> (&terms)[2],
-                                          const real* const (&co)[3][3], Quad<real>& f, const real (&d0)[4],
-                                          const real (&d1)[4], const real (&kfac)[4], const bool (&valid)[4],
-                                          int i0, int j, int k, int b) {
-  const int X = a.X, Y = a.Y, Z = a.nz + 2;
-#pragma unroll
-  for (int t = 0; t < 2; ++t) {
-    const CpmlTerm<real>& T = terms[t];
-    if (T.side[0].psi == nullptr) continue;
-    const int ax = T.axis;
-    const real* cb_ = co[ax][0];
-    const real* cc_ = co[ax][1];
-    const real* ck_ = co[ax][2];
-    if (ax == 0) {
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const int i = i0 + e;
-        const int s = a.side[KIND][0][i];
-        if (!valid[e] || s < 0) continue;
-        const CpmlSide<real>& S = T.side[s];
-        if (j < S.lo[1] || j >= S.hi[1] || k < S.lo[2] || k >= S.hi[2] || i < S.lo[0] || i >= S.hi[0]) continue;
-        const int w = S.hi[0] - S.lo[0];
-        const long long q = (((long long)b * Z + k) * Y + j) * w + (i - S.lo[0]);
-        const real d = t == 0 ? d0[e] : d1[e];
-        real ps = S.psi[q];
-        ps = ps * cb_[i];
-        ps = ps + cc_[i] * d;
-        S.psi[q] = ps;
-        const real upd = ck_[i] * d + ps;
-        f.v[e] = f.v[e] + (T.sign * kfac[e]) * upd;
-      }
-    } else {
-      const int ia = ax == 1 ? j : k;
-      const int s = a.side[KIND][ax][ia];
-      if (s < 0) continue;
-      const CpmlSide<real>& S = T.side[s];
-      const int other = ax == 1 ? k : j;
-      const int oax = ax == 1 ? 2 : 1;
-      if (other < S.lo[oax] || other >= S.hi[oax] || ia < S.lo[ax] || ia >= S.hi[ax]) continue;
-      const int w = S.hi[ax] - S.lo[ax];
-      const long long q0 = ax == 1 ? (((long long)b * Z + k) * w + (j - S.lo[1])) * X + i0
-                                   : (((long long)b * w + (k - S.lo[2])) * Y + j) * X + i0;
-      Quad<real> ps4 = ld4(S.psi + q0);
-      const real pb = cb_[ia], pc = cc_[ia], pk = ck_[ia];
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const int i = i0 + e;
-        if (!valid[e] || i < S.lo[0] || i >= S.hi[0]) continue;
-        const real d = t == 0 ? d0[e] : d1[e];
-        real ps = ps4.v[e] * pb;
-        ps = ps + pc * d;
-        ps4.v[e] = ps;
-        const real upd = pk * d + ps;
-        f.v[e] = f.v[e] + (T.sign * kfac[e]) * upd;
-      }
-      st4(S.psi + q0, ps4);
-    }
-  }
 }
 
 // Debye update of one dispersive edge with any pole count: jt = 1/2 sum_p (1 + k_p) J_p;

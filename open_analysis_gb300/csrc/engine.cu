@@ -55,7 +55,6 @@ struct EngineBase {
   int use_graph = 1;
   int profiling = 0;
   int tile_z = 16;
-  int tile_z_slab = 4;
   int staged = 1;  // bulk sweeps staged through shared memory (0: register marching)
   bool graph_dirty = false;  // launch shape or profiling changed: the graph is re-captured
   double model_bytes = 0.0;
@@ -65,7 +64,7 @@ template <typename real>
 struct Engine final : EngineBase {
   int device = 0;
   cudaStream_t stream = nullptr;
-  oafdtd::SweepStreams streams{};
+  oafdtd::CpmlPass<real> cpml{};
   std::vector<void*> allocs;
   int nx = 0, ny = 0, nz = 0, X = 0, Y = 0, Z = 0, B = 0;
   long long bs = 0;
@@ -92,9 +91,6 @@ struct Engine final : EngineBase {
     if (t_start) cudaEventDestroy(t_start);
     if (t_stop) cudaEventDestroy(t_stop);
     for (void* p : allocs) cudaFree(p);
-    if (streams.fork) cudaEventDestroy(streams.fork);
-    if (streams.join) cudaEventDestroy(streams.join);
-    if (streams.side) cudaStreamDestroy(streams.side);
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -171,10 +167,6 @@ int Engine<real>::build(const oafdtd_problem& p) {
     return fail(OAFDTD_E_INVALID, "at most 16 Debye poles are supported");
   OA_CUDA(cudaGetDevice(&device));
   OA_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-  OA_CUDA(cudaStreamCreateWithFlags(&streams.side, cudaStreamNonBlocking));
-  OA_CUDA(cudaEventCreateWithFlags(&streams.fork, cudaEventDisableTiming));
-  OA_CUDA(cudaEventCreateWithFlags(&streams.join, cudaEventDisableTiming));
-  streams.main = stream;
 
   auto in_range = [&](long long f) { return f >= 0 && f < bs; };
 
@@ -369,11 +361,6 @@ int Engine<real>::build(const oafdtd_problem& p) {
       sw.hcorr[c][s] = oafdtd::CpmlTerm<real>{};
     }
   int last_slot[2][3] = {{-1, -1, -1}, {-1, -1, -1}};
-  std::vector<uint8_t> slab[3] = {std::vector<uint8_t>(X, 0), std::vector<uint8_t>(Y, 0),
-                                  std::vector<uint8_t>(Z, 0)};
-  std::vector<int8_t> side_map[2][3];
-  for (int kind = 0; kind < 2; ++kind)
-    for (int ax = 0; ax < 3; ++ax) side_map[kind][ax].assign((size_t)len[ax], (int8_t)-1);
   for (int n = 0; n < p.n_corr; ++n) {
     const oafdtd_correction& k = p.corr[n];
     if (k.kind < 0 || k.kind > 1 || k.c < 0 || k.c > 2 || k.a < 0 || k.a > 2 || k.b < 0 || k.b > 2)
@@ -398,17 +385,11 @@ int Engine<real>::build(const oafdtd_problem& p) {
     // psi spans the slab along the derivative axis and the full storage extent on the others
     long long vol = B;
     for (int ax = 0; ax < 3; ++ax) vol *= (ax == k.a) ? (k.hi[ax] - k.lo[ax]) : len[ax];
-    for (int q = k.lo[k.a]; q < k.hi[k.a]; ++q) {
-      slab[k.a][q] = 1;
-      int8_t& sm = side_map[k.kind][k.a][q];
-      if (sm >= 0 && sm != side)
-        return fail(OAFDTD_E_INVALID, "CPML sides of one kind disagree on their slab ranges");
-      sm = (int8_t)side;
-    }
     real* psi = nullptr;
     int rc = alloc(&psi, (size_t)vol);
     if (rc) return rc;
     term_ref.axis = k.a;
+    term_ref.src = k.b;
     term_ref.sign = (real)k.sign;
     term_ref.side[side].psi = psi;
     for (int ax = 0; ax < 3; ++ax) {
@@ -416,45 +397,22 @@ int Engine<real>::build(const oafdtd_problem& p) {
       term_ref.side[side].hi[ax] = k.hi[ax];
     }
   }
-  {
-    uint8_t* d = nullptr;
-    int rc = upload_vec(&d, slab[0]);
-    if (rc) return rc;
-    sw.slab_x = d;
-    if ((rc = upload_vec(&d, slab[1]))) return rc;
-    sw.slab_y = d;
-    if ((rc = upload_vec(&d, slab[2]))) return rc;
-    sw.slab_z = d;
-    for (int kind = 0; kind < 2; ++kind)
-      for (int ax = 0; ax < 3; ++ax) {
-        int8_t* dsm = nullptr;
-        if ((rc = upload_vec(&dsm, side_map[kind][ax]))) return rc;
-        sw.side[kind][ax] = dsm;
+  // correction passes: per kind and derivative axis, every (component, side) with a psi array
+  for (int kind = 0; kind < 2; ++kind)
+    for (int c = 0; c < 3; ++c)
+      for (int t = 0; t < 2; ++t) {
+        const oafdtd::CpmlTerm<real>& T = kind == 0 ? sw.ecorr[c][t] : sw.hcorr[c][t];
+        for (int sd = 0; sd < 2; ++sd) {
+          if (T.side[sd].psi == nullptr) continue;
+          oafdtd::CpmlAxisPass<real>& ap = cpml.axis[kind][T.axis];
+          if (ap.n >= 4) return fail(OAFDTD_E_INVALID, "more than four CPML corrections on one axis");
+          ap.comp[ap.n] = c;
+          ap.src[ap.n] = T.src;
+          ap.sign[ap.n] = T.sign;
+          ap.side[ap.n] = &T.side[sd];
+          ++ap.n;
+        }
       }
-    // planes [zi0, zi1) hold no z-slab cell; the z slabs sit at the two ends
-    int zi0 = 1, zi1 = nz + 2;
-    while (zi0 < nz + 2 && slab[2][zi0]) ++zi0;
-    while (zi1 > zi0 && slab[2][zi1 - 1]) --zi1;
-    for (int k = zi0; k < zi1; ++k)
-      if (slab[2][k]) return fail(OAFDTD_E_INVALID, "a z CPML slab lies inside the domain");
-    sw.zi0 = zi0;
-    sw.zi1 = zi1;
-    // quads whose column meets an x or y slab
-    std::vector<int> quads;
-    const int X4 = X / 4;
-    for (int j = 1; j <= ny + 1; ++j)
-      for (int q = 0; q < X4; ++q) {
-        const int i0 = 4 * q;
-        if (i0 > nx + 1) break;
-        bool col = slab[1][j] != 0;
-        for (int e = 0; e < 4; ++e) col = col || slab[0][i0 + e] != 0;
-        if (col) quads.push_back(j * X4 + q);
-      }
-    sw.n_slab_quads = (int)quads.size();
-    int* dq = nullptr;
-    if ((rc = upload_vec(&dq, quads))) return rc;
-    sw.slab_quads = dq;
-  }
   sw.dtmu = (real)p.dtmu;
   sw.nx = nx;
   sw.ny = ny;
@@ -464,7 +422,6 @@ int Engine<real>::build(const oafdtd_problem& p) {
   sw.bs = bs;
   sw.B = B;
   sw.tile_z = tile_z;
-  sw.tile_z_slab = tile_z_slab;
   sw.staged = staged;
 
   // ---- edge list: surface impedance, injection targets, deferred ADE edges
@@ -746,7 +703,8 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing) {
   // inside a stream capture an event record becomes a graph node only with the external flag
   const unsigned rec = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[0], stream, rec));
-  err = oafdtd::launch_h_sweep<real>(sw, streams);
+  err = oafdtd::launch_h_sweep<real>(sw, stream);
+  if (err == cudaSuccess && sw.has_cpml) err = oafdtd::launch_cpml_pass<real>(cpml, sw, 1, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("h_sweep: ") + cudaGetErrorString(err));
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[1], stream, rec));
   if (pmc_mask) {
@@ -757,7 +715,8 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing) {
   err = oafdtd::launch_pre_e<real>(pr, off, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("pre_e: ") + cudaGetErrorString(err));
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[3], stream, rec));
-  err = oafdtd::launch_e_sweep<real>(sw, streams);
+  err = oafdtd::launch_e_sweep<real>(sw, stream);
+  if (err == cudaSuccess && sw.has_cpml) err = oafdtd::launch_cpml_pass<real>(cpml, sw, 0, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("e_sweep: ") + cudaGetErrorString(err));
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[4], stream, rec));
   err = oafdtd::launch_edges<real>(ed, off, stream);
@@ -813,7 +772,6 @@ int Engine<real>::step(int64_t n) {
     graph_ready = false;
   }
   sw.tile_z = tile_z;
-  sw.tile_z_slab = tile_z_slab;
   sw.staged = staged;
   if (profiling) {
     for (double& v : prof_ms) v = 0.0;
@@ -1068,13 +1026,11 @@ int oafdtd_set_graph(oafdtd_engine* engine, int32_t use_graph) {
   return OAFDTD_OK;
 }
 
-int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_z, int32_t tile_z_slab, int32_t variant) {
+int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_z, int32_t variant) {
   if (!engine) return fail(OAFDTD_E_INVALID, "null engine");
-  if (tile_z < 0 || tile_z_slab < 0 || tile_z > 4096 || tile_z_slab > 4096)
-    return fail(OAFDTD_E_INVALID, "tile sizes must be 0..4096 planes");
+  if (tile_z < 0 || tile_z > 4096) return fail(OAFDTD_E_INVALID, "tile_z must be 0..4096 planes");
   if (variant < -1 || variant > 1) return fail(OAFDTD_E_INVALID, "variant must be -1, 0 or 1");
   if (tile_z) engine->impl->tile_z = tile_z;
-  if (tile_z_slab) engine->impl->tile_z_slab = tile_z_slab;
   if (variant >= 0) engine->impl->staged = variant;
   engine->impl->graph_dirty = true;  // a new launch shape needs a new graph
   return OAFDTD_OK;

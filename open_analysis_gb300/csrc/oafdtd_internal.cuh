@@ -10,7 +10,8 @@
 //    its index. It replaces both the reference's material index and its per-edge ADE arrays:
 //    the E sweep reads one 2-byte index per edge, shared by every batch member.
 //  * psi: one array per CPML correction, (B, Z', Y', X') with the slab width along the
-//    derivative axis and the full storage extent along the other two axes.
+//    derivative axis and the full storage extent along the other two axes, so psi rows of y and z
+//    slabs line up with the field rows.
 //  * J[c]: dense Debye currents (P, B, nzA, Y, X) over the z range that holds dispersive edges.
 //  * edge list (surface impedance, injection, dispersive edges with injection), sorted by
 //    (component, flat index), one thread per edge.
@@ -33,8 +34,24 @@ struct CpmlSide {
 template <typename real>
 struct CpmlTerm {    // the correction of one (kind, component, derivative axis)
   int axis;
+  int src;           // source component of the derivative
   real sign;
   CpmlSide<real> side[2];
+};
+
+// The corrections of one (kind, derivative axis): up to two components times two sides.
+template <typename real>
+struct CpmlAxisPass {
+  int n;
+  int comp[4];
+  int src[4];
+  real sign[4];
+  const CpmlSide<real>* side[4];
+};
+
+template <typename real>
+struct CpmlPass {
+  CpmlAxisPass<real> axis[2][3];  // [kind 0 E / 1 H][axis]
 };
 
 // One entry of the combined material table: update coefficients of the averaged material and,
@@ -55,13 +72,6 @@ struct SweepArgs {
   const real* ade_kp;       // [p]
   const real* ade_onekp;    // [p]: 1 + kp in the field precision
   int ade_P;
-  const uint8_t* slab_x;    // [storage x]: inside some CPML slab along x
-  const uint8_t* slab_y;
-  const uint8_t* slab_z;
-  const int8_t* side[2][3]; // [kind 0 E / 1 H][axis][storage index]: CPML side slot or -1
-  int zi0, zi1;             // planes [zi0, zi1) meet no z slab; [1, zi0) and [zi1, nz + 2) do
-  const int* slab_quads;    // quads (flattened y, x/4 index) whose column meets an x or y slab
-  int n_slab_quads;
   real* J[3];
   int jk0[3];
   int jnk[3];
@@ -76,18 +86,8 @@ struct SweepArgs {
   int nx, ny, nz, X, Y;
   long long bs;             // Z * Y * X
   int B;
-  int tile_z;       // planes per thread in the bulk launch
-  int tile_z_slab;  // planes per thread in the slab launches (fewer: more blocks)
-  int staged;       // 1: one shared-memory staged launch per sweep; 0: register-marching launches
-};
-
-// Streams of one sweep: the bulk launch runs on `main`, the slab launches on `side`, forked and
-// joined with the two events (inside a captured graph this becomes two parallel branches).
-struct SweepStreams {
-  cudaStream_t main;
-  cudaStream_t side;
-  cudaEvent_t fork;
-  cudaEvent_t join;
+  int tile_z;       // planes marched per thread (register variant) or per block (staged)
+  int staged;       // 1: shared-memory staged sweeps; 0: register marching
 };
 
 template <typename real>
@@ -176,9 +176,11 @@ struct EnergyArgs {
 
 // kernel launchers (kernels.cu)
 template <typename real>
-cudaError_t launch_h_sweep(const SweepArgs<real>& a, const SweepStreams& s);
+cudaError_t launch_h_sweep(const SweepArgs<real>& a, cudaStream_t s);
 template <typename real>
-cudaError_t launch_e_sweep(const SweepArgs<real>& a, const SweepStreams& s);
+cudaError_t launch_e_sweep(const SweepArgs<real>& a, cudaStream_t s);
+template <typename real>
+cudaError_t launch_cpml_pass(const CpmlPass<real>& pass, const SweepArgs<real>& a, int kind, cudaStream_t s);
 template <typename real>
 cudaError_t launch_ghosts(real* const H[3], int pmc_mask, int nx, int ny, int nz, int X, int Y, int B,
                           cudaStream_t s);

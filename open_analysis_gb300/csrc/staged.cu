@@ -8,11 +8,10 @@
 // registers; the Debye currents of the next plane are prefetched into registers. Neighbours in
 // x and y are read from the staged tile; results go straight to global memory.
 //
-// One launch per sweep updates every cell: shared memory already limits residency to two
-// blocks per SM, so the CPML corrections are fused inline at no occupancy cost. A quad runs them
-// only where its column or plane meets a slab. The arithmetic is the reference's, operation by
-// operation (packages/oa-fdtd/src/oa_fdtd/reference.py:152-207, :119-127): bulk update, then the
-// corrections by ascending derivative axis, then the Debye update.
+// One launch per sweep gives every cell its bulk update (and, in the E sweep, its Debye update);
+// the CPML corrections follow in the correction passes (cpml.cu). The arithmetic is the
+// reference's, operation by operation (packages/oa-fdtd/src/oa_fdtd/reference.py:152-180,
+// :119-127).
 
 #include "device_common.cuh"
 
@@ -23,14 +22,6 @@ constexpr int kTY = 8;        // rows per tile
 constexpr int kTW = 4 * kTQ;  // tile width in cells
 constexpr int kHW = kTW + 4;  // staged width with a one-quad halo
 constexpr int kStages = 3;
-
-template <typename real>
-__device__ __forceinline__ bool column_slab(const SweepArgs<real>& a, int i0, int j) {
-  bool col = a.slab_y[j] != 0;
-#pragma unroll
-  for (int e = 0; e < 4; ++e) col |= a.slab_x[i0 + e] != 0;
-  return col;
-}
 
 // ------------------------------------------------------------------------------------- H sweep
 // Slot: E[3][kTY + 1][kHW] (rows y0..y0+8, x0..x0+131), H[3][kTY][kTW].
@@ -71,7 +62,7 @@ __device__ __forceinline__ void h_stage(const SweepArgs<real>& a, HSlot<real>& s
   }
 }
 
-template <typename real, bool CPML>
+template <typename real>
 __global__ void __launch_bounds__(256, 2) h_staged_kernel(const __grid_constant__ SweepArgs<real> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   HSlot<real>* slot = reinterpret_cast<HSlot<real>*>(smem_raw);
@@ -83,10 +74,8 @@ __global__ void __launch_bounds__(256, 2) h_staged_kernel(const __grid_constant_
   const int k0 = 1 + kc * a.tile_z, k1 = min(k0 + a.tile_z, nz + 2);
   const int i0 = x0 + 4 * tx, j = y0 + ty;
   const bool live = i0 < X && j <= ny + 1 && i0 <= nx + 1;
-  const bool col = CPML && live && column_slab(a, i0, j);
   const long long base = (long long)b * a.bs;
   const real dtmu = a.dtmu;
-  const real kd[4] = {dtmu, dtmu, dtmu, dtmu};
   const Quad<real> ipx = i0 < X ? ld4(a.ip[0] + i0) : Quad<real>{};
   const real ipy = a.ip[1][min(j, Y - 1)];
 #pragma unroll
@@ -102,7 +91,6 @@ __global__ void __launch_bounds__(256, 2) h_staged_kernel(const __grid_constant_
     if (live) {
       const long long p = base + (long long)k * X * Y + (long long)j * X + i0;
       const bool kin = k <= nz;
-      const bool slow = CPML && (col || a.slab_z[k] != 0);
       const real ipz = a.ip[2][k];
       const Quad<real> ex = ld4(&cur.e[0][ty][4 * tx]), ey = ld4(&cur.e[1][ty][4 * tx]);
       const Quad<real> ez = ld4(&cur.e[2][ty][4 * tx]);
@@ -121,7 +109,6 @@ __global__ void __launch_bounds__(256, 2) h_staged_kernel(const __grid_constant_
           d1[e] = (ey1.v[e] - ey.v[e]) * ipz;  // axis z
           if (valid[e]) h.v[e] = h.v[e] + dtmu * ((-d0[e]) + d1[e]);
         }
-        if (slow) cpml_quad<real, 1>(a, a.hcorr[0], a.ph, h, d0, d1, kd, valid, i0, j, k, b);
         st4(a.H[0] + p, h);
       }
       if (kin) {  // Hy: cell along x (1..nx), node along y (1..ny+1), cell along z
@@ -138,7 +125,6 @@ __global__ void __launch_bounds__(256, 2) h_staged_kernel(const __grid_constant_
           d1[e] = (ex1.v[e] - ex.v[e]) * ipz;  // axis z
           if (valid[e]) h.v[e] = h.v[e] + dtmu * ((-d1[e]) + d0[e]);
         }
-        if (slow) cpml_quad<real, 1>(a, a.hcorr[1], a.ph, h, d0, d1, kd, valid, i0, j, k, b);
         st4(a.H[1] + p, h);
       }
       if (j <= ny) {  // Hz: cell along x and y, node along z (1..nz+1)
@@ -155,7 +141,6 @@ __global__ void __launch_bounds__(256, 2) h_staged_kernel(const __grid_constant_
           d1[e] = (exy.v[e] - ex.v[e]) * ipy;  // axis y
           if (valid[e]) h.v[e] = h.v[e] + dtmu * ((-d0[e]) + d1[e]);
         }
-        if (slow) cpml_quad<real, 1>(a, a.hcorr[2], a.ph, h, d0, d1, kd, valid, i0, j, k, b);
         st4(a.H[2] + p, h);
       }
     }
@@ -215,10 +200,10 @@ __device__ __forceinline__ void e_stage(const SweepArgs<real>& a, ESlot<real>& s
 // Bulk update, CPML and the Debye update of one E component on one quad. d0/d1 are the
 // derivatives along the component's two axes in ascending order; the reference's term order is
 // (d0, -d1) when first_plus, else (d1, -d0). j4 holds the prefetched Debye current (P = 1).
-template <typename real, bool CPML>
+template <typename real>
 __device__ __forceinline__ void e_apply(const SweepArgs<real>& a, int c, real* __restrict__ E, long long p,
                                         const Quad<real>& e_old, const uint16_t* m, const real (&d0)[4],
-                                        const real (&d1)[4], bool first_plus, bool slow, const Quad<real>& j4in,
+                                        const real (&d1)[4], bool first_plus, const Quad<real>& j4in,
                                         int i0, int j, int k, int b) {
   const int X = a.X, Y = a.Y, nx = a.nx;
   Quad<real> e4 = e_old;
@@ -236,7 +221,6 @@ __device__ __forceinline__ void e_apply(const SweepArgs<real>& a, int c, real* _
     if (valid[e]) e4.v[e] = cf[e].ca * e4.v[e] + cf[e].cb * acc;
     disp |= valid[e] && m[e] >= a.ade_lo && m[e] < a.ade_hi;
   }
-  if (CPML && slow) cpml_quad<real, 0>(a, a.ecorr[c], a.pe, e4, d0, d1, kf, valid, i0, j, k, b);
   if (disp) {
     const long long jstride = (long long)a.B * a.jnk[c] * Y * X;
     const long long jq = (((long long)b * a.jnk[c] + (k - a.jk0[c])) * Y + j) * X + i0;
@@ -280,7 +264,7 @@ __device__ __forceinline__ void j_prefetch(const SweepArgs<real>& a, Quad<real> 
   }
 }
 
-template <typename real, bool CPML>
+template <typename real>
 __global__ void __launch_bounds__(256, 2) e_staged_kernel(const __grid_constant__ SweepArgs<real> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ESlot<real>* slot = reinterpret_cast<ESlot<real>*>(smem_raw);
@@ -292,7 +276,6 @@ __global__ void __launch_bounds__(256, 2) e_staged_kernel(const __grid_constant_
   const int k0 = 1 + kc * a.tile_z, k1 = min(k0 + a.tile_z, nz + 2);
   const int i0 = x0 + 4 * tx, j = y0 + ty;
   const bool live = i0 < X && j <= ny + 1 && i0 <= nx + 1;
-  const bool col = CPML && live && column_slab(a, i0, j);
   const long long base = (long long)b * a.bs;
   const Quad<real> idx4 = i0 < X ? ld4(a.idd[0] + i0) : Quad<real>{};
   const real idy = a.idd[1][min(j, Y - 1)];
@@ -317,7 +300,6 @@ __global__ void __launch_bounds__(256, 2) e_staged_kernel(const __grid_constant_
     const ESlot<real>& cur = slot[(k - k0) % kStages];
     if (live) {
       const long long q = (long long)k * X * Y + (long long)j * X + i0;
-      const bool slow = CPML && (col || a.slab_z[k] != 0);
       const real idz = a.idd[2][k];
       const Quad<real> hx = ld4(&cur.h[0][ty + 1][4 * tx + 4]), hy = ld4(&cur.h[1][ty + 1][4 * tx + 4]);
       const Quad<real> hz = ld4(&cur.h[2][ty + 1][4 * tx + 4]);
@@ -330,8 +312,7 @@ __global__ void __launch_bounds__(256, 2) e_staged_kernel(const __grid_constant_
         d0[e] = (hz.v[e] - hzy.v[e]) * idy;
         d1[e] = (hy.v[e] - hy_m.v[e]) * idz;
       }
-      e_apply<real, CPML>(a, 0, a.E[0] + base, q, ld4(&cur.e[0][ty][4 * tx]), &cur.m[0][ty][4 * tx], d0, d1, true,
-                          slow, jcur[0], i0, j, k, b);
+      e_apply<real>(a, 0, a.E[0] + base, q, ld4(&cur.e[0][ty][4 * tx]), &cur.m[0][ty][4 * tx], d0, d1, true, jcur[0], i0, j, k, b);
       // Ey: terms (a = z, +Hx) then (a = x, -Hz); d0 is the x term, d1 the z term
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
@@ -339,8 +320,7 @@ __global__ void __launch_bounds__(256, 2) e_staged_kernel(const __grid_constant_
         d0[e] = (hz.v[e] - hzl) * idx4.v[e];
         d1[e] = (hx.v[e] - hx_m.v[e]) * idz;
       }
-      e_apply<real, CPML>(a, 1, a.E[1] + base, q, ld4(&cur.e[1][ty][4 * tx]), &cur.m[1][ty][4 * tx], d0, d1, false,
-                          slow, jcur[1], i0, j, k, b);
+      e_apply<real>(a, 1, a.E[1] + base, q, ld4(&cur.e[1][ty][4 * tx]), &cur.m[1][ty][4 * tx], d0, d1, false, jcur[1], i0, j, k, b);
       // Ez: terms (a = x, +Hy) then (a = y, -Hx)
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
@@ -348,8 +328,7 @@ __global__ void __launch_bounds__(256, 2) e_staged_kernel(const __grid_constant_
         d0[e] = (hy.v[e] - hyl) * idx4.v[e];
         d1[e] = (hx.v[e] - hxy.v[e]) * idy;
       }
-      e_apply<real, CPML>(a, 2, a.E[2] + base, q, ld4(&cur.e[2][ty][4 * tx]), &cur.m[2][ty][4 * tx], d0, d1, true,
-                          slow, jcur[2], i0, j, k, b);
+      e_apply<real>(a, 2, a.E[2] + base, q, ld4(&cur.e[2][ty][4 * tx]), &cur.m[2][ty][4 * tx], d0, d1, true, jcur[2], i0, j, k, b);
       hx_m = hx;
       hy_m = hy;
     }
@@ -363,29 +342,24 @@ __global__ void __launch_bounds__(256, 2) e_staged_kernel(const __grid_constant_
 }
 
 // ------------------------------------------------------------------------------------- launch
-template <typename real, bool CPML>
-static cudaError_t launch_staged(const SweepArgs<real>& a, cudaStream_t s, bool h) {
+template <typename real>
+cudaError_t launch_staged_sweep(const SweepArgs<real>& a, cudaStream_t s, bool h) {
   const int nkc = (a.nz + 1 + a.tile_z - 1) / a.tile_z;
   dim3 block(kTQ, kTY);
   dim3 grid((a.X + kTW - 1) / kTW, (a.ny + 1 + kTY - 1) / kTY, nkc * a.B);
   cudaError_t err;
   if (h) {
     const size_t bytes = sizeof(HSlot<real>) * kStages;
-    err = cudaFuncSetAttribute(h_staged_kernel<real, CPML>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    err = cudaFuncSetAttribute(h_staged_kernel<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (err != cudaSuccess) return err;
-    h_staged_kernel<real, CPML><<<grid, block, bytes, s>>>(a);
+    h_staged_kernel<real><<<grid, block, bytes, s>>>(a);
   } else {
     const size_t bytes = sizeof(ESlot<real>) * kStages;
-    err = cudaFuncSetAttribute(e_staged_kernel<real, CPML>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    err = cudaFuncSetAttribute(e_staged_kernel<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (err != cudaSuccess) return err;
-    e_staged_kernel<real, CPML><<<grid, block, bytes, s>>>(a);
+    e_staged_kernel<real><<<grid, block, bytes, s>>>(a);
   }
   return cudaGetLastError();
-}
-
-template <typename real>
-cudaError_t launch_staged_sweep(const SweepArgs<real>& a, cudaStream_t s, bool h) {
-  return a.has_cpml ? launch_staged<real, true>(a, s, h) : launch_staged<real, false>(a, s, h);
 }
 
 template cudaError_t launch_staged_sweep<float>(const SweepArgs<float>&, cudaStream_t, bool);

@@ -1,87 +1,49 @@
-// The two Yee sweeps of a time step, fused with every per-cell correction.
+// Register-marching sweeps (the fallback variant; the staged variant in staged.cu is the
+// default).
 //
 // Thread mapping: each thread owns a "quad", four consecutive x cells of one storage row (a
 // 16-byte float4 for float32), and marches up a chunk of z planes, carrying the neighbouring
 // plane in registers. Quads are numbered over the flattened (y, x/4) plane. The x neighbour in
-// the next (H sweep) or previous (E sweep) quad comes from a warp shuffle when the neighbouring
-// lane holds that quad and loaded the plane; otherwise the lane reads it itself.
-//
-// This file holds the register-marching variant (the staged variant is in staged.cu). Every sweep
-// is three launches that split the cells between them, each cell exactly once:
-//  * bulk: planes [zi0, zi1) outside every z slab, quads whose column meets no x or y slab; no
-//    CPML code, few registers, high occupancy;
-//  * slab planes: every quad of the z-slab planes, CPML applied;
-//  * slab columns: the quads whose column meets an x or y slab (a short list), planes
-//    [zi0, zi1), CPML applied.
-// Cells are independent within a sweep (H reads only E, E reads only H), so the split changes no
-// value. The CPML corrections follow the reference's order: bulk update, then the corrections
-// by ascending derivative axis, each rounded to the field precision. Material coefficients come
-// from a packed table (ca, cb, cbe, beta_0) indexed by the 16-bit combined index; entries
-// [ade_lo, ade_hi) are dispersive, so no flag lookup is needed.
+// the next (H sweep) or previous (E sweep) quad comes from a warp shuffle; a lane at a warp edge
+// reads it itself. Every cell gets its bulk update here; the CPML corrections follow in the
+// correction passes (cpml.cu). Material coefficients come from a packed table (ca, cb, cbe,
+// beta_0) indexed by the 16-bit combined index; entries [ade_lo, ade_hi) are dispersive.
 //
 // The library is compiled with -fmad=false: every product and sum is rounded separately, as in
-// the NumPy reference (packages/oa-fdtd/src/oa_fdtd/reference.py:152-207, :119-127).
+// the NumPy reference (packages/oa-fdtd/src/oa_fdtd/reference.py:152-180, :119-127).
 
 #include "device_common.cuh"
 
 namespace oafdtd {
 
-// Where a launch's thread works: its quad and its plane range.
+// Where a thread works: its quad and its plane range.
 struct Work {
   int t;        // quad index in the flattened (y, x/4) plane
   int j, i0;
-  bool live;    // the quad holds real edges and belongs to this launch
+  bool live;    // the quad holds real edges
   bool row_end;
   int k0, k1;
 };
 
-template <typename real, int MODE>
+template <typename real>
 __device__ __forceinline__ Work work_of(const SweepArgs<real>& a) {
   const int X = a.X, Y = a.Y, X4 = X >> 2, nx = a.nx, ny = a.ny, nz = a.nz;
-  const int tz = a.tile_z;
   Work w;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  bool in_launch;
-  if (MODE == kSlabColumns) {
-    in_launch = g < a.n_slab_quads;
-    w.t = a.slab_quads[min(g, a.n_slab_quads - 1)];
-  } else {
-    in_launch = g < Y * X4;
-    w.t = min(g, Y * X4 - 1);
-  }
+  w.t = min(g, Y * X4 - 1);
   w.j = w.t / X4;
   w.i0 = (w.t - w.j * X4) * 4;
   w.row_end = w.i0 + 4 >= X;
-  bool live = in_launch && w.j >= 1 && w.j <= ny + 1 && w.i0 <= nx + 1;
-  if (MODE == kBulk && live && a.has_cpml) {
-    bool col = a.slab_y[w.j] != 0;
-#pragma unroll
-    for (int e = 0; e < 4; ++e) col |= a.slab_x[w.i0 + e] != 0;
-    live = !col;
-  }
-  w.live = live;
-  if (MODE == kSlabPlanes) {
-    const int na = (a.zi0 - 1 + tz - 1) / tz;  // chunks of [1, zi0)
-    const int c = blockIdx.y;
-    if (c < na) {
-      w.k0 = 1 + c * tz;
-      w.k1 = min(w.k0 + tz, a.zi0);
-    } else {
-      w.k0 = a.zi1 + (c - na) * tz;
-      w.k1 = min(w.k0 + tz, nz + 2);
-    }
-  } else {
-    w.k0 = a.zi0 + blockIdx.y * tz;
-    w.k1 = min(w.k0 + tz, a.zi1);
-  }
+  w.live = g < Y * X4 && w.j >= 1 && w.j <= ny + 1 && w.i0 <= nx + 1;
+  w.k0 = 1 + blockIdx.y * a.tile_z;
+  w.k1 = min(w.k0 + a.tile_z, nz + 2);
   return w;
 }
 
 // ------------------------------------------------------------------------------------- H sweep
-template <typename real, int MODE>
-__global__ void __launch_bounds__(256, MODE == kBulk ? 4 : 2) h_sweep_kernel(const __grid_constant__ SweepArgs<real> a) {
-  constexpr bool SLAB = MODE != kBulk;
-  const Work w = work_of<real, MODE>(a);
+template <typename real>
+__global__ void __launch_bounds__(256, 4) h_sweep_kernel(const __grid_constant__ SweepArgs<real> a) {
+  const Work w = work_of<real>(a);
   const int X = a.X, Y = a.Y, nx = a.nx, ny = a.ny, nz = a.nz;
   const int j = w.j, i0 = w.i0;
   const int b = blockIdx.z;
@@ -107,7 +69,6 @@ __global__ void __launch_bounds__(256, MODE == kBulk ? 4 : 2) h_sweep_kernel(con
     ex = ld4(Ex + p);
     ey = ld4(Ey + p);
   }
-  const real kd[4] = {dtmu, dtmu, dtmu, dtmu};
   for (int k = w.k0; k < w.k1; ++k, p += sz) {
     const bool kin = k <= nz;
     Quad<real> ex1 = zero4<real>(), ey1 = zero4<real>(), ez = zero4<real>();
@@ -141,7 +102,6 @@ __global__ void __launch_bounds__(256, MODE == kBulk ? 4 : 2) h_sweep_kernel(con
         const real acc = (-d0[e]) + d1[e];
         if (valid[e]) h.v[e] = h.v[e] + dtmu * acc;
       }
-      if (SLAB) cpml_quad<real, 1>(a, a.hcorr[0], a.ph, h, d0, d1, kd, valid, i0, j, k, b);
       st4(Hx + p, h);
     }
     if (kin) {  // Hy: cell along x (1..nx), node along y (1..ny+1), cell along z
@@ -158,7 +118,6 @@ __global__ void __launch_bounds__(256, MODE == kBulk ? 4 : 2) h_sweep_kernel(con
         const real acc = (-d1[e]) + d0[e];
         if (valid[e]) h.v[e] = h.v[e] + dtmu * acc;
       }
-      if (SLAB) cpml_quad<real, 1>(a, a.hcorr[1], a.ph, h, d0, d1, kd, valid, i0, j, k, b);
       st4(Hy + p, h);
     }
     if (j <= ny) {  // Hz: cell along x and y, node along z (1..nz+1)
@@ -176,7 +135,6 @@ __global__ void __launch_bounds__(256, MODE == kBulk ? 4 : 2) h_sweep_kernel(con
         const real acc = (-d0[e]) + d1[e];
         if (valid[e]) h.v[e] = h.v[e] + dtmu * acc;
       }
-      if (SLAB) cpml_quad<real, 1>(a, a.hcorr[2], a.ph, h, d0, d1, kd, valid, i0, j, k, b);
       st4(Hz + p, h);
     }
     ex = ex1;
@@ -185,10 +143,10 @@ __global__ void __launch_bounds__(256, MODE == kBulk ? 4 : 2) h_sweep_kernel(con
 }
 
 // ------------------------------------------------------------------------------------- E sweep
-// Bulk update, CPML (slab launches) and the Debye update of one E component on one quad.
+// Bulk update and the Debye update of one E component on one quad.
 // d0/d1 are the derivatives along the component's two axes in ascending order; the bulk term
 // order of the reference is (d0, -d1) when first_plus, else (d1, -d0).
-template <typename real, bool SLAB>
+template <typename real>
 __device__ __forceinline__ void e_quad(const SweepArgs<real>& a, int c, real* __restrict__ E, long long p,
                                        const Quad<uint16_t>& m, const real (&d0)[4], const real (&d1)[4],
                                        bool first_plus, int i0, int j, int k, int b) {
@@ -210,7 +168,6 @@ __device__ __forceinline__ void e_quad(const SweepArgs<real>& a, int c, real* __
     if (valid[e]) e4.v[e] = cf[e].ca * e4.v[e] + cf[e].cb * acc;
     disp |= valid[e] && m.v[e] >= a.ade_lo && m.v[e] < a.ade_hi;
   }
-  if (SLAB) cpml_quad<real, 0>(a, a.ecorr[c], a.pe, e4, d0, d1, kf, valid, i0, j, k, b);
   if (disp) {
     const long long jstride = (long long)a.B * a.jnk[c] * Y * X;
     const long long jq = (((long long)b * a.jnk[c] + (k - a.jk0[c])) * Y + j) * X + i0;
@@ -240,10 +197,9 @@ __device__ __forceinline__ void e_quad(const SweepArgs<real>& a, int c, real* __
   st4(E + p, e4);
 }
 
-template <typename real, int MODE>
-__global__ void __launch_bounds__(256, MODE == kBulk ? 3 : 2) e_sweep_kernel(const __grid_constant__ SweepArgs<real> a) {
-  constexpr bool SLAB = MODE != kBulk;
-  const Work w = work_of<real, MODE>(a);
+template <typename real>
+__global__ void __launch_bounds__(256, 3) e_sweep_kernel(const __grid_constant__ SweepArgs<real> a) {
+  const Work w = work_of<real>(a);
   const int X = a.X, Y = a.Y;
   const int j = w.j, i0 = w.i0;
   const int b = blockIdx.z;
@@ -288,7 +244,7 @@ __global__ void __launch_bounds__(256, MODE == kBulk ? 3 : 2) e_sweep_kernel(con
       d0[e] = (hz.v[e] - hzy.v[e]) * idy;
       d1[e] = (hy.v[e] - hy_m.v[e]) * idz;
     }
-    e_quad<real, SLAB>(a, 0, a.E[0] + b * bs, p, ld4(a.mat[0] + p), d0, d1, true, i0, j, k, b);
+    e_quad<real>(a, 0, a.E[0] + b * bs, p, ld4(a.mat[0] + p), d0, d1, true, i0, j, k, b);
     // Ey: terms (a = z, +Hx) then (a = x, -Hz); d0 is the x term, d1 the z term
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
@@ -296,7 +252,7 @@ __global__ void __launch_bounds__(256, MODE == kBulk ? 3 : 2) e_sweep_kernel(con
       d0[e] = (hz.v[e] - hzl) * idx4.v[e];
       d1[e] = (hx.v[e] - hx_m.v[e]) * idz;
     }
-    e_quad<real, SLAB>(a, 1, a.E[1] + b * bs, p, ld4(a.mat[1] + p), d0, d1, false, i0, j, k, b);
+    e_quad<real>(a, 1, a.E[1] + b * bs, p, ld4(a.mat[1] + p), d0, d1, false, i0, j, k, b);
     // Ez: terms (a = x, +Hy) then (a = y, -Hx)
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
@@ -304,7 +260,7 @@ __global__ void __launch_bounds__(256, MODE == kBulk ? 3 : 2) e_sweep_kernel(con
       d0[e] = (hy.v[e] - hyl) * idx4.v[e];
       d1[e] = (hx.v[e] - hxy.v[e]) * idy;
     }
-    e_quad<real, SLAB>(a, 2, a.E[2] + b * bs, p, ld4(a.mat[2] + p), d0, d1, true, i0, j, k, b);
+    e_quad<real>(a, 2, a.E[2] + b * bs, p, ld4(a.mat[2] + p), d0, d1, true, i0, j, k, b);
     hx_m = hx;
     hy_m = hy;
   }
@@ -312,65 +268,26 @@ __global__ void __launch_bounds__(256, MODE == kBulk ? 3 : 2) e_sweep_kernel(con
 
 // ------------------------------------------------------------------------------------- launchers
 template <typename real>
-static cudaError_t launch_modes(const SweepArgs<real>& a, const SweepStreams& st, bool h) {
-  if (a.staged) return launch_staged_sweep<real>(a, st.main, h);
+cudaError_t launch_h_sweep(const SweepArgs<real>& a, cudaStream_t s) {
+  if (a.staged) return launch_staged_sweep<real>(a, s, true);
   const long long quads = (long long)a.Y * (a.X / 4);
-  const int inner = a.zi1 - a.zi0;
-  const int bx = (int)((quads + 255) / 256);
-  cudaError_t err;
-  // slab launches on the side stream, concurrent with the bulk launch
-  const bool slabs = a.has_cpml != 0;
-  if (slabs) {
-    if ((err = cudaEventRecord(st.fork, st.main)) != cudaSuccess) return err;
-    if ((err = cudaStreamWaitEvent(st.side, st.fork, 0)) != cudaSuccess) return err;
-    SweepArgs<real> s = a;
-    s.tile_z = a.tile_z_slab;
-    const int tz = s.tile_z;
-    const int na = (a.zi0 - 1 + tz - 1) / tz, nb = (a.nz + 2 - a.zi1 + tz - 1) / tz;
-    if (na + nb > 0) {
-      dim3 grid(bx, na + nb, a.B);
-      if (h)
-        h_sweep_kernel<real, kSlabPlanes><<<grid, 256, 0, st.side>>>(s);
-      else
-        e_sweep_kernel<real, kSlabPlanes><<<grid, 256, 0, st.side>>>(s);
-      if ((err = cudaGetLastError()) != cudaSuccess) return err;
-    }
-    if (a.n_slab_quads > 0 && inner > 0) {
-      dim3 grid((a.n_slab_quads + 255) / 256, (inner + tz - 1) / tz, a.B);
-      if (h)
-        h_sweep_kernel<real, kSlabColumns><<<grid, 256, 0, st.side>>>(s);
-      else
-        e_sweep_kernel<real, kSlabColumns><<<grid, 256, 0, st.side>>>(s);
-      if ((err = cudaGetLastError()) != cudaSuccess) return err;
-    }
-    if ((err = cudaEventRecord(st.join, st.side)) != cudaSuccess) return err;
-  }
-  if (inner > 0) {
-    const int tz = a.tile_z;
-    dim3 grid(bx, (inner + tz - 1) / tz, a.B);
-    if (h)
-      h_sweep_kernel<real, kBulk><<<grid, 256, 0, st.main>>>(a);
-    else
-      e_sweep_kernel<real, kBulk><<<grid, 256, 0, st.main>>>(a);
-    if ((err = cudaGetLastError()) != cudaSuccess) return err;
-  }
-  if (slabs && (err = cudaStreamWaitEvent(st.main, st.join, 0)) != cudaSuccess) return err;
-  return cudaSuccess;
+  dim3 grid((unsigned)((quads + 255) / 256), (a.nz + 1 + a.tile_z - 1) / a.tile_z, a.B);
+  h_sweep_kernel<real><<<grid, 256, 0, s>>>(a);
+  return cudaGetLastError();
 }
 
 template <typename real>
-cudaError_t launch_h_sweep(const SweepArgs<real>& a, const SweepStreams& s) {
-  return launch_modes<real>(a, s, true);
+cudaError_t launch_e_sweep(const SweepArgs<real>& a, cudaStream_t s) {
+  if (a.staged) return launch_staged_sweep<real>(a, s, false);
+  const long long quads = (long long)a.Y * (a.X / 4);
+  dim3 grid((unsigned)((quads + 255) / 256), (a.nz + 1 + a.tile_z - 1) / a.tile_z, a.B);
+  e_sweep_kernel<real><<<grid, 256, 0, s>>>(a);
+  return cudaGetLastError();
 }
 
-template <typename real>
-cudaError_t launch_e_sweep(const SweepArgs<real>& a, const SweepStreams& s) {
-  return launch_modes<real>(a, s, false);
-}
-
-template cudaError_t launch_h_sweep<float>(const SweepArgs<float>&, const SweepStreams&);
-template cudaError_t launch_e_sweep<float>(const SweepArgs<float>&, const SweepStreams&);
-template cudaError_t launch_h_sweep<double>(const SweepArgs<double>&, const SweepStreams&);
-template cudaError_t launch_e_sweep<double>(const SweepArgs<double>&, const SweepStreams&);
+template cudaError_t launch_h_sweep<float>(const SweepArgs<float>&, cudaStream_t);
+template cudaError_t launch_e_sweep<float>(const SweepArgs<float>&, cudaStream_t);
+template cudaError_t launch_h_sweep<double>(const SweepArgs<double>&, cudaStream_t);
+template cudaError_t launch_e_sweep<double>(const SweepArgs<double>&, cudaStream_t);
 
 }  // namespace oafdtd

@@ -260,12 +260,10 @@ class Gb300Engine:
     def set_graph(self, on: bool) -> None:
         native.check(self._lib.oafdtd_set_graph(self._h, int(bool(on))), "set_graph")
 
-    def set_tuning(self, tile_z: int = 0, tile_z_slab: int = 0, variant: int = -1) -> None:
-        """Planes marched per thread in the bulk and the CPML-slab launches (0 keeps), and the
-        bulk variant (1 shared-memory staged, 0 register marching, -1 keeps)."""
-        native.check(
-            self._lib.oafdtd_set_tuning(self._h, int(tile_z), int(tile_z_slab), int(variant)), "set_tuning"
-        )
+    def set_tuning(self, tile_z: int = 0, variant: int = -1) -> None:
+        """Planes marched per block (0 keeps) and the sweep variant (1 shared-memory staged,
+        0 register marching, -1 keeps)."""
+        native.check(self._lib.oafdtd_set_tuning(self._h, int(tile_z), int(variant)), "set_tuning")
 
     def set_profiling(self, on: bool) -> None:
         native.check(self._lib.oafdtd_set_profiling(self._h, int(bool(on))), "set_profiling")

@@ -129,7 +129,7 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "oafdtd_fields": (C.c_int, [C.c_void_p, _i32, _pd]),
     "oafdtd_peak_bytes": (C.c_int, [C.c_void_p, _pi64]),
     "oafdtd_set_graph": (C.c_int, [C.c_void_p, _i32]),
-    "oafdtd_set_tuning": (C.c_int, [C.c_void_p, _i32, _i32, _i32]),
+    "oafdtd_set_tuning": (C.c_int, [C.c_void_p, _i32, _i32]),
     "oafdtd_set_profiling": (C.c_int, [C.c_void_p, _i32]),
     "oafdtd_kernel_times": (C.c_int, [C.c_void_p, _pd, _i32]),
     "oafdtd_model_bytes": (C.c_int, [C.c_void_p, _pd]),
