@@ -11,6 +11,13 @@
 // Every thread owns one cell (x slabs) or one quad of four x cells (y and z slabs, whose psi rows
 // are contiguous in x) and nothing else, so the passes have no carried dependency and keep many
 // loads in flight.
+//
+// Debye edges inside an E slab: the reference applies the CPML correction t before the Debye
+// update, whose current update J_p = k_p J_p + beta_p (E^{n+1} - E^n) depends on it; the sweep
+// has already done the Debye update without t. Adding t to E and beta_p t to every J_p gives the
+// same E^{n+1} and J^{n+1}; only the rounding of these edges differs from the reference's order.
+// (Dispersive edges with injection are updated by the edge pass, after the corrections, in the
+// reference's order.)
 
 #include "device_common.cuh"
 
@@ -39,9 +46,27 @@ struct CorrArgs {
   real dtmu;
   const uint16_t* mat[3];
   const Coef<real>* coef;
+  int ade_lo, ade_hi, ade_P;
+  const real* ade_beta;     // [entry * P + p]
+  real* J[3];
+  int jk0[3], jnk[3];
   int X, Y, Z, B;
   long long bs;
 };
+
+// E^{n+1} of a dispersive edge has moved by t after its Debye update: move every J_p by beta_p t.
+template <typename real>
+__device__ __forceinline__ void debye_shift(const CorrArgs<real>& a, int c, int m, real t, int b, int k, int j,
+                                            int i) {
+  if (m < a.ade_lo || m >= a.ade_hi) return;
+  const long long plane = (long long)a.Y * a.X;
+  const long long jq = ((long long)b * a.jnk[c] + (k - a.jk0[c])) * plane + (long long)j * a.X + i;
+  const long long stride = (long long)a.B * a.jnk[c] * plane;
+  for (int p = 0; p < a.ade_P; ++p) {
+    const real beta = p == 0 ? a.coef[m].beta0 : a.ade_beta[(long long)m * a.ade_P + p];
+    a.J[c][jq + p * stride] = a.J[c][jq + p * stride] + beta * t;
+  }
+}
 
 template <typename real>
 __global__ void __launch_bounds__(256) cpml_pass_kernel(const __grid_constant__ CorrArgs<real> a) {
@@ -78,8 +103,14 @@ __global__ void __launch_bounds__(256) cpml_pass_kernel(const __grid_constant__ 
       ps = ps + a.cc_[i] * d;
       it.psi[pq] = ps;
       const real upd = a.ck_[i] * d + ps;
-      const real kf = is_h ? a.dtmu : a.coef[a.mat[it.c][q]].cb;
-      it.F[p] = it.F[p] + (it.sign * kf) * upd;
+      if (is_h) {
+        it.F[p] = it.F[p] + (it.sign * a.dtmu) * upd;
+      } else {
+        const int m = a.mat[it.c][q];
+        const real tc = (it.sign * a.coef[m].cb) * upd;
+        it.F[p] = it.F[p] + tc;
+        debye_shift(a, it.c, m, tc, b, k, j, i);
+      }
     } else {
       const int i0 = q0 + 4 * xq;
       const long long q = (long long)k * X * Y + (long long)j * X + i0;
@@ -103,8 +134,13 @@ __global__ void __launch_bounds__(256) cpml_pass_kernel(const __grid_constant__ 
         v = v + pc * d;
         ps.v[e] = v;
         const real upd = pk * d + v;
-        const real kf = is_h ? a.dtmu : a.coef[m.v[e]].cb;
-        f.v[e] = f.v[e] + (it.sign * kf) * upd;
+        if (is_h) {
+          f.v[e] = f.v[e] + (it.sign * a.dtmu) * upd;
+        } else {
+          const real tc = (it.sign * a.coef[m.v[e]].cb) * upd;
+          f.v[e] = f.v[e] + tc;
+          debye_shift(a, it.c, m.v[e], tc, b, k, j, i);
+        }
       }
       st4(it.psi + pq, ps);
       st4(it.F + p, f);
@@ -147,8 +183,17 @@ cudaError_t launch_cpml_pass(const CpmlPass<real>& pass, const SweepArgs<real>& 
     c.ck_ = co[2];
     c.inv = kind == 0 ? a.idd[ax] : a.ip[ax];
     c.dtmu = a.dtmu;
-    for (int d = 0; d < 3; ++d) c.mat[d] = a.mat[d];
+    for (int d = 0; d < 3; ++d) {
+      c.mat[d] = a.mat[d];
+      c.J[d] = a.J[d];
+      c.jk0[d] = a.jk0[d];
+      c.jnk[d] = a.jnk[d];
+    }
     c.coef = a.coef;
+    c.ade_lo = a.ade_lo;
+    c.ade_hi = a.ade_hi;
+    c.ade_P = a.ade_P;
+    c.ade_beta = a.ade_beta;
     c.X = a.X;
     c.Y = a.Y;
     c.Z = a.nz + 2;

@@ -35,6 +35,24 @@ def test_report_numpy_pole_sum_order() -> None:
     print("einsum sequential:", _einsum_is_sequential())
 
 
+def _ade_in_cpml(c) -> bool:  # type: ignore[no-untyped-def]
+    """Whether a Debye edge lies inside an E CPML box: there the engine applies the correction
+    after the Debye update (adding beta t to the currents), the same result up to rounding."""
+    if c.ade is None:
+        return False
+    Y, X = c.grid.shape[1], c.grid.shape[2]
+    for comp, flat in zip(c.ade.comp, c.ade.flat, strict=True):
+        k, rem = np.divmod(np.asarray(flat), Y * X)
+        j, i = np.divmod(rem, X)
+        for corr in c.pml.corrections:
+            if corr.kind != "E" or corr.c != comp:
+                continue
+            (x0, x1), (y0, y1), (z0, z1) = corr.box
+            if np.any((i >= x0) & (i < x1) & (j >= y0) & (j < y1) & (k >= z0) & (k < z1)):
+                return True
+    return False
+
+
 def _einsum_is_sequential() -> bool:
     """Whether this host's NumPy sums Debye poles as a plain float32 loop (the kernel's order)."""
     rng = np.random.default_rng(0)
@@ -55,7 +73,7 @@ def test_fields_match_oracle(case: str, dtype: str) -> None:
     ref = OracleEngine(c, dtype)
     gpu.step(steps)
     ref.step(steps)
-    exact = case != "dispersive_copper" or _einsum_is_sequential()
+    exact = (case != "dispersive_copper" or _einsum_is_sequential()) and not _ade_in_cpml(c)
     for k, name in enumerate(NAMES):
         got = gpu.field(k)
         want = (ref.E + ref.H)[k].astype(np.float64)
@@ -63,7 +81,7 @@ def test_fields_match_oracle(case: str, dtype: str) -> None:
             assert np.array_equal(got, want), f"{name}: max |d| = {np.abs(got - want).max()}"
         else:
             rel = np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-300)
-            assert rel <= 1e-5, f"{name}: rel-L2 {rel}"
+            assert rel <= (1e-5 if dtype == "float32" else 1e-12), f"{name}: rel-L2 {rel}"
     r_gpu, r_ref = gpu.results(), ref.results()
     assert set(r_gpu) == set(r_ref)
     # identical fields: the DFTs differ only by float64 summation order; otherwise by the ulps
@@ -176,11 +194,14 @@ def test_via_transition_small_matches_oracle() -> None:
     from open_analysis_gb300.structures import via_transition
 
     c = compile_model(via_transition(nx=48, ny=40, nz=32, n_freq=16, cpml_cells=6), "float32")
+    assert _ade_in_cpml(c)  # the Debye stack reaches into the x and y slabs
     gpu = _engine(c)
     ref = OracleEngine(c, "float32")
     gpu.step(50)
     ref.step(50)
     for k in range(6):
-        assert np.array_equal(gpu.field(k), (ref.E + ref.H)[k].astype(np.float64)), NAMES[k]
+        got, want = gpu.field(k), (ref.E + ref.H)[k].astype(np.float64)
+        rel = np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-300)
+        assert rel <= 1e-5, f"{NAMES[k]}: rel-L2 {rel}"
     for name, v in ref.results().items():
-        assert np.abs(gpu.results()[name] - v).max() <= 1e-9 * max(np.abs(v).max(), 1e-300), name
+        assert np.abs(gpu.results()[name] - v).max() <= 1e-6 * max(np.abs(v).max(), 1e-300), name
