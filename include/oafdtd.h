@@ -198,6 +198,35 @@ int oafdtd_kernel_times(oafdtd_engine* engine, double* out_ms, int32_t n);
  * engine: fields, index, CPML psi, ADE J, SIBC state. Used for the roofline report. */
 int oafdtd_model_bytes(const oafdtd_engine* engine, double* out);
 
+/* Field arrays already resident on the device, described for oafdtd_energy_noalloc: the six
+ * components (E0..E2, H0..H2) of shape (batch, nz+2, ny+2, pitch) in float32 (real_bytes 4) or
+ * float64 (8), the three uint16 material index arrays (nz+2, ny+2, pitch), the relative
+ * permittivity table indexed by them, and the node and cell weights of each axis (float64, length
+ * pitch, ny+2, nz+2). All pointers are device pointers; stream may be NULL (default stream). */
+typedef struct oafdtd_energy_view {
+  int32_t real_bytes;
+  int32_t nx, ny, nz, pitch, batch;
+  const void* field[6];
+  const uint16_t* idx[3];
+  const double* eps_tab;
+  const double* node_w[3];
+  const double* cell_w[3];
+  void* stream;
+} oafdtd_energy_view;
+
+/* Field energy 1/2 sum eps E^2 V + 1/2 mu0 sum H^2 V (float64, written to the host double *out)
+ * of device-resident fields, without allocating any device memory: no cudaMalloc, cudaFree or
+ * allocating library call. For callers that cannot allocate on the device, such as a plugin
+ * whose host application owns every allocation or code that must not grow the memory pool while
+ * a graph region is open. This entry point has no counterpart in the reference.
+ * Its partial sums live in a fixed device array of 65536 doubles (512 KiB, held on every GPU that
+ * loads the library until the process exits): a problem with 6 * batch * (nz + 2) > 65536 is
+ * rejected with OAFDTD_E_INVALID. All calls share that array, so calls that overlap on the GPU
+ * race; serialise them. The first call on a device looks the array's address up for that device
+ * (make it before any stream capture). Same formula as oafdtd_energy; the summation order
+ * differs (per-plane partial sums), so results agree to float64 rounding. */
+int oafdtd_energy_noalloc(const oafdtd_energy_view* view, double* out);
+
 #ifdef __cplusplus
 }
 #endif

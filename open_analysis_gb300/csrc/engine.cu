@@ -896,6 +896,10 @@ int Engine<real>::fields(int comp, double* out) {
 
 }  // namespace
 
+namespace oafdtd {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace oafdtd
+
 struct oafdtd_engine {
   std::unique_ptr<EngineBase> impl;
 };

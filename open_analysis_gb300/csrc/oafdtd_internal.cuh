@@ -20,6 +20,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 namespace oafdtd {
 
 constexpr int kChunk = 64;        // steps per captured graph (the reference's CHUNK)
@@ -196,6 +198,9 @@ cudaError_t launch_energy(const EnergyArgs<real>& a, double* partial, int nblock
 cudaError_t launch_bump(long long* step_base, int n, cudaStream_t s);
 template <typename real>
 cudaError_t launch_staged_sweep(const SweepArgs<real>& a, cudaStream_t s, bool h);
+
+// Message returned by oafdtd_last_error() on the calling thread.
+void set_last_error(const std::string& msg);
 
 constexpr int kEnergyBlocks = 1216;  // 8 per SM on a 152-SM GB300; fixed for a deterministic sum
 

@@ -111,6 +111,25 @@ class Problem(C.Structure):
     ]
 
 
+class EnergyView(C.Structure):
+    """``oafdtd_energy_view``: device pointers of resident fields for the no-allocation energy."""
+
+    _fields_ = [
+        ("real_bytes", _i32),
+        ("nx", _i32),
+        ("ny", _i32),
+        ("nz", _i32),
+        ("pitch", _i32),
+        ("batch", _i32),
+        ("field", C.c_void_p * 6),
+        ("idx", C.c_void_p * 3),
+        ("eps_tab", C.c_void_p),
+        ("node_w", C.c_void_p * 3),
+        ("cell_w", C.c_void_p * 3),
+        ("stream", C.c_void_p),
+    ]
+
+
 # every exported symbol with its argument types; tests check the library exports exactly these
 SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "oafdtd_abi_version": (_i32, []),
@@ -133,6 +152,7 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "oafdtd_set_profiling": (C.c_int, [C.c_void_p, _i32]),
     "oafdtd_kernel_times": (C.c_int, [C.c_void_p, _pd, _i32]),
     "oafdtd_model_bytes": (C.c_int, [C.c_void_p, _pd]),
+    "oafdtd_energy_noalloc": (C.c_int, [C.POINTER(EnergyView), _pd]),
 }
 
 _lock = threading.Lock()
