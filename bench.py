@@ -309,6 +309,7 @@ def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
         ranks.barrier()
         t0 = time.perf_counter()
         eng2 = Gb300Engine(c, "float32", max_steps=max_steps)
+        t_create = time.perf_counter() - t0
         h2d = eng2.h2d_bytes
         for _ in range(args.steps):
             eng2.step(CHUNK)
@@ -323,6 +324,7 @@ def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
             "h2d_bytes_per_step": h2d / args.steps,
             "d2h_bytes_per_step": d2h / args.steps,
             "seconds": e2e_s,
+            "create_seconds": t_create,
         }
 
     cpu = None

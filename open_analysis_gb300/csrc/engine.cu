@@ -73,6 +73,7 @@ struct Engine final : EngineBase {
   int n_probe = 0, n_freq = 0, record_series = 0;
   oafdtd::SweepArgs<real> sw{};
   oafdtd::EdgeArgs<real> ed{};
+  oafdtd::SibcArgs<real> sb{};
   oafdtd::ProbeArgs<real> pr{};
   oafdtd::EnergyArgs<real> en{};
   long long* step_base = nullptr;
@@ -202,7 +203,9 @@ int Engine<real>::build(const oafdtd_problem& p) {
   // ---- combined table. Entry key: (category, material index, ADE row); categories 0 plain,
   // 1 dispersive, 2 dispersive with injection (deferred). The map orders entries by category, so
   // the kernels tell dispersive entries by an index range.
-  std::map<std::vector<uint64_t>, int> ade_row_id;  // (cbe bits, beta bits...) -> row
+  // Debye rows (cbe, beta_0..P-1) in the field precision; consecutive edges mostly share a row,
+  // so the last row is checked first and a hash map finds the others.
+  std::unordered_map<uint64_t, std::vector<int>> ade_row_by_hash;
   std::vector<std::vector<real>> ade_rows;          // cbe, beta_0..P-1
   std::vector<uint8_t> present(p.n_mat, 0);
   struct AdeEdge {
@@ -214,6 +217,22 @@ int Engine<real>::build(const oafdtd_problem& p) {
   std::vector<std::pair<int, long long>> deferred;  // (comp, flat) in component order
   int kmin[3] = {0, 0, 0}, kmax[3] = {-1, -1, -1};
   std::map<std::tuple<int, int, int>, int> entry;   // (category, v, rid) -> id
+  std::tuple<int, int, int> last_key{-1, -1, -1};
+  real row[1 + oafdtd::kMaxAdePoles];
+  int last_rid = -1;
+  auto row_id = [&]() -> int {
+    if (last_rid >= 0 && std::memcmp(row, ade_rows[last_rid].data(), sizeof(real) * (1 + P)) == 0) return last_rid;
+    uint64_t h = 1469598103934665603ull;
+    const unsigned char* bytes = reinterpret_cast<const unsigned char*>(row);
+    for (size_t q = 0; q < sizeof(real) * (1 + P); ++q) h = (h ^ bytes[q]) * 1099511628211ull;
+    std::vector<int>& bucket = ade_row_by_hash[h];
+    for (int cand : bucket)
+      if (std::memcmp(row, ade_rows[cand].data(), sizeof(real) * (1 + P)) == 0) return last_rid = cand;
+    const int rid = (int)ade_rows.size();
+    ade_rows.emplace_back(row, row + 1 + P);
+    bucket.push_back(rid);
+    return last_rid = rid;
+  };
   for (int c = 0; c < 3; ++c) {
     const uint16_t* idx = p.idx[c];
     for (long long q = 0; q < bs; ++q) {
@@ -225,27 +244,16 @@ int Engine<real>::build(const oafdtd_problem& p) {
     for (int64_t e = 0; e < ne; ++e) {
       const long long f = p.ade_flat[c][e];
       if (!in_range(f)) return fail(OAFDTD_E_INVALID, "ADE edge out of range");
-      std::vector<uint64_t> key(1 + P);
-      std::vector<real> row(1 + P);
       row[0] = (real)p.ade_cbe[c][e];
       for (int q = 0; q < P; ++q) row[1 + q] = (real)p.ade_beta[c][(size_t)q * ne + e];
-      for (int q = 0; q <= P; ++q) {
-        uint64_t bits = 0;
-        std::memcpy(&bits, &row[q], sizeof(real));
-        key[q] = bits;
-      }
-      auto it = ade_row_id.find(key);
-      int rid;
-      if (it == ade_row_id.end()) {
-        rid = (int)ade_rows.size();
-        ade_rows.push_back(row);
-        ade_row_id.emplace(key, rid);
-      } else {
-        rid = it->second;
-      }
+      const int rid = row_id();
       const int defer = injected(c, f) ? 1 : 0;
       ade_edges[c].push_back({f, rid, defer});
-      entry[{1 + defer, idx[f], rid}] = 0;
+      const std::tuple<int, int, int> key{1 + defer, idx[f], rid};
+      if (key != last_key) {
+        entry[key] = 0;
+        last_key = key;
+      }
       if (defer) deferred.emplace_back(c, f);
       const int k = (int)(f / ((long long)X * Y));
       if (kmax[c] < kmin[c]) {
@@ -285,7 +293,16 @@ int Engine<real>::build(const oafdtd_problem& p) {
     std::vector<uint16_t> m((size_t)bs);
     const uint16_t* idx = p.idx[c];
     for (long long q = 0; q < bs; ++q) m[q] = (uint16_t)plain[idx[q]];
-    for (const AdeEdge& ae : ade_edges[c]) m[ae.f] = (uint16_t)entry[{1 + ae.defer, idx[ae.f], ae.rid}];
+    std::tuple<int, int, int> lk{-1, -1, -1};
+    int lid = 0;
+    for (const AdeEdge& ae : ade_edges[c]) {
+      const std::tuple<int, int, int> key{1 + ae.defer, idx[ae.f], ae.rid};
+      if (key != lk) {
+        lid = entry[key];
+        lk = key;
+      }
+      m[ae.f] = (uint16_t)lid;
+    }
     uint16_t* dm = nullptr;
     int rc = upload_vec(&dm, m);
     if (rc) return rc;
@@ -468,22 +485,22 @@ int Engine<real>::build(const oafdtd_problem& p) {
     std::vector<int8_t> comp;
     std::vector<long long> flat, dflat;
     std::vector<int8_t> dcomp;
-    std::vector<int> sslot, ibeg, iend, dslot, ichan;
+    std::vector<int> ibeg, iend, dslot, ichan;
     std::vector<double> iamp;
     std::vector<std::pair<int, long long>> def_sorted = deferred;
     std::sort(def_sorted.begin(), def_sorted.end());
     for (auto& kv : edges) {
       EdgeRec& r = kv.second;
+      const bool is_def = std::binary_search(def_sorted.begin(), def_sorted.end(), kv.first);
+      if (r.inj.empty() && !is_def) continue;  // surface impedance only: the SIBC pass covers it
       comp.push_back((int8_t)r.comp);
       flat.push_back(r.flat);
-      sslot.push_back(r.sibc);
       ibeg.push_back((int)ichan.size());
       for (int t : r.inj) {
         ichan.push_back(p.inj_chan[t]);
         iamp.push_back(p.inj_amp[t]);
       }
       iend.push_back((int)ichan.size());
-      const bool is_def = std::binary_search(def_sorted.begin(), def_sorted.end(), kv.first);
       if (is_def) {
         dslot.push_back((int)dflat.size());
         dflat.push_back(r.flat);
@@ -502,8 +519,6 @@ int Engine<real>::build(const oafdtd_problem& p) {
     ed.comp = d8;
     if ((rc = upload_vec(&dll, flat))) return rc;
     ed.flat = dll;
-    if ((rc = upload_vec(&di, sslot))) return rc;
-    ed.sibc_slot = di;
     if ((rc = upload_vec(&di, ibeg))) return rc;
     ed.inj_beg = di;
     if ((rc = upload_vec(&di, iend))) return rc;
@@ -523,18 +538,25 @@ int Engine<real>::build(const oafdtd_problem& p) {
     if ((rc = alloc(&eold, (size_t)B * std::max<size_t>(dflat.size(), 1)))) return rc;
     ed.eold = pr.eold = eold;
   }
-  // surface impedance tables
+  // surface impedance: one packed record per edge, in the compiled order
   {
     const int ns = (int)p.sibc_n, SP = p.sibc_poles;
-    ed.sibc_n = ns;
-    ed.sibc_P = SP;
-    std::vector<int> hc(2 * (size_t)ns);
-    std::vector<long long> hf(2 * (size_t)ns);
-    std::vector<real> hs(2 * (size_t)ns);
-    for (int64_t k = 0; k < 2 * p.sibc_n; ++k) {
-      hc[k] = p.sibc_hcomp[k];
-      hf[k] = p.sibc_hflat[k];
-      hs[k] = (real)p.sibc_hsign[k];
+    if (bs > 2147483647LL) return fail(OAFDTD_E_INVALID, "storage larger than 2^31 cells per member");
+    sb.n = ns;
+    sb.P = SP;
+    std::vector<oafdtd::SibcEdge<real>> recs((size_t)std::max(ns, 1));
+    for (int64_t k = 0; k < p.sibc_n; ++k) {
+      oafdtd::SibcEdge<real>& r = recs[k];
+      r.flat = (int)p.sibc_flat[k];
+      r.comp = (unsigned char)p.sibc_comp[k];
+      r.mat = p.sibc_mat[k];
+      for (int q = 0; q < 2; ++q) {
+        r.sign[q] = (real)p.sibc_hsign[2 * k + q];
+        r.hflat[q] = r.sign[q] != (real)0 ? (int)p.sibc_hflat[2 * k + q] : 0;
+      }
+      r.hcomp0 = (unsigned char)p.sibc_hcomp[2 * k];
+      r.hcomp1 = (unsigned char)p.sibc_hcomp[2 * k + 1];
+      r.pad = 0;
     }
     std::vector<real> r0(std::max(p.sibc_nmat, 1)), alpha(std::max(p.sibc_nmat * SP, 1)), gp(std::max(SP, 1));
     for (int m = 0; m < p.sibc_nmat; ++m) {
@@ -542,29 +564,21 @@ int Engine<real>::build(const oafdtd_problem& p) {
       for (int q = 0; q < SP; ++q) alpha[m * SP + q] = (real)(p.sibc_rp[m * SP + q] * p.sibc_cp[q]);
     }
     for (int q = 0; q < SP; ++q) gp[q] = (real)p.sibc_gp[q];
-    std::vector<int> smat(p.sibc_mat, p.sibc_mat + p.sibc_n);
     int rc;
-    int* di = nullptr;
-    long long* dll = nullptr;
+    oafdtd::SibcEdge<real>* dre = nullptr;
     real* dr = nullptr;
-    if ((rc = upload_vec(&di, hc))) return rc;
-    ed.s_hcomp = di;
-    if ((rc = upload_vec(&dll, hf))) return rc;
-    ed.s_hflat = dll;
-    if ((rc = upload_vec(&dr, hs))) return rc;
-    ed.s_hsign = dr;
-    if ((rc = upload_vec(&di, smat))) return rc;
-    ed.s_mat = di;
+    if ((rc = upload_vec(&dre, recs))) return rc;
+    sb.edge = dre;
     if ((rc = upload_vec(&dr, r0))) return rc;
-    ed.s_r0 = dr;
+    sb.r0 = dr;
     if ((rc = upload_vec(&dr, alpha))) return rc;
-    ed.s_alpha = dr;
+    sb.alpha = dr;
     if ((rc = upload_vec(&dr, gp))) return rc;
-    ed.s_gp = dr;
+    sb.gp = dr;
     if ((rc = alloc(&dr, (size_t)B * std::max(ns, 1)))) return rc;
-    ed.s_jprev = dr;
+    sb.jprev = dr;
     if ((rc = alloc(&dr, (size_t)SP * B * std::max(ns, 1)))) return rc;
-    ed.s_v = dr;
+    sb.v = dr;
   }
   // sources
   {
@@ -581,13 +595,16 @@ int Engine<real>::build(const oafdtd_problem& p) {
   for (int c = 0; c < 3; ++c) {
     ed.E[c] = sw.E[c];
     ed.H[c] = sw.H[c];
+    sb.E[c] = sw.E[c];
+    sb.H[c] = sw.H[c];
     pr.E[c] = sw.E[c];
     pr.F[c] = sw.E[c];
     pr.F[3 + c] = sw.H[c];
     en.F[c] = sw.E[c];
     en.F[3 + c] = sw.H[c];
   }
-  ed.bs = pr.bs = bs;
+  ed.bs = pr.bs = sb.bs = bs;
+  sb.B = B;
   ed.X = X;
   ed.Y = Y;
   ed.B = pr.B = en.B = B;
@@ -719,7 +736,8 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing) {
   if (err == cudaSuccess && sw.has_cpml) err = oafdtd::launch_cpml_pass<real>(cpml, sw, 0, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("e_sweep: ") + cudaGetErrorString(err));
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[4], stream, rec));
-  err = oafdtd::launch_edges<real>(ed, off, stream);
+  err = oafdtd::launch_sibc<real>(sb, stream);
+  if (err == cudaSuccess) err = oafdtd::launch_edges<real>(ed, off, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("edges: ") + cudaGetErrorString(err));
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[5], stream, rec));
   err = oafdtd::launch_probe_e<real>(pr, off, stream);

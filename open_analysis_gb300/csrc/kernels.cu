@@ -5,7 +5,8 @@
 //  * ghosts: PMC mirror planes, one launch per wall in wall order.
 //  * pre_e: H probe sums + running DFT at (n + 1/2) dt; saves E^n of dispersive edges that also
 //    receive injection (their ADE update runs after the injection, in the edge pass).
-//  * edges: surface impedance, injection and the deferred ADE updates on the edge list.
+//  * sibc, edges: surface impedance on its edge list, then injection and the deferred Debye
+//    updates on theirs.
 //  * probe_e: E probe sums + running DFT at (n + 1) dt.
 //
 // Arithmetic follows the reference engine (packages/oa-fdtd/src/oa_fdtd/reference.py:115-249)
@@ -101,7 +102,59 @@ __global__ void __launch_bounds__(256) probe_e_kernel(const __grid_constant__ Pr
   probe_block(a, a.list[0][pi], b, step, 1.0);
 }
 
-// ----------------------------------------------------------------------------- edge pass
+// ----------------------------------------------------------------------------- surface impedance
+// E_face = r0 J + sum_p v_p, v_p = alpha_p (J - J_prev) + g_p v_p, J = sum of the signed outside
+// H samples (reference.py:129-150). One thread per edge handles every batch member; BB and PP
+// unroll the batch and pole loops so all loads of an edge are issued together.
+template <typename real, int BB, int PP>
+__global__ void __launch_bounds__(128) sibc_kernel(const __grid_constant__ SibcArgs<real> a) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.n) return;
+  const int B = BB > 0 ? BB : a.B;  // compile-time when specialised: the loops unroll
+  const int P = PP > 0 ? PP : a.P;
+  const SibcEdge<real> ed = a.edge[s];
+  const real* r0 = a.r0;
+  const real* alpha = a.alpha + (long long)ed.mat * P;
+  const long long n = a.n;
+#pragma unroll
+  for (int b = 0; b < B; ++b) {
+    const long long off = (long long)b * a.bs;
+    real jj = (real)0;
+    if (ed.sign[0] != (real)0) jj = jj + ed.sign[0] * a.H[ed.hcomp0][off + ed.hflat[0]];
+    if (ed.sign[1] != (real)0) jj = jj + ed.sign[1] * a.H[ed.hcomp1][off + ed.hflat[1]];
+    const long long be = (long long)b * n + s;
+    const real dj = jj - a.jprev[be];
+    real vsum = (real)0;
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      real* vp = a.v + ((long long)p * B) * n + be;
+      const real nv = alpha[p] * dj + a.gp[p] * (*vp);
+      *vp = nv;
+      vsum = p == 0 ? nv : vsum + nv;
+    }
+    a.jprev[be] = jj;
+    a.E[ed.comp][off + ed.flat] = r0[ed.mat] * jj + vsum;
+  }
+}
+
+template <typename real>
+cudaError_t launch_sibc(const SibcArgs<real>& a, cudaStream_t s) {
+  if (a.n == 0) return cudaSuccess;
+  const unsigned blocks = (unsigned)((a.n + 127) / 128);
+  if (a.B == 2 && a.P == 16)
+    sibc_kernel<real, 2, 16><<<blocks, 128, 0, s>>>(a);
+  else if (a.B == 1 && a.P == 16)
+    sibc_kernel<real, 1, 16><<<blocks, 128, 0, s>>>(a);
+  else if (a.B == 4 && a.P == 16)
+    sibc_kernel<real, 4, 16><<<blocks, 128, 0, s>>>(a);
+  else
+    sibc_kernel<real, 0, 0><<<blocks, 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// ----------------------------------------------------------------------------- injection pass
+// Injection (reference.py:223-234) and the Debye update of dispersive edges with injection
+// (reference.py:119-127), in the reference's order after the surface impedance.
 template <typename real>
 __global__ void __launch_bounds__(128) edge_kernel(const __grid_constant__ EdgeArgs<real> a, int off) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -109,36 +162,11 @@ __global__ void __launch_bounds__(128) edge_kernel(const __grid_constant__ EdgeA
   const long long step = *a.step_base + off;
   const int c = a.comp[e];
   const long long f = a.flat[e];
-  const int ss = a.sibc_slot[e];
   const int ib = a.inj_beg[e], ie = a.inj_end[e];
   const int ds = a.def_slot[e];
-  const int ns = a.sibc_n, P = a.sibc_P;
   for (int b = 0; b < a.B; ++b) {
     real* Ec = a.E[c] + (long long)b * a.bs;
     real val = Ec[f];
-    if (ss >= 0) {
-      // J = sum of the signed outside H samples; v_p = alpha_p (J - J_prev) + g_p v_p;
-      // E = r0 J + sum_p v_p  (reference.py:129-150)
-      real jj = (real)0;
-#pragma unroll
-      for (int s = 0; s < 2; ++s) {
-        const real sg = a.s_hsign[2 * ss + s];
-        if (sg != (real)0)
-          jj = jj + sg * a.H[a.s_hcomp[2 * ss + s]][(long long)b * a.bs + a.s_hflat[2 * ss + s]];
-      }
-      const int m = a.s_mat[ss];
-      const long long be = (long long)b * ns + ss;
-      const real dj = jj - a.s_jprev[be];
-      real vsum = (real)0;
-      for (int p = 0; p < P; ++p) {
-        real* vp = a.s_v + (long long)p * a.B * ns + be;
-        const real nv = a.s_alpha[m * P + p] * dj + a.s_gp[p] * (*vp);
-        *vp = nv;
-        vsum = p == 0 ? nv : vsum + nv;
-      }
-      a.s_jprev[be] = jj;
-      val = a.s_r0[m] * jj + vsum;
-    }
     for (int t = ib; t < ie; ++t) {
       const int ch = a.i_chan[t];
       const double w = a.wave[(long long)ch * a.max_steps + step];
@@ -284,6 +312,7 @@ cudaError_t launch_bump(long long* step_base, int n, cudaStream_t s) {
   template cudaError_t launch_pre_e<real>(const ProbeArgs<real>&, int, cudaStream_t);              \
   template cudaError_t launch_probe_e<real>(const ProbeArgs<real>&, int, cudaStream_t);            \
   template cudaError_t launch_edges<real>(const EdgeArgs<real>&, int, cudaStream_t);               \
+  template cudaError_t launch_sibc<real>(const SibcArgs<real>&, cudaStream_t);                      \
   template cudaError_t launch_energy<real>(const EnergyArgs<real>&, double*, int, double*,         \
                                            cudaStream_t);
 

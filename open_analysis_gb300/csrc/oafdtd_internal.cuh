@@ -92,28 +92,43 @@ struct SweepArgs {
   int staged;       // 1: shared-memory staged sweeps; 0: register marching
 };
 
+// One surface-impedance edge: the E edge it sets and its two outside H samples (weight 0: unused).
+template <typename real>
+struct __align__(16) SibcEdge {
+  int flat;                  // storage index of the E edge (one batch member)
+  int hflat[2];
+  int mat;                   // row of the impedance tables
+  real sign[2];
+  unsigned char comp, hcomp0, hcomp1, pad;
+};
+
+template <typename real>
+struct SibcArgs {
+  real* E[3];
+  const real* H[3];
+  int n, P;                  // edges, poles
+  const SibcEdge<real>* edge;
+  const real* r0;            // [m]
+  const real* alpha;         // [m * P + p] = rp * cp (rounded once to the field precision)
+  const real* gp;            // [p]
+  real* jprev;               // (B, n)
+  real* v;                   // (P, B, n)
+  long long bs;
+  int B;
+};
+
+// Injection and the Debye update of dispersive edges with injection, after the surface
+// impedance pass, on the edges that have either.
 template <typename real>
 struct EdgeArgs {
   real* E[3];
   const real* H[3];
-  int n;                     // union edges
+  int n;                     // edges of this list
   const int8_t* comp;
   const long long* flat;
-  const int* sibc_slot;      // -1: none
   const int* inj_beg;
   const int* inj_end;
   const int* def_slot;       // -1: none
-  // surface impedance
-  int sibc_n, sibc_P;
-  const int* s_hcomp;        // (ns, 2)
-  const long long* s_hflat;  // (ns, 2)
-  const real* s_hsign;       // (ns, 2)
-  const int* s_mat;
-  const real* s_r0;          // [m]
-  const real* s_alpha;       // [m * P + p] = rp * cp (rounded once to the field precision)
-  const real* s_gp;          // [p]
-  real* s_jprev;             // (B, ns)
-  real* s_v;                 // (P, B, ns)
   // injection contributions, ordered by edge then channel
   const int* i_chan;
   const double* i_amp;
@@ -190,6 +205,8 @@ template <typename real>
 cudaError_t launch_pre_e(const ProbeArgs<real>& a, int off, cudaStream_t s);
 template <typename real>
 cudaError_t launch_edges(const EdgeArgs<real>& a, int off, cudaStream_t s);
+template <typename real>
+cudaError_t launch_sibc(const SibcArgs<real>& a, cudaStream_t s);
 template <typename real>
 cudaError_t launch_probe_e(const ProbeArgs<real>& a, int off, cudaStream_t s);
 template <typename real>
