@@ -110,13 +110,52 @@ template <typename real, int BB, int PP>
 __global__ void __launch_bounds__(128) sibc_kernel(const __grid_constant__ SibcArgs<real> a) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= a.n) return;
-  const int B = BB > 0 ? BB : a.B;  // compile-time when specialised: the loops unroll
-  const int P = PP > 0 ? PP : a.P;
   const SibcEdge<real> ed = a.edge[s];
-  const real* r0 = a.r0;
-  const real* alpha = a.alpha + (long long)ed.mat * P;
+  const real* __restrict__ alpha = a.alpha + (long long)ed.mat * PP;
   const long long n = a.n;
+  // every load of this edge first (the stores below would otherwise order them one by one)
+  real vv[BB][PP], hs[BB][2], jp[BB];
 #pragma unroll
+  for (int b = 0; b < BB; ++b) {
+    const long long off = (long long)b * a.bs;
+    const long long be = (long long)b * n + s;
+    hs[b][0] = ed.sign[0] != (real)0 ? a.H[ed.hcomp0][off + ed.hflat[0]] : (real)0;
+    hs[b][1] = ed.sign[1] != (real)0 ? a.H[ed.hcomp1][off + ed.hflat[1]] : (real)0;
+    jp[b] = a.jprev[be];
+#pragma unroll
+    for (int p = 0; p < PP; ++p) vv[b][p] = a.v[((long long)p * BB) * n + be];
+  }
+  const real r0 = a.r0[ed.mat];
+#pragma unroll
+  for (int b = 0; b < BB; ++b) {
+    real jj = (real)0;
+    if (ed.sign[0] != (real)0) jj = jj + ed.sign[0] * hs[b][0];
+    if (ed.sign[1] != (real)0) jj = jj + ed.sign[1] * hs[b][1];
+    const real dj = jj - jp[b];
+    real vsum = (real)0;
+#pragma unroll
+    for (int p = 0; p < PP; ++p) {
+      const real nv = alpha[p] * dj + a.gp[p] * vv[b][p];
+      vv[b][p] = nv;
+      vsum = p == 0 ? nv : vsum + nv;
+    }
+    const long long be = (long long)b * n + s;
+#pragma unroll
+    for (int p = 0; p < PP; ++p) a.v[((long long)p * BB) * n + be] = vv[b][p];
+    a.jprev[be] = jj;
+    a.E[ed.comp][(long long)b * a.bs + ed.flat] = r0 * jj + vsum;
+  }
+}
+
+// Any batch size and pole count (loops not unrolled).
+template <typename real>
+__global__ void __launch_bounds__(128) sibc_generic_kernel(const __grid_constant__ SibcArgs<real> a) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.n) return;
+  const SibcEdge<real> ed = a.edge[s];
+  const int B = a.B, P = a.P;
+  const real* __restrict__ alpha = a.alpha + (long long)ed.mat * P;
+  const long long n = a.n;
   for (int b = 0; b < B; ++b) {
     const long long off = (long long)b * a.bs;
     real jj = (real)0;
@@ -125,7 +164,6 @@ __global__ void __launch_bounds__(128) sibc_kernel(const __grid_constant__ SibcA
     const long long be = (long long)b * n + s;
     const real dj = jj - a.jprev[be];
     real vsum = (real)0;
-#pragma unroll
     for (int p = 0; p < P; ++p) {
       real* vp = a.v + ((long long)p * B) * n + be;
       const real nv = alpha[p] * dj + a.gp[p] * (*vp);
@@ -133,7 +171,7 @@ __global__ void __launch_bounds__(128) sibc_kernel(const __grid_constant__ SibcA
       vsum = p == 0 ? nv : vsum + nv;
     }
     a.jprev[be] = jj;
-    a.E[ed.comp][off + ed.flat] = r0[ed.mat] * jj + vsum;
+    a.E[ed.comp][off + ed.flat] = a.r0[ed.mat] * jj + vsum;
   }
 }
 
@@ -148,7 +186,7 @@ cudaError_t launch_sibc(const SibcArgs<real>& a, cudaStream_t s) {
   else if (a.B == 4 && a.P == 16)
     sibc_kernel<real, 4, 16><<<blocks, 128, 0, s>>>(a);
   else
-    sibc_kernel<real, 0, 0><<<blocks, 128, 0, s>>>(a);
+    sibc_generic_kernel<real><<<blocks, 128, 0, s>>>(a);
   return cudaGetLastError();
 }
 
