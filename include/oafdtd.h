@@ -184,8 +184,11 @@ int oafdtd_peak_bytes(const oafdtd_engine* engine, int64_t* out);
 int oafdtd_set_graph(oafdtd_engine* engine, int32_t use_graph);
 
 /* Launch shape of the sweeps: z planes marched per block (tile_z, 0 keeps the current value) and
- * the sweep variant (1 stages the planes through shared memory, the default; 0 marches them in
- * registers; -1 keeps it). The autotuner sets these. */
+ * the sweep variant (2 stages the planes through shared memory with TMA tensor copies, the
+ * default where the driver encodes the descriptors; 1 stages them with cp.async; 0 marches them
+ * in registers; -1 keeps it). Variant 2 without descriptors is OAFDTD_E_INVALID. The autotuner
+ * sets these. A staged sweep whose copies do not arrive within its bounded wait makes the step
+ * return OAFDTD_E_TIMEOUT. */
 int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_z, int32_t variant);
 
 /* Average device time per step of each kernel class over the last oafdtd_step call, measured

@@ -55,7 +55,8 @@ struct EngineBase {
   int use_graph = 1;
   int profiling = 0;
   int tile_z = 16;
-  int staged = 1;  // bulk sweeps staged through shared memory (0: register marching)
+  int staged = 2;     // 2: sweeps staged by TMA; 1: staged by cp.async; 0: register marching
+  bool tma_ok = false;  // the TMA descriptors were encoded (variant 2 available)
   bool graph_dirty = false;  // launch shape or profiling changed: the graph is re-captured
   double model_bytes = 0.0;
 };
@@ -72,6 +73,8 @@ struct Engine final : EngineBase {
   int max_steps = 0;
   int n_probe = 0, n_freq = 0, record_series = 0;
   oafdtd::SweepArgs<real> sw{};
+  oafdtd::SweepMaps maps{};
+  int* status = nullptr;  // device status word of the bounded waits
   oafdtd::EdgeArgs<real> ed{};
   oafdtd::SibcArgs<real> sb{};
   oafdtd::ProbeArgs<real> pr{};
@@ -139,6 +142,7 @@ struct Engine final : EngineBase {
   int capture();
 
   int step(int64_t n) override;
+  int check_status();
   int energy(double* out) override;
   int dft(double* out) override;
   int series(double* out) override;
@@ -439,6 +443,13 @@ int Engine<real>::build(const oafdtd_problem& p) {
   sw.bs = bs;
   sw.B = B;
   sw.tile_z = tile_z;
+  if (int rc = alloc(&status, 1)) return rc;
+  sw.status = status;
+  {
+    std::string why;
+    tma_ok = oafdtd::encode_sweep_maps<real>(sw, &maps, &why);
+    if (!tma_ok && staged == 2) staged = 1;
+  }
   sw.staged = staged;
 
   // ---- edge list: surface impedance, injection targets, deferred ADE edges
@@ -720,7 +731,7 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing) {
   // inside a stream capture an event record becomes a graph node only with the external flag
   const unsigned rec = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[0], stream, rec));
-  err = oafdtd::launch_h_sweep<real>(sw, stream);
+  err = oafdtd::launch_h_sweep<real>(sw, maps, stream);
   if (err == cudaSuccess && sw.has_cpml) err = oafdtd::launch_cpml_pass<real>(cpml, sw, 1, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("h_sweep: ") + cudaGetErrorString(err));
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[1], stream, rec));
@@ -732,7 +743,7 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing) {
   err = oafdtd::launch_pre_e<real>(pr, off, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("pre_e: ") + cudaGetErrorString(err));
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[3], stream, rec));
-  err = oafdtd::launch_e_sweep<real>(sw, stream);
+  err = oafdtd::launch_e_sweep<real>(sw, maps, stream);
   if (err == cudaSuccess && sw.has_cpml) err = oafdtd::launch_cpml_pass<real>(cpml, sw, 0, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("e_sweep: ") + cudaGetErrorString(err));
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[4], stream, rec));
@@ -833,6 +844,15 @@ int Engine<real>::step(int64_t n) {
   }
   OA_CUDA(cudaStreamSynchronize(stream));
   OA_CUDA(cudaGetLastError());
+  return check_status();
+}
+
+template <typename real>
+int Engine<real>::check_status() {
+  int word = 0;
+  OA_CUDA(cudaMemcpy(&word, status, sizeof(word), cudaMemcpyDeviceToHost));
+  if (word & oafdtd::kStatusWaitTimeout)
+    return fail(OAFDTD_E_TIMEOUT, "a staged sweep gave up waiting for its plane copies (bounded mbarrier wait)");
   return OAFDTD_OK;
 }
 
@@ -1051,7 +1071,9 @@ int oafdtd_set_graph(oafdtd_engine* engine, int32_t use_graph) {
 int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_z, int32_t variant) {
   if (!engine) return fail(OAFDTD_E_INVALID, "null engine");
   if (tile_z < 0 || tile_z > 4096) return fail(OAFDTD_E_INVALID, "tile_z must be 0..4096 planes");
-  if (variant < -1 || variant > 1) return fail(OAFDTD_E_INVALID, "variant must be -1, 0 or 1");
+  if (variant < -1 || variant > 2) return fail(OAFDTD_E_INVALID, "variant must be -1, 0, 1 or 2");
+  if (variant == 2 && !engine->impl->tma_ok)
+    return fail(OAFDTD_E_INVALID, "variant 2 needs TMA descriptors, which the driver did not encode");
   if (tile_z) engine->impl->tile_z = tile_z;
   if (variant >= 0) engine->impl->staged = variant;
   engine->impl->graph_dirty = true;  // a new launch shape needs a new graph

@@ -17,6 +17,7 @@
 //    (component, flat index), one thread per edge.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (the descriptors are encoded through the runtime's driver entry point)
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -89,8 +90,20 @@ struct SweepArgs {
   long long bs;             // Z * Y * X
   int B;
   int tile_z;       // planes marched per thread (register variant) or per block (staged)
-  int staged;       // 1: shared-memory staged sweeps; 0: register marching
+  int staged;       // 2: staged by TMA tensor copies; 1: staged by cp.async; 0: register marching
+  int* status;      // device status word: bit 0 set when a bounded wait of a sweep gave up
 };
+
+// TMA descriptors of the staged sweeps: per component, the field arrays as 4-D tensors
+// (x, y, z, batch) with a wide box (132 x 9: the tile plus its one-quad / one-row halo) and a
+// tile box (128 x 8), and the material index arrays (x, y, z) with a 128 x 8 box.
+struct SweepMaps {
+  CUtensorMap e_wide[3], e_tile[3];
+  CUtensorMap h_wide[3], h_tile[3];
+  CUtensorMap mat[3];
+};
+
+constexpr int kStatusWaitTimeout = 1;
 
 // One surface-impedance edge: the E edge it sets and its two outside H samples (weight 0: unused).
 template <typename real>
@@ -193,9 +206,9 @@ struct EnergyArgs {
 
 // kernel launchers (kernels.cu)
 template <typename real>
-cudaError_t launch_h_sweep(const SweepArgs<real>& a, cudaStream_t s);
+cudaError_t launch_h_sweep(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_t s);
 template <typename real>
-cudaError_t launch_e_sweep(const SweepArgs<real>& a, cudaStream_t s);
+cudaError_t launch_e_sweep(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_t s);
 template <typename real>
 cudaError_t launch_cpml_pass(const CpmlPass<real>& pass, const SweepArgs<real>& a, int kind, cudaStream_t s);
 template <typename real>
@@ -214,7 +227,11 @@ cudaError_t launch_energy(const EnergyArgs<real>& a, double* partial, int nblock
                           cudaStream_t s);
 cudaError_t launch_bump(long long* step_base, int n, cudaStream_t s);
 template <typename real>
-cudaError_t launch_staged_sweep(const SweepArgs<real>& a, cudaStream_t s, bool h);
+cudaError_t launch_staged_sweep(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_t s, bool h);
+// Encodes the TMA descriptors of the staged sweeps for the fields and indices in a; false (with
+// a message) when the driver entry point is missing or rejects a descriptor.
+template <typename real>
+bool encode_sweep_maps(const SweepArgs<real>& a, SweepMaps* m, std::string* why);
 
 // Message returned by oafdtd_last_error() on the calling thread.
 void set_last_error(const std::string& msg);

@@ -1,17 +1,27 @@
-// Sweeps with the planes staged through shared memory by a cp.async pipeline (the default
-// variant).
+// Sweeps with the planes staged through shared memory (variants 1 and 2; the default is 2).
 //
 // A block owns a 2-D tile of 32 quads (128 x cells) by 8 rows and marches up a chunk of z
 // planes. Each plane's inputs (the tile plus the one-cell halo the curl needs) are copied into a
-// ring of three shared-memory slots with 16-byte cp.async copies, two planes ahead of the plane
-// being computed, so every SM keeps ~100 KB of loads in flight without holding them in
-// registers; the Debye currents of the next plane are prefetched into registers. Neighbours in
-// x and y are read from the staged tile; results go straight to global memory.
+// ring of three shared-memory slots, two planes ahead of the plane being computed, so every SM
+// keeps ~130 KB of loads in flight without holding them in registers; the Debye currents of the
+// next plane are prefetched into registers. Neighbours in x and y are read from the staged tile;
+// results go straight to global memory.
+//
+// Variant 2 moves each array of a plane with one TMA tensor copy (cp.async.bulk.tensor) issued
+// by one thread and completing on the slot's mbarrier; parts of a box past the grid are
+// zero-filled. Variant 1 spreads 16-byte cp.async copies over the block and leaves those parts
+// unwritten. Either way the cells they feed are never updated.
+//
+// Every mbarrier wait is bounded (about two seconds): a block whose copies do not arrive sets
+// bit 0 of the status word, waits (bounded again) for the copies it issued and returns; the host
+// reports OAFDTD_E_TIMEOUT.
 //
 // One launch per sweep gives every cell its bulk update (and, in the E sweep, its Debye update);
 // the CPML corrections follow in the correction passes (cpml.cu). The arithmetic is the
 // reference's, operation by operation (packages/oa-fdtd/src/oa_fdtd/reference.py:152-180,
 // :119-127).
+
+#include <mutex>
 
 #include "device_common.cuh"
 
@@ -23,16 +33,109 @@ constexpr int kTW = 4 * kTQ;  // tile width in cells
 constexpr int kHW = kTW + 4;  // staged width with a one-quad halo
 constexpr int kStages = 3;
 
-// ------------------------------------------------------------------------------------- H sweep
-// Slot: E[3][kTY + 1][kHW] (rows y0..y0+8, x0..x0+131), H[3][kTY][kTW].
-template <typename real>
-struct HSlot {
-  real e[3][kTY + 1][kHW];
-  real h[3][kTY][kTW];
+// One staged array: rows x width, dense (the layout a TMA box lands in), 128-byte aligned.
+template <typename T, int R, int W>
+struct alignas(128) Box {
+  T v[R][W];
 };
 
-// Stage plane k: E for k <= k1 (plane k1 only feeds the z derivative of plane k1 - 1), H for
-// k < k1.
+// ------------------------------------------------------------------------------ TMA + mbarrier
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+  return t;
+}
+constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s: far above any plane's copy time
+constexpr unsigned long long kDrainNs = 100000000ull;  // 0.1 s per copy still in flight at abort
+constexpr unsigned kWaitPolls = 1u << 28;              // hard cap on polls whatever the timer says
+
+// Waits for the phase of the given parity; false when the time or poll limit ran out.
+__device__ __noinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, unsigned long long limit_ns) {
+  const unsigned long long t0 = global_ns();
+  for (unsigned n = 0; n < kWaitPolls; ++n) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((n & 63u) == 63u && global_ns() - t0 > limit_ns) return false;
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load4(void* dst, const CUtensorMap* map, unsigned long long* bar, int x, int y,
+                                          int z, int w) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* map, unsigned long long* bar, int x, int y,
+                                          int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void prefetch_map(const CUtensorMap* map) {
+  asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<unsigned long long>(map)) : "memory");
+}
+// Barrier setup of the block's leader, made visible to the TMA unit before the first copy.
+__device__ __forceinline__ void mbar_setup(unsigned long long* bar) {
+#pragma unroll
+  for (int s = 0; s < kStages; ++s) mbar_init(&bar[s], 1);
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+// Orders the block's reads of a slot (generic proxy) before the TMA writes that refill it.
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+
+// Plane t of a block's march uses slot t % 3 in phase (t / 3) & 1.
+__device__ __forceinline__ bool wait_plane(unsigned long long* bar, int t) {
+  return mbar_wait(&bar[t % kStages], (unsigned)((t / kStages) & 1), kWaitNs);
+}
+
+// A wait gave up: the leader records it and waits (bounded) for the planes [t, issued) it has
+// issued and not yet seen arrive, so no copy lands after the block has exited.
+__device__ __noinline__ void abort_march(unsigned long long* bar, int t, int issued, int* status, bool leader) {
+  if (!leader) return;
+  if (status) atomicOr(status, kStatusWaitTimeout);
+  for (int p = t; p < issued; ++p) mbar_wait(&bar[p % kStages], (unsigned)((p / kStages) & 1), kDrainNs);
+}
+
+__device__ __forceinline__ unsigned char* align_smem(unsigned char* raw) {
+  return raw + ((128u - (smem_addr(raw) & 127u)) & 127u);
+}
+
+// ------------------------------------------------------------------------------------- H sweep
+// Slot: E[3] rows y0..y0+8, x0..x0+131; H[3] rows y0..y0+7, x0..x0+127.
+template <typename real>
+struct HSlot {
+  Box<real, kTY + 1, kHW> e[3];
+  Box<real, kTY, kTW> h[3];
+};
+
+// Planes k0..k1 are staged: E for all of them (plane k1 only feeds the z derivative of plane
+// k1 - 1), H for k < k1.
 template <typename real>
 __device__ __forceinline__ void h_stage(const SweepArgs<real>& a, HSlot<real>& s, int b, int k, int k1, int x0,
                                         int y0) {
@@ -50,114 +153,155 @@ __device__ __forceinline__ void h_stage(const SweepArgs<real>& a, HSlot<real>& s
       const int c = t / CQ / (kHW / 4) / (kTY + 1);
       const int x = x0 + 4 * q, y = y0 + r;
       if (x >= X || y >= Y) continue;
-      cp_async16(&s.e[c][r][4 * q] + part * EL, a.E[c] + base + (long long)y * X + x + part * EL);
+      cp_async16(&s.e[c].v[r][4 * q] + part * EL, a.E[c] + base + (long long)y * X + x + part * EL);
     } else {
       const int u = t - ecount;
       const int part = u % CQ, q = (u / CQ) % (kTW / 4), r = (u / CQ / (kTW / 4)) % kTY;
       const int c = u / CQ / (kTW / 4) / kTY;
       const int x = x0 + 4 * q, y = y0 + r;
       if (x >= X || y >= Y) continue;
-      cp_async16(&s.h[c][r][4 * q] + part * EL, a.H[c] + base + (long long)y * X + x + part * EL);
+      cp_async16(&s.h[c].v[r][4 * q] + part * EL, a.H[c] + base + (long long)y * X + x + part * EL);
     }
   }
 }
 
 template <typename real>
-__global__ void __launch_bounds__(256, 2) h_staged_kernel(const __grid_constant__ SweepArgs<real> a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  HSlot<real>* slot = reinterpret_cast<HSlot<real>*>(smem_raw);
+__device__ __forceinline__ void h_issue(const SweepMaps& tm, HSlot<real>& s, unsigned long long* bar, int b, int k,
+                                        int k1, int x0, int y0) {
+  constexpr unsigned eb = 3u * (kTY + 1) * kHW * sizeof(real);
+  constexpr unsigned hb = 3u * kTY * kTW * sizeof(real);
+  const bool with_h = k < k1;
+  mbar_expect_tx(bar, with_h ? eb + hb : eb);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) tma_load4(&s.e[c], &tm.e_wide[c], bar, x0, y0, k, b);
+  if (with_h) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) tma_load4(&s.h[c], &tm.h_tile[c], bar, x0, y0, k, b);
+  }
+}
+
+template <typename real, bool kTma>
+__global__ void __launch_bounds__(256, 2)
+    h_staged_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SweepMaps tm) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ unsigned long long bar[kStages];
+  HSlot<real>* slot = reinterpret_cast<HSlot<real>*>(align_smem(smem_raw));
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const int nx = a.nx, ny = a.ny, nz = a.nz, X = a.X, Y = a.Y;
+  const bool leader = tx == 0 && ty == 0;
+  const int nx = a.nx, ny = a.ny, nz = a.nz, X = a.X, Y = a.Y, Z = nz + 2;
   const int x0 = blockIdx.x * kTW, y0 = 1 + blockIdx.y * kTY;
   const int nkc = (nz + 1 + a.tile_z - 1) / a.tile_z;
   const int b = blockIdx.z / nkc, kc = blockIdx.z % nkc;
   const int k0 = 1 + kc * a.tile_z, k1 = min(k0 + a.tile_z, nz + 2);
+  const int n_stage = k1 < Z ? k1 - k0 + 1 : k1 - k0;
   const int i0 = x0 + 4 * tx, j = y0 + ty;
   const bool live = i0 < X && j <= ny + 1 && i0 <= nx + 1;
   const long long base = (long long)b * a.bs;
   const real dtmu = a.dtmu;
   const Quad<real> ipx = i0 < X ? ld4(a.ip[0] + i0) : Quad<real>{};
   const real ipy = a.ip[1][min(j, Y - 1)];
+  if (kTma) {
+    if (leader) {
+      mbar_setup(bar);
 #pragma unroll
-  for (int s = 0; s < kStages; ++s) {
-    h_stage(a, slot[s], b, k0 + s, k1, x0, y0);
-    cp_commit();
+      for (int c = 0; c < 3; ++c) {
+        prefetch_map(&tm.e_wide[c]);
+        prefetch_map(&tm.h_tile[c]);
+      }
+    }
+    __syncthreads();
+    if (leader)
+      for (int s = 0; s < kStages && s < n_stage; ++s) h_issue(tm, slot[s], &bar[s], b, k0 + s, k1, x0, y0);
+  } else {
+#pragma unroll
+    for (int s = 0; s < kStages; ++s) {
+      h_stage(a, slot[s], b, k0 + s, k1, x0, y0);
+      cp_commit();
+    }
   }
   for (int k = k0; k < k1; ++k) {
-    cp_wait<kStages - 2>();
-    __syncthreads();
-    const HSlot<real>& cur = slot[(k - k0) % kStages];
-    const HSlot<real>& nxt = slot[(k - k0 + 1) % kStages];
+    const int t = k - k0;
+    if (kTma) {
+      bool ok = wait_plane(bar, t);
+      if (ok && t + 1 < n_stage) ok = wait_plane(bar, t + 1);
+      if (__syncthreads_or(!ok)) {
+        abort_march(bar, t, min(n_stage, t + kStages), a.status, leader);
+        return;
+      }
+    } else {
+      cp_wait<kStages - 2>();
+      __syncthreads();
+    }
+    const HSlot<real>& cur = slot[t % kStages];
+    const HSlot<real>& nxt = slot[(t + 1) % kStages];
     if (live) {
       const long long p = base + (long long)k * X * Y + (long long)j * X + i0;
       const bool kin = k <= nz;
       const real ipz = a.ip[2][k];
-      const Quad<real> ex = ld4(&cur.e[0][ty][4 * tx]), ey = ld4(&cur.e[1][ty][4 * tx]);
-      const Quad<real> ez = ld4(&cur.e[2][ty][4 * tx]);
-      const real ez_r = cur.e[2][ty][4 * tx + 4], ey_r = cur.e[1][ty][4 * tx + 4];
+      const Quad<real> ex = ld4(&cur.e[0].v[ty][4 * tx]), ey = ld4(&cur.e[1].v[ty][4 * tx]);
+      const Quad<real> ez = ld4(&cur.e[2].v[ty][4 * tx]);
+      const real ez_r = cur.e[2].v[ty][4 * tx + 4], ey_r = cur.e[1].v[ty][4 * tx + 4];
       if (j <= ny && kin) {  // Hx: node along x (1..nx+1), cell along y and z
-        const Quad<real> ezy = ld4(&cur.e[2][ty + 1][4 * tx]);
-        const Quad<real> ey1 = ld4(&nxt.e[1][ty][4 * tx]);
-        Quad<real> h = ld4(&cur.h[0][ty][4 * tx]);
-        real d0[4], d1[4];
-        bool valid[4];
+        const Quad<real> ezy = ld4(&cur.e[2].v[ty + 1][4 * tx]);
+        const Quad<real> ey1 = ld4(&nxt.e[1].v[ty][4 * tx]);
+        Quad<real> h = ld4(&cur.h[0].v[ty][4 * tx]);
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
           const int i = i0 + e;
-          valid[e] = i >= 1 && i <= nx + 1;
-          d0[e] = (ezy.v[e] - ez.v[e]) * ipy;  // axis y
-          d1[e] = (ey1.v[e] - ey.v[e]) * ipz;  // axis z
-          if (valid[e]) h.v[e] = h.v[e] + dtmu * ((-d0[e]) + d1[e]);
+          const real d0 = (ezy.v[e] - ez.v[e]) * ipy;  // axis y
+          const real d1 = (ey1.v[e] - ey.v[e]) * ipz;  // axis z
+          if (i >= 1 && i <= nx + 1) h.v[e] = h.v[e] + dtmu * ((-d0) + d1);
         }
         st4(a.H[0] + p, h);
       }
       if (kin) {  // Hy: cell along x (1..nx), node along y (1..ny+1), cell along z
-        const Quad<real> ex1 = ld4(&nxt.e[0][ty][4 * tx]);
-        Quad<real> h = ld4(&cur.h[1][ty][4 * tx]);
-        real d0[4], d1[4];
-        bool valid[4];
+        const Quad<real> ex1 = ld4(&nxt.e[0].v[ty][4 * tx]);
+        Quad<real> h = ld4(&cur.h[1].v[ty][4 * tx]);
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
           const int i = i0 + e;
-          valid[e] = i >= 1 && i <= nx;
           const real ezr = e < 3 ? ez.v[e + 1] : ez_r;
-          d0[e] = (ezr - ez.v[e]) * ipx.v[e];  // axis x
-          d1[e] = (ex1.v[e] - ex.v[e]) * ipz;  // axis z
-          if (valid[e]) h.v[e] = h.v[e] + dtmu * ((-d1[e]) + d0[e]);
+          const real d0 = (ezr - ez.v[e]) * ipx.v[e];  // axis x
+          const real d1 = (ex1.v[e] - ex.v[e]) * ipz;  // axis z
+          if (i >= 1 && i <= nx) h.v[e] = h.v[e] + dtmu * ((-d1) + d0);
         }
         st4(a.H[1] + p, h);
       }
       if (j <= ny) {  // Hz: cell along x and y, node along z (1..nz+1)
-        const Quad<real> exy = ld4(&cur.e[0][ty + 1][4 * tx]);
-        Quad<real> h = ld4(&cur.h[2][ty][4 * tx]);
-        real d0[4], d1[4];
-        bool valid[4];
+        const Quad<real> exy = ld4(&cur.e[0].v[ty + 1][4 * tx]);
+        Quad<real> h = ld4(&cur.h[2].v[ty][4 * tx]);
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
           const int i = i0 + e;
-          valid[e] = i >= 1 && i <= nx;
           const real eyr = e < 3 ? ey.v[e + 1] : ey_r;
-          d0[e] = (eyr - ey.v[e]) * ipx.v[e];  // axis x
-          d1[e] = (exy.v[e] - ex.v[e]) * ipy;  // axis y
-          if (valid[e]) h.v[e] = h.v[e] + dtmu * ((-d0[e]) + d1[e]);
+          const real d0 = (eyr - ey.v[e]) * ipx.v[e];  // axis x
+          const real d1 = (exy.v[e] - ex.v[e]) * ipy;  // axis y
+          if (i >= 1 && i <= nx) h.v[e] = h.v[e] + dtmu * ((-d0) + d1);
         }
         st4(a.H[2] + p, h);
       }
     }
     __syncthreads();  // every thread is done with the slot of plane k
-    h_stage(a, slot[(k - k0) % kStages], b, k + kStages, k1, x0, y0);
-    cp_commit();
+    if (kTma) {
+      if (leader && t + kStages < n_stage) {
+        fence_proxy_async();
+        h_issue(tm, slot[t % kStages], &bar[t % kStages], b, k + kStages, k1, x0, y0);
+      }
+    } else {
+      h_stage(a, slot[t % kStages], b, k + kStages, k1, x0, y0);
+      cp_commit();
+    }
   }
-  cp_wait<0>();
+  if (!kTma) cp_wait<0>();
 }
 
 // ------------------------------------------------------------------------------------- E sweep
-// Slot: H[3][kTY + 1][kHW] (rows y0-1..y0+7, x0-4..x0+127), E[3][kTY][kTW], mat[3][kTY][kTW].
+// Slot: H[3] rows y0-1..y0+7, x0-4..x0+127; E[3] and mat[3] rows y0..y0+7, x0..x0+127.
 template <typename real>
 struct ESlot {
-  real h[3][kTY + 1][kHW];
-  real e[3][kTY][kTW];
-  uint16_t m[3][kTY][kTW];
+  Box<real, kTY + 1, kHW> h[3];
+  Box<real, kTY, kTW> e[3];
+  Box<uint16_t, kTY, kTW> m[3];
 };
 
 template <typename real>
@@ -179,21 +323,35 @@ __device__ __forceinline__ void e_stage(const SweepArgs<real>& a, ESlot<real>& s
       const int c = t / CQ / (kHW / 4) / (kTY + 1);
       const int x = x0 - 4 + 4 * q, y = y0 - 1 + r;
       if (x < 0 || x >= X || y >= Y) continue;
-      cp_async16(&s.h[c][r][4 * q] + part * EL, a.H[c] + base + (long long)y * X + x + part * EL);
+      cp_async16(&s.h[c].v[r][4 * q] + part * EL, a.H[c] + base + (long long)y * X + x + part * EL);
     } else if (t < hcount + ecount) {
       const int u = t - hcount;
       const int part = u % CQ, q = (u / CQ) % (kTW / 4), r = (u / CQ / (kTW / 4)) % kTY;
       const int c = u / CQ / (kTW / 4) / kTY;
       const int x = x0 + 4 * q, y = y0 + r;
       if (x >= X || y >= Y) continue;
-      cp_async16(&s.e[c][r][4 * q] + part * EL, a.E[c] + base + (long long)y * X + x + part * EL);
+      cp_async16(&s.e[c].v[r][4 * q] + part * EL, a.E[c] + base + (long long)y * X + x + part * EL);
     } else {
       const int u = t - hcount - ecount;
       const int q = u % (kTW / 8), r = (u / (kTW / 8)) % kTY, c = u / (kTW / 8) / kTY;
       const int x = x0 + 8 * q, y = y0 + r;
       if (x >= X || y >= Y) continue;
-      cp_async16(&s.m[c][r][8 * q], a.mat[c] + plane + (long long)y * X + x);
+      cp_async16(&s.m[c].v[r][8 * q], a.mat[c] + plane + (long long)y * X + x);
     }
+  }
+}
+
+template <typename real>
+__device__ __forceinline__ void e_issue(const SweepMaps& tm, ESlot<real>& s, unsigned long long* bar, int b, int k,
+                                        int x0, int y0) {
+  constexpr unsigned bytes =
+      3u * ((kTY + 1) * kHW * sizeof(real) + kTY * kTW * sizeof(real) + kTY * kTW * sizeof(uint16_t));
+  mbar_expect_tx(bar, bytes);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    tma_load4(&s.h[c], &tm.h_wide[c], bar, x0 - 4, y0 - 1, k, b);
+    tma_load4(&s.e[c], &tm.e_tile[c], bar, x0, y0, k, b);
+    tma_load3(&s.m[c], &tm.mat[c], bar, x0, y0, k);
   }
 }
 
@@ -208,14 +366,12 @@ __device__ __forceinline__ void e_apply(const SweepArgs<real>& a, int c, real* _
   const int X = a.X, Y = a.Y, nx = a.nx;
   Quad<real> e4 = e_old;
   Coef<real> cf[4];
-  real kf[4];
   bool valid[4];
   bool disp = false;
 #pragma unroll
   for (int e = 0; e < 4; ++e) {
     const int i = i0 + e;
     cf[e] = a.coef[m[e]];
-    kf[e] = cf[e].cb;
     valid[e] = i >= 1 && i <= nx + 1;
     const real acc = first_plus ? d0[e] + (-d1[e]) : d1[e] + (-d0[e]);
     if (valid[e]) e4.v[e] = cf[e].ca * e4.v[e] + cf[e].cb * acc;
@@ -264,16 +420,20 @@ __device__ __forceinline__ void j_prefetch(const SweepArgs<real>& a, Quad<real> 
   }
 }
 
-template <typename real>
-__global__ void __launch_bounds__(256, 2) e_staged_kernel(const __grid_constant__ SweepArgs<real> a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  ESlot<real>* slot = reinterpret_cast<ESlot<real>*>(smem_raw);
+template <typename real, bool kTma>
+__global__ void __launch_bounds__(256, 2)
+    e_staged_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SweepMaps tm) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ unsigned long long bar[kStages];
+  ESlot<real>* slot = reinterpret_cast<ESlot<real>*>(align_smem(smem_raw));
   const int tx = threadIdx.x, ty = threadIdx.y;
+  const bool leader = tx == 0 && ty == 0;
   const int nx = a.nx, ny = a.ny, nz = a.nz, X = a.X, Y = a.Y;
   const int x0 = blockIdx.x * kTW, y0 = 1 + blockIdx.y * kTY;
   const int nkc = (nz + 1 + a.tile_z - 1) / a.tile_z;
   const int b = blockIdx.z / nkc, kc = blockIdx.z % nkc;
   const int k0 = 1 + kc * a.tile_z, k1 = min(k0 + a.tile_z, nz + 2);
+  const int n_stage = k1 - k0;
   const int i0 = x0 + 4 * tx, j = y0 + ty;
   const bool live = i0 < X && j <= ny + 1 && i0 <= nx + 1;
   const long long base = (long long)b * a.bs;
@@ -287,24 +447,48 @@ __global__ void __launch_bounds__(256, 2) e_staged_kernel(const __grid_constant_
   }
   Quad<real> jcur[3];
   j_prefetch(a, jcur, k0, j, i0, b, live);
+  if (kTma) {
+    if (leader) {
+      mbar_setup(bar);
 #pragma unroll
-  for (int s = 0; s < kStages; ++s) {
-    e_stage(a, slot[s], b, k0 + s, k1, x0, y0);
-    cp_commit();
+      for (int c = 0; c < 3; ++c) {
+        prefetch_map(&tm.h_wide[c]);
+        prefetch_map(&tm.e_tile[c]);
+        prefetch_map(&tm.mat[c]);
+      }
+    }
+    __syncthreads();
+    if (leader)
+      for (int s = 0; s < kStages && s < n_stage; ++s) e_issue(tm, slot[s], &bar[s], b, k0 + s, x0, y0);
+  } else {
+#pragma unroll
+    for (int s = 0; s < kStages; ++s) {
+      e_stage(a, slot[s], b, k0 + s, k1, x0, y0);
+      cp_commit();
+    }
   }
   for (int k = k0; k < k1; ++k) {
+    const int t = k - k0;
     Quad<real> jnext[3];
     j_prefetch(a, jnext, k + 1 < k1 ? k + 1 : -1, j, i0, b, live);
-    cp_wait<kStages - 1>();
-    __syncthreads();
-    const ESlot<real>& cur = slot[(k - k0) % kStages];
+    if (kTma) {
+      const bool ok = wait_plane(bar, t);
+      if (__syncthreads_or(!ok)) {
+        abort_march(bar, t, min(n_stage, t + kStages), a.status, leader);
+        return;
+      }
+    } else {
+      cp_wait<kStages - 1>();
+      __syncthreads();
+    }
+    const ESlot<real>& cur = slot[t % kStages];
     if (live) {
       const long long q = (long long)k * X * Y + (long long)j * X + i0;
       const real idz = a.idd[2][k];
-      const Quad<real> hx = ld4(&cur.h[0][ty + 1][4 * tx + 4]), hy = ld4(&cur.h[1][ty + 1][4 * tx + 4]);
-      const Quad<real> hz = ld4(&cur.h[2][ty + 1][4 * tx + 4]);
-      const Quad<real> hzy = ld4(&cur.h[2][ty][4 * tx + 4]), hxy = ld4(&cur.h[0][ty][4 * tx + 4]);
-      const real hz_l = cur.h[2][ty + 1][4 * tx + 3], hy_l = cur.h[1][ty + 1][4 * tx + 3];
+      const Quad<real> hx = ld4(&cur.h[0].v[ty + 1][4 * tx + 4]), hy = ld4(&cur.h[1].v[ty + 1][4 * tx + 4]);
+      const Quad<real> hz = ld4(&cur.h[2].v[ty + 1][4 * tx + 4]);
+      const Quad<real> hzy = ld4(&cur.h[2].v[ty][4 * tx + 4]), hxy = ld4(&cur.h[0].v[ty][4 * tx + 4]);
+      const real hz_l = cur.h[2].v[ty + 1][4 * tx + 3], hy_l = cur.h[1].v[ty + 1][4 * tx + 3];
       real d0[4], d1[4];
       // Ex: terms (a = y, +Hz) then (a = z, -Hy)
 #pragma unroll
@@ -312,7 +496,8 @@ __global__ void __launch_bounds__(256, 2) e_staged_kernel(const __grid_constant_
         d0[e] = (hz.v[e] - hzy.v[e]) * idy;
         d1[e] = (hy.v[e] - hy_m.v[e]) * idz;
       }
-      e_apply<real>(a, 0, a.E[0] + base, q, ld4(&cur.e[0][ty][4 * tx]), &cur.m[0][ty][4 * tx], d0, d1, true, jcur[0], i0, j, k, b);
+      e_apply<real>(a, 0, a.E[0] + base, q, ld4(&cur.e[0].v[ty][4 * tx]), &cur.m[0].v[ty][4 * tx], d0, d1, true,
+                    jcur[0], i0, j, k, b);
       // Ey: terms (a = z, +Hx) then (a = x, -Hz); d0 is the x term, d1 the z term
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
@@ -320,7 +505,8 @@ __global__ void __launch_bounds__(256, 2) e_staged_kernel(const __grid_constant_
         d0[e] = (hz.v[e] - hzl) * idx4.v[e];
         d1[e] = (hx.v[e] - hx_m.v[e]) * idz;
       }
-      e_apply<real>(a, 1, a.E[1] + base, q, ld4(&cur.e[1][ty][4 * tx]), &cur.m[1][ty][4 * tx], d0, d1, false, jcur[1], i0, j, k, b);
+      e_apply<real>(a, 1, a.E[1] + base, q, ld4(&cur.e[1].v[ty][4 * tx]), &cur.m[1].v[ty][4 * tx], d0, d1, false,
+                    jcur[1], i0, j, k, b);
       // Ez: terms (a = x, +Hy) then (a = y, -Hx)
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
@@ -328,41 +514,124 @@ __global__ void __launch_bounds__(256, 2) e_staged_kernel(const __grid_constant_
         d0[e] = (hy.v[e] - hyl) * idx4.v[e];
         d1[e] = (hx.v[e] - hxy.v[e]) * idy;
       }
-      e_apply<real>(a, 2, a.E[2] + base, q, ld4(&cur.e[2][ty][4 * tx]), &cur.m[2][ty][4 * tx], d0, d1, true, jcur[2], i0, j, k, b);
+      e_apply<real>(a, 2, a.E[2] + base, q, ld4(&cur.e[2].v[ty][4 * tx]), &cur.m[2].v[ty][4 * tx], d0, d1, true,
+                    jcur[2], i0, j, k, b);
       hx_m = hx;
       hy_m = hy;
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c) jcur[c] = jnext[c];
     __syncthreads();
-    e_stage(a, slot[(k - k0) % kStages], b, k + kStages, k1, x0, y0);
-    cp_commit();
+    if (kTma) {
+      if (leader && t + kStages < n_stage) {
+        fence_proxy_async();
+        e_issue(tm, slot[t % kStages], &bar[t % kStages], b, k + kStages, x0, y0);
+      }
+    } else {
+      e_stage(a, slot[t % kStages], b, k + kStages, k1, x0, y0);
+      cp_commit();
+    }
   }
-  cp_wait<0>();
+  if (!kTma) cp_wait<0>();
 }
 
 // ------------------------------------------------------------------------------------- launch
 template <typename real>
-cudaError_t launch_staged_sweep(const SweepArgs<real>& a, cudaStream_t s, bool h) {
+cudaError_t launch_staged_sweep(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_t s, bool h) {
   const int nkc = (a.nz + 1 + a.tile_z - 1) / a.tile_z;
   dim3 block(kTQ, kTY);
   dim3 grid((a.X + kTW - 1) / kTW, (a.ny + 1 + kTY - 1) / kTY, nkc * a.B);
+  const bool tma = a.staged == 2;
   cudaError_t err;
   if (h) {
-    const size_t bytes = sizeof(HSlot<real>) * kStages;
-    err = cudaFuncSetAttribute(h_staged_kernel<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    const size_t bytes = sizeof(HSlot<real>) * kStages + 128;
+    auto kern = tma ? h_staged_kernel<real, true> : h_staged_kernel<real, false>;
+    err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (err != cudaSuccess) return err;
-    h_staged_kernel<real><<<grid, block, bytes, s>>>(a);
+    kern<<<grid, block, bytes, s>>>(a, m);
   } else {
-    const size_t bytes = sizeof(ESlot<real>) * kStages;
-    err = cudaFuncSetAttribute(e_staged_kernel<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    const size_t bytes = sizeof(ESlot<real>) * kStages + 128;
+    auto kern = tma ? e_staged_kernel<real, true> : e_staged_kernel<real, false>;
+    err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (err != cudaSuccess) return err;
-    e_staged_kernel<real><<<grid, block, bytes, s>>>(a);
+    kern<<<grid, block, bytes, s>>>(a, m);
   }
   return cudaGetLastError();
 }
 
-template cudaError_t launch_staged_sweep<float>(const SweepArgs<float>&, cudaStream_t, bool);
-template cudaError_t launch_staged_sweep<double>(const SweepArgs<double>&, cudaStream_t, bool);
+// ------------------------------------------------------------------------------- descriptors
+namespace {
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encoder() {
+  static EncodeTiled fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(p);
+  });
+  return fn;
+}
+
+// dims/box innermost first; strides in bytes for dims 1..rank-1.
+bool encode(EncodeTiled f, CUtensorMap* m, CUtensorMapDataType dt, int rank, const void* base, const cuuint64_t* dims,
+            const cuuint64_t* strides, const cuuint32_t* box, const char* what, std::string* why) {
+  const cuuint32_t ones[4] = {1, 1, 1, 1};
+  const CUresult r = f(m, dt, (cuuint32_t)rank, const_cast<void*>(base), dims, strides, box, ones,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    *why = std::string("cuTensorMapEncodeTiled(") + what + ") returned " + std::to_string((int)r);
+    return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+template <typename real>
+bool encode_sweep_maps(const SweepArgs<real>& a, SweepMaps* m, std::string* why) {
+  const EncodeTiled f = encoder();
+  if (f == nullptr) {
+    *why = "the driver does not provide cuTensorMapEncodeTiled";
+    return false;
+  }
+  const CUtensorMapDataType dt = sizeof(real) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  const cuuint64_t X = (cuuint64_t)a.X, Y = (cuuint64_t)a.Y, Z = (cuuint64_t)a.nz + 2, B = (cuuint64_t)a.B;
+  const cuuint64_t dims[4] = {X, Y, Z, B};
+  const cuuint64_t rs = sizeof(real);
+  const cuuint64_t strides[3] = {X * rs, X * Y * rs, X * Y * Z * rs};
+  const cuuint32_t wide[4] = {kHW, kTY + 1, 1, 1};
+  const cuuint32_t tile[4] = {kTW, kTY, 1, 1};
+  const cuuint64_t mdims[3] = {X, Y, Z};
+  const cuuint64_t mstrides[2] = {X * 2, X * Y * 2};
+  for (int c = 0; c < 3; ++c) {
+    if (!encode(f, &m->e_wide[c], dt, 4, a.E[c], dims, strides, wide, "E wide", why) ||
+        !encode(f, &m->e_tile[c], dt, 4, a.E[c], dims, strides, tile, "E tile", why) ||
+        !encode(f, &m->h_wide[c], dt, 4, a.H[c], dims, strides, wide, "H wide", why) ||
+        !encode(f, &m->h_tile[c], dt, 4, a.H[c], dims, strides, tile, "H tile", why) ||
+        !encode(f, &m->mat[c], CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, a.mat[c], mdims, mstrides, tile, "mat", why))
+      return false;
+  }
+  return true;
+}
+
+static_assert(sizeof(Box<float, kTY + 1, kHW>) % 128 == 0 && sizeof(Box<uint16_t, kTY, kTW>) % 128 == 0,
+              "staged arrays keep the 128-byte alignment TMA destinations need");
+static_assert((kHW * sizeof(float)) % 16 == 0 && (kTW * sizeof(uint16_t)) % 16 == 0,
+              "TMA box rows are whole 16-byte units");
+static_assert(sizeof(ESlot<float>) * kStages + 128 <= 113 * 1024, "two E blocks per SM");
+
+template cudaError_t launch_staged_sweep<float>(const SweepArgs<float>&, const SweepMaps&, cudaStream_t, bool);
+template cudaError_t launch_staged_sweep<double>(const SweepArgs<double>&, const SweepMaps&, cudaStream_t, bool);
+template bool encode_sweep_maps<float>(const SweepArgs<float>&, SweepMaps*, std::string*);
+template bool encode_sweep_maps<double>(const SweepArgs<double>&, SweepMaps*, std::string*);
 
 }  // namespace oafdtd

@@ -268,8 +268,8 @@ __global__ void __launch_bounds__(256, 3) e_sweep_kernel(const __grid_constant__
 
 // ------------------------------------------------------------------------------------- launchers
 template <typename real>
-cudaError_t launch_h_sweep(const SweepArgs<real>& a, cudaStream_t s) {
-  if (a.staged) return launch_staged_sweep<real>(a, s, true);
+cudaError_t launch_h_sweep(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_t s) {
+  if (a.staged) return launch_staged_sweep<real>(a, m, s, true);
   const long long quads = (long long)a.Y * (a.X / 4);
   dim3 grid((unsigned)((quads + 255) / 256), (a.nz + 1 + a.tile_z - 1) / a.tile_z, a.B);
   h_sweep_kernel<real><<<grid, 256, 0, s>>>(a);
@@ -277,17 +277,17 @@ cudaError_t launch_h_sweep(const SweepArgs<real>& a, cudaStream_t s) {
 }
 
 template <typename real>
-cudaError_t launch_e_sweep(const SweepArgs<real>& a, cudaStream_t s) {
-  if (a.staged) return launch_staged_sweep<real>(a, s, false);
+cudaError_t launch_e_sweep(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_t s) {
+  if (a.staged) return launch_staged_sweep<real>(a, m, s, false);
   const long long quads = (long long)a.Y * (a.X / 4);
   dim3 grid((unsigned)((quads + 255) / 256), (a.nz + 1 + a.tile_z - 1) / a.tile_z, a.B);
   e_sweep_kernel<real><<<grid, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 
-template cudaError_t launch_h_sweep<float>(const SweepArgs<float>&, cudaStream_t);
-template cudaError_t launch_e_sweep<float>(const SweepArgs<float>&, cudaStream_t);
-template cudaError_t launch_h_sweep<double>(const SweepArgs<double>&, cudaStream_t);
-template cudaError_t launch_e_sweep<double>(const SweepArgs<double>&, cudaStream_t);
+template cudaError_t launch_h_sweep<float>(const SweepArgs<float>&, const SweepMaps&, cudaStream_t);
+template cudaError_t launch_e_sweep<float>(const SweepArgs<float>&, const SweepMaps&, cudaStream_t);
+template cudaError_t launch_h_sweep<double>(const SweepArgs<double>&, const SweepMaps&, cudaStream_t);
+template cudaError_t launch_e_sweep<double>(const SweepArgs<double>&, const SweepMaps&, cudaStream_t);
 
 }  // namespace oafdtd

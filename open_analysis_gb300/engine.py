@@ -261,8 +261,8 @@ class Gb300Engine:
         native.check(self._lib.oafdtd_set_graph(self._h, int(bool(on))), "set_graph")
 
     def set_tuning(self, tile_z: int = 0, variant: int = -1) -> None:
-        """Planes marched per block (0 keeps) and the sweep variant (1 shared-memory staged,
-        0 register marching, -1 keeps)."""
+        """Planes marched per block (0 keeps) and the sweep variant (2 staged by TMA, 1 staged
+        by cp.async, 0 register marching, -1 keeps)."""
         native.check(self._lib.oafdtd_set_tuning(self._h, int(tile_z), int(variant)), "set_tuning")
 
     def set_profiling(self, on: bool) -> None:

@@ -16,6 +16,17 @@ float32 fields bit for bit and a float64 run is the FP64 error yardstick:
 
 Its agreement with the reference itself is pinned by ``tests/golden`` (fixtures generated by
 importing the reference; see ``tests/golden/make_golden.py``).
+
+``order="engine"`` restates the GPU engine's order of the same arithmetic, so that the engine can be
+checked bit for bit where its order differs from the reference's:
+
+* the Debye update of a dispersive edge runs right after its bulk E update, before the CPML
+  corrections; each correction t of such an edge then also moves every current J_p by beta_p t
+  (the reference corrects first, then updates J_p from the corrected field: the same values up
+  to rounding). Dispersive edges that take an injection keep the reference's place, after SIBC
+  and injection;
+* the pole sum of the Debye update is a plain loop over the poles in index order (NumPy's einsum
+  may reorder or fuse it on some hosts).
 """
 
 from __future__ import annotations
@@ -55,7 +66,12 @@ class OracleEngine:
 
     name = "oracle"
 
-    def __init__(self, c: Any, dtype: str = "float64", record_series: bool = False, **_: Any) -> None:
+    def __init__(
+        self, c: Any, dtype: str = "float64", record_series: bool = False, order: str = "reference", **_: Any
+    ) -> None:
+        if order not in ("reference", "engine"):
+            raise ValueError(f"order must be 'reference' or 'engine', not {order!r}")
+        self.order = order
         self.c = c
         self.record_series = record_series
         self.dtype = np.dtype(dtype)
@@ -108,6 +124,14 @@ class OracleEngine:
                 }
             )
         self._kp = a.kp.astype(real)
+        # dispersive edges that take an injection (the engine updates them after the injection)
+        injected: list[set[int]] = [set(), set(), set()]
+        for ch in c.channels:
+            comps = np.broadcast_to(np.asarray(ch["comp"]), ch["flat"].shape)
+            for cc, f in zip(comps.tolist(), np.asarray(ch["flat"]).tolist(), strict=True):
+                injected[int(cc)].add(int(f))
+        for st in self._ade:
+            st["late"] = np.array([int(f) in injected[st["c"]] for f in st["flat"].tolist()], bool)
 
     def _setup_sibc(self) -> None:
         c, real, batch = self.c, self.dtype, self.c.batch
@@ -129,7 +153,12 @@ class OracleEngine:
         for st in self._ade:
             st["eold"][...] = self._flat(st["c"])[:, st["flat"]]
 
-    def _ade_update(self) -> None:
+    def _ade_update(self, which: str = "all") -> None:
+        """Debye update of the dispersive edges (``which``: all, early = without injection,
+        late = with injection)."""
+        if which != "all":
+            self._ade_update_engine(late=which == "late")
+            return
         for st in self._ade:
             ef = self._flat(st["c"])
             e = ef[:, st["flat"]]
@@ -138,6 +167,38 @@ class OracleEngine:
             de = en - st["eold"]
             st["J"][...] = self._kp[:, None, None] * st["J"] + st["beta"][:, None, :] * de[None]
             ef[:, st["flat"]] = en
+
+    def _ade_update_engine(self, late: bool) -> None:
+        for st in self._ade:
+            sel = st["late"] if late else ~st["late"]
+            if not sel.any():
+                continue
+            ef = self._flat(st["c"])
+            fl = st["flat"][sel]
+            e = ef[:, fl]
+            J = st["J"][:, :, sel]
+            onekp = (1.0 + self._kp).astype(self.dtype)
+            jt = np.zeros_like(e)
+            for p in range(J.shape[0]):
+                jt = jt + onekp[p] * J[p]
+            jt = self.dtype.type(0.5) * jt
+            en = e - st["cbe"][None, sel] * jt
+            de = en - st["eold"][:, sel]
+            st["J"][:, :, sel] = self._kp[:, None, None] * J + st["beta"][:, None, sel] * de[None]
+            ef[:, fl] = en
+
+    def _debye_shift(self, comp: int, rng: Rng, t: Any) -> None:
+        """Engine order: a CPML correction t of an early-updated dispersive edge moves each J_p by
+        beta_p t."""
+        full = np.zeros_like(self.E[comp])
+        _window(full, rng)[...] = t
+        ff = full.reshape(self.c.batch, -1)
+        for st in self._ade:
+            if st["c"] != comp:
+                continue
+            sel = ~st["late"]
+            tt = ff[:, st["flat"][sel]]
+            st["J"][:, :, sel] = st["J"][:, :, sel] + st["beta"][:, None, sel] * tt[None]
 
     def _sibc(self) -> None:
         sb = self._sb
@@ -215,7 +276,10 @@ class OracleEngine:
             psi += _coef(cc_.astype(real), a, rng) * d
             upd = _coef(ck_.astype(real), a, rng) * d + psi
             if kind == "E":
-                _window(self.E[corr.c], rng)[...] += corr.sign * _window(self.cb[corr.c], rng) * upd
+                t = corr.sign * _window(self.cb[corr.c], rng) * upd
+                _window(self.E[corr.c], rng)[...] += t
+                if self.order == "engine" and self._ade:
+                    self._debye_shift(corr.c, rng, t)
             else:
                 _window(self.H[corr.c], rng)[...] += corr.sign * self.dtmu * upd
 
@@ -270,10 +334,12 @@ class OracleEngine:
             self._record("H", (k + 0.5) * dt)
             self._ade_save()
             self._e_update()
+            if self.order == "engine":
+                self._ade_update("early")
             self._pml("E")
             self._sibc()
             self._inject(k)
-            self._ade_update()
+            self._ade_update("late" if self.order == "engine" else "all")
             self._record("E", (k + 1) * dt)
             self.step_count += 1
 

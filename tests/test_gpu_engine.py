@@ -1,9 +1,11 @@
-"""GPU engine against the CPU oracle: bit-exact float32 fields, DFTs, energy, S-parameters.
+"""GPU engine against the CPU oracle: bit-exact fields, DFTs, energy, S-parameters.
 
 The oracle (``oracle/numpy_engine.py``) is pinned against the reference itself by
 ``test_golden_compile.py``; here the CUDA engine runs the same compiled problems through the
-C ABI and must reproduce the oracle's float32 fields bit for bit (the library is built without
-FMA contraction and keeps the reference's operation order, including the fused CPML order).
+C ABI. The library is built without FMA contraction and keeps the reference's operations, so its
+fields equal the oracle's bit for bit in the engine's order (``order="engine"``: Debye edges
+inside CPML slabs updated before their corrections), and equal the reference-order oracle's bit
+for bit wherever the two orders coincide, otherwise within float32 rounding noise.
 """
 
 from __future__ import annotations
@@ -64,35 +66,62 @@ def _einsum_is_sequential() -> bool:
     return bool(np.array_equal(np.einsum("p,pbe->be", a, j), seq))
 
 
+def _rel(got, want) -> float:  # type: ignore[no-untyped-def]
+    return float(np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-300))
+
+
+def _fields(e) -> list:  # type: ignore[no-untyped-def]
+    return [f.astype(np.float64) for f in (e.E + e.H)]
+
+
+def _reference_tolerance(c, steps: int, dtype: str, ref_fields: list) -> list[float]:  # type: ignore[no-untyped-def]
+    """Per component: 1e-5 (float32) or 1e-12 (float64) rel-L2, or twice the distance of the
+    reference-order float32 run from its float64 run where the case itself is worse conditioned
+    than that (a thin field component that float32 rounding alone moves by more than 1e-5)."""
+    base = 1e-5 if dtype == "float32" else 1e-12
+    if dtype != "float32":
+        return [base] * 6
+    r64 = OracleEngine(c, "float64")
+    r64.step(steps)
+    return [max(base, 2.0 * _rel(ref_fields[k], f)) for k, f in enumerate(_fields(r64))]
+
+
+def check_against_oracles(c, gpu, steps: int, dtype: str = "float32", results: bool = True) -> None:  # type: ignore[no-untyped-def]
+    """The engine's fields equal the engine-order oracle's bit for bit, its DFTs and energy agree
+    to float64 summation order, and its fields are within the reference-order oracle's rounding
+    noise (identical where the two orders coincide)."""
+    eng = OracleEngine(c, dtype, order="engine")
+    eng.step(steps)
+    for k, want in enumerate(_fields(eng)):
+        got = gpu.field(k)
+        assert np.array_equal(got, want), f"{NAMES[k]}: max |d| = {np.abs(got - want).max()}"
+    if results:
+        r_gpu, r_eng = gpu.results(), eng.results()
+        assert set(r_gpu) == set(r_eng)
+        for name, v in r_eng.items():
+            assert r_gpu[name].shape == v.shape
+            assert np.abs(r_gpu[name] - v).max() <= 1e-9 * max(np.abs(v).max(), 1e-300), name
+        e_gpu, e_eng = gpu.energy(), eng.energy()
+        assert abs(e_gpu - e_eng) <= 1e-10 * abs(e_eng)
+    ref = OracleEngine(c, dtype)
+    ref.step(steps)
+    ref_fields = _fields(ref)
+    if all(np.array_equal(a, b) for a, b in zip(ref_fields, _fields(eng), strict=True)):
+        return
+    tol = _reference_tolerance(c, steps, dtype, ref_fields)
+    for k, want in enumerate(ref_fields):
+        rel = _rel(gpu.field(k), want)
+        assert rel <= tol[k], f"{NAMES[k]}: rel-L2 {rel} against the reference order (bound {tol[k]})"
+
+
 @pytest.mark.parametrize("case", sorted(CASES))
 @pytest.mark.parametrize("dtype", ["float32", "float64"])
 def test_fields_match_oracle(case: str, dtype: str) -> None:
     builder, steps = CASES[case]
     c = compile_model(builder(namespace("gb300")), "float32")
     gpu = _engine(c, dtype)
-    ref = OracleEngine(c, dtype)
     gpu.step(steps)
-    ref.step(steps)
-    exact = (case != "dispersive_copper" or _einsum_is_sequential()) and not _ade_in_cpml(c)
-    for k, name in enumerate(NAMES):
-        got = gpu.field(k)
-        want = (ref.E + ref.H)[k].astype(np.float64)
-        if exact:
-            assert np.array_equal(got, want), f"{name}: max |d| = {np.abs(got - want).max()}"
-        else:
-            rel = np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-300)
-            assert rel <= (1e-5 if dtype == "float32" else 1e-12), f"{name}: rel-L2 {rel}"
-    r_gpu, r_ref = gpu.results(), ref.results()
-    assert set(r_gpu) == set(r_ref)
-    # identical fields: the DFTs differ only by float64 summation order; otherwise by the ulps
-    # of the pole sum propagated through the fields
-    tol = 1e-9 if exact else 1e-6
-    for name, v in r_ref.items():
-        assert r_gpu[name].shape == v.shape
-        scale = max(np.abs(v).max(), 1e-300)
-        assert np.abs(r_gpu[name] - v).max() <= tol * scale, name
-    e_gpu, e_ref = gpu.energy(), ref.energy()
-    assert abs(e_gpu - e_ref) <= (1e-10 if exact else 1e-6) * abs(e_ref)
+    check_against_oracles(c, gpu, steps, dtype)
 
 
 @pytest.mark.parametrize("case", ["mixed_walls", "microstrip"])
@@ -175,18 +204,38 @@ def test_kernel_profile_and_model_bytes() -> None:
     assert eng.model_bytes() > 0
 
 
-@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("variant", [0, 1, 2])
 @pytest.mark.parametrize("tile_z", [3, 32])
 def test_launch_shapes_match_oracle(variant: int, tile_z: int) -> None:
     """Every sweep variant and z tiling gives the oracle's float32 fields bit for bit."""
     c = compile_model(CASES["microstrip"][0](namespace("gb300")), "float32")
     gpu = _engine(c)
     gpu.set_tuning(tile_z, variant)
-    ref = OracleEngine(c, "float32")
     gpu.step(70)
-    ref.step(70)
+    check_against_oracles(c, gpu, 70, results=False)
+
+
+def test_variants_agree_across_x_tiles() -> None:
+    """A grid two tiles wide in x (the second one past the grid's edge, where TMA boxes are
+    zero-filled) with the benchmark's Debye stack, copper SIBC and CPML: the three sweep variants
+    give identical fields, equal to the engine-order oracle's. Its Ey is thin: float32 rounding
+    alone moves it by 2e-5 rel-L2, which sets the bound against the reference order."""
+    from open_analysis_gb300.structures import via_transition
+
+    c = compile_model(via_transition(nx=150, ny=20, nz=14, n_freq=8, cpml_cells=6), "float32")
+    assert c.grid.shape[2] > 128 and _ade_in_cpml(c)
+    fields = {}
+    for variant in (0, 1, 2):
+        gpu = _engine(c)
+        gpu.set_tuning(5, variant)
+        gpu.step(40)
+        fields[variant] = [gpu.field(k) for k in range(6)]
+        if variant == 2:
+            check_against_oracles(c, gpu, 40)
+        gpu.close()
     for k in range(6):
-        assert np.array_equal(gpu.field(k), (ref.E + ref.H)[k].astype(np.float64)), NAMES[k]
+        assert np.array_equal(fields[2][k], fields[1][k]), NAMES[k]
+        assert np.array_equal(fields[2][k], fields[0][k]), NAMES[k]
 
 
 def test_via_transition_small_matches_oracle() -> None:
@@ -196,12 +245,5 @@ def test_via_transition_small_matches_oracle() -> None:
     c = compile_model(via_transition(nx=48, ny=40, nz=32, n_freq=16, cpml_cells=6), "float32")
     assert _ade_in_cpml(c)  # the Debye stack reaches into the x and y slabs
     gpu = _engine(c)
-    ref = OracleEngine(c, "float32")
     gpu.step(50)
-    ref.step(50)
-    for k in range(6):
-        got, want = gpu.field(k), (ref.E + ref.H)[k].astype(np.float64)
-        rel = np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-300)
-        assert rel <= 1e-5, f"{NAMES[k]}: rel-L2 {rel}"
-    for name, v in ref.results().items():
-        assert np.abs(gpu.results()[name] - v).max() <= 1e-6 * max(np.abs(v).max(), 1e-300), name
+    check_against_oracles(c, gpu, 50)
