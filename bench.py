@@ -140,49 +140,33 @@ class ClockSampler:
 
 # ---------------------------------------------------------------------------- traffic model
 def kernel_bytes(c: Any, real: int = 4) -> dict[str, float]:
-    """Algorithmic DRAM bytes per launch of each kernel (all batch members).
+    """Algorithmic DRAM bytes per step of each kernel class (all batch members).
 
-    h_sweep: read 3 E, read-modify-write 3 H per interior cell and member (36 B in float32) plus
-    psi read+write (8 B) per cell of every H correction box. e_sweep: read 3 H, read-modify-write
-    3 E (36 B) per cell and member, the three uint16 indices once per cell (6 B), psi (8 B) per
-    cell of every E correction box, the Debye current J read+write (8 B per pole) per dispersive
-    edge. edges: per surface-impedance edge J_prev and v_p read+write (8 B (1 + P)), two H samples
+    h_sweep: read 3 E, read-modify-write 3 H per interior cell and member (36 B in float32).
+    e_sweep: read 3 H, read-modify-write 3 E (36 B) per cell and member, the three uint16 indices
+    once per cell (6 B), the Debye current J read+write (8 B per pole) per dispersive edge.
+    h_cpml / e_cpml (the correction passes, one launch per derivative axis): per cell of every
+    correction box and member, psi read+write and the corrected field read+write (16 B), the
+    source field once (4 B), and for E the uint16 index (2 B, once per cell).
+    edges: per surface-impedance edge J_prev and v_p read+write (8 B (1 + P)), two H samples
     (8 B) and the E write (4 B), per member.
     """
     nx, ny, nz = c.grid.n
     cells = float(nx * ny * nz)
     b = c.batch
-    psi = {"E": 0.0, "H": 0.0}
+    box = {"E": 0.0, "H": 0.0}
     for k in c.pml.corrections:
-        psi[k.kind] += float(np.prod(k.shape))
-    h = cells * b * 9 * real + psi["H"] * b * 2 * real
-    e = cells * b * 9 * real + cells * 6 + psi["E"] * b * 2 * real
+        box[k.kind] += float(np.prod(k.shape))
+    h = cells * b * 9 * real
+    e = cells * b * 9 * real + cells * 6
     if c.ade is not None:
         e += sum(f.size for f in c.ade.flat) * b * c.ade.tau.size * 2 * real
+    h_cpml = box["H"] * b * 5 * real
+    e_cpml = box["E"] * (b * 5 * real + 2)
     edges = 0.0
     if c.sibc is not None:
         edges = c.sibc.flat.size * b * (2 * real * (1 + c.sibc.cp.size) + 2 * real + real)
-    return {"h_sweep": h, "e_sweep": e, "edges": edges}
-
-
-def launches_per_step(c: Any) -> int:
-    n = 2  # h_sweep, e_sweep
-    n += sum(1 for w in c.walls if w == "pmc")
-    kinds = {p["kind"] for p in c.probes}
-    n += 1 if "E" in kinds else 0
-    has_h = "H" in kinds
-    deferred = False
-    if c.ade is not None and c.channels:
-        for comp, fl in zip(c.ade.comp, c.ade.flat, strict=True):
-            targets = [
-                np.asarray(ch["flat"])[np.broadcast_to(np.asarray(ch["comp"]), np.asarray(ch["flat"]).shape) == comp]
-                for ch in c.channels
-            ]
-            if np.isin(fl, np.concatenate(targets)).any():
-                deferred = True
-    n += 1 if (has_h or deferred) else 0
-    n += 1 if (c.sibc is not None or c.channels) else 0
-    return n
+    return {"h_sweep": h, "h_cpml": h_cpml, "e_sweep": e, "e_cpml": e_cpml, "edges": edges}
 
 
 def measured_peak() -> tuple[float, str]:
@@ -297,7 +281,8 @@ def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
     updates = float(cells) * c.batch * CHUNK * args.steps * ranks.world
     value = updates / (total_ms / 1e3) / 1e9
     kb = kernel_bytes(c)
-    dominant = max(("h_sweep", "e_sweep", "edges"), key=lambda k: ktimes.get(k, 0.0))
+    dominant = max(kb, key=lambda k: ktimes.get(k, 0.0))
+    graph_kernels = eng.graph_kernels()
     peak, peak_kind = measured_peak()
     achieved = kb[dominant] / (ktimes[dominant] / 1e3) / 1e9
     step_bytes = sum(kb.values())
@@ -371,7 +356,7 @@ def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
                 "step_frac": step_bytes / (ktimes["step"] / 1e3) / 1e9 / peak,
             },
             "e2e": e2e,
-            "gpu_launches": (launches_per_step(c) * CHUNK + 1) * args.steps,
+            "gpu_launches": graph_kernels * args.steps,
             "clocks": clocks,
             "cpu_baseline": cpu,
         }

@@ -193,9 +193,13 @@ int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_z, int32_t variant);
 
 /* Average device time per step of each kernel class over the last oafdtd_step call, measured
  * with CUDA events when profiling is on (oafdtd_set_profiling). Writes up to n values in the
- * order: h_sweep, ghosts, pre_e, e_sweep, edges, probe_e, whole step. */
+ * order: h_sweep, h_cpml, ghosts, pre_e, e_sweep, e_cpml, edges, probe_e, whole step. */
 int oafdtd_set_profiling(oafdtd_engine* engine, int32_t on);
 int oafdtd_kernel_times(oafdtd_engine* engine, double* out_ms, int32_t n);
+
+/* Kernel launches in one replay of the captured 64-step graph (0 before the first capture). A
+ * diagnostic of this library; the reference has no counterpart. */
+int oafdtd_graph_kernels(oafdtd_engine* engine, int64_t* out);
 
 /* Algorithmic DRAM bytes of one time step (all batch members) under the traffic model of the
  * engine: fields, index, CPML psi, ADE J, SIBC state. Used for the roofline report. */

@@ -58,6 +58,7 @@ struct EngineBase {
   int staged = 2;     // 2: sweeps staged by TMA; 1: staged by cp.async; 0: register marching
   bool tma_ok = false;  // the TMA descriptors were encoded (variant 2 available)
   bool graph_dirty = false;  // launch shape or profiling changed: the graph is re-captured
+  int64_t graph_kernels = 0;  // kernel nodes of the current captured 64-step graph (0: none)
   double model_bytes = 0.0;
 };
 
@@ -84,7 +85,8 @@ struct Engine final : EngineBase {
   double* energy_out = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   bool graph_ready = false;
-  static constexpr int kClasses = 6;  // h_sweep, ghosts, pre_e, e_sweep, edges, probe_e
+  // h_sweep, h_cpml, ghosts, pre_e, e_sweep, e_cpml, edges, probe_e
+  static constexpr int kClasses = 8;
   std::vector<cudaEvent_t> events;    // (kChunk, kClasses + 1) in profiling mode
   double prof_ms[kClasses + 1] = {};
   int64_t prof_steps = 0;
@@ -732,28 +734,36 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing) {
   const unsigned rec = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[0], stream, rec));
   err = oafdtd::launch_h_sweep<real>(sw, maps, stream);
-  if (err == cudaSuccess && sw.has_cpml) err = oafdtd::launch_cpml_pass<real>(cpml, sw, 1, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("h_sweep: ") + cudaGetErrorString(err));
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[1], stream, rec));
+  if (sw.has_cpml) {
+    err = oafdtd::launch_cpml_pass<real>(cpml, sw, 1, stream);
+    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("h_cpml: ") + cudaGetErrorString(err));
+  }
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[2], stream, rec));
   if (pmc_mask) {
     err = oafdtd::launch_ghosts<real>(sw.H, pmc_mask, nx, ny, nz, X, Y, B, stream);
     if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("ghosts: ") + cudaGetErrorString(err));
   }
-  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[2], stream, rec));
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[3], stream, rec));
   err = oafdtd::launch_pre_e<real>(pr, off, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("pre_e: ") + cudaGetErrorString(err));
-  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[3], stream, rec));
-  err = oafdtd::launch_e_sweep<real>(sw, maps, stream);
-  if (err == cudaSuccess && sw.has_cpml) err = oafdtd::launch_cpml_pass<real>(cpml, sw, 0, stream);
-  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("e_sweep: ") + cudaGetErrorString(err));
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[4], stream, rec));
+  err = oafdtd::launch_e_sweep<real>(sw, maps, stream);
+  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("e_sweep: ") + cudaGetErrorString(err));
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[5], stream, rec));
+  if (sw.has_cpml) {
+    err = oafdtd::launch_cpml_pass<real>(cpml, sw, 0, stream);
+    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("e_cpml: ") + cudaGetErrorString(err));
+  }
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[6], stream, rec));
   err = oafdtd::launch_sibc<real>(sb, stream);
   if (err == cudaSuccess) err = oafdtd::launch_edges<real>(ed, off, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("edges: ") + cudaGetErrorString(err));
-  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[5], stream, rec));
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[7], stream, rec));
   err = oafdtd::launch_probe_e<real>(pr, off, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("probe_e: ") + cudaGetErrorString(err));
-  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[6], stream, rec));
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[8], stream, rec));
   return OAFDTD_OK;
 }
 
@@ -764,6 +774,7 @@ int Engine<real>::capture() {
     graph_exec = nullptr;
   }
   graph_ready = false;
+  graph_kernels = 0;
   cudaGraph_t graph = nullptr;
   OA_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
   int rc = OAFDTD_OK;
@@ -779,9 +790,29 @@ int Engine<real>::capture() {
     return rc;
   }
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(err));
+  {
+    size_t n = 0;
+    err = cudaGraphGetNodes(graph, nullptr, &n);
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (err == cudaSuccess && n) err = cudaGraphGetNodes(graph, nodes.data(), &n);
+    int64_t kernels = 0;
+    for (size_t q = 0; q < n && err == cudaSuccess; ++q) {
+      cudaGraphNodeType t;
+      err = cudaGraphNodeGetType(nodes[q], &t);
+      if (err == cudaSuccess && t == cudaGraphNodeTypeKernel) ++kernels;
+    }
+    if (err != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      return fail(OAFDTD_E_CUDA, std::string("graph nodes: ") + cudaGetErrorString(err));
+    }
+    graph_kernels = kernels;
+  }
   err = cudaGraphInstantiate(&graph_exec, graph, 0);
   cudaGraphDestroy(graph);
-  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(err));
+  if (err != cudaSuccess) {
+    graph_kernels = 0;
+    return fail(OAFDTD_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(err));
+  }
   graph_ready = true;
   return OAFDTD_OK;
 }
@@ -793,6 +824,7 @@ int Engine<real>::step(int64_t n) {
   OA_CUDA(cudaSetDevice(device));
   if (graph_dirty) {
     graph_ready = false;
+    graph_kernels = 0;
     graph_dirty = false;
   }
   if (profiling && events.empty()) {
@@ -1077,6 +1109,12 @@ int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_z, int32_t variant) {
   if (tile_z) engine->impl->tile_z = tile_z;
   if (variant >= 0) engine->impl->staged = variant;
   engine->impl->graph_dirty = true;  // a new launch shape needs a new graph
+  return OAFDTD_OK;
+}
+
+int oafdtd_graph_kernels(oafdtd_engine* engine, int64_t* out) {
+  if (!engine || !out) return fail(OAFDTD_E_INVALID, "null argument");
+  *out = engine->impl->graph_kernels;
   return OAFDTD_OK;
 }
 

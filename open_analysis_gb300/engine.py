@@ -268,7 +268,13 @@ class Gb300Engine:
     def set_profiling(self, on: bool) -> None:
         native.check(self._lib.oafdtd_set_profiling(self._h, int(bool(on))), "set_profiling")
 
-    KERNELS = ("h_sweep", "ghosts", "pre_e", "e_sweep", "edges", "probe_e", "step")
+    KERNELS = ("h_sweep", "h_cpml", "ghosts", "pre_e", "e_sweep", "e_cpml", "edges", "probe_e", "step")
+
+    def graph_kernels(self) -> int:
+        """Kernel launches in one replay of the captured 64-step graph (0 before a capture)."""
+        out = C.c_int64()
+        native.check(self._lib.oafdtd_graph_kernels(self._h, C.byref(out)), "graph_kernels")
+        return int(out.value)
 
     def kernel_times(self) -> dict[str, float]:
         """Average device ms per time step of each kernel class over the last ``step`` call."""

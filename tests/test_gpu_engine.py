@@ -200,7 +200,10 @@ def test_kernel_profile_and_model_bytes() -> None:
     eng.set_profiling(True)
     eng.step(64)
     t = eng.kernel_times()
-    assert t["step"] > 0 and t["h_sweep"] > 0 and t["e_sweep"] > 0
+    assert t["step"] > 0 and t["h_sweep"] > 0 and t["e_sweep"] > 0 and t["e_cpml"] > 0
+    assert t["step"] >= t["h_sweep"] + t["e_sweep"]
+    # one replay: two sweeps, six correction passes, pre_e / edges / probe_e per time step
+    assert eng.graph_kernels() >= 64 * 8
     assert eng.model_bytes() > 0
 
 
