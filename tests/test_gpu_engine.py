@@ -202,8 +202,9 @@ def test_kernel_profile_and_model_bytes() -> None:
     t = eng.kernel_times()
     assert t["step"] > 0 and t["h_sweep"] > 0 and t["e_sweep"] > 0 and t["e_cpml"] > 0
     assert t["step"] >= t["h_sweep"] + t["e_sweep"]
-    # one replay: two sweeps, six correction passes, pre_e / edges / probe_e per time step
-    assert eng.graph_kernels() >= 64 * 8
+    # one replay: the same kernels for each of the 64 time steps, then the step-counter bump
+    n = eng.graph_kernels()
+    assert n >= 64 * 2 + 1 and (n - 1) % 64 == 0, n
     assert eng.model_bytes() > 0
 
 
