@@ -14,8 +14,9 @@ advances between energy checks. Gcell-updates/s = interior cells x batch x time 
 * ``e2e``: the same metric through the public API from host buffers: engine creation (the host
   ``Compiled`` arrays copied to the device), K chunks each followed by the energy check (a device
   to host read, as the run loop does), the probe DFTs read back at the end; host wall clock.
-* ``roofline``: the dominant kernel's algorithmic bytes per launch (traffic model below) over its
-  average launch time measured with CUDA events inside the timed region.
+* ``roofline``: the dominant kernel's algorithmic bytes per launch (the engine's traffic model,
+  ``Gb300Engine.kernel_bytes``) over its average launch time measured with CUDA events inside the
+  timed region.
 * ``cpu_baseline``: the CPU oracle (the reference's NumPy engine restated) in float32 on the same
   compiled problem, a bounded sample of time steps, one host thread.
 
@@ -138,37 +139,7 @@ class ClockSampler:
         }
 
 
-# ---------------------------------------------------------------------------- traffic model
-def kernel_bytes(c: Any, real: int = 4) -> dict[str, float]:
-    """Algorithmic DRAM bytes per step of each kernel class (all batch members).
-
-    h_sweep: read 3 E, read-modify-write 3 H per interior cell and member (36 B in float32).
-    e_sweep: read 3 H, read-modify-write 3 E (36 B) per cell and member, the three uint16 indices
-    once per cell (6 B), the Debye current J read+write (8 B per pole) per dispersive edge.
-    h_cpml / e_cpml (the correction passes, one launch per derivative axis): per cell of every
-    correction box and member, psi read+write and the corrected field read+write (16 B), the
-    source field once (4 B), and for E the uint16 index (2 B, once per cell).
-    edges: per surface-impedance edge J_prev and v_p read+write (8 B (1 + P)), two H samples
-    (8 B) and the E write (4 B), per member.
-    """
-    nx, ny, nz = c.grid.n
-    cells = float(nx * ny * nz)
-    b = c.batch
-    box = {"E": 0.0, "H": 0.0}
-    for k in c.pml.corrections:
-        box[k.kind] += float(np.prod(k.shape))
-    h = cells * b * 9 * real
-    e = cells * b * 9 * real + cells * 6
-    if c.ade is not None:
-        e += sum(f.size for f in c.ade.flat) * b * c.ade.tau.size * 2 * real
-    h_cpml = box["H"] * b * 5 * real
-    e_cpml = box["E"] * (b * 5 * real + 2)
-    edges = 0.0
-    if c.sibc is not None:
-        edges = c.sibc.flat.size * b * (2 * real * (1 + c.sibc.cp.size) + 2 * real + real)
-    return {"h_sweep": h, "h_cpml": h_cpml, "e_sweep": e, "e_cpml": e_cpml, "edges": edges}
-
-
+# ---------------------------------------------------------------------------- roofline inputs
 def measured_peak() -> tuple[float, str]:
     path = ROOT / "MEASURED_PEAKS.json"
     if path.exists():
@@ -280,12 +251,13 @@ def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
     total_ms = ranks.max(float(sum(times)))
     updates = float(cells) * c.batch * CHUNK * args.steps * ranks.world
     value = updates / (total_ms / 1e3) / 1e9
-    kb = kernel_bytes(c)
+    all_bytes = eng.kernel_bytes()  # the engine's traffic model, per time step and kernel class
+    kb = {k: v for k, v in all_bytes.items() if k != "step" and v > 0}
     dominant = max(kb, key=lambda k: ktimes.get(k, 0.0))
     graph_kernels = eng.graph_kernels()
     peak, peak_kind = measured_peak()
     achieved = kb[dominant] / (ktimes[dominant] / 1e3) / 1e9
-    step_bytes = sum(kb.values())
+    step_bytes = all_bytes["step"]
     eng.close()
 
     # e2e through the public API with host buffers

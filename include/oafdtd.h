@@ -193,9 +193,17 @@ int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_z, int32_t variant);
 
 /* Average device time per step of each kernel class over the last oafdtd_step call, measured
  * with CUDA events when profiling is on (oafdtd_set_profiling). Writes up to n values in the
- * order: h_sweep, h_cpml, ghosts, pre_e, e_sweep, e_cpml, edges, probe_e, whole step. */
+ * order: h_sweep (interior, staged), h_slab (CPML slabs, or everything in variant 0), ghosts,
+ * pre_e, e_sweep, e_slab, edges, probe_e, whole step. */
 int oafdtd_set_profiling(oafdtd_engine* engine, int32_t on);
 int oafdtd_kernel_times(oafdtd_engine* engine, double* out_ms, int32_t n);
+
+/* Algorithmic DRAM bytes per time step of each kernel class under the current sweep variant, in
+ * the order of oafdtd_kernel_times, then their sum; up to n values. The traffic model: 9 field
+ * values per grid cell and batch member for each sweep (E also its three uint16 indices per
+ * cell and the Debye currents), psi read+write per CPML cell, the surface-impedance state per
+ * edge. A diagnostic of this library; the reference has no counterpart. */
+int oafdtd_kernel_bytes(oafdtd_engine* engine, double* out, int32_t n);
 
 /* Kernel launches in one replay of the captured 64-step graph (0 before the first capture). A
  * diagnostic of this library; the reference has no counterpart. */

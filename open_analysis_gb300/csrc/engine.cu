@@ -59,6 +59,9 @@ struct EngineBase {
   bool tma_ok = false;  // the TMA descriptors were encoded (variant 2 available)
   bool graph_dirty = false;  // launch shape or profiling changed: the graph is re-captured
   int64_t graph_kernels = 0;  // kernel nodes of the current captured 64-step graph (0: none)
+  // kernel classes: h_sweep, h_slab, ghosts, pre_e, e_sweep, e_slab, edges, probe_e
+  static constexpr int kClasses = 8;
+  double class_bytes[2][kClasses] = {};  // algorithmic bytes per step and class ([staged?][class])
   double model_bytes = 0.0;
 };
 
@@ -66,7 +69,10 @@ template <typename real>
 struct Engine final : EngineBase {
   int device = 0;
   cudaStream_t stream = nullptr;
-  oafdtd::CpmlPass<real> cpml{};
+  oafdtd::Span3 inner_staged[2]{};     // interior boxes (E, H) when the staged sweeps run
+  oafdtd::Span3 slab_staged[2][6]{};   // the slab boxes around them
+  int n_slab_staged[2] = {0, 0};
+  oafdtd::Span3 whole{};               // the whole update domain (variant 0: slab kernel only)
   std::vector<void*> allocs;
   int nx = 0, ny = 0, nz = 0, X = 0, Y = 0, Z = 0, B = 0;
   long long bs = 0;
@@ -85,8 +91,6 @@ struct Engine final : EngineBase {
   double* energy_out = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   bool graph_ready = false;
-  // h_sweep, h_cpml, ghosts, pre_e, e_sweep, e_cpml, edges, probe_e
-  static constexpr int kClasses = 8;
   std::vector<cudaEvent_t> events;    // (kChunk, kClasses + 1) in profiling mode
   double prof_ms[kClasses + 1] = {};
   int64_t prof_steps = 0;
@@ -145,6 +149,21 @@ struct Engine final : EngineBase {
 
   int step(int64_t n) override;
   int check_status();
+  // The sweep regions of the current variant: interior + slab boxes, or the slab kernel alone.
+  void use_regions() {
+    sw.staged = staged;
+    for (int kind = 0; kind < 2; ++kind) {
+      if (staged) {
+        sw.inner[kind] = inner_staged[kind];
+        sw.n_slab[kind] = n_slab_staged[kind];
+        for (int n = 0; n < 6; ++n) sw.slab[kind][n] = slab_staged[kind][n];
+      } else {
+        sw.inner[kind] = oafdtd::Span3{0, 0, 0, 0, 0, 0};
+        sw.n_slab[kind] = 1;
+        sw.slab[kind][0] = whole;
+      }
+    }
+  }
   int energy(double* out) override;
   int dft(double* out) override;
   int series(double* out) override;
@@ -205,10 +224,19 @@ int Engine<real>::build(const oafdtd_problem& p) {
   auto injected = [&](int c, long long f) {
     return std::binary_search(inj_sorted.begin(), inj_sorted.end(), std::make_pair(c, f));
   };
+  // surface-impedance edges: a dispersive one is updated after the surface impedance sets it
+  std::vector<std::pair<int, long long>> sibc_sorted;
+  sibc_sorted.reserve((size_t)p.sibc_n);
+  for (int64_t s = 0; s < p.sibc_n; ++s) sibc_sorted.emplace_back(p.sibc_comp[s], p.sibc_flat[s]);
+  std::sort(sibc_sorted.begin(), sibc_sorted.end());
+  auto on_sibc = [&](int c, long long f) {
+    return std::binary_search(sibc_sorted.begin(), sibc_sorted.end(), std::make_pair(c, f));
+  };
 
   // ---- combined table. Entry key: (category, material index, ADE row); categories 0 plain,
-  // 1 dispersive, 2 dispersive with injection (deferred). The map orders entries by category, so
-  // the kernels tell dispersive entries by an index range.
+  // 1 dispersive, 2 dispersive with injection or surface impedance (deferred to the edge pass,
+  // after those). The map orders entries by category, so the kernels tell dispersive entries by
+  // an index range.
   // Debye rows (cbe, beta_0..P-1) in the field precision; consecutive edges mostly share a row,
   // so the last row is checked first and a hash map finds the others.
   std::unordered_map<uint64_t, std::vector<int>> ade_row_by_hash;
@@ -253,7 +281,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
       row[0] = (real)p.ade_cbe[c][e];
       for (int q = 0; q < P; ++q) row[1 + q] = (real)p.ade_beta[c][(size_t)q * ne + e];
       const int rid = row_id();
-      const int defer = injected(c, f) ? 1 : 0;
+      const int defer = (injected(c, f) || on_sibc(c, f)) ? 1 : 0;
       ade_edges[c].push_back({f, rid, defer});
       const std::tuple<int, int, int> key{1 + defer, idx[f], rid};
       if (key != last_key) {
@@ -420,22 +448,6 @@ int Engine<real>::build(const oafdtd_problem& p) {
       term_ref.side[side].hi[ax] = k.hi[ax];
     }
   }
-  // correction passes: per kind and derivative axis, every (component, side) with a psi array
-  for (int kind = 0; kind < 2; ++kind)
-    for (int c = 0; c < 3; ++c)
-      for (int t = 0; t < 2; ++t) {
-        const oafdtd::CpmlTerm<real>& T = kind == 0 ? sw.ecorr[c][t] : sw.hcorr[c][t];
-        for (int sd = 0; sd < 2; ++sd) {
-          if (T.side[sd].psi == nullptr) continue;
-          oafdtd::CpmlAxisPass<real>& ap = cpml.axis[kind][T.axis];
-          if (ap.n >= 4) return fail(OAFDTD_E_INVALID, "more than four CPML corrections on one axis");
-          ap.comp[ap.n] = c;
-          ap.src[ap.n] = T.src;
-          ap.sign[ap.n] = T.sign;
-          ap.side[ap.n] = &T.side[sd];
-          ++ap.n;
-        }
-      }
   sw.dtmu = (real)p.dtmu;
   sw.nx = nx;
   sw.ny = ny;
@@ -489,10 +501,6 @@ int Engine<real>::build(const oafdtd_problem& p) {
       r.flat = p.inj_flat[t];
       r.inj.push_back((int)t);
     }
-  }
-  for (auto& cf : deferred) {
-    EdgeRec& r = edges[cf];
-    if (r.sibc >= 0) return fail(OAFDTD_E_INVALID, "an edge is both dispersive and surface-impedance");
   }
   {
     std::vector<int8_t> comp;
@@ -703,24 +711,90 @@ int Engine<real>::build(const oafdtd_problem& p) {
     if (int rc = alloc(&energy_partial, (size_t)6 * oafdtd::kEnergyBlocks)) return rc;
     if (int rc = alloc(&energy_out, 6)) return rc;
   }
-  // ---- traffic model (bytes per time step, all batch members)
+  // ---- sweep regions: per kind, an interior box free of CPML cells (staged sweeps) and the slab
+  // boxes around it (slab kernel)
   {
-    // H sweep: read 3 E, read-modify-write 3 H; E sweep: read 3 H, read-modify-write 3 E:
-    // 18 values per interior cell and batch member, plus the three uint16 indices per cell.
-    const double cells = (double)nx * ny * nz;
+    const int Q = X / 4;
+    whole = oafdtd::Span3{0, Q, 1, ny + 2, 1, nz + 2};
+    for (int kind = 0; kind < 2; ++kind) {
+      int lo[3] = {0, 1, 1}, hi[3] = {X, ny + 2, nz + 2};
+      for (int c = 0; c < 3; ++c)
+        for (int t = 0; t < 2; ++t) {
+          const oafdtd::CpmlTerm<real>& T = kind == 0 ? sw.ecorr[c][t] : sw.hcorr[c][t];
+          for (int sd = 0; sd < 2; ++sd) {
+            const oafdtd::CpmlSide<real>& S = T.side[sd];
+            if (S.psi == nullptr) continue;
+            const int ax = T.axis;
+            if (S.lo[ax] <= 1)
+              lo[ax] = std::max(lo[ax], S.hi[ax]);
+            else
+              hi[ax] = std::min(hi[ax], S.lo[ax]);
+          }
+        }
+      const int qa = std::min((lo[0] + 3) / 4, Q), qb = std::max(std::min(hi[0] / 4, Q), qa);
+      const int ja = std::min(std::max(lo[1], 1), ny + 2), jb = std::max(std::min(hi[1], ny + 2), ja);
+      const int ka = std::min(std::max(lo[2], 1), nz + 2), kb = std::max(std::min(hi[2], nz + 2), ka);
+      inner_staged[kind] = oafdtd::Span3{qa, qb, ja, jb, ka, kb};
+      const oafdtd::Span3 boxes[6] = {{0, Q, 1, ny + 2, 1, ka},  {0, Q, 1, ny + 2, kb, nz + 2},
+                                      {0, Q, 1, ja, ka, kb},     {0, Q, jb, ny + 2, ka, kb},
+                                      {0, qa, ja, jb, ka, kb},   {qb, Q, ja, jb, ka, kb}};
+      int n = 0;
+      for (const oafdtd::Span3& bx : boxes)
+        if (bx.q1 > bx.q0 && bx.j1 > bx.j0 && bx.k1 > bx.k0) slab_staged[kind][n++] = bx;
+      n_slab_staged[kind] = n;
+    }
+    use_regions();
+  }
+  // ---- traffic model: algorithmic bytes per time step and kernel class, all batch members.
+  // Sweeps: read 3 source components, read-modify-write 3 updated ones (9 values) per grid cell
+  // and member; E also the three uint16 indices per cell and J read+write (2 P values) per
+  // dispersive edge. Slab kernel: the same for its cells plus psi read+write per correction cell.
+  // Edges: surface-impedance v_p and J_prev read+write, two H samples and the E write per edge.
+  {
     const double rb = sizeof(real);
-    double mb = cells * B * 18.0 * rb + cells * 6.0;
-    double psi_cells = 0.0;
+    auto cells_in = [&](const oafdtd::Span3& s) {
+      const double x = std::max(0, std::min(4 * s.q1, nx + 1) - std::max(4 * s.q0, 1));
+      const double y = std::max(0, std::min(s.j1, ny + 1) - std::max(s.j0, 1));
+      const double z = std::max(0, std::min(s.k1, nz + 1) - std::max(s.k0, 1));
+      return x * y * z;
+    };
+    auto inside = [](const oafdtd::Span3& s, long long f, long long X_, long long Y_) {
+      const long long k = f / (X_ * Y_), j = (f / X_) % Y_, i = f % X_;
+      return i >= 4 * s.q0 && i < 4 * s.q1 && j >= s.j0 && j < s.j1 && k >= s.k0 && k < s.k1;
+    };
+    const double cells = (double)nx * ny * nz;
+    double psi[2] = {0.0, 0.0};
     for (int n = 0; n < p.n_corr; ++n) {
       const oafdtd_correction& k = p.corr[n];
-      psi_cells += (double)(k.hi[0] - k.lo[0]) * (k.hi[1] - k.lo[1]) * (k.hi[2] - k.lo[2]);
+      psi[k.kind] += (double)(k.hi[0] - k.lo[0]) * (k.hi[1] - k.lo[1]) * (k.hi[2] - k.lo[2]) * B * 2.0 * rb;
     }
-    mb += psi_cells * B * 2.0 * rb;  // psi read + write
-    double ade_edges = 0.0;
-    for (int c = 0; c < 3; ++c) ade_edges += (double)(P > 0 ? p.ade_n[c] : 0);
-    mb += ade_edges * B * P * 2.0 * rb;  // J read + write
-    mb += (double)p.sibc_n * B * (2.0 * rb * (1 + p.sibc_poles) + 2.0 * rb);  // v, Jprev RMW; 2 H samples
-    model_bytes = mb;
+    double j_in = 0.0, j_all = 0.0, j_def = 0.0;
+    for (int c = 0; c < 3; ++c)
+      for (const AdeEdge& ae : ade_edges[c]) {
+        const double v = (double)B * P * 2.0 * rb;
+        if (ae.defer) {
+          j_def += v;
+          continue;
+        }
+        j_all += v;
+        if (inside(inner_staged[0], ae.f, X, Y)) j_in += v;
+      }
+    const double h_in = cells_in(inner_staged[1]), e_in = cells_in(inner_staged[0]);
+    const double per_h = B * 9.0 * rb, per_e = B * 9.0 * rb + 6.0;
+    const double edges = (double)p.sibc_n * B * (2.0 * rb * (1 + p.sibc_poles) + 3.0 * rb) + j_def;
+    // classes: h_sweep, h_slab, ghosts, pre_e, e_sweep, e_slab, edges, probe_e
+    double* st = class_bytes[1];
+    st[0] = h_in * per_h;
+    st[1] = (cells - h_in) * per_h + psi[1];
+    st[4] = e_in * per_e + j_in;
+    st[5] = (cells - e_in) * per_e + psi[0] + (j_all - j_in);
+    st[6] = edges;
+    double* sl = class_bytes[0];
+    sl[1] = cells * per_h + psi[1];
+    sl[5] = cells * per_e + psi[0] + j_all;
+    sl[6] = edges;
+    model_bytes = 0.0;
+    for (int k = 0; k < kClasses; ++k) model_bytes += st[k];
   }
   OA_CUDA(cudaStreamSynchronize(stream));
   return OAFDTD_OK;
@@ -733,13 +807,13 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing) {
   // inside a stream capture an event record becomes a graph node only with the external flag
   const unsigned rec = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[0], stream, rec));
-  err = oafdtd::launch_h_sweep<real>(sw, maps, stream);
-  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("h_sweep: ") + cudaGetErrorString(err));
-  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[1], stream, rec));
-  if (sw.has_cpml) {
-    err = oafdtd::launch_cpml_pass<real>(cpml, sw, 1, stream);
-    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("h_cpml: ") + cudaGetErrorString(err));
+  if (sw.staged) {
+    err = oafdtd::launch_staged_sweep<real>(sw, maps, stream, true);
+    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("h_sweep: ") + cudaGetErrorString(err));
   }
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[1], stream, rec));
+  err = oafdtd::launch_slab<real>(sw, 1, stream);
+  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("h_slab: ") + cudaGetErrorString(err));
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[2], stream, rec));
   if (pmc_mask) {
     err = oafdtd::launch_ghosts<real>(sw.H, pmc_mask, nx, ny, nz, X, Y, B, stream);
@@ -749,13 +823,13 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing) {
   err = oafdtd::launch_pre_e<real>(pr, off, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("pre_e: ") + cudaGetErrorString(err));
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[4], stream, rec));
-  err = oafdtd::launch_e_sweep<real>(sw, maps, stream);
-  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("e_sweep: ") + cudaGetErrorString(err));
-  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[5], stream, rec));
-  if (sw.has_cpml) {
-    err = oafdtd::launch_cpml_pass<real>(cpml, sw, 0, stream);
-    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("e_cpml: ") + cudaGetErrorString(err));
+  if (sw.staged) {
+    err = oafdtd::launch_staged_sweep<real>(sw, maps, stream, false);
+    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("e_sweep: ") + cudaGetErrorString(err));
   }
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[5], stream, rec));
+  err = oafdtd::launch_slab<real>(sw, 0, stream);
+  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("e_slab: ") + cudaGetErrorString(err));
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[6], stream, rec));
   err = oafdtd::launch_sibc<real>(sb, stream);
   if (err == cudaSuccess) err = oafdtd::launch_edges<real>(ed, off, stream);
@@ -833,7 +907,7 @@ int Engine<real>::step(int64_t n) {
     graph_ready = false;
   }
   sw.tile_z = tile_z;
-  sw.staged = staged;
+  use_regions();
   if (profiling) {
     for (double& v : prof_ms) v = 0.0;
     prof_steps = 0;
@@ -1115,6 +1189,19 @@ int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_z, int32_t variant) {
 int oafdtd_graph_kernels(oafdtd_engine* engine, int64_t* out) {
   if (!engine || !out) return fail(OAFDTD_E_INVALID, "null argument");
   *out = engine->impl->graph_kernels;
+  return OAFDTD_OK;
+}
+
+int oafdtd_kernel_bytes(oafdtd_engine* engine, double* out, int32_t n) {
+  if (!engine || !out || n < 0) return fail(OAFDTD_E_INVALID, "null argument");
+  EngineBase& e = *engine->impl;
+  const double* cls = e.class_bytes[e.staged ? 1 : 0];
+  double total = 0.0;
+  for (int k = 0; k < EngineBase::kClasses; ++k) {
+    if (k < n) out[k] = cls[k];
+    total += cls[k];
+  }
+  if (n > EngineBase::kClasses) out[EngineBase::kClasses] = total;
   return OAFDTD_OK;
 }
 

@@ -42,19 +42,10 @@ struct CpmlTerm {    // the correction of one (kind, component, derivative axis)
   CpmlSide<real> side[2];
 };
 
-// The corrections of one (kind, derivative axis): up to two components times two sides.
-template <typename real>
-struct CpmlAxisPass {
-  int n;
-  int comp[4];
-  int src[4];
-  real sign[4];
-  const CpmlSide<real>* side[4];
-};
-
-template <typename real>
-struct CpmlPass {
-  CpmlAxisPass<real> axis[2][3];  // [kind 0 E / 1 H][axis]
+// A box of the update domain: quads [q0, q1) (x cells 4 q0 .. 4 q1), rows [j0, j1), planes
+// [k0, k1).
+struct Span3 {
+  int q0, q1, j0, j1, k0, k1;
 };
 
 // One entry of the combined material table: update coefficients of the averaged material and,
@@ -89,9 +80,15 @@ struct SweepArgs {
   int nx, ny, nz, X, Y;
   long long bs;             // Z * Y * X
   int B;
-  int tile_z;       // planes marched per thread (register variant) or per block (staged)
-  int staged;       // 2: staged by TMA tensor copies; 1: staged by cp.async; 0: register marching
+  int tile_z;       // planes marched per thread (slab kernel) or per block (staged sweeps)
+  int staged;       // 2: staged by TMA tensor copies; 1: staged by cp.async; 0: slab kernel only
   int* status;      // device status word: bit 0 set when a bounded wait of a sweep gave up
+  // Per kind ([0] E, [1] H): the interior box, which holds no CPML correction cell and is swept
+  // by the staged kernels, and up to six disjoint boxes covering the rest of the update domain,
+  // marched by the slab kernel (bulk update, corrections, Debye update).
+  Span3 inner[2];
+  Span3 slab[2][6];
+  int n_slab[2];
 };
 
 // TMA descriptors of the staged sweeps: per component, the field arrays as 4-D tensors
@@ -210,7 +207,7 @@ cudaError_t launch_h_sweep(const SweepArgs<real>& a, const SweepMaps& m, cudaStr
 template <typename real>
 cudaError_t launch_e_sweep(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_t s);
 template <typename real>
-cudaError_t launch_cpml_pass(const CpmlPass<real>& pass, const SweepArgs<real>& a, int kind, cudaStream_t s);
+cudaError_t launch_slab(const SweepArgs<real>& a, int kind, cudaStream_t s);
 template <typename real>
 cudaError_t launch_ghosts(real* const H[3], int pmc_mask, int nx, int ny, int nz, int X, int Y, int B,
                           cudaStream_t s);

@@ -16,10 +16,10 @@
 // bit 0 of the status word, waits (bounded again) for the copies it issued and returns; the host
 // reports OAFDTD_E_TIMEOUT.
 //
-// One launch per sweep gives every cell its bulk update (and, in the E sweep, its Debye update);
-// the CPML corrections follow in the correction passes (cpml.cu). The arithmetic is the
-// reference's, operation by operation (packages/oa-fdtd/src/oa_fdtd/reference.py:152-180,
-// :119-127).
+// These kernels cover the interior box of each sweep, which holds no CPML correction cell: every
+// cell gets its bulk update (and, in the E sweep, its Debye update). The slab kernel (slab.cu)
+// covers the rest. The arithmetic is the reference's, operation by operation
+// (packages/oa-fdtd/src/oa_fdtd/reference.py:152-180, :119-127).
 
 #include <mutex>
 
@@ -189,13 +189,14 @@ __global__ void __launch_bounds__(256, 2)
   const int tx = threadIdx.x, ty = threadIdx.y;
   const bool leader = tx == 0 && ty == 0;
   const int nx = a.nx, ny = a.ny, nz = a.nz, X = a.X, Y = a.Y, Z = nz + 2;
-  const int x0 = blockIdx.x * kTW, y0 = 1 + blockIdx.y * kTY;
-  const int nkc = (nz + 1 + a.tile_z - 1) / a.tile_z;
+  const Span3 in = a.inner[1];
+  const int x0 = 4 * (in.q0 + blockIdx.x * kTQ), y0 = in.j0 + blockIdx.y * kTY;
+  const int nkc = (in.k1 - in.k0 + a.tile_z - 1) / a.tile_z;
   const int b = blockIdx.z / nkc, kc = blockIdx.z % nkc;
-  const int k0 = 1 + kc * a.tile_z, k1 = min(k0 + a.tile_z, nz + 2);
+  const int k0 = in.k0 + kc * a.tile_z, k1 = min(k0 + a.tile_z, in.k1);
   const int n_stage = k1 < Z ? k1 - k0 + 1 : k1 - k0;
   const int i0 = x0 + 4 * tx, j = y0 + ty;
-  const bool live = i0 < X && j <= ny + 1 && i0 <= nx + 1;
+  const bool live = i0 < 4 * in.q1 && j < in.j1 && i0 <= nx + 1;
   const long long base = (long long)b * a.bs;
   const real dtmu = a.dtmu;
   const Quad<real> ipx = i0 < X ? ld4(a.ip[0] + i0) : Quad<real>{};
@@ -428,14 +429,15 @@ __global__ void __launch_bounds__(256, 2)
   ESlot<real>* slot = reinterpret_cast<ESlot<real>*>(align_smem(smem_raw));
   const int tx = threadIdx.x, ty = threadIdx.y;
   const bool leader = tx == 0 && ty == 0;
-  const int nx = a.nx, ny = a.ny, nz = a.nz, X = a.X, Y = a.Y;
-  const int x0 = blockIdx.x * kTW, y0 = 1 + blockIdx.y * kTY;
-  const int nkc = (nz + 1 + a.tile_z - 1) / a.tile_z;
+  const int nx = a.nx, X = a.X, Y = a.Y;
+  const Span3 in = a.inner[0];
+  const int x0 = 4 * (in.q0 + blockIdx.x * kTQ), y0 = in.j0 + blockIdx.y * kTY;
+  const int nkc = (in.k1 - in.k0 + a.tile_z - 1) / a.tile_z;
   const int b = blockIdx.z / nkc, kc = blockIdx.z % nkc;
-  const int k0 = 1 + kc * a.tile_z, k1 = min(k0 + a.tile_z, nz + 2);
+  const int k0 = in.k0 + kc * a.tile_z, k1 = min(k0 + a.tile_z, in.k1);
   const int n_stage = k1 - k0;
   const int i0 = x0 + 4 * tx, j = y0 + ty;
-  const bool live = i0 < X && j <= ny + 1 && i0 <= nx + 1;
+  const bool live = i0 < 4 * in.q1 && j < in.j1 && i0 <= nx + 1;
   const long long base = (long long)b * a.bs;
   const Quad<real> idx4 = i0 < X ? ld4(a.idd[0] + i0) : Quad<real>{};
   const real idy = a.idd[1][min(j, Y - 1)];
@@ -538,9 +540,11 @@ __global__ void __launch_bounds__(256, 2)
 // ------------------------------------------------------------------------------------- launch
 template <typename real>
 cudaError_t launch_staged_sweep(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_t s, bool h) {
-  const int nkc = (a.nz + 1 + a.tile_z - 1) / a.tile_z;
+  const Span3 in = a.inner[h ? 1 : 0];
+  if (in.q1 <= in.q0 || in.j1 <= in.j0 || in.k1 <= in.k0) return cudaSuccess;
+  const int nkc = (in.k1 - in.k0 + a.tile_z - 1) / a.tile_z;
   dim3 block(kTQ, kTY);
-  dim3 grid((a.X + kTW - 1) / kTW, (a.ny + 1 + kTY - 1) / kTY, nkc * a.B);
+  dim3 grid((in.q1 - in.q0 + kTQ - 1) / kTQ, (in.j1 - in.j0 + kTY - 1) / kTY, nkc * a.B);
   const bool tma = a.staged == 2;
   cudaError_t err;
   if (h) {

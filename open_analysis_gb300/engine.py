@@ -268,7 +268,14 @@ class Gb300Engine:
     def set_profiling(self, on: bool) -> None:
         native.check(self._lib.oafdtd_set_profiling(self._h, int(bool(on))), "set_profiling")
 
-    KERNELS = ("h_sweep", "h_cpml", "ghosts", "pre_e", "e_sweep", "e_cpml", "edges", "probe_e", "step")
+    KERNELS = ("h_sweep", "h_slab", "ghosts", "pre_e", "e_sweep", "e_slab", "edges", "probe_e", "step")
+
+    def kernel_bytes(self) -> dict[str, float]:
+        """Algorithmic DRAM bytes per time step of each kernel class (keys of ``kernel_times``;
+        ``step`` is their sum) under the current sweep variant."""
+        out = np.zeros(len(self.KERNELS))
+        native.check(self._lib.oafdtd_kernel_bytes(self._h, _ptr(out, C.c_double), len(out)), "kernel_bytes")
+        return dict(zip(self.KERNELS, out.tolist(), strict=True))
 
     def graph_kernels(self) -> int:
         """Kernel launches in one replay of the captured 64-step graph (0 before a capture)."""

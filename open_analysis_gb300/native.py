@@ -153,6 +153,7 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "oafdtd_kernel_times": (C.c_int, [C.c_void_p, _pd, _i32]),
     "oafdtd_model_bytes": (C.c_int, [C.c_void_p, _pd]),
     "oafdtd_graph_kernels": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "oafdtd_kernel_bytes": (C.c_int, [C.c_void_p, _pd, _i32]),
     "oafdtd_energy_noalloc": (C.c_int, [C.POINTER(EnergyView), _pd]),
 }
 

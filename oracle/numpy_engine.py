@@ -17,16 +17,9 @@ float32 fields bit for bit and a float64 run is the FP64 error yardstick:
 Its agreement with the reference itself is pinned by ``tests/golden`` (fixtures generated by
 importing the reference; see ``tests/golden/make_golden.py``).
 
-``order="engine"`` restates the GPU engine's order of the same arithmetic, so that the engine can be
-checked bit for bit where its order differs from the reference's:
-
-* the Debye update of a dispersive edge runs right after its bulk E update, before the CPML
-  corrections; each correction t of such an edge then also moves every current J_p by beta_p t
-  (the reference corrects first, then updates J_p from the corrected field: the same values up
-  to rounding). Dispersive edges that take an injection keep the reference's place, after SIBC
-  and injection;
-* the pole sum of the Debye update is a plain loop over the poles in index order (NumPy's einsum
-  may reorder or fuse it on some hosts).
+``pole_sum="loop"`` sums the Debye poles in a plain loop in index order, the order the GPU engine
+uses; the reference's ``np.einsum`` (the default here) may reorder or fuse that sum on some hosts,
+which changes the rounding of multi-pole runs only.
 """
 
 from __future__ import annotations
@@ -67,11 +60,11 @@ class OracleEngine:
     name = "oracle"
 
     def __init__(
-        self, c: Any, dtype: str = "float64", record_series: bool = False, order: str = "reference", **_: Any
+        self, c: Any, dtype: str = "float64", record_series: bool = False, pole_sum: str = "einsum", **_: Any
     ) -> None:
-        if order not in ("reference", "engine"):
-            raise ValueError(f"order must be 'reference' or 'engine', not {order!r}")
-        self.order = order
+        if pole_sum not in ("einsum", "loop"):
+            raise ValueError(f"pole_sum must be 'einsum' or 'loop', not {pole_sum!r}")
+        self.pole_sum = pole_sum
         self.c = c
         self.record_series = record_series
         self.dtype = np.dtype(dtype)
@@ -124,14 +117,6 @@ class OracleEngine:
                 }
             )
         self._kp = a.kp.astype(real)
-        # dispersive edges that take an injection (the engine updates them after the injection)
-        injected: list[set[int]] = [set(), set(), set()]
-        for ch in c.channels:
-            comps = np.broadcast_to(np.asarray(ch["comp"]), ch["flat"].shape)
-            for cc, f in zip(comps.tolist(), np.asarray(ch["flat"]).tolist(), strict=True):
-                injected[int(cc)].add(int(f))
-        for st in self._ade:
-            st["late"] = np.array([int(f) in injected[st["c"]] for f in st["flat"].tolist()], bool)
 
     def _setup_sibc(self) -> None:
         c, real, batch = self.c, self.dtype, self.c.batch
@@ -153,52 +138,22 @@ class OracleEngine:
         for st in self._ade:
             st["eold"][...] = self._flat(st["c"])[:, st["flat"]]
 
-    def _ade_update(self, which: str = "all") -> None:
-        """Debye update of the dispersive edges (``which``: all, early = without injection,
-        late = with injection)."""
-        if which != "all":
-            self._ade_update_engine(late=which == "late")
-            return
+    def _ade_update(self) -> None:
         for st in self._ade:
             ef = self._flat(st["c"])
             e = ef[:, st["flat"]]
-            jt = 0.5 * np.einsum("p,pbe->be", 1.0 + self._kp, st["J"])
+            if self.pole_sum == "loop":
+                onekp = (1.0 + self._kp).astype(self.dtype)
+                acc = np.zeros_like(e)
+                for p in range(st["J"].shape[0]):
+                    acc = acc + onekp[p] * st["J"][p]
+                jt = 0.5 * acc
+            else:
+                jt = 0.5 * np.einsum("p,pbe->be", 1.0 + self._kp, st["J"])
             en = e - st["cbe"][None, :] * jt
             de = en - st["eold"]
             st["J"][...] = self._kp[:, None, None] * st["J"] + st["beta"][:, None, :] * de[None]
             ef[:, st["flat"]] = en
-
-    def _ade_update_engine(self, late: bool) -> None:
-        for st in self._ade:
-            sel = st["late"] if late else ~st["late"]
-            if not sel.any():
-                continue
-            ef = self._flat(st["c"])
-            fl = st["flat"][sel]
-            e = ef[:, fl]
-            J = st["J"][:, :, sel]
-            onekp = (1.0 + self._kp).astype(self.dtype)
-            jt = np.zeros_like(e)
-            for p in range(J.shape[0]):
-                jt = jt + onekp[p] * J[p]
-            jt = self.dtype.type(0.5) * jt
-            en = e - st["cbe"][None, sel] * jt
-            de = en - st["eold"][:, sel]
-            st["J"][:, :, sel] = self._kp[:, None, None] * J + st["beta"][:, None, sel] * de[None]
-            ef[:, fl] = en
-
-    def _debye_shift(self, comp: int, rng: Rng, t: Any) -> None:
-        """Engine order: a CPML correction t of an early-updated dispersive edge moves each J_p by
-        beta_p t."""
-        full = np.zeros_like(self.E[comp])
-        _window(full, rng)[...] = t
-        ff = full.reshape(self.c.batch, -1)
-        for st in self._ade:
-            if st["c"] != comp:
-                continue
-            sel = ~st["late"]
-            tt = ff[:, st["flat"][sel]]
-            st["J"][:, :, sel] = st["J"][:, :, sel] + st["beta"][:, None, sel] * tt[None]
 
     def _sibc(self) -> None:
         sb = self._sb
@@ -276,10 +231,7 @@ class OracleEngine:
             psi += _coef(cc_.astype(real), a, rng) * d
             upd = _coef(ck_.astype(real), a, rng) * d + psi
             if kind == "E":
-                t = corr.sign * _window(self.cb[corr.c], rng) * upd
-                _window(self.E[corr.c], rng)[...] += t
-                if self.order == "engine" and self._ade:
-                    self._debye_shift(corr.c, rng, t)
+                _window(self.E[corr.c], rng)[...] += corr.sign * _window(self.cb[corr.c], rng) * upd
             else:
                 _window(self.H[corr.c], rng)[...] += corr.sign * self.dtmu * upd
 
@@ -334,12 +286,10 @@ class OracleEngine:
             self._record("H", (k + 0.5) * dt)
             self._ade_save()
             self._e_update()
-            if self.order == "engine":
-                self._ade_update("early")
             self._pml("E")
             self._sibc()
             self._inject(k)
-            self._ade_update("late" if self.order == "engine" else "all")
+            self._ade_update()
             self._record("E", (k + 1) * dt)
             self.step_count += 1
 

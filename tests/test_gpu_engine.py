@@ -2,10 +2,11 @@
 
 The oracle (``oracle/numpy_engine.py``) is pinned against the reference itself by
 ``test_golden_compile.py``; here the CUDA engine runs the same compiled problems through the
-C ABI. The library is built without FMA contraction and keeps the reference's operations, so its
-fields equal the oracle's bit for bit in the engine's order (``order="engine"``: Debye edges
-inside CPML slabs updated before their corrections), and equal the reference-order oracle's bit
-for bit wherever the two orders coincide, otherwise within float32 rounding noise.
+C ABI. The library is built without FMA contraction and keeps the reference's operations in the
+reference's order, so its fields equal the oracle's bit for bit. The one exception is the Debye
+pole sum of multi-pole runs, which NumPy's einsum may reorder on some hosts: there the engine
+equals the oracle with the poles summed in index order (``pole_sum="loop"``) and the einsum
+oracle within float32 rounding noise.
 """
 
 from __future__ import annotations
@@ -76,8 +77,8 @@ def _fields(e) -> list:  # type: ignore[no-untyped-def]
 
 def _reference_tolerance(c, steps: int, dtype: str, ref_fields: list) -> list[float]:  # type: ignore[no-untyped-def]
     """Per component: 1e-5 (float32) or 1e-12 (float64) rel-L2, or twice the distance of the
-    reference-order float32 run from its float64 run where the case itself is worse conditioned
-    than that (a thin field component that float32 rounding alone moves by more than 1e-5)."""
+    float32 oracle from the float64 oracle where the case itself is worse conditioned than that
+    (a thin field component that float32 rounding alone moves by more than 1e-5)."""
     base = 1e-5 if dtype == "float32" else 1e-12
     if dtype != "float32":
         return [base] * 6
@@ -87,10 +88,10 @@ def _reference_tolerance(c, steps: int, dtype: str, ref_fields: list) -> list[fl
 
 
 def check_against_oracles(c, gpu, steps: int, dtype: str = "float32", results: bool = True) -> None:  # type: ignore[no-untyped-def]
-    """The engine's fields equal the engine-order oracle's bit for bit, its DFTs and energy agree
-    to float64 summation order, and its fields are within the reference-order oracle's rounding
-    noise (identical where the two orders coincide)."""
-    eng = OracleEngine(c, dtype, order="engine")
+    """The engine's fields equal the oracle's (poles summed in index order) bit for bit, its DFTs
+    and energy agree to float64 summation order, and its fields equal the einsum oracle's, or
+    are within its rounding noise where einsum reorders the pole sum."""
+    eng = OracleEngine(c, dtype, pole_sum="loop")
     eng.step(steps)
     for k, want in enumerate(_fields(eng)):
         got = gpu.field(k)
@@ -111,7 +112,7 @@ def check_against_oracles(c, gpu, steps: int, dtype: str = "float32", results: b
     tol = _reference_tolerance(c, steps, dtype, ref_fields)
     for k, want in enumerate(ref_fields):
         rel = _rel(gpu.field(k), want)
-        assert rel <= tol[k], f"{NAMES[k]}: rel-L2 {rel} against the reference order (bound {tol[k]})"
+        assert rel <= tol[k], f"{NAMES[k]}: rel-L2 {rel} against the einsum oracle (bound {tol[k]})"
 
 
 @pytest.mark.parametrize("case", sorted(CASES))
@@ -200,7 +201,7 @@ def test_kernel_profile_and_model_bytes() -> None:
     eng.set_profiling(True)
     eng.step(64)
     t = eng.kernel_times()
-    assert t["step"] > 0 and t["h_sweep"] > 0 and t["e_sweep"] > 0 and t["e_cpml"] > 0
+    assert t["step"] > 0 and t["h_sweep"] > 0 and t["e_sweep"] > 0 and t["e_slab"] > 0
     assert t["step"] >= t["h_sweep"] + t["e_sweep"]
     # one replay: the same kernels for each of the 64 time steps, then the step-counter bump
     n = eng.graph_kernels()
@@ -222,8 +223,7 @@ def test_launch_shapes_match_oracle(variant: int, tile_z: int) -> None:
 def test_variants_agree_across_x_tiles() -> None:
     """A grid two tiles wide in x (the second one past the grid's edge, where TMA boxes are
     zero-filled) with the benchmark's Debye stack, copper SIBC and CPML: the three sweep variants
-    give identical fields, equal to the engine-order oracle's. Its Ey is thin: float32 rounding
-    alone moves it by 2e-5 rel-L2, which sets the bound against the reference order."""
+    give identical fields, equal to the oracle's."""
     from open_analysis_gb300.structures import via_transition
 
     c = compile_model(via_transition(nx=150, ny=20, nz=14, n_freq=8, cpml_cells=6), "float32")
