@@ -731,7 +731,9 @@ int Engine<real>::build(const oafdtd_problem& p) {
               hi[ax] = std::min(hi[ax], S.lo[ax]);
           }
         }
-      const int qa = std::min((lo[0] + 3) / 4, Q), qb = std::max(std::min(hi[0] / 4, Q), qa);
+      // The interior starts on an even quad: its TMA boxes then start at a multiple of 8 cells,
+      // 16 bytes for the uint16 index boxes as for the field boxes.
+      const int qa = std::min(((lo[0] + 3) / 4 + 1) & ~1, Q), qb = std::max(std::min(hi[0] / 4, Q), qa);
       const int ja = std::min(std::max(lo[1], 1), ny + 2), jb = std::max(std::min(hi[1], ny + 2), ja);
       const int ka = std::min(std::max(lo[2], 1), nz + 2), kb = std::max(std::min(hi[2], nz + 2), ka);
       inner_staged[kind] = oafdtd::Span3{qa, qb, ja, jb, ka, kb};

@@ -542,6 +542,10 @@ template <typename real>
 cudaError_t launch_staged_sweep(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_t s, bool h) {
   const Span3 in = a.inner[h ? 1 : 0];
   if (in.q1 <= in.q0 || in.j1 <= in.j0 || in.k1 <= in.k0) return cudaSuccess;
+  // Every TMA box starts at x = 4 (q0 + 32 n) (the E sweep's halo box 4 cells earlier, which may
+  // be -4: a load may start before the grid): a multiple of 8 cells keeps the start 16-byte
+  // aligned for the 2-byte index boxes too.
+  if (in.q0 % 2 != 0) return cudaErrorInvalidValue;
   const int nkc = (in.k1 - in.k0 + a.tile_z - 1) / a.tile_z;
   dim3 block(kTQ, kTY);
   dim3 grid((in.q1 - in.q0 + kTQ - 1) / kTQ, (in.j1 - in.j0 + kTY - 1) / kTY, nkc * a.B);

@@ -220,13 +220,15 @@ def test_launch_shapes_match_oracle(variant: int, tile_z: int) -> None:
     check_against_oracles(c, gpu, 70, results=False)
 
 
-def test_variants_agree_across_x_tiles() -> None:
+@pytest.mark.parametrize("cpml_cells", [6, 10])
+def test_variants_agree_across_x_tiles(cpml_cells: int) -> None:
     """A grid two tiles wide in x (the second one past the grid's edge, where TMA boxes are
     zero-filled) with the benchmark's Debye stack, copper SIBC and CPML: the three sweep variants
-    give identical fields, equal to the oracle's."""
+    give identical fields, equal to the oracle's. With 10 CPML cells the interior starts after
+    x = 10, as in the benchmark (its first quad is rounded up to an even one)."""
     from open_analysis_gb300.structures import via_transition
 
-    c = compile_model(via_transition(nx=150, ny=20, nz=14, n_freq=8, cpml_cells=6), "float32")
+    c = compile_model(via_transition(nx=150, ny=24, nz=24, n_freq=8, cpml_cells=cpml_cells), "float32")
     assert c.grid.shape[2] > 128 and _ade_in_cpml(c)
     fields = {}
     for variant in (0, 1, 2):
