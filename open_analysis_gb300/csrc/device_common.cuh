@@ -42,6 +42,18 @@ __device__ __forceinline__ Quad<uint16_t> ld4(const uint16_t* p) {
   return Quad<uint16_t>{{t.x, t.y, t.z, t.w}};
 }
 
+// One entry of the combined material table through the read-only data path (the table does
+// not change during a run).
+__device__ __forceinline__ Coef<float> ldg_coef(const Coef<float>* p) {
+  const float4 t = __ldg(reinterpret_cast<const float4*>(p));
+  return Coef<float>{t.x, t.y, t.z, t.w};
+}
+__device__ __forceinline__ Coef<double> ldg_coef(const Coef<double>* p) {
+  const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+  const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+  return Coef<double>{a.x, a.y, b.x, b.y};
+}
+
 template <typename real>
 __device__ __forceinline__ Quad<real> zero4() {
   return Quad<real>{{(real)0, (real)0, (real)0, (real)0}};
