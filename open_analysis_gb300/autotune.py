@@ -27,7 +27,8 @@ class TuneResult:
 
 
 def _candidates(tiles: tuple[int, ...], variants: tuple[int, ...]) -> list[tuple[int, int]]:
-    return [(tz, v) for v in variants for tz in tiles]
+    # variant 0 runs the slab kernel alone, whose march does not depend on the tile
+    return [(tz, v) for v in variants for tz in (tiles if v != 0 else tiles[:1])]
 
 
 def tune(engine: Any, chunks: int = 2, tiles: tuple[int, ...] = TILES, variants: tuple[int, ...] = VARIANTS) -> TuneResult:

@@ -224,14 +224,16 @@ int Engine<real>::build(const oafdtd_problem& p) {
   auto injected = [&](int c, long long f) {
     return std::binary_search(inj_sorted.begin(), inj_sorted.end(), std::make_pair(c, f));
   };
-  // surface-impedance edges: a dispersive one is updated after the surface impedance sets it
-  std::vector<std::pair<int, long long>> sibc_sorted;
-  sibc_sorted.reserve((size_t)p.sibc_n);
-  for (int64_t s = 0; s < p.sibc_n; ++s) sibc_sorted.emplace_back(p.sibc_comp[s], p.sibc_flat[s]);
-  std::sort(sibc_sorted.begin(), sibc_sorted.end());
-  auto on_sibc = [&](int c, long long f) {
-    return std::binary_search(sibc_sorted.begin(), sibc_sorted.end(), std::make_pair(c, f));
-  };
+  // surface-impedance edges (one bit per storage cell and component): a dispersive one is
+  // updated after the surface impedance sets it
+  std::vector<bool> sibc_bits;
+  if (p.sibc_n > 0) {
+    sibc_bits.assign((size_t)(3 * bs), false);
+    for (int64_t s = 0; s < p.sibc_n; ++s)
+      if (p.sibc_comp[s] >= 0 && p.sibc_comp[s] <= 2 && in_range(p.sibc_flat[s]))
+        sibc_bits[(size_t)(p.sibc_comp[s] * bs + p.sibc_flat[s])] = true;
+  }
+  auto on_sibc = [&](int c, long long f) { return !sibc_bits.empty() && sibc_bits[(size_t)(c * bs + f)]; };
 
   // ---- combined table. Entry key: (category, material index, ADE row); categories 0 plain,
   // 1 dispersive, 2 dispersive with injection or surface impedance (deferred to the edge pass,

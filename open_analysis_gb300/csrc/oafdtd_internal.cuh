@@ -80,7 +80,7 @@ struct SweepArgs {
   int nx, ny, nz, X, Y;
   long long bs;             // Z * Y * X
   int B;
-  int tile_z;       // planes marched per thread (slab kernel) or per block (staged sweeps)
+  int tile_z;       // planes marched per block by the staged sweeps
   int staged;       // 2: staged by TMA tensor copies; 1: staged by cp.async; 0: slab kernel only
   int* status;      // device status word: bit 0 set when a bounded wait of a sweep gave up
   // Per kind ([0] E, [1] H): the interior box, which holds no CPML correction cell and is swept

@@ -26,6 +26,9 @@
 namespace oafdtd {
 
 constexpr int kSlabThreads = 256;
+// Planes marched per thread. The slab boxes are thin (CPML slabs of ~10 cells): short marches
+// give the kernel enough independent threads to hide its load latency.
+constexpr int kSlabPlanes = 4;
 
 // Launch geometry: the boxes of one kind with their first block.
 struct SlabLaunch {
@@ -132,7 +135,7 @@ struct SlabWork {
   bool live;
 };
 
-__device__ __forceinline__ SlabWork slab_work(const SlabLaunch& L, int tile_z, int nx) {
+__device__ __forceinline__ SlabWork slab_work(const SlabLaunch& L, int nx) {
   int s = 0;
   while (s + 1 < L.n && (int)blockIdx.x >= L.first[s + 1]) ++s;
   const Span3 bx = L.box[s];
@@ -148,8 +151,8 @@ __device__ __forceinline__ SlabWork slab_work(const SlabLaunch& L, int tile_z, i
   const int c = min(col, ncol - 1);
   w.j = bx.j0 + c / nq;
   w.i0 = 4 * (bx.q0 + c % nq);
-  w.k0 = bx.k0 + ch * tile_z;
-  w.k1 = min(w.k0 + tile_z, bx.k1);
+  w.k0 = bx.k0 + ch * kSlabPlanes;
+  w.k1 = min(w.k0 + kSlabPlanes, bx.k1);
   w.live = col < ncol && w.i0 <= nx + 1;
   return w;
 }
@@ -215,7 +218,7 @@ __device__ __forceinline__ void e_update(const SweepArgs<real>& a, int c, Quad<r
 template <typename real>
 __global__ void __launch_bounds__(kSlabThreads, 2)
     slab_e_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SlabLaunch L) {
-  const SlabWork w = slab_work(L, a.tile_z, a.nx);
+  const SlabWork w = slab_work(L, a.nx);
   if (!w.live || w.k0 >= w.k1) return;
   const int X = a.X, Y = a.Y, Z = a.nz + 2, b = w.b, j = w.j, i0 = w.i0;
   const long long sz = (long long)X * Y;
@@ -307,7 +310,7 @@ __device__ __forceinline__ void h_update(const SweepArgs<real>& a, int c, Quad<r
 template <typename real>
 __global__ void __launch_bounds__(kSlabThreads, 2)
     slab_h_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SlabLaunch L) {
-  const SlabWork w = slab_work(L, a.tile_z, a.nx);
+  const SlabWork w = slab_work(L, a.nx);
   if (!w.live || w.k0 >= w.k1) return;
   const int X = a.X, Y = a.Y, Z = a.nz + 2, nx = a.nx, ny = a.ny, nz = a.nz, b = w.b, j = w.j, i0 = w.i0;
   const long long sz = (long long)X * Y;
@@ -405,7 +408,7 @@ cudaError_t launch_slab(const SweepArgs<real>& a, int kind, cudaStream_t s) {
     L.box[L.n] = bx;
     L.first[L.n] = (int)total;
     L.cblk[L.n] = (int)((cols + kSlabThreads - 1) / kSlabThreads);
-    L.nch[L.n] = (bx.k1 - bx.k0 + a.tile_z - 1) / a.tile_z;
+    L.nch[L.n] = (bx.k1 - bx.k0 + kSlabPlanes - 1) / kSlabPlanes;
     total += (long long)L.cblk[L.n] * L.nch[L.n] * a.B;
     ++L.n;
   }
