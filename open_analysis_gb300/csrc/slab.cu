@@ -129,21 +129,25 @@ __device__ __forceinline__ void psi_apply(const CpmlTerm<real>& T, PsiQuad<real>
   }
 }
 
-// Where a thread works: member, box, quad column and plane range.
+// Where a thread works: field component, member, box, quad column and plane range. The
+// component is the fastest-varying block index, so the three components of a region run side by
+// side and share their source-field reads through L1 and L2.
 struct SlabWork {
-  int b, j, i0, k0, k1;
+  int comp, b, j, i0, k0, k1;
   bool live;
 };
 
 __device__ __forceinline__ SlabWork slab_work(const SlabLaunch& L, int nx) {
+  const int blk = (int)blockIdx.x / 3;
   int s = 0;
-  while (s + 1 < L.n && (int)blockIdx.x >= L.first[s + 1]) ++s;
+  while (s + 1 < L.n && blk >= L.first[s + 1]) ++s;
   const Span3 bx = L.box[s];
-  int r = (int)blockIdx.x - L.first[s];
+  int r = blk - L.first[s];
   const int cb = r % L.cblk[s];
   r /= L.cblk[s];
   const int ch = r % L.nch[s];
   SlabWork w;
+  w.comp = (int)blockIdx.x % 3;
   w.b = r / L.nch[s];
   const int nq = bx.q1 - bx.q0;
   const int col = cb * kSlabThreads + (int)threadIdx.x;
@@ -164,235 +168,236 @@ __device__ __forceinline__ long long jindex(const SweepArgs<real>& a, int c, int
   return (((long long)b * a.jnk[c] + (k - a.jk0[c])) * a.Y + j) * a.X + i;
 }
 
-// Per plane: every load first (H, E, indices, Debye currents, psi), then the arithmetic, then every
-// store, so no load waits behind a store it cannot be proven not to alias.
-template <typename real>
-__device__ __forceinline__ void e_update(const SweepArgs<real>& a, int c, Quad<real>& e4, const Quad<uint16_t>& m,
-                                         const real (&d0)[4], const real (&d1)[4], bool first_plus,
-                                         PsiQuad<real> (&ps)[2], Quad<real>& j4, bool& disp, int i0, int j,
-                                         int k, int b) {
-  const int nx = a.nx;
-  const Quad<real> e0 = e4;
-  Coef<real> cf[4];
-  real kf[4];
-  bool valid[4];
-#pragma unroll
-  for (int e = 0; e < 4; ++e) {
-    const int i = i0 + e;
-    cf[e] = ldg_coef(a.coef + m.v[e]);
-    kf[e] = cf[e].cb;
-    valid[e] = i >= 1 && i <= nx + 1;
-    const real acc = first_plus ? d0[e] + (-d1[e]) : d1[e] + (-d0[e]);
-    if (valid[e]) e4.v[e] = cf[e].ca * e4.v[e] + cf[e].cb * acc;
-  }
-  psi_apply<real>(a.ecorr[c][0], ps[0], a.pe, e4, d0, kf, k, j, i0);
-  psi_apply<real>(a.ecorr[c][1], ps[1], a.pe, e4, d1, kf, k, j, i0);
-  disp = false;
-#pragma unroll
-  for (int e = 0; e < 4; ++e) disp |= valid[e] && m.v[e] >= a.ade_lo && m.v[e] < a.ade_hi;
-  if (!disp) return;
-  if (a.ade_P == 1) {
-    const real onekp = a.ade_onekp[0], kp = a.ade_kp[0];
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      if (!(valid[e] && m.v[e] >= a.ade_lo && m.v[e] < a.ade_hi)) continue;
-      const real jt = (real)0.5 * (onekp * j4.v[e]);
-      const real en = e4.v[e] - cf[e].cbe * jt;
-      const real de = en - e0.v[e];
-      j4.v[e] = kp * j4.v[e] + cf[e].beta0 * de;
-      e4.v[e] = en;
-    }
-  } else {
-    const long long jstride = (long long)a.B * a.jnk[c] * a.Y * a.X;
-    disp = false;  // the general-pole update writes its currents itself
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      if (!(valid[e] && m.v[e] >= a.ade_lo && m.v[e] < a.ade_hi)) continue;
-      e4.v[e] = ade_cell(e4.v[e], e0.v[e], cf[e].cbe, cf[e].beta0, m.v[e], a.J[c], jindex(a, c, b, k, j, i0) + e,
-                         jstride, a.ade_kp,
-                         a.ade_onekp, a.ade_beta, a.ade_P);
-    }
-  }
-}
-
-template <typename real>
-__global__ void __launch_bounds__(kSlabThreads, 2)
-    slab_e_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SlabLaunch L) {
-  const SlabWork w = slab_work(L, a.nx);
-  if (!w.live || w.k0 >= w.k1) return;
-  const int X = a.X, Y = a.Y, Z = a.nz + 2, b = w.b, j = w.j, i0 = w.i0;
+// One E component on one quad column. Per plane: every load first (H, E, index, Debye current,
+// psi), then the arithmetic, then every store, so no load waits behind a store it cannot be proven
+// not to alias. C: 0 Ex (terms y +Hz, z -Hy), 1 Ey (z +Hx, x -Hz), 2 Ez (x +Hy, y -Hx); d0 is
+// the derivative along the first axis in ascending order, d1 along the second.
+template <typename real, int C>
+__device__ __forceinline__ void slab_e_column(const SweepArgs<real>& a, const SlabWork& w) {
+  const int X = a.X, Y = a.Y, Z = a.nz + 2, nx = a.nx, b = w.b, j = w.j, i0 = w.i0;
   const long long sz = (long long)X * Y;
   const long long base = (long long)b * a.bs;
   const real* Hx = a.H[0] + base;
   const real* Hy = a.H[1] + base;
   const real* Hz = a.H[2] + base;
+  real* E = a.E[C] + base;
   const Quad<real> idx4 = ld4(a.idd[0] + i0);
   const real idy = a.idd[1][j];
   long long q = (long long)w.k0 * sz + (long long)j * X + i0;  // offset within one member
-  Quad<real> hx_m = ld4(Hx + q - sz), hy_m = ld4(Hy + q - sz);
+  // the z-derivative source at plane k - 1, carried (Ex: Hy, Ey: Hx)
+  Quad<real> hm = zero4<real>();
+  if (C == 0) hm = ld4(Hy + q - sz);
+  if (C == 1) hm = ld4(Hx + q - sz);
   for (int k = w.k0; k < w.k1; ++k, q += sz) {
     // ---- loads
-    const real idz = a.idd[2][k];
-    const Quad<real> hx = ld4(Hx + q), hy = ld4(Hy + q), hz = ld4(Hz + q);
-    const Quad<real> hzy = ld4(Hz + q - X), hxy = ld4(Hx + q - X);
-    const real hz_l = Hz[q - 1], hy_l = Hy[q - 1];
-    Quad<uint16_t> m[3];
-    Quad<real> ev[3], jv[3];
-    PsiQuad<real> ps[3][2];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      m[c] = ld4(a.mat[c] + q);
-      ev[c] = ld4(a.E[c] + base + q);
-      jv[c] = zero4<real>();
-      if (a.ade_P == 1 && k >= a.jk0[c] && k < a.jk0[c] + a.jnk[c]) jv[c] = ld4(a.J[c] + jindex(a, c, b, k, j, i0));
-#pragma unroll
-      for (int t = 0; t < 2; ++t) {
-        ps[c][t].sd = -1;
-        if (a.has_cpml) psi_load<real>(a.ecorr[c][t], ps[c][t], b, k, j, i0, X, Y, Z);
-      }
+    Quad<real> s0, s1, s2;  // sources of the two derivatives
+    real sl = (real)0;      // x - 1 neighbour of element 0
+    if (C == 0) {
+      s0 = ld4(Hz + q);
+      s1 = ld4(Hz + q - X);
+      s2 = ld4(Hy + q);
+    } else if (C == 1) {
+      s0 = ld4(Hz + q);
+      sl = Hz[q - 1];
+      s2 = ld4(Hx + q);
+    } else {
+      s0 = ld4(Hy + q);
+      sl = Hy[q - 1];
+      s2 = ld4(Hx + q);
+      s1 = ld4(Hx + q - X);
+    }
+    const Quad<uint16_t> m = ld4(a.mat[C] + q);
+    Quad<real> e4 = ld4(E + q);
+    const bool jrange = a.ade_P == 1 && k >= a.jk0[C] && k < a.jk0[C] + a.jnk[C];
+    Quad<real> j4 = zero4<real>();
+    if (jrange) j4 = ld4(a.J[C] + jindex(a, C, b, k, j, i0));
+    PsiQuad<real> ps[2];
+    ps[0].sd = ps[1].sd = -1;
+    if (a.has_cpml) {
+      psi_load<real>(a.ecorr[C][0], ps[0], b, k, j, i0, X, Y, Z);
+      psi_load<real>(a.ecorr[C][1], ps[1], b, k, j, i0, X, Y, Z);
     }
     // ---- arithmetic
-    bool disp[3];
     real d0[4], d1[4];
-    // Ex: terms (a = y, +Hz) then (a = z, -Hy)
+    const real idz = a.idd[2][k];
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-      d0[e] = (hz.v[e] - hzy.v[e]) * idy;
-      d1[e] = (hy.v[e] - hy_m.v[e]) * idz;
+      if (C == 0) {
+        d0[e] = (s0.v[e] - s1.v[e]) * idy;  // y: Hz
+        d1[e] = (s2.v[e] - hm.v[e]) * idz;  // z: Hy
+      } else if (C == 1) {
+        const real l = e > 0 ? s0.v[e - 1] : sl;
+        d0[e] = (s0.v[e] - l) * idx4.v[e];  // x: Hz
+        d1[e] = (s2.v[e] - hm.v[e]) * idz;  // z: Hx
+      } else {
+        const real l = e > 0 ? s0.v[e - 1] : sl;
+        d0[e] = (s0.v[e] - l) * idx4.v[e];  // x: Hy
+        d1[e] = (s2.v[e] - s1.v[e]) * idy;  // y: Hx
+      }
     }
-    e_update<real>(a, 0, ev[0], m[0], d0, d1, true, ps[0], jv[0], disp[0], i0, j, k, b);
-    // Ey: terms (a = z, +Hx) then (a = x, -Hz); d0 is the x term, d1 the z term
+    const bool first_plus = C != 1;  // the reference's term order: (d0, -d1), for Ey (d1, -d0)
+    const Quad<real> e0 = e4;
+    real kf[4];
+    bool valid[4], dis[4];
+    bool disp = false;
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-      const real hzl = e > 0 ? hz.v[e - 1] : hz_l;
-      d0[e] = (hz.v[e] - hzl) * idx4.v[e];
-      d1[e] = (hx.v[e] - hx_m.v[e]) * idz;
+      const int i = i0 + e;
+      const Coef<real> cf = ldg_coef(a.coef + m.v[e]);
+      kf[e] = cf.cb;
+      valid[e] = i >= 1 && i <= nx + 1;
+      const real acc = first_plus ? d0[e] + (-d1[e]) : d1[e] + (-d0[e]);
+      if (valid[e]) e4.v[e] = cf.ca * e4.v[e] + cf.cb * acc;
+      dis[e] = valid[e] && m.v[e] >= a.ade_lo && m.v[e] < a.ade_hi;
+      disp |= dis[e];
     }
-    e_update<real>(a, 1, ev[1], m[1], d0, d1, false, ps[1], jv[1], disp[1], i0, j, k, b);
-    // Ez: terms (a = x, +Hy) then (a = y, -Hx)
+    psi_apply<real>(a.ecorr[C][0], ps[0], a.pe, e4, d0, kf, k, j, i0);
+    psi_apply<real>(a.ecorr[C][1], ps[1], a.pe, e4, d1, kf, k, j, i0);
+    if (disp) {
+      if (a.ade_P == 1) {
+        const real onekp = a.ade_onekp[0], kp = a.ade_kp[0];
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const real hyl = e > 0 ? hy.v[e - 1] : hy_l;
-      d0[e] = (hy.v[e] - hyl) * idx4.v[e];
-      d1[e] = (hx.v[e] - hxy.v[e]) * idy;
+        for (int e = 0; e < 4; ++e) {
+          if (!dis[e]) continue;
+          const Coef<real> cf = ldg_coef(a.coef + m.v[e]);  // the Debye coefficients (cbe, beta_0)
+          const real jt = (real)0.5 * (onekp * j4.v[e]);
+          const real en = e4.v[e] - cf.cbe * jt;
+          const real de = en - e0.v[e];
+          j4.v[e] = kp * j4.v[e] + cf.beta0 * de;
+          e4.v[e] = en;
+        }
+      } else {
+        const long long jstride = (long long)a.B * a.jnk[C] * Y * X;
+        const long long jq = jindex(a, C, b, k, j, i0);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          if (!dis[e]) continue;
+          const Coef<real> cf = ldg_coef(a.coef + m.v[e]);
+          e4.v[e] = ade_cell(e4.v[e], e0.v[e], cf.cbe, cf.beta0, m.v[e], a.J[C], jq + e, jstride, a.ade_kp,
+                             a.ade_onekp, a.ade_beta, a.ade_P);
+        }
+      }
     }
-    e_update<real>(a, 2, ev[2], m[2], d0, d1, true, ps[2], jv[2], disp[2], i0, j, k, b);
     // ---- stores
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      st4(a.E[c] + base + q, ev[c]);
-      if (disp[c]) st4(a.J[c] + jindex(a, c, b, k, j, i0), jv[c]);
-#pragma unroll
-      for (int t = 0; t < 2; ++t) psi_store<real>(a.ecorr[c][t], ps[c][t], b, k, j, i0, X, Y, Z);
-    }
-    hx_m = hx;
-    hy_m = hy;
+    st4(E + q, e4);
+    if (disp && a.ade_P == 1) st4(a.J[C] + jindex(a, C, b, k, j, i0), j4);
+    psi_store<real>(a.ecorr[C][0], ps[0], b, k, j, i0, X, Y, Z);
+    psi_store<real>(a.ecorr[C][1], ps[1], b, k, j, i0, X, Y, Z);
+    if (C == 0) hm = s2;
+    if (C == 1) hm = s2;
   }
+}
+
+template <typename real>
+__global__ void __launch_bounds__(kSlabThreads, 3)
+    slab_e_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SlabLaunch L) {
+  const SlabWork w = slab_work(L, a.nx);
+  if (!w.live || w.k0 >= w.k1) return;
+  if (w.comp == 0)
+    slab_e_column<real, 0>(a, w);
+  else if (w.comp == 1)
+    slab_e_column<real, 1>(a, w);
+  else
+    slab_e_column<real, 2>(a, w);
 }
 
 // ------------------------------------------------------------------------------------- H
-template <typename real>
-__device__ __forceinline__ void h_update(const SweepArgs<real>& a, int c, Quad<real>& h, const real (&d0)[4],
-                                         const real (&d1)[4], const real (&acc)[4], int ilast,
-                                         PsiQuad<real> (&ps)[2], int i0, int j, int k) {
-  const real dtmu = a.dtmu;
-  real kf[4];
-#pragma unroll
-  for (int e = 0; e < 4; ++e) {
-    const int i = i0 + e;
-    kf[e] = dtmu;
-    if (i >= 1 && i <= ilast) h.v[e] = h.v[e] + dtmu * acc[e];
-  }
-  psi_apply<real>(a.hcorr[c][0], ps[0], a.ph, h, d0, kf, k, j, i0);
-  psi_apply<real>(a.hcorr[c][1], ps[1], a.ph, h, d1, kf, k, j, i0);
-}
-
-template <typename real>
-__global__ void __launch_bounds__(kSlabThreads, 2)
-    slab_h_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SlabLaunch L) {
-  const SlabWork w = slab_work(L, a.nx);
-  if (!w.live || w.k0 >= w.k1) return;
+// One H component on one quad column. C: 0 Hx (terms y -Ez, z +Ey), 1 Hy (z -Ex, x +Ez),
+// 2 Hz (x -Ey, y +Ex); d0 along the first axis in ascending order, d1 along the second.
+template <typename real, int C>
+__device__ __forceinline__ void slab_h_column(const SweepArgs<real>& a, const SlabWork& w) {
   const int X = a.X, Y = a.Y, Z = a.nz + 2, nx = a.nx, ny = a.ny, nz = a.nz, b = w.b, j = w.j, i0 = w.i0;
+  // the cells this component updates: Hx i in 1..nx+1, j <= ny, k <= nz; Hy i <= nx, k <= nz;
+  // Hz i <= nx, j <= ny
+  if ((C == 0 || C == 2) && j > ny) return;
+  const int ilast = C == 0 ? nx + 1 : nx;
   const long long sz = (long long)X * Y;
   const long long base = (long long)b * a.bs;
   const real* Ex = a.E[0] + base;
   const real* Ey = a.E[1] + base;
   const real* Ez = a.E[2] + base;
+  real* H = a.H[C] + base;
   const Quad<real> ipx = ld4(a.ip[0] + i0);
   const real ipy = a.ip[1][j];
   const bool right = i0 + 4 < X;  // the x + 1 neighbour of element 3 is in the row
-  const bool jin = j <= ny;
+  const real dtmu = a.dtmu;
   long long q = (long long)w.k0 * sz + (long long)j * X + i0;
-  Quad<real> ex = ld4(Ex + q), ey = ld4(Ey + q);
+  // the z-derivative source at plane k, carried from the previous plane's k + 1 (Hx: Ey, Hy: Ex)
+  Quad<real> sc = zero4<real>();
+  if (C == 0) sc = ld4(Ey + q);
+  if (C == 1) sc = ld4(Ex + q);
   for (int k = w.k0; k < w.k1; ++k, q += sz) {
+    if (C != 2 && k > nz) break;
     // ---- loads
-    const bool kin = k <= nz;
-    const real ipz = a.ip[2][k];
-    Quad<real> ex1 = zero4<real>(), ey1 = zero4<real>(), ezy = zero4<real>(), exy = zero4<real>();
-    if (kin) {
-      ex1 = ld4(Ex + q + sz);
-      ey1 = ld4(Ey + q + sz);
+    Quad<real> s0, s1, s2;
+    real sr = (real)0;  // x + 1 neighbour of element 3
+    if (C == 0) {
+      s0 = ld4(Ez + q + X);   // y: Ez(j + 1)
+      s1 = ld4(Ez + q);
+      s2 = ld4(Ey + q + sz);  // z: Ey(k + 1)
+    } else if (C == 1) {
+      s0 = ld4(Ez + q);       // x: Ez
+      sr = right ? Ez[q + 4] : (real)0;
+      s2 = ld4(Ex + q + sz);  // z: Ex(k + 1)
+    } else {
+      s0 = ld4(Ey + q);       // x: Ey
+      sr = right ? Ey[q + 4] : (real)0;
+      s2 = ld4(Ex + q + X);   // y: Ex(j + 1)
+      s1 = ld4(Ex + q);
     }
-    if (jin) {
-      ezy = ld4(Ez + q + X);
-      exy = ld4(Ex + q + X);
-    }
-    const Quad<real> ez = ld4(Ez + q);
-    const real ez_r = right ? Ez[q + 4] : (real)0, ey_r = right ? Ey[q + 4] : (real)0;
-    Quad<real> hv[3];
-    PsiQuad<real> ps[3][2];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      hv[c] = ld4(a.H[c] + base + q);
-#pragma unroll
-      for (int t = 0; t < 2; ++t) {
-        ps[c][t].sd = -1;
-        if (a.has_cpml) psi_load<real>(a.hcorr[c][t], ps[c][t], b, k, j, i0, X, Y, Z);
-      }
+    Quad<real> h = ld4(H + q);
+    PsiQuad<real> ps[2];
+    ps[0].sd = ps[1].sd = -1;
+    if (a.has_cpml) {
+      psi_load<real>(a.hcorr[C][0], ps[0], b, k, j, i0, X, Y, Z);
+      psi_load<real>(a.hcorr[C][1], ps[1], b, k, j, i0, X, Y, Z);
     }
     // ---- arithmetic
-    real d0[4], d1[4], acc[4];
-    const bool upd[3] = {jin && kin, kin, jin};
-    if (upd[0]) {  // Hx: node along x (1..nx+1), cell along y and z
+    const real ipz = a.ip[2][k];
+    real d0[4], d1[4], kf[4];
 #pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        d0[e] = (ezy.v[e] - ez.v[e]) * ipy;  // axis y
-        d1[e] = (ey1.v[e] - ey.v[e]) * ipz;  // axis z
-        acc[e] = (-d0[e]) + d1[e];
+    for (int e = 0; e < 4; ++e) {
+      real acc;
+      if (C == 0) {
+        d0[e] = (s0.v[e] - s1.v[e]) * ipy;  // y
+        d1[e] = (s2.v[e] - sc.v[e]) * ipz;  // z
+        acc = (-d0[e]) + d1[e];
+      } else if (C == 1) {
+        const real r = e < 3 ? s0.v[e + 1] : sr;
+        d0[e] = (r - s0.v[e]) * ipx.v[e];   // x
+        d1[e] = (s2.v[e] - sc.v[e]) * ipz;  // z
+        acc = (-d1[e]) + d0[e];
+      } else {
+        const real r = e < 3 ? s0.v[e + 1] : sr;
+        d0[e] = (r - s0.v[e]) * ipx.v[e];   // x
+        d1[e] = (s2.v[e] - s1.v[e]) * ipy;  // y
+        acc = (-d0[e]) + d1[e];
       }
-      h_update<real>(a, 0, hv[0], d0, d1, acc, nx + 1, ps[0], i0, j, k);
+      const int i = i0 + e;
+      kf[e] = dtmu;
+      if (i >= 1 && i <= ilast) h.v[e] = h.v[e] + dtmu * acc;
     }
-    if (upd[1]) {  // Hy: cell along x (1..nx), node along y (1..ny+1), cell along z
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const real ezr = e < 3 ? ez.v[e + 1] : ez_r;
-        d0[e] = (ezr - ez.v[e]) * ipx.v[e];  // axis x
-        d1[e] = (ex1.v[e] - ex.v[e]) * ipz;  // axis z
-        acc[e] = (-d1[e]) + d0[e];
-      }
-      h_update<real>(a, 1, hv[1], d0, d1, acc, nx, ps[1], i0, j, k);
-    }
-    if (upd[2]) {  // Hz: cell along x and y, node along z (1..nz+1)
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const real eyr = e < 3 ? ey.v[e + 1] : ey_r;
-        d0[e] = (eyr - ey.v[e]) * ipx.v[e];  // axis x
-        d1[e] = (exy.v[e] - ex.v[e]) * ipy;  // axis y
-        acc[e] = (-d0[e]) + d1[e];
-      }
-      h_update<real>(a, 2, hv[2], d0, d1, acc, nx, ps[2], i0, j, k);
-    }
+    psi_apply<real>(a.hcorr[C][0], ps[0], a.ph, h, d0, kf, k, j, i0);
+    psi_apply<real>(a.hcorr[C][1], ps[1], a.ph, h, d1, kf, k, j, i0);
     // ---- stores
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      if (!upd[c]) continue;
-      st4(a.H[c] + base + q, hv[c]);
-#pragma unroll
-      for (int t = 0; t < 2; ++t) psi_store<real>(a.hcorr[c][t], ps[c][t], b, k, j, i0, X, Y, Z);
-    }
-    ex = ex1;
-    ey = ey1;
+    st4(H + q, h);
+    psi_store<real>(a.hcorr[C][0], ps[0], b, k, j, i0, X, Y, Z);
+    psi_store<real>(a.hcorr[C][1], ps[1], b, k, j, i0, X, Y, Z);
+    if (C != 2) sc = s2;
   }
+}
+
+template <typename real>
+__global__ void __launch_bounds__(kSlabThreads, 4)
+    slab_h_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SlabLaunch L) {
+  const SlabWork w = slab_work(L, a.nx);
+  if (!w.live || w.k0 >= w.k1) return;
+  if (w.comp == 0)
+    slab_h_column<real, 0>(a, w);
+  else if (w.comp == 1)
+    slab_h_column<real, 1>(a, w);
+  else
+    slab_h_column<real, 2>(a, w);
 }
 
 // ------------------------------------------------------------------------------------- launch
@@ -413,12 +418,12 @@ cudaError_t launch_slab(const SweepArgs<real>& a, int kind, cudaStream_t s) {
     ++L.n;
   }
   if (L.n == 0) return cudaSuccess;
-  if (total > 2147483647LL) return cudaErrorInvalidConfiguration;
+  if (3 * total > 2147483647LL) return cudaErrorInvalidConfiguration;
   L.first[L.n] = (int)total;
   if (kind == 0)
-    slab_e_kernel<real><<<(unsigned)total, kSlabThreads, 0, s>>>(a, L);
+    slab_e_kernel<real><<<(unsigned)(3 * total), kSlabThreads, 0, s>>>(a, L);
   else
-    slab_h_kernel<real><<<(unsigned)total, kSlabThreads, 0, s>>>(a, L);
+    slab_h_kernel<real><<<(unsigned)(3 * total), kSlabThreads, 0, s>>>(a, L);
   return cudaGetLastError();
 }
 
