@@ -70,6 +70,8 @@ struct Engine final : EngineBase {
   int device = 0;
   cudaStream_t stream = nullptr;
   oafdtd::Span3 inner_staged[2]{};     // interior boxes (E, H) when the staged sweeps run
+  oafdtd::Span3 zin_staged[2][2]{};    // z-slab planes over the interior's x-y extent
+  int zsd[2][2][2] = {};               // side of the z-term psi per (kind, low/high, component)
   oafdtd::Span3 slab_staged[2][6]{};   // the slab boxes around them
   int n_slab_staged[2] = {0, 0};
   oafdtd::Span3 whole{};               // the whole update domain (variant 0: slab kernel only)
@@ -153,12 +155,17 @@ struct Engine final : EngineBase {
   void use_regions() {
     sw.staged = staged;
     for (int kind = 0; kind < 2; ++kind) {
+      for (int zr = 0; zr < 2; ++zr)
+        for (int cc = 0; cc < 2; ++cc) sw.zsd[kind][zr][cc] = zsd[kind][zr][cc];
       if (staged) {
         sw.inner[kind] = inner_staged[kind];
+        sw.zin[kind][0] = zin_staged[kind][0];
+        sw.zin[kind][1] = zin_staged[kind][1];
         sw.n_slab[kind] = n_slab_staged[kind];
         for (int n = 0; n < 6; ++n) sw.slab[kind][n] = slab_staged[kind][n];
       } else {
         sw.inner[kind] = oafdtd::Span3{0, 0, 0, 0, 0, 0};
+        sw.zin[kind][0] = sw.zin[kind][1] = oafdtd::Span3{0, 0, 0, 0, 0, 0};
         sw.n_slab[kind] = 1;
         sw.slab[kind][0] = whole;
       }
@@ -461,11 +468,6 @@ int Engine<real>::build(const oafdtd_problem& p) {
   sw.tile_z = tile_z;
   if (int rc = alloc(&status, 1)) return rc;
   sw.status = status;
-  {
-    std::string why;
-    tma_ok = oafdtd::encode_sweep_maps<real>(sw, &maps, &why);
-    if (!tma_ok && staged == 2) staged = 1;
-  }
   sw.staged = staged;
 
   // ---- edge list: surface impedance, injection targets, deferred ADE edges
@@ -739,21 +741,43 @@ int Engine<real>::build(const oafdtd_problem& p) {
       const int ja = std::min(std::max(lo[1], 1), ny + 2), jb = std::max(std::min(hi[1], ny + 2), ja);
       const int ka = std::min(std::max(lo[2], 1), nz + 2), kb = std::max(std::min(hi[2], nz + 2), ka);
       inner_staged[kind] = oafdtd::Span3{qa, qb, ja, jb, ka, kb};
-      const oafdtd::Span3 boxes[6] = {{0, Q, 1, ny + 2, 1, ka},  {0, Q, 1, ny + 2, kb, nz + 2},
-                                      {0, Q, 1, ja, ka, kb},     {0, Q, jb, ny + 2, ka, kb},
-                                      {0, qa, ja, jb, ka, kb},   {qb, Q, ja, jb, ka, kb}};
+      // the z-slab planes of the interior's x-y extent hold z corrections only: staged too
+      zin_staged[kind][0] = oafdtd::Span3{qa, qb, ja, jb, 1, ka};
+      zin_staged[kind][1] = oafdtd::Span3{qa, qb, ja, jb, kb, nz + 2};
+      for (int zr = 0; zr < 2; ++zr)
+        for (int cc = 0; cc < 2; ++cc) {
+          zsd[kind][zr][cc] = -1;
+          const oafdtd::CpmlTerm<real>& T = kind == 0 ? sw.ecorr[cc][1] : sw.hcorr[cc][1];
+          if (T.axis != 2) continue;
+          for (int sd = 0; sd < 2; ++sd) {
+            const oafdtd::CpmlSide<real>& S = T.side[sd];
+            if (S.psi != nullptr && (S.lo[2] <= 1) == (zr == 0)) zsd[kind][zr][cc] = sd;
+          }
+        }
+      // the slab kernel: the y and x slabs over every plane
+      const oafdtd::Span3 boxes[4] = {{0, Q, 1, ja, 1, nz + 2},
+                                      {0, Q, jb, ny + 2, 1, nz + 2},
+                                      {0, qa, ja, jb, 1, nz + 2},
+                                      {qb, Q, ja, jb, 1, nz + 2}};
       int n = 0;
       for (const oafdtd::Span3& bx : boxes)
         if (bx.q1 > bx.q0 && bx.j1 > bx.j0 && bx.k1 > bx.k0) slab_staged[kind][n++] = bx;
       n_slab_staged[kind] = n;
     }
     use_regions();
+    std::string why;
+    tma_ok = oafdtd::encode_sweep_maps<real>(sw, &maps, &why);
+    if (!tma_ok && staged == 2) {
+      staged = 1;
+      use_regions();
+    }
   }
   // ---- traffic model: algorithmic bytes per time step and kernel class, all batch members.
   // Sweeps: read 3 source components, read-modify-write 3 updated ones (9 values) per grid cell
   // and member; E also the three uint16 indices per cell and J read+write (2 P values) per
-  // dispersive edge. Slab kernel: the same for its cells plus psi read+write per correction cell.
-  // Edges: surface-impedance v_p and J_prev read+write, two H samples and the E write per edge.
+  // dispersive edge; psi read+write per correction cell, in the class of the kernel that applies
+  // it. Edges: surface-impedance v_p and J_prev read+write, two H samples and the E write per
+  // edge.
   {
     const double rb = sizeof(real);
     auto cells_in = [&](const oafdtd::Span3& s) {
@@ -766,11 +790,27 @@ int Engine<real>::build(const oafdtd_problem& p) {
       const long long k = f / (X_ * Y_), j = (f / X_) % Y_, i = f % X_;
       return i >= 4 * s.q0 && i < 4 * s.q1 && j >= s.j0 && j < s.j1 && k >= s.k0 && k < s.k1;
     };
+    // the staged kernels' share of a kind: the interior and the two z-slab boxes
+    auto staged_cells = [&](int kind) {
+      return cells_in(inner_staged[kind]) + cells_in(zin_staged[kind][0]) + cells_in(zin_staged[kind][1]);
+    };
+    auto in_staged = [&](int kind, long long f) {
+      return inside(inner_staged[kind], f, X, Y) || inside(zin_staged[kind][0], f, X, Y) ||
+             inside(zin_staged[kind][1], f, X, Y);
+    };
     const double cells = (double)nx * ny * nz;
-    double psi[2] = {0.0, 0.0};
+    double psi[2] = {0.0, 0.0}, psi_st[2] = {0.0, 0.0};
     for (int n = 0; n < p.n_corr; ++n) {
       const oafdtd_correction& k = p.corr[n];
-      psi[k.kind] += (double)(k.hi[0] - k.lo[0]) * (k.hi[1] - k.lo[1]) * (k.hi[2] - k.lo[2]) * B * 2.0 * rb;
+      const double per = (double)B * 2.0 * rb;
+      psi[k.kind] += (double)(k.hi[0] - k.lo[0]) * (k.hi[1] - k.lo[1]) * (k.hi[2] - k.lo[2]) * per;
+      for (int zr = 0; zr < 2; ++zr) {  // the part inside a staged z-slab box
+        const oafdtd::Span3& z = zin_staged[k.kind][zr];
+        const double x = std::max(0, std::min(4 * z.q1, (int)k.hi[0]) - std::max(4 * z.q0, (int)k.lo[0]));
+        const double y = std::max(0, std::min(z.j1, (int)k.hi[1]) - std::max(z.j0, (int)k.lo[1]));
+        const double zz = std::max(0, std::min(z.k1, (int)k.hi[2]) - std::max(z.k0, (int)k.lo[2]));
+        psi_st[k.kind] += x * y * zz * per;
+      }
     }
     double j_in = 0.0, j_all = 0.0, j_def = 0.0;
     for (int c = 0; c < 3; ++c)
@@ -781,17 +821,17 @@ int Engine<real>::build(const oafdtd_problem& p) {
           continue;
         }
         j_all += v;
-        if (inside(inner_staged[0], ae.f, X, Y)) j_in += v;
+        if (in_staged(0, ae.f)) j_in += v;
       }
-    const double h_in = cells_in(inner_staged[1]), e_in = cells_in(inner_staged[0]);
+    const double h_in = staged_cells(1), e_in = staged_cells(0);
     const double per_h = B * 9.0 * rb, per_e = B * 9.0 * rb + 6.0;
     const double edges = (double)p.sibc_n * B * (2.0 * rb * (1 + p.sibc_poles) + 3.0 * rb) + j_def;
     // classes: h_sweep, h_slab, ghosts, pre_e, e_sweep, e_slab, edges, probe_e
     double* st = class_bytes[1];
-    st[0] = h_in * per_h;
-    st[1] = (cells - h_in) * per_h + psi[1];
-    st[4] = e_in * per_e + j_in;
-    st[5] = (cells - e_in) * per_e + psi[0] + (j_all - j_in);
+    st[0] = h_in * per_h + psi_st[1];
+    st[1] = (cells - h_in) * per_h + psi[1] - psi_st[1];
+    st[4] = e_in * per_e + j_in + psi_st[0];
+    st[5] = (cells - e_in) * per_e + psi[0] - psi_st[0] + (j_all - j_in);
     st[6] = edges;
     double* sl = class_bytes[0];
     sl[1] = cells * per_h + psi[1];

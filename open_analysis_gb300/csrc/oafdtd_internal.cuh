@@ -84,9 +84,12 @@ struct SweepArgs {
   int staged;       // 2: staged by TMA tensor copies; 1: staged by cp.async; 0: slab kernel only
   int* status;      // device status word: bit 0 set when a bounded wait of a sweep gave up
   // Per kind ([0] E, [1] H): the interior box, which holds no CPML correction cell and is swept
-  // by the staged kernels, and up to six disjoint boxes covering the rest of the update domain,
-  // marched by the slab kernel (bulk update, corrections, Debye update).
+  // by the staged kernels; the z-slab planes over the interior's x-y extent ([low, high]), swept
+  // by the staged kernels with their z corrections; and up to six disjoint boxes covering the rest
+  // of the update domain, marched by the slab kernel (bulk update, corrections, Debye update).
   Span3 inner[2];
+  Span3 zin[2][2];
+  int zsd[2][2][2];  // [kind][low/high][component 0/1]: side of the z-term psi, -1 if none
   Span3 slab[2][6];
   int n_slab[2];
 };
@@ -98,6 +101,9 @@ struct SweepMaps {
   CUtensorMap e_wide[3], e_tile[3];
   CUtensorMap h_wide[3], h_tile[3];
   CUtensorMap mat[3];
+  // z-term psi of the two components that have one (E: Ex, Ey; H: Hx, Hy) as (x, y, z', batch)
+  // tensors with a tile box: [kind][component][low/high]
+  CUtensorMap psi_z[2][2][2];
 };
 
 constexpr int kStatusWaitTimeout = 1;

@@ -22,6 +22,7 @@
 // (packages/oa-fdtd/src/oa_fdtd/reference.py:152-180, :119-127).
 
 #include <mutex>
+#include <type_traits>
 
 #include "device_common.cuh"
 
@@ -31,7 +32,6 @@ constexpr int kTQ = 32;       // quads per tile row (128 cells)
 constexpr int kTY = 8;        // rows per tile
 constexpr int kTW = 4 * kTQ;  // tile width in cells
 constexpr int kHW = kTW + 4;  // staged width with a one-quad halo
-constexpr int kStages = 3;
 
 // One staged array: rows x width, dense (the layout a TMA box lands in), 128-byte aligned.
 template <typename T, int R, int W>
@@ -99,9 +99,10 @@ __device__ __forceinline__ void prefetch_map(const CUtensorMap* map) {
   asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<unsigned long long>(map)) : "memory");
 }
 // Barrier setup of the block's leader, made visible to the TMA unit before the first copy.
+template <int S>
 __device__ __forceinline__ void mbar_setup(unsigned long long* bar) {
 #pragma unroll
-  for (int s = 0; s < kStages; ++s) mbar_init(&bar[s], 1);
+  for (int s = 0; s < S; ++s) mbar_init(&bar[s], 1);
   asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
 }
 // Orders the block's reads of a slot (generic proxy) before the TMA writes that refill it.
@@ -109,36 +110,184 @@ __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
 }
 
-// Plane t of a block's march uses slot t % 3 in phase (t / 3) & 1.
+// Plane t of a block's march uses slot t % S in phase (t / S) & 1.
+template <int S>
 __device__ __forceinline__ bool wait_plane(unsigned long long* bar, int t) {
-  return mbar_wait(&bar[t % kStages], (unsigned)((t / kStages) & 1), kWaitNs);
+  return mbar_wait(&bar[t % S], (unsigned)((t / S) & 1), kWaitNs);
 }
 
 // A wait gave up: the leader records it and waits (bounded) for the planes [t, issued) it has
 // issued and not yet seen arrive, so no copy lands after the block has exited.
+template <int S>
 __device__ __noinline__ void abort_march(unsigned long long* bar, int t, int issued, int* status, bool leader) {
   if (!leader) return;
   if (status) atomicOr(status, kStatusWaitTimeout);
-  for (int p = t; p < issued; ++p) mbar_wait(&bar[p % kStages], (unsigned)((p / kStages) & 1), kDrainNs);
+  for (int p = t; p < issued; ++p) mbar_wait(&bar[p % S], (unsigned)((p / S) & 1), kDrainNs);
 }
 
 __device__ __forceinline__ unsigned char* align_smem(unsigned char* raw) {
   return raw + ((128u - (smem_addr(raw) & 127u)) & 127u);
 }
 
-// ------------------------------------------------------------------------------------- H sweep
-// Slot: E[3] rows y0..y0+8, x0..x0+131; H[3] rows y0..y0+7, x0..x0+127.
+// ------------------------------------------------------------------------------------- blocks
+// Stages per kernel: three planes in flight, two for the E sweep with z corrections (its slot is
+// larger; two blocks per SM must fit).
+template <bool kE, bool kZ>
+__host__ __device__ constexpr int stages() {
+  return kE && kZ ? 2 : 3;
+}
+
+// The z-term psi tiles of the two components that have one (E: Ex, Ey; H: Hx, Hy).
 template <typename real>
+struct ZPart {
+  Box<real, kTY, kTW> p[2];
+};
+struct NoPart {};
+
+// The box a block works on and its plane range. Plain sweeps cover the interior box in chunks of
+// tile_z planes; z sweeps cover one whole z-slab box (low or high) per block.
+struct BlockSpan {
+  int x0, y0, b, zr, k0, k1;
+  Span3 box;
+  bool empty;
+};
+
+template <typename real, bool kZ>
+__device__ __forceinline__ BlockSpan block_span(const SweepArgs<real>& a, int kind) {
+  BlockSpan s;
+  if (kZ) {
+    s.zr = (int)blockIdx.z & 1;
+    s.b = (int)blockIdx.z >> 1;
+    s.box = a.zin[kind][s.zr];
+    s.k0 = s.box.k0;
+    s.k1 = s.box.k1;
+  } else {
+    s.zr = 0;
+    s.box = a.inner[kind];
+    const int nkc = (s.box.k1 - s.box.k0 + a.tile_z - 1) / a.tile_z;
+    s.b = (int)blockIdx.z / nkc;
+    const int kc = (int)blockIdx.z % nkc;
+    s.k0 = s.box.k0 + kc * a.tile_z;
+    s.k1 = min(s.k0 + a.tile_z, s.box.k1);
+  }
+  s.x0 = 4 * (s.box.q0 + (int)blockIdx.x * kTQ);
+  s.y0 = s.box.j0 + (int)blockIdx.y * kTY;
+  s.empty = s.k1 <= s.k0 || s.x0 >= 4 * s.box.q1 || s.y0 >= s.box.j1;
+  return s;
+}
+
+// A z-term correction of one quad: psi <- b psi + c d; F <- F + (sign k)(ek d + psi), with the
+// plane's coefficients and psi staged in shared memory, for the cells of the correction box; the
+// updated psi row goes back to global memory.
+template <typename real>
+struct ZTerm {
+  const real* sm;  // staged psi of the quad
+  real* g;         // psi of the quad in global memory
+  real eb, ec, ek, sign;
+  int lo0, hi0;
+  bool on;         // the row and plane lie in the correction box
+};
+
+template <typename real>
+__device__ __forceinline__ ZTerm<real> z_term(const SweepArgs<real>& a, const CpmlTerm<real>& T, int sd,
+                                              const real* sm, int b, int k, int j, int i0, int kind) {
+  ZTerm<real> z;
+  z.on = false;
+  if (sd < 0) return z;
+  const CpmlSide<real>& s = sd == 0 ? T.side[0] : T.side[1];
+  z.on = j >= s.lo[1] && j < s.hi[1] && k >= s.lo[2] && k < s.hi[2];
+  if (!z.on) return z;
+  const int w = s.hi[2] - s.lo[2];
+  z.sm = sm;
+  z.g = s.psi + ((((long long)b * w + (k - s.lo[2])) * a.Y + j) * a.X + i0);
+  const real* const* co = kind == 0 ? a.pe[2] : a.ph[2];
+  z.eb = __ldg(co[0] + k);
+  z.ec = __ldg(co[1] + k);
+  z.ek = __ldg(co[2] + k);
+  z.sign = T.sign;
+  z.lo0 = s.lo[0];
+  z.hi0 = s.hi[0];
+  return z;
+}
+
+template <typename real>
+__device__ __forceinline__ void z_apply(const ZTerm<real>& z, Quad<real>& f, const real (&d)[4], const real (&kf)[4],
+                                        int i0) {
+  if (!z.on) return;
+  Quad<real> ps = ld4(z.sm);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const int i = i0 + e;
+    if (i < z.lo0 || i >= z.hi0) continue;
+    real p = ps.v[e] * z.eb;
+    p = p + z.ec * d[e];
+    ps.v[e] = p;
+    const real upd = z.ek * d[e] + p;
+    f.v[e] = f.v[e] + (z.sign * kf[e]) * upd;
+  }
+  st4(z.g, ps);
+}
+
+// psi tile copies of one plane of a z sweep (cp.async variant): [component][row][quad]
+template <typename real>
+__device__ __forceinline__ void z_stage(const SweepArgs<real>& a, ZPart<real>& zp, int kind, int zr, int b, int k,
+                                        int x0, int y0) {
+  constexpr int CQ = (int)(4 * sizeof(real) / 16);
+  constexpr int EL = 16 / sizeof(real);
+  constexpr int count = 2 * kTY * (kTW / 4) * CQ;
+  for (int t = threadIdx.x + threadIdx.y * blockDim.x; t < count; t += blockDim.x * blockDim.y) {
+    const int part = t % CQ, q = (t / CQ) % (kTW / 4), r = (t / CQ / (kTW / 4)) % kTY;
+    const int cc = t / CQ / (kTW / 4) / kTY;
+    const int sd = a.zsd[kind][zr][cc];
+    if (sd < 0) continue;
+    const CpmlTerm<real>& T = kind == 0 ? a.ecorr[cc][1] : a.hcorr[cc][1];
+    const CpmlSide<real>& s = sd == 0 ? T.side[0] : T.side[1];
+    const int x = x0 + 4 * q, y = y0 + r;
+    if (x >= a.X || y >= a.Y || k < s.lo[2] || k >= s.hi[2]) continue;
+    const int w = s.hi[2] - s.lo[2];
+    cp_async16(&zp.p[cc].v[r][4 * q] + part * EL,
+               s.psi + (((long long)b * w + (k - s.lo[2])) * a.Y + y) * a.X + x + part * EL);
+  }
+}
+
+// psi tile copies of one plane of a z sweep (TMA variant); returns the bytes they bring.
+template <typename real>
+__device__ __forceinline__ unsigned z_bytes(const SweepArgs<real>& a, int kind, int zr) {
+  unsigned n = 0;
+#pragma unroll
+  for (int cc = 0; cc < 2; ++cc)
+    if (a.zsd[kind][zr][cc] >= 0) n += kTY * kTW * sizeof(real);
+  return n;
+}
+template <typename real>
+__device__ __forceinline__ void z_issue(const SweepArgs<real>& a, const SweepMaps& tm, ZPart<real>& zp,
+                                        unsigned long long* bar, int kind, int zr, int b, int k, int x0, int y0) {
+#pragma unroll
+  for (int cc = 0; cc < 2; ++cc) {
+    const int sd = a.zsd[kind][zr][cc];
+    if (sd < 0) continue;
+    const CpmlTerm<real>& T = kind == 0 ? a.ecorr[cc][1] : a.hcorr[cc][1];
+    const CpmlSide<real>& s = sd == 0 ? T.side[0] : T.side[1];
+    // a plane outside the slab (H's high box reaches one plane past it) reads zero fill
+    tma_load4(&zp.p[cc], &tm.psi_z[kind][cc][zr], bar, x0, y0, k - s.lo[2], b);
+  }
+}
+
+// ------------------------------------------------------------------------------------- H sweep
+// Slot: E[3] rows y0..y0+8, x0..x0+131; H[3] rows y0..y0+7, x0..x0+127; z sweeps also the psi
+// of Hx and Hy.
+template <typename real, bool kZ>
 struct HSlot {
   Box<real, kTY + 1, kHW> e[3];
   Box<real, kTY, kTW> h[3];
+  typename std::conditional<kZ, ZPart<real>, NoPart>::type z;
 };
 
 // Planes k0..k1 are staged: E for all of them (plane k1 only feeds the z derivative of plane
 // k1 - 1), H for k < k1.
-template <typename real>
-__device__ __forceinline__ void h_stage(const SweepArgs<real>& a, HSlot<real>& s, int b, int k, int k1, int x0,
-                                        int y0) {
+template <typename real, bool kZ>
+__device__ __forceinline__ void h_stage(const SweepArgs<real>& a, HSlot<real, kZ>& s, int b, int zr, int k, int k1,
+                                        int x0, int y0) {
   const int X = a.X, Y = a.Y, Z = a.nz + 2;
   if (k >= Z || k > k1) return;
   const long long base = (long long)b * a.bs + (long long)k * X * Y;
@@ -163,47 +312,54 @@ __device__ __forceinline__ void h_stage(const SweepArgs<real>& a, HSlot<real>& s
       cp_async16(&s.h[c].v[r][4 * q] + part * EL, a.H[c] + base + (long long)y * X + x + part * EL);
     }
   }
+  if constexpr (kZ) {
+    if (k < k1) z_stage(a, s.z, 1, zr, b, k, x0, y0);
+  }
 }
 
-template <typename real>
-__device__ __forceinline__ void h_issue(const SweepMaps& tm, HSlot<real>& s, unsigned long long* bar, int b, int k,
-                                        int k1, int x0, int y0) {
+template <typename real, bool kZ>
+__device__ __forceinline__ void h_issue(const SweepArgs<real>& a, const SweepMaps& tm, HSlot<real, kZ>& s,
+                                        unsigned long long* bar, int b, int zr, int k, int k1, int x0, int y0) {
   constexpr unsigned eb = 3u * (kTY + 1) * kHW * sizeof(real);
   constexpr unsigned hb = 3u * kTY * kTW * sizeof(real);
   const bool with_h = k < k1;
-  mbar_expect_tx(bar, with_h ? eb + hb : eb);
+  unsigned bytes = with_h ? eb + hb : eb;
+  if constexpr (kZ) {
+    if (with_h) bytes += z_bytes(a, 1, zr);
+  }
+  mbar_expect_tx(bar, bytes);
 #pragma unroll
   for (int c = 0; c < 3; ++c) tma_load4(&s.e[c], &tm.e_wide[c], bar, x0, y0, k, b);
   if (with_h) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) tma_load4(&s.h[c], &tm.h_tile[c], bar, x0, y0, k, b);
+    if constexpr (kZ) z_issue(a, tm, s.z, bar, 1, zr, b, k, x0, y0);
   }
 }
 
-template <typename real, bool kTma>
+template <typename real, bool kTma, bool kZ>
 __global__ void __launch_bounds__(256, 2)
     h_staged_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SweepMaps tm) {
+  constexpr int S = stages<false, kZ>();
   extern __shared__ unsigned char smem_raw[];
-  __shared__ unsigned long long bar[kStages];
-  HSlot<real>* slot = reinterpret_cast<HSlot<real>*>(align_smem(smem_raw));
+  __shared__ unsigned long long bar[S];
+  HSlot<real, kZ>* slot = reinterpret_cast<HSlot<real, kZ>*>(align_smem(smem_raw));
   const int tx = threadIdx.x, ty = threadIdx.y;
   const bool leader = tx == 0 && ty == 0;
   const int nx = a.nx, ny = a.ny, nz = a.nz, X = a.X, Y = a.Y, Z = nz + 2;
-  const Span3 in = a.inner[1];
-  const int x0 = 4 * (in.q0 + blockIdx.x * kTQ), y0 = in.j0 + blockIdx.y * kTY;
-  const int nkc = (in.k1 - in.k0 + a.tile_z - 1) / a.tile_z;
-  const int b = blockIdx.z / nkc, kc = blockIdx.z % nkc;
-  const int k0 = in.k0 + kc * a.tile_z, k1 = min(k0 + a.tile_z, in.k1);
+  const BlockSpan sp = block_span<real, kZ>(a, 1);
+  if (sp.empty) return;
+  const int x0 = sp.x0, y0 = sp.y0, b = sp.b, zr = sp.zr, k0 = sp.k0, k1 = sp.k1;
   const int n_stage = k1 < Z ? k1 - k0 + 1 : k1 - k0;
   const int i0 = x0 + 4 * tx, j = y0 + ty;
-  const bool live = i0 < 4 * in.q1 && j < in.j1 && i0 <= nx + 1;
+  const bool live = i0 < 4 * sp.box.q1 && j < sp.box.j1 && i0 <= nx + 1;
   const long long base = (long long)b * a.bs;
   const real dtmu = a.dtmu;
   const Quad<real> ipx = i0 < X ? ld4(a.ip[0] + i0) : Quad<real>{};
   const real ipy = a.ip[1][min(j, Y - 1)];
   if (kTma) {
     if (leader) {
-      mbar_setup(bar);
+      mbar_setup<S>(bar);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         prefetch_map(&tm.e_wide[c]);
@@ -212,29 +368,29 @@ __global__ void __launch_bounds__(256, 2)
     }
     __syncthreads();
     if (leader)
-      for (int s = 0; s < kStages && s < n_stage; ++s) h_issue(tm, slot[s], &bar[s], b, k0 + s, k1, x0, y0);
+      for (int s = 0; s < S && s < n_stage; ++s) h_issue(a, tm, slot[s], &bar[s], b, zr, k0 + s, k1, x0, y0);
   } else {
 #pragma unroll
-    for (int s = 0; s < kStages; ++s) {
-      h_stage(a, slot[s], b, k0 + s, k1, x0, y0);
+    for (int s = 0; s < S; ++s) {
+      h_stage(a, slot[s], b, zr, k0 + s, k1, x0, y0);
       cp_commit();
     }
   }
   for (int k = k0; k < k1; ++k) {
     const int t = k - k0;
     if (kTma) {
-      bool ok = wait_plane(bar, t);
-      if (ok && t + 1 < n_stage) ok = wait_plane(bar, t + 1);
+      bool ok = wait_plane<S>(bar, t);
+      if (ok && t + 1 < n_stage) ok = wait_plane<S>(bar, t + 1);
       if (__syncthreads_or(!ok)) {
-        abort_march(bar, t, min(n_stage, t + kStages), a.status, leader);
+        abort_march<S>(bar, t, min(n_stage, t + S), a.status, leader);
         return;
       }
     } else {
-      cp_wait<kStages - 2>();
+      cp_wait<S - 2>();
       __syncthreads();
     }
-    const HSlot<real>& cur = slot[t % kStages];
-    const HSlot<real>& nxt = slot[(t + 1) % kStages];
+    const HSlot<real, kZ>& cur = slot[t % S];
+    const HSlot<real, kZ>& nxt = slot[(t + 1) % S];
     if (live) {
       const long long p = base + (long long)k * X * Y + (long long)j * X + i0;
       const bool kin = k <= nz;
@@ -242,30 +398,39 @@ __global__ void __launch_bounds__(256, 2)
       const Quad<real> ex = ld4(&cur.e[0].v[ty][4 * tx]), ey = ld4(&cur.e[1].v[ty][4 * tx]);
       const Quad<real> ez = ld4(&cur.e[2].v[ty][4 * tx]);
       const real ez_r = cur.e[2].v[ty][4 * tx + 4], ey_r = cur.e[1].v[ty][4 * tx + 4];
+      const real kf[4] = {dtmu, dtmu, dtmu, dtmu};
       if (j <= ny && kin) {  // Hx: node along x (1..nx+1), cell along y and z
         const Quad<real> ezy = ld4(&cur.e[2].v[ty + 1][4 * tx]);
         const Quad<real> ey1 = ld4(&nxt.e[1].v[ty][4 * tx]);
         Quad<real> h = ld4(&cur.h[0].v[ty][4 * tx]);
+        real d0[4], d1[4];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
           const int i = i0 + e;
-          const real d0 = (ezy.v[e] - ez.v[e]) * ipy;  // axis y
-          const real d1 = (ey1.v[e] - ey.v[e]) * ipz;  // axis z
-          if (i >= 1 && i <= nx + 1) h.v[e] = h.v[e] + dtmu * ((-d0) + d1);
+          d0[e] = (ezy.v[e] - ez.v[e]) * ipy;  // axis y
+          d1[e] = (ey1.v[e] - ey.v[e]) * ipz;  // axis z
+          if (i >= 1 && i <= nx + 1) h.v[e] = h.v[e] + dtmu * ((-d0[e]) + d1[e]);
         }
+        if constexpr (kZ)
+          z_apply(z_term(a, a.hcorr[0][1], a.zsd[1][zr][0], &cur.z.p[0].v[ty][4 * tx], b, k, j, i0, 1), h, d1, kf,
+                  i0);
         st4(a.H[0] + p, h);
       }
       if (kin) {  // Hy: cell along x (1..nx), node along y (1..ny+1), cell along z
         const Quad<real> ex1 = ld4(&nxt.e[0].v[ty][4 * tx]);
         Quad<real> h = ld4(&cur.h[1].v[ty][4 * tx]);
+        real d0[4], d1[4];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
           const int i = i0 + e;
           const real ezr = e < 3 ? ez.v[e + 1] : ez_r;
-          const real d0 = (ezr - ez.v[e]) * ipx.v[e];  // axis x
-          const real d1 = (ex1.v[e] - ex.v[e]) * ipz;  // axis z
-          if (i >= 1 && i <= nx) h.v[e] = h.v[e] + dtmu * ((-d1) + d0);
+          d0[e] = (ezr - ez.v[e]) * ipx.v[e];  // axis x
+          d1[e] = (ex1.v[e] - ex.v[e]) * ipz;  // axis z
+          if (i >= 1 && i <= nx) h.v[e] = h.v[e] + dtmu * ((-d1[e]) + d0[e]);
         }
+        if constexpr (kZ)
+          z_apply(z_term(a, a.hcorr[1][1], a.zsd[1][zr][1], &cur.z.p[1].v[ty][4 * tx], b, k, j, i0, 1), h, d1, kf,
+                  i0);
         st4(a.H[1] + p, h);
       }
       if (j <= ny) {  // Hz: cell along x and y, node along z (1..nz+1)
@@ -284,12 +449,12 @@ __global__ void __launch_bounds__(256, 2)
     }
     __syncthreads();  // every thread is done with the slot of plane k
     if (kTma) {
-      if (leader && t + kStages < n_stage) {
+      if (leader && t + S < n_stage) {
         fence_proxy_async();
-        h_issue(tm, slot[t % kStages], &bar[t % kStages], b, k + kStages, k1, x0, y0);
+        h_issue(a, tm, slot[t % S], &bar[t % S], b, zr, k + S, k1, x0, y0);
       }
     } else {
-      h_stage(a, slot[t % kStages], b, k + kStages, k1, x0, y0);
+      h_stage(a, slot[t % S], b, zr, k + S, k1, x0, y0);
       cp_commit();
     }
   }
@@ -297,17 +462,19 @@ __global__ void __launch_bounds__(256, 2)
 }
 
 // ------------------------------------------------------------------------------------- E sweep
-// Slot: H[3] rows y0-1..y0+7, x0-4..x0+127; E[3] and mat[3] rows y0..y0+7, x0..x0+127.
-template <typename real>
+// Slot: H[3] rows y0-1..y0+7, x0-4..x0+127; E[3] and mat[3] rows y0..y0+7, x0..x0+127; z sweeps
+// also the psi of Ex and Ey.
+template <typename real, bool kZ>
 struct ESlot {
   Box<real, kTY + 1, kHW> h[3];
   Box<real, kTY, kTW> e[3];
   Box<uint16_t, kTY, kTW> m[3];
+  typename std::conditional<kZ, ZPart<real>, NoPart>::type z;
 };
 
-template <typename real>
-__device__ __forceinline__ void e_stage(const SweepArgs<real>& a, ESlot<real>& s, int b, int k, int kend, int x0,
-                                        int y0) {
+template <typename real, bool kZ>
+__device__ __forceinline__ void e_stage(const SweepArgs<real>& a, ESlot<real, kZ>& s, int b, int zr, int k, int kend,
+                                        int x0, int y0) {
   const int X = a.X, Y = a.Y;
   if (k >= kend) return;
   const long long plane = (long long)k * X * Y;
@@ -340,13 +507,14 @@ __device__ __forceinline__ void e_stage(const SweepArgs<real>& a, ESlot<real>& s
       cp_async16(&s.m[c].v[r][8 * q], a.mat[c] + plane + (long long)y * X + x);
     }
   }
+  if constexpr (kZ) z_stage(a, s.z, 0, zr, b, k, x0, y0);
 }
 
-template <typename real>
-__device__ __forceinline__ void e_issue(const SweepMaps& tm, ESlot<real>& s, unsigned long long* bar, int b, int k,
-                                        int x0, int y0) {
-  constexpr unsigned bytes =
-      3u * ((kTY + 1) * kHW * sizeof(real) + kTY * kTW * sizeof(real) + kTY * kTW * sizeof(uint16_t));
+template <typename real, bool kZ>
+__device__ __forceinline__ void e_issue(const SweepArgs<real>& a, const SweepMaps& tm, ESlot<real, kZ>& s,
+                                        unsigned long long* bar, int b, int zr, int k, int x0, int y0) {
+  unsigned bytes = 3u * ((kTY + 1) * kHW * sizeof(real) + kTY * kTW * sizeof(real) + kTY * kTW * sizeof(uint16_t));
+  if constexpr (kZ) bytes += z_bytes(a, 0, zr);
   mbar_expect_tx(bar, bytes);
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
@@ -354,30 +522,35 @@ __device__ __forceinline__ void e_issue(const SweepMaps& tm, ESlot<real>& s, uns
     tma_load4(&s.e[c], &tm.e_tile[c], bar, x0, y0, k, b);
     tma_load3(&s.m[c], &tm.mat[c], bar, x0, y0, k);
   }
+  if constexpr (kZ) z_issue(a, tm, s.z, bar, 0, zr, b, k, x0, y0);
 }
 
-// Bulk update, CPML and the Debye update of one E component on one quad. d0/d1 are the
-// derivatives along the component's two axes in ascending order; the reference's term order is
-// (d0, -d1) when first_plus, else (d1, -d0). j4 holds the prefetched Debye current (P = 1).
-template <typename real>
+// Bulk update, z correction (z sweeps) and the Debye update of one E component on one quad, in
+// the reference's order. d0/d1 are the derivatives along the component's two axes in ascending
+// order; the reference's term order is (d0, -d1) when first_plus, else (d1, -d0). j4 holds the
+// prefetched Debye current (P = 1).
+template <typename real, bool kZ>
 __device__ __forceinline__ void e_apply(const SweepArgs<real>& a, int c, real* __restrict__ E, long long p,
                                         const Quad<real>& e_old, const uint16_t* m, const real (&d0)[4],
                                         const real (&d1)[4], bool first_plus, const Quad<real>& j4in,
-                                        int i0, int j, int k, int b) {
+                                        const ZTerm<real>& zt, int i0, int j, int k, int b) {
   const int X = a.X, Y = a.Y, nx = a.nx;
   Quad<real> e4 = e_old;
   Coef<real> cf[4];
+  real kf[4];
   bool valid[4];
   bool disp = false;
 #pragma unroll
   for (int e = 0; e < 4; ++e) {
     const int i = i0 + e;
     cf[e] = a.coef[m[e]];
+    kf[e] = cf[e].cb;
     valid[e] = i >= 1 && i <= nx + 1;
     const real acc = first_plus ? d0[e] + (-d1[e]) : d1[e] + (-d0[e]);
     if (valid[e]) e4.v[e] = cf[e].ca * e4.v[e] + cf[e].cb * acc;
     disp |= valid[e] && m[e] >= a.ade_lo && m[e] < a.ade_hi;
   }
+  if constexpr (kZ) z_apply(zt, e4, d1, kf, i0);
   if (disp) {
     const long long jstride = (long long)a.B * a.jnk[c] * Y * X;
     const long long jq = (((long long)b * a.jnk[c] + (k - a.jk0[c])) * Y + j) * X + i0;
@@ -421,23 +594,22 @@ __device__ __forceinline__ void j_prefetch(const SweepArgs<real>& a, Quad<real> 
   }
 }
 
-template <typename real, bool kTma>
+template <typename real, bool kTma, bool kZ>
 __global__ void __launch_bounds__(256, 2)
     e_staged_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SweepMaps tm) {
+  constexpr int S = stages<true, kZ>();
   extern __shared__ unsigned char smem_raw[];
-  __shared__ unsigned long long bar[kStages];
-  ESlot<real>* slot = reinterpret_cast<ESlot<real>*>(align_smem(smem_raw));
+  __shared__ unsigned long long bar[S];
+  ESlot<real, kZ>* slot = reinterpret_cast<ESlot<real, kZ>*>(align_smem(smem_raw));
   const int tx = threadIdx.x, ty = threadIdx.y;
   const bool leader = tx == 0 && ty == 0;
   const int nx = a.nx, X = a.X, Y = a.Y;
-  const Span3 in = a.inner[0];
-  const int x0 = 4 * (in.q0 + blockIdx.x * kTQ), y0 = in.j0 + blockIdx.y * kTY;
-  const int nkc = (in.k1 - in.k0 + a.tile_z - 1) / a.tile_z;
-  const int b = blockIdx.z / nkc, kc = blockIdx.z % nkc;
-  const int k0 = in.k0 + kc * a.tile_z, k1 = min(k0 + a.tile_z, in.k1);
+  const BlockSpan sp = block_span<real, kZ>(a, 0);
+  if (sp.empty) return;
+  const int x0 = sp.x0, y0 = sp.y0, b = sp.b, zr = sp.zr, k0 = sp.k0, k1 = sp.k1;
   const int n_stage = k1 - k0;
   const int i0 = x0 + 4 * tx, j = y0 + ty;
-  const bool live = i0 < 4 * in.q1 && j < in.j1 && i0 <= nx + 1;
+  const bool live = i0 < 4 * sp.box.q1 && j < sp.box.j1 && i0 <= nx + 1;
   const long long base = (long long)b * a.bs;
   const Quad<real> idx4 = i0 < X ? ld4(a.idd[0] + i0) : Quad<real>{};
   const real idy = a.idd[1][min(j, Y - 1)];
@@ -451,7 +623,7 @@ __global__ void __launch_bounds__(256, 2)
   j_prefetch(a, jcur, k0, j, i0, b, live);
   if (kTma) {
     if (leader) {
-      mbar_setup(bar);
+      mbar_setup<S>(bar);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         prefetch_map(&tm.h_wide[c]);
@@ -461,11 +633,11 @@ __global__ void __launch_bounds__(256, 2)
     }
     __syncthreads();
     if (leader)
-      for (int s = 0; s < kStages && s < n_stage; ++s) e_issue(tm, slot[s], &bar[s], b, k0 + s, x0, y0);
+      for (int s = 0; s < S && s < n_stage; ++s) e_issue(a, tm, slot[s], &bar[s], b, zr, k0 + s, x0, y0);
   } else {
 #pragma unroll
-    for (int s = 0; s < kStages; ++s) {
-      e_stage(a, slot[s], b, k0 + s, k1, x0, y0);
+    for (int s = 0; s < S; ++s) {
+      e_stage(a, slot[s], b, zr, k0 + s, k1, x0, y0);
       cp_commit();
     }
   }
@@ -474,16 +646,16 @@ __global__ void __launch_bounds__(256, 2)
     Quad<real> jnext[3];
     j_prefetch(a, jnext, k + 1 < k1 ? k + 1 : -1, j, i0, b, live);
     if (kTma) {
-      const bool ok = wait_plane(bar, t);
+      const bool ok = wait_plane<S>(bar, t);
       if (__syncthreads_or(!ok)) {
-        abort_march(bar, t, min(n_stage, t + kStages), a.status, leader);
+        abort_march<S>(bar, t, min(n_stage, t + S), a.status, leader);
         return;
       }
     } else {
-      cp_wait<kStages - 1>();
+      cp_wait<S - 1>();
       __syncthreads();
     }
-    const ESlot<real>& cur = slot[t % kStages];
+    const ESlot<real, kZ>& cur = slot[t % S];
     if (live) {
       const long long q = (long long)k * X * Y + (long long)j * X + i0;
       const real idz = a.idd[2][k];
@@ -491,6 +663,12 @@ __global__ void __launch_bounds__(256, 2)
       const Quad<real> hz = ld4(&cur.h[2].v[ty + 1][4 * tx + 4]);
       const Quad<real> hzy = ld4(&cur.h[2].v[ty][4 * tx + 4]), hxy = ld4(&cur.h[0].v[ty][4 * tx + 4]);
       const real hz_l = cur.h[2].v[ty + 1][4 * tx + 3], hy_l = cur.h[1].v[ty + 1][4 * tx + 3];
+      ZTerm<real> zt[2];
+      zt[0].on = zt[1].on = false;
+      if constexpr (kZ) {
+        zt[0] = z_term(a, a.ecorr[0][1], a.zsd[0][zr][0], &cur.z.p[0].v[ty][4 * tx], b, k, j, i0, 0);
+        zt[1] = z_term(a, a.ecorr[1][1], a.zsd[0][zr][1], &cur.z.p[1].v[ty][4 * tx], b, k, j, i0, 0);
+      }
       real d0[4], d1[4];
       // Ex: terms (a = y, +Hz) then (a = z, -Hy)
 #pragma unroll
@@ -498,8 +676,8 @@ __global__ void __launch_bounds__(256, 2)
         d0[e] = (hz.v[e] - hzy.v[e]) * idy;
         d1[e] = (hy.v[e] - hy_m.v[e]) * idz;
       }
-      e_apply<real>(a, 0, a.E[0] + base, q, ld4(&cur.e[0].v[ty][4 * tx]), &cur.m[0].v[ty][4 * tx], d0, d1, true,
-                    jcur[0], i0, j, k, b);
+      e_apply<real, kZ>(a, 0, a.E[0] + base, q, ld4(&cur.e[0].v[ty][4 * tx]), &cur.m[0].v[ty][4 * tx], d0, d1,
+                        true, jcur[0], zt[0], i0, j, k, b);
       // Ey: terms (a = z, +Hx) then (a = x, -Hz); d0 is the x term, d1 the z term
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
@@ -507,17 +685,19 @@ __global__ void __launch_bounds__(256, 2)
         d0[e] = (hz.v[e] - hzl) * idx4.v[e];
         d1[e] = (hx.v[e] - hx_m.v[e]) * idz;
       }
-      e_apply<real>(a, 1, a.E[1] + base, q, ld4(&cur.e[1].v[ty][4 * tx]), &cur.m[1].v[ty][4 * tx], d0, d1, false,
-                    jcur[1], i0, j, k, b);
-      // Ez: terms (a = x, +Hy) then (a = y, -Hx)
+      e_apply<real, kZ>(a, 1, a.E[1] + base, q, ld4(&cur.e[1].v[ty][4 * tx]), &cur.m[1].v[ty][4 * tx], d0, d1,
+                        false, jcur[1], zt[1], i0, j, k, b);
+      // Ez: terms (a = x, +Hy) then (a = y, -Hx); no z term
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const real hyl = e > 0 ? hy.v[e - 1] : hy_l;
         d0[e] = (hy.v[e] - hyl) * idx4.v[e];
         d1[e] = (hx.v[e] - hxy.v[e]) * idy;
       }
-      e_apply<real>(a, 2, a.E[2] + base, q, ld4(&cur.e[2].v[ty][4 * tx]), &cur.m[2].v[ty][4 * tx], d0, d1, true,
-                    jcur[2], i0, j, k, b);
+      ZTerm<real> none;
+      none.on = false;
+      e_apply<real, false>(a, 2, a.E[2] + base, q, ld4(&cur.e[2].v[ty][4 * tx]), &cur.m[2].v[ty][4 * tx], d0, d1,
+                           true, jcur[2], none, i0, j, k, b);
       hx_m = hx;
       hy_m = hy;
     }
@@ -525,12 +705,12 @@ __global__ void __launch_bounds__(256, 2)
     for (int c = 0; c < 3; ++c) jcur[c] = jnext[c];
     __syncthreads();
     if (kTma) {
-      if (leader && t + kStages < n_stage) {
+      if (leader && t + S < n_stage) {
         fence_proxy_async();
-        e_issue(tm, slot[t % kStages], &bar[t % kStages], b, k + kStages, x0, y0);
+        e_issue(a, tm, slot[t % S], &bar[t % S], b, zr, k + S, x0, y0);
       }
     } else {
-      e_stage(a, slot[t % kStages], b, k + kStages, k1, x0, y0);
+      e_stage(a, slot[t % S], b, zr, k + S, k1, x0, y0);
       cp_commit();
     }
   }
@@ -538,33 +718,57 @@ __global__ void __launch_bounds__(256, 2)
 }
 
 // ------------------------------------------------------------------------------------- launch
-template <typename real>
-cudaError_t launch_staged_sweep(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_t s, bool h) {
-  const Span3 in = a.inner[h ? 1 : 0];
-  if (in.q1 <= in.q0 || in.j1 <= in.j0 || in.k1 <= in.k0) return cudaSuccess;
-  // Every TMA box starts at x = 4 (q0 + 32 n) (the E sweep's halo box 4 cells earlier, which may
-  // be -4: a load may start before the grid): a multiple of 8 cells keeps the start 16-byte
-  // aligned for the 2-byte index boxes too.
-  if (in.q0 % 2 != 0) return cudaErrorInvalidValue;
-  const int nkc = (in.k1 - in.k0 + a.tile_z - 1) / a.tile_z;
+template <typename real, bool kTma, bool kZ>
+cudaError_t launch_one(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_t s, bool h, dim3 grid) {
   dim3 block(kTQ, kTY);
-  dim3 grid((in.q1 - in.q0 + kTQ - 1) / kTQ, (in.j1 - in.j0 + kTY - 1) / kTY, nkc * a.B);
-  const bool tma = a.staged == 2;
-  cudaError_t err;
   if (h) {
-    const size_t bytes = sizeof(HSlot<real>) * kStages + 128;
-    auto kern = tma ? h_staged_kernel<real, true> : h_staged_kernel<real, false>;
-    err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    const size_t bytes = sizeof(HSlot<real, kZ>) * stages<false, kZ>() + 128;
+    auto kern = h_staged_kernel<real, kTma, kZ>;
+    const cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (err != cudaSuccess) return err;
     kern<<<grid, block, bytes, s>>>(a, m);
   } else {
-    const size_t bytes = sizeof(ESlot<real>) * kStages + 128;
-    auto kern = tma ? e_staged_kernel<real, true> : e_staged_kernel<real, false>;
-    err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    const size_t bytes = sizeof(ESlot<real, kZ>) * stages<true, kZ>() + 128;
+    auto kern = e_staged_kernel<real, kTma, kZ>;
+    const cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (err != cudaSuccess) return err;
     kern<<<grid, block, bytes, s>>>(a, m);
   }
   return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_staged_sweep(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_t s, bool h) {
+  const int kind = h ? 1 : 0;
+  const bool tma = a.staged == 2;
+  // Every TMA box starts at x = 4 (q0 + 32 n) (the E sweep's halo box 4 cells earlier, which may
+  // be -4: a load may start before the grid): a multiple of 8 cells keeps the start 16-byte
+  // aligned for the 2-byte index boxes too.
+  const Span3 in = a.inner[kind];
+  if (in.q1 > in.q0 && in.j1 > in.j0 && in.k1 > in.k0) {
+    if (in.q0 % 2 != 0) return cudaErrorInvalidValue;
+    const int nkc = (in.k1 - in.k0 + a.tile_z - 1) / a.tile_z;
+    const dim3 grid((in.q1 - in.q0 + kTQ - 1) / kTQ, (in.j1 - in.j0 + kTY - 1) / kTY, nkc * a.B);
+    const cudaError_t err = tma ? launch_one<real, true, false>(a, m, s, h, grid)
+                                : launch_one<real, false, false>(a, m, s, h, grid);
+    if (err != cudaSuccess) return err;
+  }
+  // the z-slab planes over the same x-y extent: one block per tile, member and side
+  int nq = 0, nj = 0;
+  for (int zr = 0; zr < 2; ++zr) {
+    const Span3& z = a.zin[kind][zr];
+    if (z.k1 <= z.k0 || z.q1 <= z.q0 || z.j1 <= z.j0) continue;
+    if (z.q0 % 2 != 0) return cudaErrorInvalidValue;
+    nq = max(nq, z.q1 - z.q0);
+    nj = max(nj, z.j1 - z.j0);
+  }
+  if (nq > 0 && nj > 0) {
+    const dim3 grid((nq + kTQ - 1) / kTQ, (nj + kTY - 1) / kTY, 2 * a.B);
+    const cudaError_t err = tma ? launch_one<real, true, true>(a, m, s, h, grid)
+                                : launch_one<real, false, true>(a, m, s, h, grid);
+    if (err != cudaSuccess) return err;
+  }
+  return cudaSuccess;
 }
 
 // ------------------------------------------------------------------------------- descriptors
@@ -628,6 +832,17 @@ bool encode_sweep_maps(const SweepArgs<real>& a, SweepMaps* m, std::string* why)
         !encode(f, &m->mat[c], CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, a.mat[c], mdims, mstrides, tile, "mat", why))
       return false;
   }
+  for (int kind = 0; kind < 2; ++kind)
+    for (int cc = 0; cc < 2; ++cc)
+      for (int zr = 0; zr < 2; ++zr) {
+        const int sd = a.zsd[kind][zr][cc];
+        if (sd < 0) continue;
+        const CpmlSide<real>& s = (kind == 0 ? a.ecorr[cc][1] : a.hcorr[cc][1]).side[sd];
+        const cuuint64_t w = (cuuint64_t)(s.hi[2] - s.lo[2]);
+        const cuuint64_t pdims[4] = {X, Y, w, B};
+        const cuuint64_t pstrides[3] = {X * rs, X * Y * rs, X * Y * w * rs};
+        if (!encode(f, &m->psi_z[kind][cc][zr], dt, 4, s.psi, pdims, pstrides, tile, "psi", why)) return false;
+      }
   return true;
 }
 
@@ -635,7 +850,10 @@ static_assert(sizeof(Box<float, kTY + 1, kHW>) % 128 == 0 && sizeof(Box<uint16_t
               "staged arrays keep the 128-byte alignment TMA destinations need");
 static_assert((kHW * sizeof(float)) % 16 == 0 && (kTW * sizeof(uint16_t)) % 16 == 0,
               "TMA box rows are whole 16-byte units");
-static_assert(sizeof(ESlot<float>) * kStages + 128 <= 113 * 1024, "two E blocks per SM");
+static_assert(sizeof(ESlot<float, false>) * stages<true, false>() + 128 <= 113 * 1024 &&
+                  sizeof(ESlot<float, true>) * stages<true, true>() + 128 <= 113 * 1024 &&
+                  sizeof(HSlot<float, true>) * stages<false, true>() + 128 <= 113 * 1024,
+              "two blocks per SM for every float sweep");
 
 template cudaError_t launch_staged_sweep<float>(const SweepArgs<float>&, const SweepMaps&, cudaStream_t, bool);
 template cudaError_t launch_staged_sweep<double>(const SweepArgs<double>&, const SweepMaps&, cudaStream_t, bool);
