@@ -172,7 +172,9 @@ __device__ __forceinline__ long long jindex(const SweepArgs<real>& a, int c, int
 // psi), then the arithmetic, then every store, so no load waits behind a store it cannot be proven
 // not to alias. C: 0 Ex (terms y +Hz, z -Hy), 1 Ey (z +Hx, x -Hz), 2 Ez (x +Hy, y -Hx); d0 is
 // the derivative along the first axis in ascending order, d1 along the second.
-template <typename real, int C>
+// kMulti: more than one Debye pole (the general update, a call); single-pole runs compile without
+// it, so their registers never spill around the call.
+template <typename real, int C, bool kMulti>
 __device__ __forceinline__ void slab_e_column(const SweepArgs<real>& a, const SlabWork& w) {
   const int X = a.X, Y = a.Y, Z = a.nz + 2, nx = a.nx, b = w.b, j = w.j, i0 = w.i0;
   const long long sz = (long long)X * Y;
@@ -254,7 +256,7 @@ __device__ __forceinline__ void slab_e_column(const SweepArgs<real>& a, const Sl
     psi_apply<real>(a.ecorr[C][0], ps[0], a.pe, e4, d0, kf, k, j, i0);
     psi_apply<real>(a.ecorr[C][1], ps[1], a.pe, e4, d1, kf, k, j, i0);
     if (disp) {
-      if (a.ade_P == 1) {
+      if constexpr (!kMulti) {
         const real onekp = a.ade_onekp[0], kp = a.ade_kp[0];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
@@ -280,7 +282,7 @@ __device__ __forceinline__ void slab_e_column(const SweepArgs<real>& a, const Sl
     }
     // ---- stores
     st4(E + q, e4);
-    if (disp && a.ade_P == 1) st4(a.J[C] + jindex(a, C, b, k, j, i0), j4);
+    if (!kMulti && disp) st4(a.J[C] + jindex(a, C, b, k, j, i0), j4);
     psi_store<real>(a.ecorr[C][0], ps[0], b, k, j, i0, X, Y, Z);
     psi_store<real>(a.ecorr[C][1], ps[1], b, k, j, i0, X, Y, Z);
     if (C == 0) hm = s2;
@@ -288,17 +290,17 @@ __device__ __forceinline__ void slab_e_column(const SweepArgs<real>& a, const Sl
   }
 }
 
-template <typename real>
+template <typename real, bool kMulti>
 __global__ void __launch_bounds__(kSlabThreads, 3)
     slab_e_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SlabLaunch L) {
   const SlabWork w = slab_work(L, a.nx);
   if (!w.live || w.k0 >= w.k1) return;
   if (w.comp == 0)
-    slab_e_column<real, 0>(a, w);
+    slab_e_column<real, 0, kMulti>(a, w);
   else if (w.comp == 1)
-    slab_e_column<real, 1>(a, w);
+    slab_e_column<real, 1, kMulti>(a, w);
   else
-    slab_e_column<real, 2>(a, w);
+    slab_e_column<real, 2, kMulti>(a, w);
 }
 
 // ------------------------------------------------------------------------------------- H
@@ -420,8 +422,10 @@ cudaError_t launch_slab(const SweepArgs<real>& a, int kind, cudaStream_t s) {
   if (L.n == 0) return cudaSuccess;
   if (3 * total > 2147483647LL) return cudaErrorInvalidConfiguration;
   L.first[L.n] = (int)total;
-  if (kind == 0)
-    slab_e_kernel<real><<<(unsigned)(3 * total), kSlabThreads, 0, s>>>(a, L);
+  if (kind == 0 && a.ade_P > 1)
+    slab_e_kernel<real, true><<<(unsigned)(3 * total), kSlabThreads, 0, s>>>(a, L);
+  else if (kind == 0)
+    slab_e_kernel<real, false><<<(unsigned)(3 * total), kSlabThreads, 0, s>>>(a, L);
   else
     slab_h_kernel<real><<<(unsigned)(3 * total), kSlabThreads, 0, s>>>(a, L);
   return cudaGetLastError();

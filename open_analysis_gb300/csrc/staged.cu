@@ -529,7 +529,7 @@ __device__ __forceinline__ void e_issue(const SweepArgs<real>& a, const SweepMap
 // the reference's order. d0/d1 are the derivatives along the component's two axes in ascending
 // order; the reference's term order is (d0, -d1) when first_plus, else (d1, -d0). j4 holds the
 // prefetched Debye current (P = 1).
-template <typename real, bool kZ>
+template <typename real, bool kZ, bool kMulti>
 __device__ __forceinline__ void e_apply(const SweepArgs<real>& a, int c, real* __restrict__ E, long long p,
                                         const Quad<real>& e_old, const uint16_t* m, const real (&d0)[4],
                                         const real (&d1)[4], bool first_plus, const Quad<real>& j4in,
@@ -555,7 +555,7 @@ __device__ __forceinline__ void e_apply(const SweepArgs<real>& a, int c, real* _
     const long long jstride = (long long)a.B * a.jnk[c] * Y * X;
     const long long jq = (((long long)b * a.jnk[c] + (k - a.jk0[c])) * Y + j) * X + i0;
     real* J = a.J[c];
-    if (a.ade_P == 1) {
+    if constexpr (!kMulti) {
       Quad<real> j4 = j4in;
       const real onekp = a.ade_onekp[0], kp = a.ade_kp[0];
 #pragma unroll
@@ -594,7 +594,7 @@ __device__ __forceinline__ void j_prefetch(const SweepArgs<real>& a, Quad<real> 
   }
 }
 
-template <typename real, bool kTma, bool kZ>
+template <typename real, bool kTma, bool kZ, bool kMulti>
 __global__ void __launch_bounds__(256, 2)
     e_staged_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SweepMaps tm) {
   constexpr int S = stages<true, kZ>();
@@ -676,7 +676,7 @@ __global__ void __launch_bounds__(256, 2)
         d0[e] = (hz.v[e] - hzy.v[e]) * idy;
         d1[e] = (hy.v[e] - hy_m.v[e]) * idz;
       }
-      e_apply<real, kZ>(a, 0, a.E[0] + base, q, ld4(&cur.e[0].v[ty][4 * tx]), &cur.m[0].v[ty][4 * tx], d0, d1,
+      e_apply<real, kZ, kMulti>(a, 0, a.E[0] + base, q, ld4(&cur.e[0].v[ty][4 * tx]), &cur.m[0].v[ty][4 * tx], d0, d1,
                         true, jcur[0], zt[0], i0, j, k, b);
       // Ey: terms (a = z, +Hx) then (a = x, -Hz); d0 is the x term, d1 the z term
 #pragma unroll
@@ -685,7 +685,7 @@ __global__ void __launch_bounds__(256, 2)
         d0[e] = (hz.v[e] - hzl) * idx4.v[e];
         d1[e] = (hx.v[e] - hx_m.v[e]) * idz;
       }
-      e_apply<real, kZ>(a, 1, a.E[1] + base, q, ld4(&cur.e[1].v[ty][4 * tx]), &cur.m[1].v[ty][4 * tx], d0, d1,
+      e_apply<real, kZ, kMulti>(a, 1, a.E[1] + base, q, ld4(&cur.e[1].v[ty][4 * tx]), &cur.m[1].v[ty][4 * tx], d0, d1,
                         false, jcur[1], zt[1], i0, j, k, b);
       // Ez: terms (a = x, +Hy) then (a = y, -Hx); no z term
 #pragma unroll
@@ -696,7 +696,7 @@ __global__ void __launch_bounds__(256, 2)
       }
       ZTerm<real> none;
       none.on = false;
-      e_apply<real, false>(a, 2, a.E[2] + base, q, ld4(&cur.e[2].v[ty][4 * tx]), &cur.m[2].v[ty][4 * tx], d0, d1,
+      e_apply<real, false, kMulti>(a, 2, a.E[2] + base, q, ld4(&cur.e[2].v[ty][4 * tx]), &cur.m[2].v[ty][4 * tx], d0, d1,
                            true, jcur[2], none, i0, j, k, b);
       hx_m = hx;
       hy_m = hy;
@@ -729,7 +729,8 @@ cudaError_t launch_one(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_
     kern<<<grid, block, bytes, s>>>(a, m);
   } else {
     const size_t bytes = sizeof(ESlot<real, kZ>) * stages<true, kZ>() + 128;
-    auto kern = e_staged_kernel<real, kTma, kZ>;
+    // more than one Debye pole: the general update (a call); single-pole runs compile without it
+    auto kern = a.ade_P > 1 ? e_staged_kernel<real, kTma, kZ, true> : e_staged_kernel<real, kTma, kZ, false>;
     const cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (err != cudaSuccess) return err;
     kern<<<grid, block, bytes, s>>>(a, m);
