@@ -103,6 +103,9 @@ struct Engine final : EngineBase {
     if (t_start) cudaEventDestroy(t_start);
     if (t_stop) cudaEventDestroy(t_stop);
     for (void* p : allocs) cudaFree(p);
+    for (cudaEvent_t e : {fork_ev, join_ev})
+      if (e) cudaEventDestroy(e);
+    if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -178,6 +181,11 @@ struct Engine final : EngineBase {
   int kernel_times(double* out, int n) override;
   int step_timed(int64_t n, double* ms) override;
   cudaEvent_t t_start = nullptr, t_stop = nullptr;
+  // The slab kernel runs beside the staged sweep of the same kind (they write disjoint cells and
+  // read only the other field): forked onto `side` and joined back, inside the graph as well.
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  int sweep_pair(int kind, cudaEvent_t* ev, int slot, unsigned rec);
 };
 
 // ---------------------------------------------------------------------------- build
@@ -200,6 +208,9 @@ int Engine<real>::build(const oafdtd_problem& p) {
     return fail(OAFDTD_E_INVALID, "at most 16 Debye poles are supported");
   OA_CUDA(cudaGetDevice(&device));
   OA_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  OA_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+  OA_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+  OA_CUDA(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming));
 
   auto in_range = [&](long long f) { return f >= 0 && f < bs; };
 
@@ -845,20 +856,43 @@ int Engine<real>::build(const oafdtd_problem& p) {
 }
 
 // ---------------------------------------------------------------------------- step
+// The staged sweep and the slab kernel of one kind. Profiling (ev set) runs them one after the
+// other between the class events ev[slot], ev[slot + 1], ev[slot + 2]; otherwise the slab kernel
+// is forked onto the side stream and joined back.
+template <typename real>
+int Engine<real>::sweep_pair(int kind, cudaEvent_t* ev, int slot, unsigned rec) {
+  const char* names[2][2] = {{"e_sweep: ", "e_slab: "}, {"h_sweep: ", "h_slab: "}};
+  const bool fork = ev == nullptr && sw.staged;
+  cudaError_t err;
+  if (fork) {
+    OA_CUDA(cudaEventRecord(fork_ev, stream));
+    OA_CUDA(cudaStreamWaitEvent(side, fork_ev, 0));
+    err = oafdtd::launch_slab<real>(sw, kind, side);
+    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string(names[kind][1]) + cudaGetErrorString(err));
+    OA_CUDA(cudaEventRecord(join_ev, side));
+    err = oafdtd::launch_staged_sweep<real>(sw, maps, stream, kind == 1);
+    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string(names[kind][0]) + cudaGetErrorString(err));
+    OA_CUDA(cudaStreamWaitEvent(stream, join_ev, 0));
+    return OAFDTD_OK;
+  }
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[slot], stream, rec));
+  if (sw.staged) {
+    err = oafdtd::launch_staged_sweep<real>(sw, maps, stream, kind == 1);
+    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string(names[kind][0]) + cudaGetErrorString(err));
+  }
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[slot + 1], stream, rec));
+  err = oafdtd::launch_slab<real>(sw, kind, stream);
+  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string(names[kind][1]) + cudaGetErrorString(err));
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[slot + 2], stream, rec));
+  return OAFDTD_OK;
+}
+
 template <typename real>
 int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing) {
   cudaError_t err;
   // inside a stream capture an event record becomes a graph node only with the external flag
   const unsigned rec = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
-  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[0], stream, rec));
-  if (sw.staged) {
-    err = oafdtd::launch_staged_sweep<real>(sw, maps, stream, true);
-    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("h_sweep: ") + cudaGetErrorString(err));
-  }
-  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[1], stream, rec));
-  err = oafdtd::launch_slab<real>(sw, 1, stream);
-  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("h_slab: ") + cudaGetErrorString(err));
-  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[2], stream, rec));
+  if (int rc = sweep_pair(1, ev, 0, rec)) return rc;
   if (pmc_mask) {
     err = oafdtd::launch_ghosts<real>(sw.H, pmc_mask, nx, ny, nz, X, Y, B, stream);
     if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("ghosts: ") + cudaGetErrorString(err));
@@ -866,15 +900,7 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing) {
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[3], stream, rec));
   err = oafdtd::launch_pre_e<real>(pr, off, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("pre_e: ") + cudaGetErrorString(err));
-  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[4], stream, rec));
-  if (sw.staged) {
-    err = oafdtd::launch_staged_sweep<real>(sw, maps, stream, false);
-    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("e_sweep: ") + cudaGetErrorString(err));
-  }
-  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[5], stream, rec));
-  err = oafdtd::launch_slab<real>(sw, 0, stream);
-  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("e_slab: ") + cudaGetErrorString(err));
-  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[6], stream, rec));
+  if (int rc = sweep_pair(0, ev, 4, rec)) return rc;
   err = oafdtd::launch_sibc<real>(sb, stream);
   if (err == cudaSuccess) err = oafdtd::launch_edges<real>(ed, off, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("edges: ") + cudaGetErrorString(err));
