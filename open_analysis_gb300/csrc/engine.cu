@@ -3,6 +3,8 @@
 // the observables. The public contract is include/oafdtd.h.
 
 #include <algorithm>
+#include <chrono>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -188,9 +190,24 @@ struct Engine final : EngineBase {
   int sweep_pair(int kind, cudaEvent_t* ev, int slot, unsigned rec);
 };
 
+// Build phase timer: with OAFDTD_TIMING set in the environment, oafdtd_create prints the
+// host time of each phase of the build to stderr (diagnostics only).
+struct PhaseTimer {
+  bool on = std::getenv("OAFDTD_TIMING") != nullptr;
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  void mark(const char* what) {
+    if (!on) return;
+    const auto now = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "oafdtd build %-22s %8.1f ms\n", what,
+                 std::chrono::duration<double, std::milli>(now - t).count());
+    t = now;
+  }
+};
+
 // ---------------------------------------------------------------------------- build
 template <typename real>
 int Engine<real>::build(const oafdtd_problem& p) {
+  PhaseTimer timer;
   nx = p.nx;
   ny = p.ny;
   nz = p.nz;
@@ -226,6 +243,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
     sw.H[c] = h;
   }
 
+  timer.mark("fields");
   // ---- Debye ADE: per-edge coefficient rows and the set of dispersive edges
   const int P = p.ade_poles;
   // injection targets (component, flat)
@@ -253,6 +271,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
   }
   auto on_sibc = [&](int c, long long f) { return !sibc_bits.empty() && sibc_bits[(size_t)(c * bs + f)]; };
 
+  timer.mark("ade_classify");
   // ---- combined table. Entry key: (category, material index, ADE row); categories 0 plain,
   // 1 dispersive, 2 dispersive with injection or surface impedance (deferred to the edge pass,
   // after those). The map orders entries by category, so the kernels tell dispersive entries by
@@ -405,6 +424,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
     sw.J[c] = ed.J[c] = J;
   }
 
+  timer.mark("table_mat_J");
   // ---- 1-D metrics
   const int len[3] = {X, Y, Z};
   for (int a = 0; a < 3; ++a) {
@@ -414,6 +434,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
     if (rc) return rc;
   }
 
+  timer.mark("metrics");
   // ---- CPML
   sw.has_cpml = p.n_corr > 0;
   for (int a = 0; a < 3; ++a) {
@@ -481,6 +502,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
   sw.status = status;
   sw.staged = staged;
 
+  timer.mark("cpml");
   // ---- edge list: surface impedance, injection targets, deferred ADE edges
   struct EdgeRec {
     int comp;
@@ -647,6 +669,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
   if (int rc = alloc(&step_base, 1)) return rc;
   ed.step_base = pr.step_base = step_base;
 
+  timer.mark("edges_sibc");
   // ---- probes
   {
     n_probe = p.n_probe;
@@ -699,6 +722,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
       pr.series = ser;
     }
   }
+  timer.mark("probes");
   // ---- energy
   {
     en.X = X;
@@ -726,6 +750,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
     if (int rc = alloc(&energy_partial, (size_t)6 * oafdtd::kEnergyBlocks)) return rc;
     if (int rc = alloc(&energy_out, 6)) return rc;
   }
+  timer.mark("energy");
   // ---- sweep regions: per kind, an interior box free of CPML cells (staged sweeps) and the slab
   // boxes around it (slab kernel)
   {
@@ -783,6 +808,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
       use_regions();
     }
   }
+  timer.mark("regions_maps");
   // ---- traffic model: algorithmic bytes per time step and kernel class, all batch members.
   // Sweeps: read 3 source components, read-modify-write 3 updated ones (9 values) per grid cell
   // and member; E also the three uint16 indices per cell and J read+write (2 P values) per
@@ -851,7 +877,9 @@ int Engine<real>::build(const oafdtd_problem& p) {
     model_bytes = 0.0;
     for (int k = 0; k < kClasses; ++k) model_bytes += st[k];
   }
+  timer.mark("traffic_model");
   OA_CUDA(cudaStreamSynchronize(stream));
+  timer.mark("device_sync");
   return OAFDTD_OK;
 }
 
