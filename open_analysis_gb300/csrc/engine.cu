@@ -12,6 +12,7 @@
 #include <memory>
 #include <new>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <unordered_map>
 #include <vector>
@@ -204,6 +205,24 @@ struct PhaseTimer {
   }
 };
 
+// Runs f(begin, end, part) over [0, n) split into contiguous parts, one host thread each (up to
+// 16; one part below 65536 items). The split depends only on n, so two calls with the same n
+// hand the same range to the same part.
+constexpr int kMaxParts = 16;
+template <typename F>
+void parallel_parts(long long n, F&& f) {
+  int T = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), (unsigned)kMaxParts);
+  if (n < (1LL << 16)) T = 1;
+  const long long chunk = (n + T - 1) / T;
+  std::vector<std::thread> th;
+  for (int t = 1; t < T; ++t) {
+    const long long b = t * chunk, e = std::min(n, b + chunk);
+    if (b < e) th.emplace_back([&f, b, e, t] { f(b, e, t); });
+  }
+  f(0, std::min(n, chunk), 0);
+  for (std::thread& x : th) x.join();
+}
+
 // ---------------------------------------------------------------------------- build
 template <typename real>
 int Engine<real>::build(const oafdtd_problem& p) {
@@ -265,9 +284,19 @@ int Engine<real>::build(const oafdtd_problem& p) {
   std::vector<bool> sibc_bits;
   if (p.sibc_n > 0) {
     sibc_bits.assign((size_t)(3 * bs), false);
-    for (int64_t s = 0; s < p.sibc_n; ++s)
-      if (p.sibc_comp[s] >= 0 && p.sibc_comp[s] <= 2 && in_range(p.sibc_flat[s]))
-        sibc_bits[(size_t)(p.sibc_comp[s] * bs + p.sibc_flat[s])] = true;
+    for (int64_t s = 0; s < p.sibc_n; ++s) {
+      const int c = p.sibc_comp[s];
+      const long long f = p.sibc_flat[s];
+      if (c < 0 || c > 2 || !in_range(f) || p.sibc_mat[s] < 0 || p.sibc_mat[s] >= p.sibc_nmat)
+        return fail(OAFDTD_E_INVALID, "SIBC edge out of range");
+      for (int k = 0; k < 2; ++k)
+        if (p.sibc_hsign[2 * s + k] != 0.0 && (p.sibc_hcomp[2 * s + k] < 0 || p.sibc_hcomp[2 * s + k] > 2 ||
+                                               !in_range(p.sibc_hflat[2 * s + k])))
+          return fail(OAFDTD_E_INVALID, "SIBC sample out of range");
+      std::vector<bool>::reference bit = sibc_bits[(size_t)(c * bs + f)];
+      if (bit) return fail(OAFDTD_E_INVALID, "duplicate SIBC edge");
+      bit = true;
+    }
   }
   auto on_sibc = [&](int c, long long f) { return !sibc_bits.empty() && sibc_bits[(size_t)(c * bs + f)]; };
 
@@ -276,67 +305,127 @@ int Engine<real>::build(const oafdtd_problem& p) {
   // 1 dispersive, 2 dispersive with injection or surface impedance (deferred to the edge pass,
   // after those). The map orders entries by category, so the kernels tell dispersive entries by
   // an index range.
-  // Debye rows (cbe, beta_0..P-1) in the field precision; consecutive edges mostly share a row,
-  // so the last row is checked first and a hash map finds the others.
-  std::unordered_map<uint64_t, std::vector<int>> ade_row_by_hash;
-  std::vector<std::vector<real>> ade_rows;          // cbe, beta_0..P-1
-  std::vector<uint8_t> present(p.n_mat, 0);
+  // Debye rows (cbe, beta_0..P-1) in the field precision. The edges are classified in parallel
+  // parts; each part finds its rows (consecutive edges mostly share one, so the last is checked
+  // first and a hash finds the others) and its table keys, then the parts are merged in order.
   struct AdeEdge {
     long long f;
     int rid;
     int defer;
   };
+  struct RowSet {
+    std::vector<std::vector<real>> rows;
+    std::unordered_map<uint64_t, std::vector<int>> by_hash;
+    int last = -1;
+    int find_or_add(const real* row, int n) {
+      if (last >= 0 && std::memcmp(row, rows[last].data(), sizeof(real) * n) == 0) return last;
+      uint64_t h = 1469598103934665603ull;
+      const unsigned char* bytes = reinterpret_cast<const unsigned char*>(row);
+      for (size_t q = 0; q < sizeof(real) * n; ++q) h = (h ^ bytes[q]) * 1099511628211ull;
+      std::vector<int>& bucket = by_hash[h];
+      for (int cand : bucket)
+        if (std::memcmp(row, rows[cand].data(), sizeof(real) * n) == 0) return last = cand;
+      rows.emplace_back(row, row + n);
+      bucket.push_back((int)rows.size() - 1);
+      return last = (int)rows.size() - 1;
+    }
+  };
+  using Key = std::tuple<int, int, int>;  // (category, material index, Debye row)
+  RowSet global_rows;
   std::vector<AdeEdge> ade_edges[3];
   std::vector<std::pair<int, long long>> deferred;  // (comp, flat) in component order
   int kmin[3] = {0, 0, 0}, kmax[3] = {-1, -1, -1};
-  std::map<std::tuple<int, int, int>, int> entry;   // (category, v, rid) -> id
-  std::tuple<int, int, int> last_key{-1, -1, -1};
-  real row[1 + oafdtd::kMaxAdePoles];
-  int last_rid = -1;
-  auto row_id = [&]() -> int {
-    if (last_rid >= 0 && std::memcmp(row, ade_rows[last_rid].data(), sizeof(real) * (1 + P)) == 0) return last_rid;
-    uint64_t h = 1469598103934665603ull;
-    const unsigned char* bytes = reinterpret_cast<const unsigned char*>(row);
-    for (size_t q = 0; q < sizeof(real) * (1 + P); ++q) h = (h ^ bytes[q]) * 1099511628211ull;
-    std::vector<int>& bucket = ade_row_by_hash[h];
-    for (int cand : bucket)
-      if (std::memcmp(row, ade_rows[cand].data(), sizeof(real) * (1 + P)) == 0) return last_rid = cand;
-    const int rid = (int)ade_rows.size();
-    ade_rows.emplace_back(row, row + 1 + P);
-    bucket.push_back(rid);
-    return last_rid = rid;
-  };
+  std::map<Key, int> entry;  // key -> combined table id
+  // material indices: range check and the set of plain materials present
+  std::vector<uint8_t> present(p.n_mat, 0);
+  {
+    std::vector<std::vector<uint8_t>> seen(kMaxParts);
+    for (std::vector<uint8_t>& sv : seen) sv.assign(p.n_mat, 0);
+    int bad = 0;
+    for (int c = 0; c < 3 && !bad; ++c) {
+      const uint16_t* idx = p.idx[c];
+      std::vector<int> part_bad(kMaxParts, 0);
+      parallel_parts(bs, [&](long long b0, long long e0, int t) {
+        uint8_t* mark = seen[t].data();
+        for (long long q = b0; q < e0; ++q) {
+          const uint16_t v = idx[q];
+          if (v >= p.n_mat) {
+            part_bad[t] = 1;
+            return;
+          }
+          mark[v] = 1;
+        }
+      });
+      for (int t : part_bad) bad |= t;
+    }
+    if (bad) return fail(OAFDTD_E_INVALID, "material index beyond the table");
+    for (const std::vector<uint8_t>& sv : seen)
+      for (size_t v = 0; v < sv.size(); ++v) present[v] |= sv[v];
+  }
   for (int c = 0; c < 3; ++c) {
     const uint16_t* idx = p.idx[c];
-    for (long long q = 0; q < bs; ++q) {
-      if (idx[q] >= p.n_mat) return fail(OAFDTD_E_INVALID, "material index beyond the table");
-      present[idx[q]] = 1;
-    }
     const int64_t ne = P > 0 ? p.ade_n[c] : 0;
-    ade_edges[c].reserve((size_t)ne);
-    for (int64_t e = 0; e < ne; ++e) {
-      const long long f = p.ade_flat[c][e];
-      if (!in_range(f)) return fail(OAFDTD_E_INVALID, "ADE edge out of range");
-      row[0] = (real)p.ade_cbe[c][e];
-      for (int q = 0; q < P; ++q) row[1 + q] = (real)p.ade_beta[c][(size_t)q * ne + e];
-      const int rid = row_id();
-      const int defer = (injected(c, f) || on_sibc(c, f)) ? 1 : 0;
-      ade_edges[c].push_back({f, rid, defer});
-      const std::tuple<int, int, int> key{1 + defer, idx[f], rid};
-      if (key != last_key) {
-        entry[key] = 0;
-        last_key = key;
+    ade_edges[c].resize((size_t)ne);
+    struct Part {
+      RowSet rows;
+      std::vector<Key> keys;
+      Key last_key{-1, -1, -1};
+      int kmin = 1 << 30, kmax = -1;
+      bool bad = false;
+      std::vector<long long> defer;
+      std::vector<int> remap;
+    };
+    std::vector<Part> parts(kMaxParts);
+    AdeEdge* out = ade_edges[c].data();
+    parallel_parts(ne, [&](long long b0, long long e0, int t) {
+      Part& L = parts[t];
+      real row[1 + oafdtd::kMaxAdePoles];
+      for (long long e = b0; e < e0; ++e) {
+        const long long f = p.ade_flat[c][e];
+        if (!in_range(f)) {
+          L.bad = true;
+          return;
+        }
+        row[0] = (real)p.ade_cbe[c][e];
+        for (int q = 0; q < P; ++q) row[1 + q] = (real)p.ade_beta[c][(size_t)q * ne + e];
+        const int rid = L.rows.find_or_add(row, 1 + P);
+        const int defer = (injected(c, f) || on_sibc(c, f)) ? 1 : 0;
+        out[e] = AdeEdge{f, rid, defer};
+        const Key key{1 + defer, idx[f], rid};
+        if (key != L.last_key) {
+          if (std::find(L.keys.begin(), L.keys.end(), key) == L.keys.end()) L.keys.push_back(key);
+          L.last_key = key;
+        }
+        if (defer) L.defer.push_back(f);
+        const int k = (int)(f / ((long long)X * Y));
+        L.kmin = std::min(L.kmin, k);
+        L.kmax = std::max(L.kmax, k);
       }
-      if (defer) deferred.emplace_back(c, f);
-      const int k = (int)(f / ((long long)X * Y));
-      if (kmax[c] < kmin[c]) {
-        kmin[c] = kmax[c] = k;
-      } else {
-        kmin[c] = std::min(kmin[c], k);
-        kmax[c] = std::max(kmax[c], k);
+    });
+    // merge in part order: global row ids, table keys, deferred edges, plane range
+    for (Part& L : parts) {
+      if (L.bad) return fail(OAFDTD_E_INVALID, "ADE edge out of range");
+      L.remap.resize(L.rows.rows.size());
+      for (size_t r = 0; r < L.rows.rows.size(); ++r)
+        L.remap[r] = global_rows.find_or_add(L.rows.rows[r].data(), 1 + P);
+      for (const Key& k : L.keys) entry[Key{std::get<0>(k), std::get<1>(k), L.remap[std::get<2>(k)]}] = 0;
+      for (long long f : L.defer) deferred.emplace_back(c, f);
+      if (L.kmax >= 0) {
+        if (kmax[c] < kmin[c]) {
+          kmin[c] = L.kmin;
+          kmax[c] = L.kmax;
+        } else {
+          kmin[c] = std::min(kmin[c], L.kmin);
+          kmax[c] = std::max(kmax[c], L.kmax);
+        }
       }
     }
+    parallel_parts(ne, [&](long long b0, long long e0, int t) {
+      const std::vector<int>& remap = parts[t].remap;
+      for (long long e = b0; e < e0; ++e) out[e].rid = remap[out[e].rid];
+    });
   }
+  const std::vector<std::vector<real>>& ade_rows = global_rows.rows;
   for (int v = 0; v < p.n_mat; ++v)
     if (present[v]) entry[{0, v, -1}] = 0;
   if (entry.size() > 65536) return fail(OAFDTD_E_TABLE, "more than 65536 combined material entries");
@@ -362,20 +451,29 @@ int Engine<real>::build(const oafdtd_problem& p) {
     t_eps.push_back(p.eps_tab[v] * kEps0);
   }
   if (ade_lo < 0) ade_lo = ade_hi = 0;
+  // the index arrays: plain entries, then each dispersive edge's entry; kept on the host for the
+  // traffic model
+  std::vector<uint16_t> host_mat[3];
   for (int c = 0; c < 3; ++c) {
-    std::vector<uint16_t> m((size_t)bs);
+    std::vector<uint16_t>& m = host_mat[c];
+    m.resize((size_t)bs);
     const uint16_t* idx = p.idx[c];
-    for (long long q = 0; q < bs; ++q) m[q] = (uint16_t)plain[idx[q]];
-    std::tuple<int, int, int> lk{-1, -1, -1};
-    int lid = 0;
-    for (const AdeEdge& ae : ade_edges[c]) {
-      const std::tuple<int, int, int> key{1 + ae.defer, idx[ae.f], ae.rid};
-      if (key != lk) {
-        lid = entry[key];
-        lk = key;
+    parallel_parts(bs, [&](long long b0, long long e0, int) {
+      for (long long q = b0; q < e0; ++q) m[q] = (uint16_t)plain[idx[q]];
+    });
+    const AdeEdge* ae = ade_edges[c].data();
+    parallel_parts((long long)ade_edges[c].size(), [&](long long b0, long long e0, int) {
+      Key lk{-1, -1, -1};
+      int lid = 0;
+      for (long long e = b0; e < e0; ++e) {
+        const Key key{1 + ae[e].defer, idx[ae[e].f], ae[e].rid};
+        if (key != lk) {
+          lid = entry.find(key)->second;
+          lk = key;
+        }
+        m[ae[e].f] = (uint16_t)lid;
       }
-      m[ae.f] = (uint16_t)lid;
-    }
+    });
     uint16_t* dm = nullptr;
     int rc = upload_vec(&dm, m);
     if (rc) return rc;
@@ -503,29 +601,18 @@ int Engine<real>::build(const oafdtd_problem& p) {
   sw.staged = staged;
 
   timer.mark("cpml");
-  // ---- edge list: surface impedance, injection targets, deferred ADE edges
+  // ---- edge list: injection targets and deferred ADE edges (the surface-impedance edges were
+  // checked with their bit set above and have their own pass)
   struct EdgeRec {
     int comp;
     long long flat;
-    int sibc = -1;
-    int def = -1;
     std::vector<int> inj;
   };
   std::map<std::pair<int, long long>, EdgeRec> edges;
-  for (int64_t s = 0; s < p.sibc_n; ++s) {
-    const int c = p.sibc_comp[s];
-    const long long f = p.sibc_flat[s];
-    if (c < 0 || c > 2 || !in_range(f) || p.sibc_mat[s] < 0 || p.sibc_mat[s] >= p.sibc_nmat)
-      return fail(OAFDTD_E_INVALID, "SIBC edge out of range");
-    for (int k = 0; k < 2; ++k)
-      if (p.sibc_hsign[2 * s + k] != 0.0 && (p.sibc_hcomp[2 * s + k] < 0 || p.sibc_hcomp[2 * s + k] > 2 ||
-                                             !in_range(p.sibc_hflat[2 * s + k])))
-        return fail(OAFDTD_E_INVALID, "SIBC sample out of range");
-    EdgeRec& r = edges[{c, f}];
-    r.comp = c;
-    r.flat = f;
-    if (r.sibc >= 0) return fail(OAFDTD_E_INVALID, "duplicate SIBC edge");
-    r.sibc = (int)s;
+  for (const std::pair<int, long long>& cf : deferred) {
+    EdgeRec& r = edges[cf];
+    r.comp = cf.first;
+    r.flat = cf.second;
   }
   {
     // within one channel a repeated edge keeps only its last entry (NumPy fancy-index +=)
@@ -550,7 +637,6 @@ int Engine<real>::build(const oafdtd_problem& p) {
     for (auto& kv : edges) {
       EdgeRec& r = kv.second;
       const bool is_def = std::binary_search(def_sorted.begin(), def_sorted.end(), kv.first);
-      if (r.inj.empty() && !is_def) continue;  // surface impedance only: the SIBC pass covers it
       comp.push_back((int8_t)r.comp);
       flat.push_back(r.flat);
       ibeg.push_back((int)ichan.size());
@@ -823,17 +909,9 @@ int Engine<real>::build(const oafdtd_problem& p) {
       const double z = std::max(0, std::min(s.k1, nz + 1) - std::max(s.k0, 1));
       return x * y * z;
     };
-    auto inside = [](const oafdtd::Span3& s, long long f, long long X_, long long Y_) {
-      const long long k = f / (X_ * Y_), j = (f / X_) % Y_, i = f % X_;
-      return i >= 4 * s.q0 && i < 4 * s.q1 && j >= s.j0 && j < s.j1 && k >= s.k0 && k < s.k1;
-    };
     // the staged kernels' share of a kind: the interior and the two z-slab boxes
     auto staged_cells = [&](int kind) {
       return cells_in(inner_staged[kind]) + cells_in(zin_staged[kind][0]) + cells_in(zin_staged[kind][1]);
-    };
-    auto in_staged = [&](int kind, long long f) {
-      return inside(inner_staged[kind], f, X, Y) || inside(zin_staged[kind][0], f, X, Y) ||
-             inside(zin_staged[kind][1], f, X, Y);
     };
     const double cells = (double)nx * ny * nz;
     double psi[2] = {0.0, 0.0}, psi_st[2] = {0.0, 0.0};
@@ -849,17 +927,32 @@ int Engine<real>::build(const oafdtd_problem& p) {
         psi_st[k.kind] += x * y * zz * per;
       }
     }
-    double j_in = 0.0, j_all = 0.0, j_def = 0.0;
+    // Debye edges: all, deferred, and those in the staged E boxes (index entries in the
+    // dispersive range, counted over the boxes' rows)
+    const double jv = (double)B * P * 2.0 * rb;
+    double n_all = 0.0, n_def = 0.0;
     for (int c = 0; c < 3; ++c)
-      for (const AdeEdge& ae : ade_edges[c]) {
-        const double v = (double)B * P * 2.0 * rb;
-        if (ae.defer) {
-          j_def += v;
-          continue;
+      for (const AdeEdge& ae : ade_edges[c]) (ae.defer ? n_def : n_all) += 1.0;
+    double n_in = 0.0;
+    if (ade_hi > ade_lo) {
+      const oafdtd::Span3 boxes[3] = {inner_staged[0], zin_staged[0][0], zin_staged[0][1]};
+      for (int c = 0; c < 3; ++c)
+        for (const oafdtd::Span3& bx : boxes) {
+          if (bx.q1 <= bx.q0 || bx.j1 <= bx.j0 || bx.k1 <= bx.k0) continue;
+          std::vector<long long> part(kMaxParts, 0);
+          const int nj = bx.j1 - bx.j0;
+          parallel_parts((long long)(bx.k1 - bx.k0) * nj, [&](long long b0, long long e0, int t) {
+            long long n = 0;
+            for (long long r = b0; r < e0; ++r) {
+              const uint16_t* row = host_mat[c].data() + ((long long)(bx.k0 + r / nj) * Y + bx.j0 + r % nj) * X;
+              for (int i = 4 * bx.q0; i < 4 * bx.q1; ++i) n += row[i] >= ade_lo && row[i] < ade_hi;
+            }
+            part[t] = n;
+          });
+          for (long long n : part) n_in += (double)n;
         }
-        j_all += v;
-        if (in_staged(0, ae.f)) j_in += v;
-      }
+    }
+    const double j_all = n_all * jv, j_def = n_def * jv, j_in = n_in * jv;
     const double h_in = staged_cells(1), e_in = staged_cells(0);
     const double per_h = B * 9.0 * rb, per_e = B * 9.0 * rb + 6.0;
     const double edges = (double)p.sibc_n * B * (2.0 * rb * (1 + p.sibc_poles) + 3.0 * rb) + j_def;
