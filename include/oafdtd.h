@@ -176,6 +176,11 @@ int oafdtd_series(oafdtd_engine* engine, double* out);
  * 3..5 = Hx..Hz. Replaces CupyEngine.get_fields (engine.py:478-484). */
 int oafdtd_fields(oafdtd_engine* engine, int32_t comp, double* out);
 
+/* Overwrites one field component from float64 values in the oafdtd_fields layout, rounded to
+ * the field precision (restoring fields, or starting a check from a chosen state). The reference
+ * engine has no counterpart. */
+int oafdtd_set_field(oafdtd_engine* engine, int32_t comp, const double* in);
+
 /* Device bytes held by the handle: replaces CupyEngine.peak_bytes (engine.py:505-506). */
 int oafdtd_peak_bytes(const oafdtd_engine* engine, int64_t* out);
 

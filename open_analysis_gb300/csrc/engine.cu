@@ -51,6 +51,7 @@ struct EngineBase {
   virtual int dft(double* out) = 0;
   virtual int series(double* out) = 0;
   virtual int fields(int comp, double* out) = 0;
+  virtual int set_field(int comp, const double* in) = 0;
   virtual int kernel_times(double* out, int n) = 0;
   virtual int step_timed(int64_t n, double* ms) = 0;
   int64_t steps = 0;
@@ -181,6 +182,7 @@ struct Engine final : EngineBase {
   int dft(double* out) override;
   int series(double* out) override;
   int fields(int comp, double* out) override;
+  int set_field(int comp, const double* in) override;
   int kernel_times(double* out, int n) override;
   int step_timed(int64_t n, double* ms) override;
   cudaEvent_t t_start = nullptr, t_stop = nullptr;
@@ -1229,6 +1231,19 @@ int Engine<real>::fields(int comp, double* out) {
   return OAFDTD_OK;
 }
 
+template <typename real>
+int Engine<real>::set_field(int comp, const double* in) {
+  if (comp < 0 || comp > 5) return fail(OAFDTD_E_INVALID, "component must be 0..5");
+  OA_CUDA(cudaSetDevice(device));
+  real* dst = comp < 3 ? sw.E[comp] : sw.H[comp - 3];
+  const size_t count = (size_t)bs * B;
+  std::vector<real> tmp(count);
+  for (size_t k = 0; k < count; ++k) tmp[k] = (real)in[k];
+  OA_CUDA(cudaMemcpyAsync(dst, tmp.data(), count * sizeof(real), cudaMemcpyHostToDevice, stream));
+  OA_CUDA(cudaStreamSynchronize(stream));
+  return OAFDTD_OK;
+}
+
 }  // namespace
 
 namespace oafdtd {
@@ -1351,6 +1366,11 @@ int oafdtd_series(oafdtd_engine* engine, double* out) {
 int oafdtd_fields(oafdtd_engine* engine, int32_t comp, double* out) {
   if (!engine || !out) return fail(OAFDTD_E_INVALID, "null argument");
   return engine->impl->fields(comp, out);
+}
+
+int oafdtd_set_field(oafdtd_engine* engine, int32_t comp, const double* in) {
+  if (!engine || !in) return fail(OAFDTD_E_INVALID, "null argument");
+  return engine->impl->set_field(comp, in);
 }
 
 int oafdtd_peak_bytes(const oafdtd_engine* engine, int64_t* out) {

@@ -251,6 +251,12 @@ class Gb300Engine:
         names = ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")
         return {n: self.field(k) for k, n in enumerate(names)}
 
+    def set_field(self, comp: int, values: FloatArray) -> None:
+        """Overwrite one component (0..5 = Ex..Hz) with ``values`` of shape ``(B, z, y, x)``,
+        rounded to the engine's precision. No counterpart in the reference engine."""
+        a = np.ascontiguousarray(np.broadcast_to(np.asarray(values, dtype=np.float64), self.shape))
+        native.check(self._lib.oafdtd_set_field(self._h, int(comp), _ptr(a, C.c_double)), "set_field")
+
     def peak_bytes(self) -> int:
         out = C.c_int64()
         native.check(self._lib.oafdtd_peak_bytes(self._h, C.byref(out)), "peak_bytes")

@@ -50,6 +50,31 @@ def main(reference_root: str) -> None:
                 data[f"full.{comp}"] = np.ascontiguousarray(arr)
         save(str(HERE / f"{name}.npz"), data)
         print(name, "steps", steps, "batch", c.batch, "keys", len(data))
+    debye_fits(np)
+
+
+# Djordjevic-Sarkar materials fitted by the reference's multi-pole Debye fit:
+# (dk, df, f_ref, f_lo, f_hi) [-, -, Hz, Hz, Hz]
+DEBYE_CASES = (
+    (4.3, 0.02, 1e9, 0.1e9, 12e9),   # the FR-4 of the reference's DS-line test
+    (3.7, 0.008, 1e9, 0.05e9, 40e9),
+    (3.0, 0.002, 10e9, 1e9, 60e9),
+)
+
+
+def debye_fits(np):  # type: ignore[no-untyped-def]
+    from oa_fdtd.materials import fit_djordjevic_sarkar  # type: ignore[import-not-found]
+
+    out = {}
+    for n, (dk, df, fr, lo, hi) in enumerate(DEBYE_CASES):
+        fit = fit_djordjevic_sarkar(dk, df, fr, lo, hi)
+        out[f"{n}.case"] = np.array([dk, df, fr, lo, hi])
+        out[f"{n}.eps_inf"] = np.array([fit.eps_inf])
+        out[f"{n}.delta"] = fit.delta
+        out[f"{n}.tau"] = fit.tau
+        out[f"{n}.err"] = np.array([fit.err_eps, fit.err_tand])
+    np.savez(HERE / "debye_fits.npz", **out)
+    print("debye fits", len(DEBYE_CASES))
 
 
 if __name__ == "__main__":
