@@ -176,6 +176,19 @@ int oafdtd_series(oafdtd_engine* engine, double* out);
  * 3..5 = Hx..Hz. Replaces CupyEngine.get_fields (engine.py:478-484). */
 int oafdtd_fields(oafdtd_engine* engine, int32_t comp, double* out);
 
+/* One half of a time step, launched eagerly and synchronised: which 0 = the H half (H update,
+ * CPML-H, PMC ghosts, H probes), 1 = the E half (E update, CPML-E, Debye, SIBC, injection, E
+ * probes; advances the step counter). A z-slab decomposition exchanges boundary planes between
+ * the halves. OAFDTD_E_RANGE past max_steps; OAFDTD_E_INVALID when the halves come out of order.
+ * The reference engine has no counterpart (it steps whole steps only). */
+int oafdtd_step_half(oafdtd_engine* engine, int32_t which);
+
+/* Storage plane k (0 .. nz+1) of one component, all batch members, (batch, ny+2, pitch) as
+ * float64: read (oafdtd_plane) or written, rounded to the field precision (oafdtd_set_plane).
+ * The halo exchange of a z-slab decomposition; no counterpart in the reference engine. */
+int oafdtd_plane(oafdtd_engine* engine, int32_t comp, int32_t k, double* out);
+int oafdtd_set_plane(oafdtd_engine* engine, int32_t comp, int32_t k, const double* in);
+
 /* Overwrites one field component from float64 values in the oafdtd_fields layout, rounded to
  * the field precision (restoring fields, or starting a check from a chosen state). The reference
  * engine has no counterpart. */

@@ -52,6 +52,8 @@ struct EngineBase {
   virtual int series(double* out) = 0;
   virtual int fields(int comp, double* out) = 0;
   virtual int set_field(int comp, const double* in) = 0;
+  virtual int step_half(int which) = 0;
+  virtual int plane(int comp, int k, double* out, const double* in) = 0;
   virtual int kernel_times(double* out, int n) = 0;
   virtual int step_timed(int64_t n, double* ms) = 0;
   int64_t steps = 0;
@@ -153,7 +155,11 @@ struct Engine final : EngineBase {
   }
 
   int build(const oafdtd_problem& p);
-  int launch_step(int off, cudaEvent_t* ev, bool capturing = false);
+  // parts: 1 the H half (H sweeps, ghosts, pre_e), 2 the E half (E sweeps, SIBC, edges, probe_e)
+  int launch_step(int off, cudaEvent_t* ev, bool capturing = false, int parts = 3);
+  int step_half(int which) override;
+  int plane(int comp, int k, double* out, const double* in) override;
+  bool half_pending = false;  // an H half ran and its E half has not
   int capture();
 
   int step(int64_t n) override;
@@ -1011,26 +1017,30 @@ int Engine<real>::sweep_pair(int kind, cudaEvent_t* ev, int slot, unsigned rec) 
 }
 
 template <typename real>
-int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing) {
+int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing, int parts) {
   cudaError_t err;
   // inside a stream capture an event record becomes a graph node only with the external flag
   const unsigned rec = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
-  if (int rc = sweep_pair(1, ev, 0, rec)) return rc;
-  if (pmc_mask) {
-    err = oafdtd::launch_ghosts<real>(sw.H, pmc_mask, nx, ny, nz, X, Y, B, stream);
-    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("ghosts: ") + cudaGetErrorString(err));
+  if (parts & 1) {
+    if (int rc = sweep_pair(1, ev, 0, rec)) return rc;
+    if (pmc_mask) {
+      err = oafdtd::launch_ghosts<real>(sw.H, pmc_mask, nx, ny, nz, X, Y, B, stream);
+      if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("ghosts: ") + cudaGetErrorString(err));
+    }
+    if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[3], stream, rec));
+    err = oafdtd::launch_pre_e<real>(pr, off, stream);
+    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("pre_e: ") + cudaGetErrorString(err));
   }
-  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[3], stream, rec));
-  err = oafdtd::launch_pre_e<real>(pr, off, stream);
-  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("pre_e: ") + cudaGetErrorString(err));
-  if (int rc = sweep_pair(0, ev, 4, rec)) return rc;
-  err = oafdtd::launch_sibc<real>(sb, stream);
-  if (err == cudaSuccess) err = oafdtd::launch_edges<real>(ed, off, stream);
-  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("edges: ") + cudaGetErrorString(err));
-  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[7], stream, rec));
-  err = oafdtd::launch_probe_e<real>(pr, off, stream);
-  if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("probe_e: ") + cudaGetErrorString(err));
-  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[8], stream, rec));
+  if (parts & 2) {
+    if (int rc = sweep_pair(0, ev, 4, rec)) return rc;
+    err = oafdtd::launch_sibc<real>(sb, stream);
+    if (err == cudaSuccess) err = oafdtd::launch_edges<real>(ed, off, stream);
+    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("edges: ") + cudaGetErrorString(err));
+    if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[7], stream, rec));
+    err = oafdtd::launch_probe_e<real>(pr, off, stream);
+    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("probe_e: ") + cudaGetErrorString(err));
+    if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[8], stream, rec));
+  }
   return OAFDTD_OK;
 }
 
@@ -1231,6 +1241,58 @@ int Engine<real>::fields(int comp, double* out) {
   return OAFDTD_OK;
 }
 
+// One half of a time step, eagerly launched (a z-slab decomposition exchanges boundary planes
+// between the halves): 0 the H half, 1 the E half, which also advances the step counter.
+template <typename real>
+int Engine<real>::step_half(int which) {
+  OA_CUDA(cudaSetDevice(device));
+  if (which != 0 && which != 1) return fail(OAFDTD_E_INVALID, "half must be 0 (H) or 1 (E)");
+  if (which == 0) {
+    if (half_pending) return fail(OAFDTD_E_INVALID, "an H half is already pending");
+    if (steps + 1 > max_steps) return fail(OAFDTD_E_RANGE, "step count exceeds max_steps (wave table length)");
+    sw.tile_z = tile_z;
+    use_regions();
+    if (int rc = launch_step(0, nullptr, false, 1)) return rc;
+    half_pending = true;
+  } else {
+    if (!half_pending) return fail(OAFDTD_E_INVALID, "an E half needs its H half first");
+    if (int rc = launch_step(0, nullptr, false, 2)) return rc;
+    cudaError_t err = oafdtd::launch_bump(step_base, 1, stream);
+    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, cudaGetErrorString(err));
+    half_pending = false;
+    steps += 1;
+  }
+  OA_CUDA(cudaStreamSynchronize(stream));
+  OA_CUDA(cudaGetLastError());
+  return check_status();
+}
+
+// One storage plane k of a component, all batch members, (B, Y, X): read into out, or written
+// from in.
+template <typename real>
+int Engine<real>::plane(int comp, int k, double* out, const double* in) {
+  if (comp < 0 || comp > 5) return fail(OAFDTD_E_INVALID, "component must be 0..5");
+  if (k < 0 || k >= Z) return fail(OAFDTD_E_INVALID, "plane out of range");
+  OA_CUDA(cudaSetDevice(device));
+  real* f = comp < 3 ? sw.E[comp] : sw.H[comp - 3];
+  const size_t per = (size_t)X * Y;
+  std::vector<real> tmp(per * B);
+  if (in) {
+    for (size_t q = 0; q < tmp.size(); ++q) tmp[q] = (real)in[q];
+    for (int b = 0; b < B; ++b)
+      OA_CUDA(cudaMemcpyAsync(f + (size_t)b * bs + (size_t)k * per, tmp.data() + b * per, per * sizeof(real),
+                              cudaMemcpyHostToDevice, stream));
+    OA_CUDA(cudaStreamSynchronize(stream));
+  } else {
+    for (int b = 0; b < B; ++b)
+      OA_CUDA(cudaMemcpyAsync(tmp.data() + b * per, f + (size_t)b * bs + (size_t)k * per, per * sizeof(real),
+                              cudaMemcpyDeviceToHost, stream));
+    OA_CUDA(cudaStreamSynchronize(stream));
+    for (size_t q = 0; q < tmp.size(); ++q) out[q] = (double)tmp[q];
+  }
+  return OAFDTD_OK;
+}
+
 template <typename real>
 int Engine<real>::set_field(int comp, const double* in) {
   if (comp < 0 || comp > 5) return fail(OAFDTD_E_INVALID, "component must be 0..5");
@@ -1366,6 +1428,21 @@ int oafdtd_series(oafdtd_engine* engine, double* out) {
 int oafdtd_fields(oafdtd_engine* engine, int32_t comp, double* out) {
   if (!engine || !out) return fail(OAFDTD_E_INVALID, "null argument");
   return engine->impl->fields(comp, out);
+}
+
+int oafdtd_step_half(oafdtd_engine* engine, int32_t which) {
+  if (!engine) return fail(OAFDTD_E_INVALID, "null engine");
+  return engine->impl->step_half(which);
+}
+
+int oafdtd_plane(oafdtd_engine* engine, int32_t comp, int32_t k, double* out) {
+  if (!engine || !out) return fail(OAFDTD_E_INVALID, "null argument");
+  return engine->impl->plane(comp, k, out, nullptr);
+}
+
+int oafdtd_set_plane(oafdtd_engine* engine, int32_t comp, int32_t k, const double* in) {
+  if (!engine || !in) return fail(OAFDTD_E_INVALID, "null argument");
+  return engine->impl->plane(comp, k, nullptr, in);
 }
 
 int oafdtd_set_field(oafdtd_engine* engine, int32_t comp, const double* in) {

@@ -251,6 +251,25 @@ class Gb300Engine:
         names = ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")
         return {n: self.field(k) for k, n in enumerate(names)}
 
+    # ------------------------------------------------------------------ z-slab decomposition
+    def half_h(self) -> None:
+        """The H half of a step (H update, CPML-H, ghosts, H probes), synchronised."""
+        native.check(self._lib.oafdtd_step_half(self._h, 0), "step_half")
+
+    def half_e(self) -> None:
+        """The E half of a step (E update, CPML-E, Debye, SIBC, injection, E probes)."""
+        native.check(self._lib.oafdtd_step_half(self._h, 1), "step_half")
+
+    def plane(self, comp: int, k: int) -> FloatArray:
+        """Component ``comp`` (0..5 = Ex..Hz) at storage plane ``k``, shape (B, y, x)."""
+        out = np.zeros((self.B, self.shape[2], self.shape[3]))
+        native.check(self._lib.oafdtd_plane(self._h, int(comp), int(k), _ptr(out, C.c_double)), "plane")
+        return out
+
+    def set_plane(self, comp: int, k: int, values: FloatArray) -> None:
+        a = np.ascontiguousarray(np.broadcast_to(np.asarray(values, np.float64), (self.B, self.shape[2], self.shape[3])))
+        native.check(self._lib.oafdtd_set_plane(self._h, int(comp), int(k), _ptr(a, C.c_double)), "set_plane")
+
     def set_field(self, comp: int, values: FloatArray) -> None:
         """Overwrite one component (0..5 = Ex..Hz) with ``values`` of shape ``(B, z, y, x)``,
         rounded to the engine's precision. No counterpart in the reference engine."""

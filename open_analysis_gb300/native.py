@@ -147,6 +147,9 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "oafdtd_series": (C.c_int, [C.c_void_p, _pd]),
     "oafdtd_fields": (C.c_int, [C.c_void_p, _i32, _pd]),
     "oafdtd_set_field": (C.c_int, [C.c_void_p, _i32, _pd]),
+    "oafdtd_step_half": (C.c_int, [C.c_void_p, _i32]),
+    "oafdtd_plane": (C.c_int, [C.c_void_p, _i32, _i32, _pd]),
+    "oafdtd_set_plane": (C.c_int, [C.c_void_p, _i32, _i32, _pd]),
     "oafdtd_peak_bytes": (C.c_int, [C.c_void_p, _pi64]),
     "oafdtd_set_graph": (C.c_int, [C.c_void_p, _i32]),
     "oafdtd_set_tuning": (C.c_int, [C.c_void_p, _i32, _i32]),

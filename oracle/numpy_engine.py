@@ -277,21 +277,37 @@ class OracleEngine:
         self.acc[kind] += ph[:, None, None] * vals[None, :, :]
 
     def step(self, n: int = 1) -> None:
-        dt = self.c.dt
         for _ in range(n):
-            k = self.step_count
-            self._h_update()
-            self._pml("H")
-            self._ghosts()
-            self._record("H", (k + 0.5) * dt)
-            self._ade_save()
-            self._e_update()
-            self._pml("E")
-            self._sibc()
-            self._inject(k)
-            self._ade_update()
-            self._record("E", (k + 1) * dt)
-            self.step_count += 1
+            self.half_h()
+            self.half_e()
+
+    def half_h(self) -> None:
+        """First half of a step: H update, CPML-H, PMC ghosts, H probes at (n + 1/2) dt."""
+        k = self.step_count
+        self._h_update()
+        self._pml("H")
+        self._ghosts()
+        self._record("H", (k + 0.5) * self.c.dt)
+
+    def half_e(self) -> None:
+        """Second half: ADE save, E update, CPML-E, SIBC, injection at (n + 1/2) dt, ADE update,
+        E probes at (n + 1) dt."""
+        k = self.step_count
+        self._ade_save()
+        self._e_update()
+        self._pml("E")
+        self._sibc()
+        self._inject(k)
+        self._ade_update()
+        self._record("E", (k + 1) * self.c.dt)
+        self.step_count += 1
+
+    def plane(self, comp: int, k: int) -> FloatArray:
+        """Component ``comp`` (0..5 = Ex..Hz) at storage plane ``k``, shape (B, y, x)."""
+        return (self.E + self.H)[comp][:, k].astype(np.float64)
+
+    def set_plane(self, comp: int, k: int, values: FloatArray) -> None:
+        (self.E + self.H)[comp][:, k] = values
 
     # ------------------------------------------------------------------ observables
     def _weights(self, kind: str, comp: int) -> FloatArray:
