@@ -51,6 +51,7 @@ def main(reference_root: str) -> None:
         save(str(HERE / f"{name}.npz"), data)
         print(name, "steps", steps, "batch", c.batch, "keys", len(data))
     debye_fits(np)
+    touchstone_files(np)
 
 
 # Djordjevic-Sarkar materials fitted by the reference's multi-pole Debye fit:
@@ -60,6 +61,35 @@ DEBYE_CASES = (
     (3.7, 0.008, 1e9, 0.05e9, 40e9),
     (3.0, 0.002, 10e9, 1e9, 60e9),
 )
+
+
+def touchstone_files(np):  # type: ignore[no-untyped-def]
+    """Touchstone text written by the reference's writer for seeded S matrices: 1, 2 and 3 ports,
+    one reference impedance (v1.1) and per-port ones (v2.0)."""
+    import importlib.util
+
+    import oa_fdtd  # type: ignore[import-not-found]
+
+    # the module alone: the adapter package imports the framework, absent here
+    path = Path(oa_fdtd.__file__).parent / "adapter" / "touchstone.py"
+    spec = importlib.util.spec_from_file_location("reference_touchstone", path)
+    mod = importlib.util.module_from_spec(spec)  # type: ignore[arg-type]
+    spec.loader.exec_module(mod)  # type: ignore[union-attr]
+    format_touchstone = mod.format_touchstone
+
+    rng = np.random.default_rng(11)
+    out = {}
+    for n, z0 in ((1, [50.0]), (2, [50.0, 50.0]), (2, [49.2, 51.0]), (3, [50.0, 50.0, 50.0]), (3, [25.0, 50.0, 75.0])):
+        freqs = np.linspace(1e9, 5e9, 4)
+        s = rng.standard_normal((4, n, n)) + 1j * rng.standard_normal((4, n, n))
+        names = [f"port{i + 1}" for i in range(n)]
+        key = f"n{n}_" + "_".join(f"{z:g}" for z in z0)
+        out[key + ".s"] = s
+        out[key + ".freqs"] = freqs
+        out[key + ".z0"] = np.array(z0)
+        out[key + ".text"] = np.array(format_touchstone(freqs, s, z0, names, ["made by the reference"]))
+    np.savez(HERE / "touchstone.npz", **out)
+    print("touchstone", len(out) // 4)
 
 
 def debye_fits(np):  # type: ignore[no-untyped-def]
