@@ -25,10 +25,7 @@
 
 namespace oafdtd {
 
-// A block: kSlabCols quad columns x the three field components (threadIdx.y), so the three
-// threads of a column share their source-field reads through L1; every warp holds one component.
-constexpr int kSlabCols = 64;
-constexpr int kSlabThreads = 3 * kSlabCols;
+constexpr int kSlabThreads = 256;
 // Planes marched per thread. The slab boxes are thin (CPML slabs of ~10 cells): short marches
 // give the kernel enough independent threads to hide its load latency.
 constexpr int kSlabPlanes = 4;
@@ -132,14 +129,16 @@ __device__ __forceinline__ void psi_apply(const CpmlTerm<real>& T, PsiQuad<real>
   }
 }
 
-// Where a thread works: field component, member, box, quad column and plane range.
+// Where a thread works: field component, member, box, quad column and plane range. The
+// component is the fastest-varying block index, so the three components of a region run side by
+// side and share their source-field reads through L1 and L2.
 struct SlabWork {
   int comp, b, j, i0, k0, k1;
   bool live;
 };
 
 __device__ __forceinline__ SlabWork slab_work(const SlabLaunch& L, int nx) {
-  const int blk = (int)blockIdx.x;
+  const int blk = (int)blockIdx.x / 3;
   int s = 0;
   while (s + 1 < L.n && blk >= L.first[s + 1]) ++s;
   const Span3 bx = L.box[s];
@@ -148,10 +147,10 @@ __device__ __forceinline__ SlabWork slab_work(const SlabLaunch& L, int nx) {
   r /= L.cblk[s];
   const int ch = r % L.nch[s];
   SlabWork w;
-  w.comp = (int)threadIdx.y;
+  w.comp = (int)blockIdx.x % 3;
   w.b = r / L.nch[s];
   const int nq = bx.q1 - bx.q0;
-  const int col = cb * kSlabCols + (int)threadIdx.x;
+  const int col = cb * kSlabThreads + (int)threadIdx.x;
   const int ncol = nq * (bx.j1 - bx.j0);
   const int c = min(col, ncol - 1);
   w.j = bx.j0 + c / nq;
@@ -292,7 +291,7 @@ __device__ __forceinline__ void slab_e_column(const SweepArgs<real>& a, const Sl
 }
 
 template <typename real, bool kMulti>
-__global__ void __launch_bounds__(kSlabThreads, 4)
+__global__ void __launch_bounds__(kSlabThreads, 3)
     slab_e_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SlabLaunch L) {
   const SlabWork w = slab_work(L, a.nx);
   if (!w.live || w.k0 >= w.k1) return;
@@ -391,7 +390,7 @@ __device__ __forceinline__ void slab_h_column(const SweepArgs<real>& a, const Sl
 }
 
 template <typename real>
-__global__ void __launch_bounds__(kSlabThreads, 5)
+__global__ void __launch_bounds__(kSlabThreads, 4)
     slab_h_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SlabLaunch L) {
   const SlabWork w = slab_work(L, a.nx);
   if (!w.live || w.k0 >= w.k1) return;
@@ -415,21 +414,20 @@ cudaError_t launch_slab(const SweepArgs<real>& a, int kind, cudaStream_t s) {
     if (cols <= 0 || bx.k1 <= bx.k0) continue;
     L.box[L.n] = bx;
     L.first[L.n] = (int)total;
-    L.cblk[L.n] = (int)((cols + kSlabCols - 1) / kSlabCols);
+    L.cblk[L.n] = (int)((cols + kSlabThreads - 1) / kSlabThreads);
     L.nch[L.n] = (bx.k1 - bx.k0 + kSlabPlanes - 1) / kSlabPlanes;
     total += (long long)L.cblk[L.n] * L.nch[L.n] * a.B;
     ++L.n;
   }
   if (L.n == 0) return cudaSuccess;
-  if (total > 2147483647LL) return cudaErrorInvalidConfiguration;
+  if (3 * total > 2147483647LL) return cudaErrorInvalidConfiguration;
   L.first[L.n] = (int)total;
-  const dim3 block(kSlabCols, 3);
   if (kind == 0 && a.ade_P > 1)
-    slab_e_kernel<real, true><<<(unsigned)total, block, 0, s>>>(a, L);
+    slab_e_kernel<real, true><<<(unsigned)(3 * total), kSlabThreads, 0, s>>>(a, L);
   else if (kind == 0)
-    slab_e_kernel<real, false><<<(unsigned)total, block, 0, s>>>(a, L);
+    slab_e_kernel<real, false><<<(unsigned)(3 * total), kSlabThreads, 0, s>>>(a, L);
   else
-    slab_h_kernel<real><<<(unsigned)total, block, 0, s>>>(a, L);
+    slab_h_kernel<real><<<(unsigned)(3 * total), kSlabThreads, 0, s>>>(a, L);
   return cudaGetLastError();
 }
 

@@ -145,7 +145,7 @@ struct ZPart {
 struct NoPart {};
 
 // The box a block works on and its plane range. Plain sweeps cover the interior box in chunks of
-// tile_z planes; z sweeps cover one half of a z-slab box (low or high) per block.
+// tile_z planes; z sweeps cover one whole z-slab box (low or high) per block.
 struct BlockSpan {
   int x0, y0, b, zr, k0, k1;
   Span3 box;
@@ -157,12 +157,10 @@ __device__ __forceinline__ BlockSpan block_span(const SweepArgs<real>& a, int ki
   BlockSpan s;
   if (kZ) {
     s.zr = (int)blockIdx.z & 1;
-    const int half = ((int)blockIdx.z >> 1) & 1;
-    s.b = (int)blockIdx.z >> 2;
+    s.b = (int)blockIdx.z >> 1;
     s.box = a.zin[kind][s.zr];
-    const int mid = s.box.k0 + (s.box.k1 - s.box.k0 + 1) / 2;
-    s.k0 = half ? mid : s.box.k0;
-    s.k1 = half ? s.box.k1 : mid;
+    s.k0 = s.box.k0;
+    s.k1 = s.box.k1;
   } else {
     s.zr = 0;
     s.box = a.inner[kind];
@@ -756,7 +754,7 @@ cudaError_t launch_staged_sweep(const SweepArgs<real>& a, const SweepMaps& m, cu
                                 : launch_one<real, false, false>(a, m, s, h, grid);
     if (err != cudaSuccess) return err;
   }
-  // the z-slab planes over the same x-y extent: one block per tile, member, side and half
+  // the z-slab planes over the same x-y extent: one block per tile, member and side
   int nq = 0, nj = 0;
   for (int zr = 0; zr < 2; ++zr) {
     const Span3& z = a.zin[kind][zr];
@@ -766,7 +764,7 @@ cudaError_t launch_staged_sweep(const SweepArgs<real>& a, const SweepMaps& m, cu
     nj = max(nj, z.j1 - z.j0);
   }
   if (nq > 0 && nj > 0) {
-    const dim3 grid((nq + kTQ - 1) / kTQ, (nj + kTY - 1) / kTY, 4 * a.B);
+    const dim3 grid((nq + kTQ - 1) / kTQ, (nj + kTY - 1) / kTY, 2 * a.B);
     const cudaError_t err = tma ? launch_one<real, true, true>(a, m, s, h, grid)
                                 : launch_one<real, false, true>(a, m, s, h, grid);
     if (err != cudaSuccess) return err;
