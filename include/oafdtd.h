@@ -176,6 +176,13 @@ int oafdtd_series(oafdtd_engine* engine, double* out);
  * 3..5 = Hx..Hz. Replaces CupyEngine.get_fields (engine.py:478-484). */
 int oafdtd_fields(oafdtd_engine* engine, int32_t comp, double* out);
 
+/* Queues n steps on the handle's stream and returns without waiting (oafdtd_step is this and
+ * oafdtd_wait); oafdtd_wait synchronises and reports errors, including a bounded wait that gave
+ * up (OAFDTD_E_TIMEOUT). Several handles on one device then run side by side (a batched sweep
+ * of independent instances). Checks as oafdtd_step. No counterpart in the reference engine. */
+int oafdtd_step_async(oafdtd_engine* engine, int64_t n);
+int oafdtd_wait(oafdtd_engine* engine);
+
 /* One half of a time step, launched eagerly and synchronised: which 0 = the H half (H update,
  * CPML-H, PMC ghosts, H probes), 1 = the E half (E update, CPML-E, Debye, SIBC, injection, E
  * probes; advances the step counter). A z-slab decomposition exchanges boundary planes between

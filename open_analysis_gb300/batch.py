@@ -1,0 +1,118 @@
+"""Batched parameter sweeps: many independent FDTD instances on one GPU at the same time.
+
+A sweep (the reference runs one problem at a time) is a list of models with different grids.
+Each instance gets its own engine, stream and captured 64-step graphs; ``run_batched`` queues all
+their steps (``Gb300Engine.step_async``) before waiting on any, so the GPU runs kernels of many
+small grids side by side instead of one small grid at a time; ``run_looped`` is the plain way,
+one instance after the other (``step`` synchronises). Both give the same S-parameters bit for
+bit (each instance's arithmetic does not depend on what runs beside it).
+
+The host compiles the instances in a ``spawn`` process pool before any CUDA call (NumPy
+compile of one instance takes ~0.1-0.4 s).
+"""
+
+from __future__ import annotations
+
+import time
+from collections.abc import Sequence
+from concurrent.futures import ProcessPoolExecutor
+from dataclasses import dataclass, field
+from multiprocessing import get_context
+from typing import Any
+
+import numpy as np
+import numpy.typing as npt
+
+from open_analysis_gb300.model import Compiled, Model, compile_model
+from open_analysis_gb300.run import RunResult, source_spectrum, sparams
+
+ComplexArray = npt.NDArray[np.complex128]
+
+
+def _compile(args: tuple[Model, str]) -> Compiled:
+    return compile_model(*args)
+
+
+def compile_all(models: Sequence[Model], dtype: str = "float32", workers: int = 8) -> list[Compiled]:
+    """Compile every model on the host, in parallel processes (``spawn``: safe before or after
+    the process has touched the GPU)."""
+    if workers <= 1 or len(models) < 2:
+        return [compile_model(m, dtype) for m in models]
+    with ProcessPoolExecutor(max_workers=workers, mp_context=get_context("spawn")) as pool:
+        return list(pool.map(_compile, [(m, dtype) for m in models]))
+
+
+def collect(model: Model, c: Compiled, eng: Any, steps: int, dtype: str) -> RunResult:
+    """The ``RunResult`` of an engine that ran ``steps`` steps (as ``run`` assembles it: port
+    voltage sums, source spectrum, port resistances)."""
+    probes = eng.results()
+    sums = {f"V:{q['name']}": q["probe_parts"] for q in c.ports if q.get("probe_parts")}
+    sums.update(c.probe_sums)
+    for name, parts in sums.items():
+        probes[name] = sum(probes.pop(q) for q in parts)
+    return RunResult(
+        probes=probes,
+        source_dft=source_spectrum(c, steps),
+        steps=steps,
+        dt=c.dt,
+        engine=eng.name,
+        dtype=dtype,
+        stopped_by="max_steps",
+        energy_db=0.0,
+        peak_bytes=eng.peak_bytes(),
+        port_r=np.array([float(q["r_ohm"]) for q in c.ports]),
+    )
+
+
+@dataclass
+class SweepRun:
+    """S-parameters of every instance (``(N, N, F)`` each), the time of the stepping and of the
+    result read-back [s], the time to create the engines [s], and the cell-updates done."""
+
+    s: list[ComplexArray]
+    seconds: float
+    create_seconds: float
+    cell_updates: float
+    extra: dict[str, Any] = field(default_factory=dict)
+
+    @property
+    def sweeps_per_s(self) -> float:
+        return len(self.s) / self.seconds
+
+
+def _engines(compiled: Sequence[Compiled], steps: int, dtype: str) -> tuple[list[Any], float]:
+    from open_analysis_gb300.engine import Gb300Engine
+
+    t0 = time.perf_counter()
+    engines = [Gb300Engine(c, dtype, max_steps=steps) for c in compiled]
+    return engines, time.perf_counter() - t0
+
+
+def _finish(models, compiled, engines, steps, dtype, seconds, create):  # type: ignore[no-untyped-def]
+    t0 = time.perf_counter()
+    s = [sparams(m, collect(m, c, e, steps, dtype)) for m, c, e in zip(models, compiled, engines, strict=True)]
+    read = time.perf_counter() - t0
+    for e in engines:
+        e.close()
+    updates = float(sum(c.grid.cells * c.batch for c in compiled)) * steps
+    return SweepRun(s, seconds + read, create, updates, {"readback_seconds": read})
+
+
+def run_batched(models: Sequence[Model], compiled: Sequence[Compiled], steps: int, dtype: str = "float32") -> SweepRun:
+    """All instances at once: every engine's steps queued on its own stream, then waited on."""
+    engines, create = _engines(compiled, steps, dtype)
+    t0 = time.perf_counter()
+    for e in engines:
+        e.step_async(steps)
+    for e in engines:
+        e.wait()
+    return _finish(models, compiled, engines, steps, dtype, time.perf_counter() - t0, create)
+
+
+def run_looped(models: Sequence[Model], compiled: Sequence[Compiled], steps: int, dtype: str = "float32") -> SweepRun:
+    """The plain way: one instance after the other."""
+    engines, create = _engines(compiled, steps, dtype)
+    t0 = time.perf_counter()
+    for e in engines:
+        e.step(steps)
+    return _finish(models, compiled, engines, steps, dtype, time.perf_counter() - t0, create)

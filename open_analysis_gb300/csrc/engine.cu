@@ -53,6 +53,8 @@ struct EngineBase {
   virtual int fields(int comp, double* out) = 0;
   virtual int set_field(int comp, const double* in) = 0;
   virtual int step_half(int which) = 0;
+  virtual int enqueue(int64_t n) = 0;
+  virtual int wait() = 0;
   virtual int plane(int comp, int k, double* out, const double* in) = 0;
   virtual int kernel_times(double* out, int n) = 0;
   virtual int step_timed(int64_t n, double* ms) = 0;
@@ -163,6 +165,8 @@ struct Engine final : EngineBase {
   int capture();
 
   int step(int64_t n) override;
+  int enqueue(int64_t n) override;
+  int wait() override;
   int check_status();
   // The sweep regions of the current variant: interior + slab boxes, or the slab kernel alone.
   void use_regions() {
@@ -1096,7 +1100,24 @@ int Engine<real>::capture() {
 
 template <typename real>
 int Engine<real>::step(int64_t n) {
+  if (int rc = enqueue(n)) return rc;
+  return wait();
+}
+
+template <typename real>
+int Engine<real>::wait() {
+  OA_CUDA(cudaSetDevice(device));
+  OA_CUDA(cudaStreamSynchronize(stream));
+  OA_CUDA(cudaGetLastError());
+  return check_status();
+}
+
+// Queues n steps on the engine's stream (captured 64-step graphs for whole chunks) and returns;
+// wait() synchronises. Profiling reads its events chunk by chunk, so it synchronises per chunk.
+template <typename real>
+int Engine<real>::enqueue(int64_t n) {
   if (n < 0) return fail(OAFDTD_E_INVALID, "negative step count");
+  if (half_pending) return fail(OAFDTD_E_INVALID, "an H half is pending: finish the step with the E half");
   if (steps + n > max_steps) return fail(OAFDTD_E_RANGE, "step count exceeds max_steps (wave table length)");
   OA_CUDA(cudaSetDevice(device));
   if (graph_dirty) {
@@ -1151,9 +1172,7 @@ int Engine<real>::step(int64_t n) {
     steps += take;
     done += take;
   }
-  OA_CUDA(cudaStreamSynchronize(stream));
-  OA_CUDA(cudaGetLastError());
-  return check_status();
+  return OAFDTD_OK;
 }
 
 template <typename real>
@@ -1428,6 +1447,16 @@ int oafdtd_series(oafdtd_engine* engine, double* out) {
 int oafdtd_fields(oafdtd_engine* engine, int32_t comp, double* out) {
   if (!engine || !out) return fail(OAFDTD_E_INVALID, "null argument");
   return engine->impl->fields(comp, out);
+}
+
+int oafdtd_step_async(oafdtd_engine* engine, int64_t n) {
+  if (!engine) return fail(OAFDTD_E_INVALID, "null engine");
+  return engine->impl->enqueue(n);
+}
+
+int oafdtd_wait(oafdtd_engine* engine) {
+  if (!engine) return fail(OAFDTD_E_INVALID, "null engine");
+  return engine->impl->wait();
 }
 
 int oafdtd_step_half(oafdtd_engine* engine, int32_t which) {

@@ -211,6 +211,16 @@ class Gb300Engine:
             raise ValueError("step count exceeds max_steps (wave table length)")
         native.check(self._lib.oafdtd_step(self._h, int(n)), "step")
 
+    def step_async(self, n: int) -> None:
+        """Queue ``n`` steps on the engine's stream and return; ``wait()`` synchronises. Engines
+        on one device then run side by side (independent instances of a sweep)."""
+        if self.step_count + n > self.max_steps:
+            raise ValueError("step count exceeds max_steps (wave table length)")
+        native.check(self._lib.oafdtd_step_async(self._h, int(n)), "step_async")
+
+    def wait(self) -> None:
+        native.check(self._lib.oafdtd_wait(self._h), "wait")
+
     def step_timed(self, n: int) -> float:
         """``step(n)``; returns the device time of its launches [ms] (CUDA events on the engine's
         own stream)."""

@@ -13,6 +13,10 @@ geometry where the workload calls for randomness.
   layers as surface-impedance copper (sigma 5.8e7 S/m), a via (0.3 mm drill as the 1.694 r
   square barrel, 0.5 mm pads, 0.8 mm antipads), 10-cell CPML, two lumped ports, 256 DFT
   frequencies 0.1-20 GHz.
+* :func:`sweep_instances` — a seeded parameter sweep of microstrip and stripline instances with
+  uneven grids (80-240 x 40-120 x 30-80 cells of 50 um), trace width 0.1-0.6 mm, substrate
+  0.1-0.4 mm, single-pole Debye substrate (eps_inf 3.0-4.8, delta_eps 0.1-0.5, tau 2-20 ps),
+  8-cell CPML, two lumped ports, 128 DFT frequencies.
 """
 
 from __future__ import annotations
@@ -138,6 +142,75 @@ def via_transition(
     m.ports.append(LumpedPort("p1", 2, (x_p1, cy, z(planes[2] + 1)), (x_p1, cy, z(kt)), 50.0))
     m.ports.append(LumpedPort("p2", 2, (x_p2, cy, z(kb + 1)), (x_p2, cy, z(planes[0])), 50.0))
     return m
+
+
+@dataclass(frozen=True)
+class LineParams:
+    """One sweep instance: grid cells, trace width and substrate height [m], the Debye substrate
+    and whether a second ground plane makes it a stripline."""
+
+    nx: int
+    ny: int
+    nz: int
+    width: float
+    height: float
+    eps_inf: float
+    delta_eps: float
+    tau: float
+    stripline: bool
+
+
+def sweep_params(n: int, seed: int = 2026) -> list[LineParams]:
+    """``n`` instances drawn uniformly from the sweep ranges (seeded); even instances are
+    microstrips, odd ones striplines."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        out.append(
+            LineParams(
+                nx=int(rng.integers(80, 241)),
+                ny=int(rng.integers(40, 121)),
+                nz=int(rng.integers(30, 81)),
+                width=float(rng.uniform(0.1e-3, 0.6e-3)),
+                height=float(rng.uniform(0.1e-3, 0.4e-3)),
+                eps_inf=float(rng.uniform(3.0, 4.8)),
+                delta_eps=float(rng.uniform(0.1, 0.5)),
+                tau=float(rng.uniform(2e-12, 20e-12)),
+                stripline=bool(i % 2),
+            )
+        )
+    return out
+
+
+def line_instance(p: LineParams, h: float = 50e-6, n_freq: int = 128) -> Model:
+    """A microstrip (or stripline: a second PEC plane at twice the substrate height, the
+    dielectric filling both sides) on a PEC ground with a Debye substrate, 8-cell CPML on the
+    other walls, lumped ports at the two trace ends, DFT at ``n_freq`` frequencies 0.1-20 GHz."""
+    g = Grid(uniform_lines(p.nx, h), uniform_lines(p.ny, h), uniform_lines(p.nz, h))
+    m = Model(
+        g,
+        Waveform("gauss_mod", 10e9, 20e9),
+        np.linspace(0.1e9, 20e9, n_freq),
+        walls=("cpml", "cpml", "cpml", "cpml", "pec", "cpml"),
+        cpml=CpmlSpec(cells=8, m=3.0, kappa_max=5.0),
+    )
+    sub = max(2, round(p.height / h)) * h  # the substrate on whole cells
+    fill = 2 * sub if p.stripline else sub
+    m.regions.append(Region((-1.0, -1.0, 0.0), (1.0, 1.0, fill), p.eps_inf, poles=((p.delta_eps, p.tau),)))
+    if p.stripline:
+        m.regions.append(Region((-1.0, -1.0, fill), (1.0, 1.0, fill), pec=True))
+    yc = (p.ny // 2) * h
+    x0, x1 = 12 * h, (p.nx - 12) * h
+    half = max(h, round(p.width / (2 * h)) * h)
+    m.regions.append(Region((x0, yc - half, sub), (x1, yc + half, sub), pec=True))
+    m.ports.append(LumpedPort("p1", 2, (x0, yc, 0.0), (x0, yc, sub), 50.0))
+    m.ports.append(LumpedPort("p2", 2, (x1, yc, 0.0), (x1, yc, sub), 50.0))
+    return m
+
+
+def sweep_instances(n: int = 64, seed: int = 2026, h: float = 50e-6, n_freq: int = 128) -> list[Model]:
+    """The sweep's models (see :func:`sweep_params`)."""
+    return [line_instance(p, h, n_freq) for p in sweep_params(n, seed)]
 
 
 WORKLOADS = {
