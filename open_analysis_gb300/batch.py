@@ -13,6 +13,7 @@ compile of one instance takes ~0.1-0.4 s).
 
 from __future__ import annotations
 
+import os
 import time
 from collections.abc import Sequence
 from concurrent.futures import ProcessPoolExecutor
@@ -27,6 +28,11 @@ from open_analysis_gb300.model import Compiled, Model, compile_model
 from open_analysis_gb300.run import RunResult, source_spectrum, sparams
 
 ComplexArray = npt.NDArray[np.complex128]
+
+# Many engines run on many streams; CUDA maps streams onto this many hardware work queues (8 by
+# default, so streams beyond 8 share queues and serialise). Takes effect when set before the
+# process first uses CUDA.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 
 def _compile(args: tuple[Model, str]) -> Compiled:

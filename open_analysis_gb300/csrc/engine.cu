@@ -255,6 +255,9 @@ int Engine<real>::build(const oafdtd_problem& p) {
   if (p.ade_poles < 0 || p.ade_poles > oafdtd::kMaxAdePoles)
     return fail(OAFDTD_E_INVALID, "at most 16 Debye poles are supported");
   OA_CUDA(cudaGetDevice(&device));
+  OA_CUDA(oafdtd::preload_kernels<real>());
+  OA_CUDA(oafdtd::preload_staged<real>());
+  OA_CUDA(oafdtd::preload_slab<real>());
   OA_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   OA_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
   OA_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));

@@ -351,8 +351,32 @@ cudaError_t launch_bump(long long* step_base, int n, cudaStream_t s) {
   template cudaError_t launch_probe_e<real>(const ProbeArgs<real>&, int, cudaStream_t);            \
   template cudaError_t launch_edges<real>(const EdgeArgs<real>&, int, cudaStream_t);               \
   template cudaError_t launch_sibc<real>(const SibcArgs<real>&, cudaStream_t);                      \
+  template cudaError_t preload_kernels<real>();                                                     \
   template cudaError_t launch_energy<real>(const EnergyArgs<real>&, double*, int, double*,         \
                                            cudaStream_t);
+
+template <typename real>
+cudaError_t preload_kernels() {
+  cudaFuncAttributes fa;
+  const void* fns[] = {
+      reinterpret_cast<const void*>(ghost_kernel<real>),
+      reinterpret_cast<const void*>(pre_e_kernel<real>),
+      reinterpret_cast<const void*>(probe_e_kernel<real>),
+      reinterpret_cast<const void*>(sibc_kernel<real, 2, 16>),
+      reinterpret_cast<const void*>(sibc_kernel<real, 1, 16>),
+      reinterpret_cast<const void*>(sibc_kernel<real, 4, 16>),
+      reinterpret_cast<const void*>(sibc_generic_kernel<real>),
+      reinterpret_cast<const void*>(edge_kernel<real>),
+      reinterpret_cast<const void*>(energy_kernel<real>),
+      reinterpret_cast<const void*>(energy_final_kernel),
+      reinterpret_cast<const void*>(bump_kernel),
+  };
+  for (const void* f : fns) {
+    const cudaError_t err = cudaFuncGetAttributes(&fa, f);
+    if (err != cudaSuccess) return err;
+  }
+  return cudaSuccess;
+}
 
 OAFDTD_INSTANTIATE(float)
 OAFDTD_INSTANTIATE(double)

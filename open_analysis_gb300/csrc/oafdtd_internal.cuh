@@ -236,6 +236,16 @@ cudaError_t launch_staged_sweep(const SweepArgs<real>& a, const SweepMaps& m, cu
 template <typename real>
 bool encode_sweep_maps(const SweepArgs<real>& a, SweepMaps* m, std::string* why);
 
+// Loads every kernel of one precision on the current device now (cudaFuncGetAttributes), so
+// that no kernel is loaded lazily at its first launch: a lazy load synchronises the device and
+// would serialise engines that run side by side on their own streams.
+template <typename real>
+cudaError_t preload_kernels();
+template <typename real>
+cudaError_t preload_staged();
+template <typename real>
+cudaError_t preload_slab();
+
 // Message returned by oafdtd_last_error() on the calling thread.
 void set_last_error(const std::string& msg);
 

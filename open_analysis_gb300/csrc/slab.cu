@@ -431,6 +431,23 @@ cudaError_t launch_slab(const SweepArgs<real>& a, int kind, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+template <typename real>
+cudaError_t preload_slab() {
+  cudaFuncAttributes fa;
+  const void* fns[] = {
+      reinterpret_cast<const void*>(slab_e_kernel<real, false>),
+      reinterpret_cast<const void*>(slab_e_kernel<real, true>),
+      reinterpret_cast<const void*>(slab_h_kernel<real>),
+  };
+  for (const void* f : fns) {
+    const cudaError_t err = cudaFuncGetAttributes(&fa, f);
+    if (err != cudaSuccess) return err;
+  }
+  return cudaSuccess;
+}
+
+template cudaError_t preload_slab<float>();
+template cudaError_t preload_slab<double>();
 template cudaError_t launch_slab<float>(const SweepArgs<float>&, int, cudaStream_t);
 template cudaError_t launch_slab<double>(const SweepArgs<double>&, int, cudaStream_t);
 

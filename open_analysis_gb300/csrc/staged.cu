@@ -856,6 +856,32 @@ static_assert(sizeof(ESlot<float, false>) * stages<true, false>() + 128 <= 113 *
                   sizeof(HSlot<float, true>) * stages<false, true>() + 128 <= 113 * 1024,
               "two blocks per SM for every float sweep");
 
+template <typename real>
+cudaError_t preload_staged() {
+  cudaFuncAttributes fa;
+  const void* fns[] = {
+      reinterpret_cast<const void*>(h_staged_kernel<real, true, false>),
+      reinterpret_cast<const void*>(h_staged_kernel<real, true, true>),
+      reinterpret_cast<const void*>(h_staged_kernel<real, false, false>),
+      reinterpret_cast<const void*>(h_staged_kernel<real, false, true>),
+      reinterpret_cast<const void*>(e_staged_kernel<real, true, false, false>),
+      reinterpret_cast<const void*>(e_staged_kernel<real, true, true, false>),
+      reinterpret_cast<const void*>(e_staged_kernel<real, false, false, false>),
+      reinterpret_cast<const void*>(e_staged_kernel<real, false, true, false>),
+      reinterpret_cast<const void*>(e_staged_kernel<real, true, false, true>),
+      reinterpret_cast<const void*>(e_staged_kernel<real, true, true, true>),
+      reinterpret_cast<const void*>(e_staged_kernel<real, false, false, true>),
+      reinterpret_cast<const void*>(e_staged_kernel<real, false, true, true>),
+  };
+  for (const void* f : fns) {
+    const cudaError_t err = cudaFuncGetAttributes(&fa, f);
+    if (err != cudaSuccess) return err;
+  }
+  return cudaSuccess;
+}
+
+template cudaError_t preload_staged<float>();
+template cudaError_t preload_staged<double>();
 template cudaError_t launch_staged_sweep<float>(const SweepArgs<float>&, const SweepMaps&, cudaStream_t, bool);
 template cudaError_t launch_staged_sweep<double>(const SweepArgs<double>&, const SweepMaps&, cudaStream_t, bool);
 template bool encode_sweep_maps<float>(const SweepArgs<float>&, SweepMaps*, std::string*);
