@@ -19,6 +19,10 @@ advances between energy checks. Gcell-updates/s = interior cells x batch x time 
   timed region.
 * ``cpu_baseline``: the CPU oracle (the reference's NumPy engine restated) in float32 on the same
   compiled problem, a bounded sample of time steps, one host thread.
+* ``sweeps``: S-parameter sweeps/s of a seeded sweep of uneven microstrip/stripline instances
+  (``structures.sweep_instances``), all instances batched on the GPU at once against looping the
+  plain engine over them (``open_analysis_gb300.batch``); wall clock of the stepping and the
+  S-parameter read-back, engines created beforehand; both give identical S-parameters.
 
 ``--impl reference`` times the reference's CPU path (the oracle port; the reference is a Python
 package and is not installed on the GPU host) on the same workload, one time step per bench step.
@@ -40,6 +44,9 @@ from pathlib import Path
 from typing import Any
 
 import numpy as np
+
+# batched sweeps run many engines on many streams: more hardware work queues (before CUDA starts)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
@@ -209,6 +216,32 @@ def cpu_sample(c: Any, target_s: float) -> dict[str, Any]:
     }
 
 
+def sweep_measure(n: int, steps: int) -> dict[str, Any]:
+    """Batched against looped S-parameter sweeps over ``n`` seeded instances (2 ports, 128
+    frequencies each), ``steps`` time steps each."""
+    from open_analysis_gb300.batch import compile_all, run_batched, run_looped
+    from open_analysis_gb300.structures import sweep_instances
+
+    models = sweep_instances(n)
+    compiled = compile_all(models)
+    batched = run_batched(models, compiled, steps)
+    looped = run_looped(models, compiled, steps)
+    same = all(np.array_equal(a, b) for a, b in zip(batched.s, looped.s, strict=True))
+    return {
+        "metric": "S-parameter sweeps/s",
+        "instances": n,
+        "steps": steps,
+        "cells_total": int(sum(x.grid.cells for x in compiled)),
+        "batched": batched.sweeps_per_s,
+        "looped": looped.sweeps_per_s,
+        "batched_over_looped": batched.sweeps_per_s / looped.sweeps_per_s,
+        "batched_gcell_s": batched.cell_updates / batched.seconds / 1e9,
+        "looped_gcell_s": looped.cell_updates / looped.seconds / 1e9,
+        "identical_s": same,
+        "surrogate": None,
+    }
+
+
 def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
     from open_analysis_gb300 import native
     from open_analysis_gb300.engine import Gb300Engine
@@ -297,6 +330,10 @@ def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
     if ranks.rank == 0 and ranks.world == 1 and not args.no_cpu:
         cpu = cpu_sample(c, args.cpu_seconds)
 
+    sweeps = None
+    if args.sweep_instances > 0 and args.sweep_steps > 0:
+        sweeps = sweep_measure(args.sweep_instances, args.sweep_steps)
+
     if ranks.rank == 0:
         line = {
             "metric": "Gcell-updates/s",
@@ -341,6 +378,7 @@ def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
             "gpu_launches": graph_kernels * args.steps,
             "clocks": clocks,
             "cpu_baseline": cpu,
+            "sweeps": sweeps,
         }
         print(json.dumps(line), flush=True)
 
@@ -407,6 +445,8 @@ def main() -> None:
     ap.add_argument("--tile-z", type=int, default=0, help="planes per block")
     ap.add_argument("--variant", type=int, default=-1, help="1 staged sweeps, 0 register marching")
     ap.add_argument("--cells", default="", help="via-transition grid 'nx,ny,nz' (smaller profiling cases)")
+    ap.add_argument("--sweep-instances", type=int, default=64, help="batched-sweep instances (0: skip)")
+    ap.add_argument("--sweep-steps", type=int, default=2000, help="time steps per sweep instance")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

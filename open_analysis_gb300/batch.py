@@ -105,13 +105,23 @@ def _finish(models, compiled, engines, steps, dtype, seconds, create):  # type: 
 
 
 def run_batched(models: Sequence[Model], compiled: Sequence[Compiled], steps: int, dtype: str = "float32") -> SweepRun:
-    """All instances at once: every engine's steps queued on its own stream, then waited on."""
+    """All instances at once: every engine's steps queued on its own stream, then waited on.
+
+    The first 64-step chunk goes first on every engine (each captures its graph there), the
+    rest after: capturing a graph while other engines' work is queued would wait for that work
+    and run the instances one after the other."""
     engines, create = _engines(compiled, steps, dtype)
     t0 = time.perf_counter()
+    first = min(64, steps)
     for e in engines:
-        e.step_async(steps)
+        e.step_async(first)
     for e in engines:
         e.wait()
+    if steps > first:
+        for e in engines:
+            e.step_async(steps - first)
+        for e in engines:
+            e.wait()
     return _finish(models, compiled, engines, steps, dtype, time.perf_counter() - t0, create)
 
 
