@@ -176,6 +176,15 @@ int oafdtd_series(oafdtd_engine* engine, double* out);
  * 3..5 = Hx..Hz. Replaces CupyEngine.get_fields (engine.py:478-484). */
 int oafdtd_fields(oafdtd_engine* engine, int32_t comp, double* out);
 
+/* Snapshot of the run's whole device state (fields, CPML psi, Debye currents, SIBC state,
+ * deferred E^n, DFT accumulators, recorded series, step counter) into a host buffer of
+ * oafdtd_snapshot_bytes bytes; oafdtd_restore puts it back into a handle of the same problem and
+ * configuration (OAFDTD_E_INVALID otherwise), so a run can be bisected or resumed. The reference
+ * engine has no counterpart. */
+int oafdtd_snapshot_bytes(oafdtd_engine* engine, int64_t* out);
+int oafdtd_snapshot(oafdtd_engine* engine, void* out);
+int oafdtd_restore(oafdtd_engine* engine, const void* in);
+
 /* Queues n steps on the handle's stream and returns without waiting (oafdtd_step is this and
  * oafdtd_wait); oafdtd_wait synchronises and reports errors, including a bounded wait that gave
  * up (OAFDTD_E_TIMEOUT). Several handles on one device then run side by side (a batched sweep

@@ -54,6 +54,7 @@ struct EngineBase {
   virtual int set_field(int comp, const double* in) = 0;
   virtual int step_half(int which) = 0;
   virtual int enqueue(int64_t n) = 0;
+  virtual int snapshot(void* out, int64_t* bytes, const void* in) = 0;
   virtual int wait() = 0;
   virtual int plane(int comp, int k, double* out, const double* in) = 0;
   virtual int kernel_times(double* out, int n) = 0;
@@ -134,6 +135,14 @@ struct Engine final : EngineBase {
     return OAFDTD_OK;
   }
 
+  // Device buffers that hold the run's state (fields, psi, Debye currents, SIBC state, deferred
+  // E^n, DFT accumulators, recorded series, step counter), in registration order: a snapshot.
+  std::vector<std::pair<void*, size_t>> state_bufs;
+  template <typename T>
+  void keep_state(T* p, size_t count) {
+    state_bufs.emplace_back(static_cast<void*>(p), count * sizeof(T));
+  }
+
   template <typename T>
   int upload(T** out, const T* host, size_t count) {
     int rc = alloc(out, count);
@@ -166,6 +175,7 @@ struct Engine final : EngineBase {
 
   int step(int64_t n) override;
   int enqueue(int64_t n) override;
+  int snapshot(void* out, int64_t* bytes, const void* in) override;
   int wait() override;
   int check_status();
   // The sweep regions of the current variant: interior + slab boxes, or the slab kernel alone.
@@ -273,6 +283,8 @@ int Engine<real>::build(const oafdtd_problem& p) {
     if (rc) return rc;
     rc = alloc(&h, (size_t)bs * B);
     if (rc) return rc;
+    keep_state(e, (size_t)bs * B);
+    keep_state(h, (size_t)bs * B);
     sw.E[c] = e;
     sw.H[c] = h;
   }
@@ -533,6 +545,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
     if (nk > 0) {
       int rc = alloc(&J, (size_t)P * B * nk * Y * X);
       if (rc) return rc;
+      keep_state(J, (size_t)P * B * nk * Y * X);
     }
     sw.J[c] = ed.J[c] = J;
   }
@@ -593,6 +606,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
     real* psi = nullptr;
     int rc = alloc(&psi, (size_t)vol);
     if (rc) return rc;
+    keep_state(psi, (size_t)vol);
     term_ref.axis = k.a;
     term_ref.src = k.b;
     term_ref.sign = (real)k.sign;
@@ -695,6 +709,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
     ed.def_comp = pr.def_comp = d8;
     real* eold = nullptr;
     if ((rc = alloc(&eold, (size_t)B * std::max<size_t>(dflat.size(), 1)))) return rc;
+    keep_state(eold, (size_t)B * std::max<size_t>(dflat.size(), 1));
     ed.eold = pr.eold = eold;
   }
   // surface impedance: one packed record per edge, in the compiled order
@@ -735,8 +750,10 @@ int Engine<real>::build(const oafdtd_problem& p) {
     if ((rc = upload_vec(&dr, gp))) return rc;
     sb.gp = dr;
     if ((rc = alloc(&dr, (size_t)B * std::max(ns, 1)))) return rc;
+    keep_state(dr, (size_t)B * std::max(ns, 1));
     sb.jprev = dr;
     if ((rc = alloc(&dr, (size_t)SP * B * std::max(ns, 1)))) return rc;
+    keep_state(dr, (size_t)SP * B * std::max(ns, 1));
     sb.v = dr;
   }
   // sources
@@ -768,6 +785,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
   ed.Y = Y;
   ed.B = pr.B = en.B = B;
   if (int rc = alloc(&step_base, 1)) return rc;
+  keep_state(step_base, 1);
   ed.step_base = pr.step_base = step_base;
 
   timer.mark("edges_sibc");
@@ -814,12 +832,14 @@ int Engine<real>::build(const oafdtd_problem& p) {
     pr.dt = p.dt;
     double2* acc = nullptr;
     if ((rc = alloc(&acc, (size_t)std::max(p.n_probe, 1) * B * std::max(p.n_freq, 1)))) return rc;
+    keep_state(acc, (size_t)std::max(p.n_probe, 1) * B * std::max(p.n_freq, 1));
     pr.acc = acc;
     pr.max_steps = p.max_steps;
     pr.series = nullptr;
     if (p.record_series && p.n_probe > 0) {
       double* ser = nullptr;
       if ((rc = alloc(&ser, (size_t)p.n_probe * B * p.max_steps))) return rc;
+      keep_state(ser, (size_t)p.n_probe * B * p.max_steps);
       pr.series = ser;
     }
   }
@@ -1315,6 +1335,46 @@ int Engine<real>::plane(int comp, int k, double* out, const double* in) {
   return OAFDTD_OK;
 }
 
+// Snapshot layout: a 32-byte header (magic, format version, total bytes, step count), then every
+// state buffer in registration order. out == in == nullptr: report the size only.
+constexpr uint64_t kSnapshotMagic = 0x3130504E53444641ull;  // "AFDSNP01" read little-endian
+
+template <typename real>
+int Engine<real>::snapshot(void* out, int64_t* bytes, const void* in) {
+  uint64_t total = 32;
+  for (const auto& sb_ : state_bufs) total += sb_.second;
+  if (bytes) *bytes = (int64_t)total;
+  if (!out && !in) return OAFDTD_OK;
+  if (half_pending) return fail(OAFDTD_E_INVALID, "an H half is pending");
+  OA_CUDA(cudaSetDevice(device));
+  if (out) {
+    unsigned char* o = static_cast<unsigned char*>(out);
+    const uint64_t head[4] = {kSnapshotMagic, 1, total, (uint64_t)steps};
+    std::memcpy(o, head, sizeof(head));
+    size_t at = 32;
+    for (const auto& sb_ : state_bufs) {
+      OA_CUDA(cudaMemcpyAsync(o + at, sb_.first, sb_.second, cudaMemcpyDeviceToHost, stream));
+      at += sb_.second;
+    }
+    OA_CUDA(cudaStreamSynchronize(stream));
+    return OAFDTD_OK;
+  }
+  const unsigned char* i = static_cast<const unsigned char*>(in);
+  uint64_t head[4];
+  std::memcpy(head, i, sizeof(head));
+  if (head[0] != kSnapshotMagic || head[1] != 1) return fail(OAFDTD_E_INVALID, "not a snapshot of this format");
+  if (head[2] != total) return fail(OAFDTD_E_INVALID, "the snapshot was taken of another problem or configuration");
+  if ((int64_t)head[3] > max_steps) return fail(OAFDTD_E_RANGE, "the snapshot's step count exceeds max_steps");
+  size_t at = 32;
+  for (const auto& sb_ : state_bufs) {
+    OA_CUDA(cudaMemcpyAsync(sb_.first, i + at, sb_.second, cudaMemcpyHostToDevice, stream));
+    at += sb_.second;
+  }
+  OA_CUDA(cudaStreamSynchronize(stream));
+  steps = (int64_t)head[3];
+  return OAFDTD_OK;
+}
+
 template <typename real>
 int Engine<real>::set_field(int comp, const double* in) {
   if (comp < 0 || comp > 5) return fail(OAFDTD_E_INVALID, "component must be 0..5");
@@ -1450,6 +1510,21 @@ int oafdtd_series(oafdtd_engine* engine, double* out) {
 int oafdtd_fields(oafdtd_engine* engine, int32_t comp, double* out) {
   if (!engine || !out) return fail(OAFDTD_E_INVALID, "null argument");
   return engine->impl->fields(comp, out);
+}
+
+int oafdtd_snapshot_bytes(oafdtd_engine* engine, int64_t* out) {
+  if (!engine || !out) return fail(OAFDTD_E_INVALID, "null argument");
+  return engine->impl->snapshot(nullptr, out, nullptr);
+}
+
+int oafdtd_snapshot(oafdtd_engine* engine, void* out) {
+  if (!engine || !out) return fail(OAFDTD_E_INVALID, "null argument");
+  return engine->impl->snapshot(out, nullptr, nullptr);
+}
+
+int oafdtd_restore(oafdtd_engine* engine, const void* in) {
+  if (!engine || !in) return fail(OAFDTD_E_INVALID, "null argument");
+  return engine->impl->snapshot(nullptr, nullptr, in);
 }
 
 int oafdtd_step_async(oafdtd_engine* engine, int64_t n) {

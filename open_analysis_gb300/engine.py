@@ -221,6 +221,20 @@ class Gb300Engine:
     def wait(self) -> None:
         native.check(self._lib.oafdtd_wait(self._h), "wait")
 
+    # ------------------------------------------------------------------ snapshot / restore
+    def snapshot(self) -> bytes:
+        """The run's whole device state as bytes (see ``restore``)."""
+        n = C.c_int64()
+        native.check(self._lib.oafdtd_snapshot_bytes(self._h, C.byref(n)), "snapshot_bytes")
+        buf = C.create_string_buffer(int(n.value))
+        native.check(self._lib.oafdtd_snapshot(self._h, buf), "snapshot")
+        return buf.raw
+
+    def restore(self, state: bytes) -> None:
+        """Put a ``snapshot`` of an engine of the same problem and configuration back."""
+        buf = C.create_string_buffer(bytes(state), len(state))
+        native.check(self._lib.oafdtd_restore(self._h, buf), "restore")
+
     def step_timed(self, n: int) -> float:
         """``step(n)``; returns the device time of its launches [ms] (CUDA events on the engine's
         own stream)."""

@@ -149,6 +149,9 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "oafdtd_set_field": (C.c_int, [C.c_void_p, _i32, _pd]),
     "oafdtd_step_half": (C.c_int, [C.c_void_p, _i32]),
     "oafdtd_step_async": (C.c_int, [C.c_void_p, _i64]),
+    "oafdtd_snapshot_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "oafdtd_snapshot": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "oafdtd_restore": (C.c_int, [C.c_void_p, C.c_void_p]),
     "oafdtd_wait": (C.c_int, [C.c_void_p]),
     "oafdtd_plane": (C.c_int, [C.c_void_p, _i32, _i32, _pd]),
     "oafdtd_set_plane": (C.c_int, [C.c_void_p, _i32, _i32, _pd]),

@@ -138,6 +138,9 @@ def run(
     e_db = 0.0
     stopped = "max_steps"
     done = 0
+    import time
+
+    t_run = time.perf_counter()
     while done < max_steps:
         n = min(check_every, max_steps - done)
         eng.step(n)
@@ -165,6 +168,13 @@ def run(
         if done >= min_steps and peak > 0 and e_db <= end_db:
             stopped = "end_criterion"
             break
+    wall = time.perf_counter() - t_run
+    if isinstance(report, dict) and wall > 0 and done > 0:
+        # the run's own rate and, where the engine counts it, its algorithmic DRAM traffic
+        report["gcell_updates_per_s"] = float(c.grid.cells) * c.batch * done / wall / 1e9
+        if hasattr(eng, "model_bytes"):
+            report["bytes_per_step"] = float(eng.model_bytes())
+            report["gb_per_s"] = report["bytes_per_step"] * done / wall / 1e9
     probes = eng.results()
     sums = {f"V:{q['name']}": q["probe_parts"] for q in c.ports if q.get("probe_parts")}
     sums.update(c.probe_sums)

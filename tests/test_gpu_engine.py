@@ -273,3 +273,34 @@ def test_benchmark_size_from_random_fields_matches_oracle() -> None:
     for k, want in enumerate(ref.E + ref.H):
         got = gpu.field(k)
         assert np.array_equal(got, want.astype(np.float64)), f"{NAMES[k]}: max |d| = {np.abs(got - want).max()}"
+
+
+def test_snapshot_restore_resumes_bit_for_bit() -> None:
+    """A snapshot after 70 steps (mid-chunk), 50 more steps; restoring it (into the same engine
+    and into a fresh one) and stepping 50 again gives the same fields, DFTs and energy."""
+    c = compile_model(CASES["dispersive_copper"][0](namespace("gb300")), "float32")
+    a = _engine(c, max_steps=400)
+    a.step(70)
+    state = a.snapshot()
+    a.step(50)
+    want = [a.field(k) for k in range(6)]
+    want_res, want_e = a.results(), a.energy()
+    for eng in (a, _engine(c, max_steps=400)):
+        eng.restore(state)
+        assert eng.step_count == 70
+        eng.step(50)
+        for k in range(6):
+            assert np.array_equal(eng.field(k), want[k]), NAMES[k]
+        for name, v in want_res.items():
+            assert np.array_equal(eng.results()[name], v), name
+        assert eng.energy() == want_e
+    other = _engine(compile_model(CASES["mixed_walls"][0](namespace("gb300")), "float32"))
+    with pytest.raises(Exception):
+        other.restore(state)
+
+
+def test_run_report_carries_rate_and_traffic() -> None:
+    from open_analysis_gb300.run import run
+
+    res = run(CASES["microstrip"][0](namespace("gb300")), engine="gb300", end_db=None, max_steps=128)
+    assert res.report["gcell_updates_per_s"] > 0 and res.report["bytes_per_step"] > 0
