@@ -276,6 +276,49 @@ typedef struct oafdtd_energy_view {
  * differs (per-plane partial sums), so results agree to float64 rounding. */
 int oafdtd_energy_noalloc(const oafdtd_energy_view* view, double* out);
 
+/* ---------------------------------------------------------------------------------------------
+ * Learned S-parameter surrogate: the kernels its training and inference run on. The reference
+ * has no surrogate; these entry points extend the engine's sweep path (parameters -> S). All
+ * pointers are device pointers; BF16 buffers are passed as void*; stream may be NULL. Nothing here
+ * allocates. Returns 0, or -1 for bad arguments, -3 for a CUDA launch error.
+ * ------------------------------------------------------------------------------------------- */
+
+/* C = act(op(A) . op(B) + bias) on the tensor cores: BF16 operands, FP32 accumulation.
+ * op(A) is M x K: A row-major M x K (ta = 0) or row-major K x M (ta = 1), leading dimension lda;
+ * op(B) is K x N: B row-major K x N (tb = 0) or row-major N x K (tb = 1), leading dimension ldb.
+ * C32 (FP32, nullable) and C16 (BF16, nullable) are row-major M x N with leading dimension ldc;
+ * C32 = result + beta * C32. bias: N floats (nullable). act: 0 none, 1 ReLU, 2 keep only where
+ * mask (BF16, layout of C) is positive (the ReLU derivative in the backward pass), 3 tanh,
+ * 4 multiply by 1 - mask^2 (the tanh derivative, mask = the stored tanh outputs). */
+int oafdtd_mlp_gemm(const void* A, const void* B, float* C32, void* C16, const float* bias, const void* mask,
+                    int32_t M, int32_t N, int32_t K, int32_t lda, int32_t ldb, int32_t ldc, int32_t ta, int32_t tb,
+                    int32_t act, float beta, void* stream);
+
+/* out[n] = sum over m of X[m * ld + n] (FP32; bias gradients). */
+int oafdtd_mlp_colsum(const float* X, int32_t M, int32_t N, int32_t ld, float* out, void* stream);
+
+/* Mean squared error of Y against T (both M x N FP32): the gradient 2 (Y - T) / (M N) into G32
+ * (FP32) and G16 (BF16), and the sum of squared errors of each row into row_loss[M]. */
+int oafdtd_mlp_mse_grad(const float* Y, const float* T, int32_t M, int32_t N, float* G32, void* G16,
+                        float* row_loss, void* stream);
+
+/* One Adam step on n FP32 weights w (moments m1, m2), refreshing the BF16 copy w16 (nullable).
+ * The learning rate is read from *lr (device float) and the step number for the bias corrections
+ * from *step (device int32, >= 1), so a captured step replays with both moving on. */
+int oafdtd_mlp_adam(float* w, void* w16, const float* grad, float* m1, float* m2, int64_t n, const float* lr,
+                    float b1, float b2, float eps, const int32_t* step, void* stream);
+
+/* *counter += 1 on the device (the Adam step number inside a captured training step). */
+int oafdtd_mlp_count(int32_t* counter, void* stream);
+
+/* Rows idx[0..rows) (device int32) of an FP32 matrix with cols columns, into dst32 (FP32) and/or
+ * dst16 (BF16), each rows x cols. */
+int oafdtd_mlp_gather(const float* src, int32_t cols, const int32_t* idx, int32_t rows, float* dst32, void* dst16,
+                      void* stream);
+
+/* FP32 -> BF16 conversion of n values. */
+int oafdtd_mlp_to_bf16(const float* x, void* y, int64_t n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

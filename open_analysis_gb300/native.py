@@ -164,6 +164,20 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "oafdtd_graph_kernels": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "oafdtd_kernel_bytes": (C.c_int, [C.c_void_p, _pd, _i32]),
     "oafdtd_energy_noalloc": (C.c_int, [C.POINTER(EnergyView), _pd]),
+    # surrogate kernels (device pointers as void*)
+    "oafdtd_mlp_gemm": (
+        C.c_int,
+        [C.c_void_p] * 6 + [_i32] * 9 + [C.c_float, C.c_void_p],
+    ),
+    "oafdtd_mlp_colsum": (C.c_int, [C.c_void_p, _i32, _i32, _i32, C.c_void_p, C.c_void_p]),
+    "oafdtd_mlp_mse_grad": (C.c_int, [C.c_void_p, C.c_void_p, _i32, _i32] + [C.c_void_p] * 4),
+    "oafdtd_mlp_adam": (
+        C.c_int,
+        [C.c_void_p] * 5 + [_i64, C.c_void_p] + [C.c_float] * 3 + [C.c_void_p, C.c_void_p],
+    ),
+    "oafdtd_mlp_count": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "oafdtd_mlp_gather": (C.c_int, [C.c_void_p, _i32, C.c_void_p, _i32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "oafdtd_mlp_to_bf16": (C.c_int, [C.c_void_p, C.c_void_p, _i64, C.c_void_p]),
 }
 
 _lock = threading.Lock()
