@@ -23,6 +23,9 @@ advances between energy checks. Gcell-updates/s = interior cells x batch x time 
   (``structures.sweep_instances``), all instances batched on the GPU at once against looping the
   plain engine over them (``open_analysis_gb300.batch``); wall clock of the stepping and the
   S-parameter read-back, engines created beforehand; both give identical S-parameters.
+  ``sweeps.surrogate``: batched + learned surrogate against batched alone and against the plain
+  loop, on a three-parameter sweep of small via transitions (``surrogate.experiment``: data from
+  the batched engine, the ensemble trained on the GPU, held-out answers judged against FDTD).
 
 ``--impl reference`` times the reference's CPU path (the oracle port; the reference is a Python
 package and is not installed on the GPU host) on the same workload, one time step per bench step.
@@ -238,8 +241,28 @@ def sweep_measure(n: int, steps: int) -> dict[str, Any]:
         "batched_gcell_s": batched.cell_updates / batched.seconds / 1e9,
         "looped_gcell_s": looped.cell_updates / looped.seconds / 1e9,
         "identical_s": same,
-        "surrogate": None,
     }
+
+
+def surrogate_measure(n: int) -> dict[str, Any]:
+    """The learned surrogate on a sweep of small via transitions (48 x 48 x 60 cells; stack
+    height, eps_inf and delta_eps free, the rest fixed): generate ``n`` instances with the
+    batched engine, train the ensemble on the GPU (BF16 tensor-core kernels), answer the held-out
+    instances with FDTD fallback, judge every answer against FDTD, and compare the sweep rates."""
+    from open_analysis_gb300.surrogate import ViaGrid, experiment
+
+    g = ViaGrid(nx=48, ny=48, nz=60, h=50e-6, dz=100e-6, n_freq=32, cpml=6, span=560e-12)
+    fixed = {"drill": 0.3e-3, "pad": 0.5e-3, "antipad": 0.9e-3, "stub": 0.6e-3}
+    n_tr, n_vc = (n * 2) // 3, n // 12
+    rep = experiment(g, n, seed=21, fixed=fixed, split=(n_tr / n, n_vc / n, n_vc / n), batch=64, epochs=3000,
+                     lrs=(1e-3,), chunk=64)
+    keep = ("grid", "steps", "folds", "network", "activation", "members", "train_seconds", "tol_db", "accepted",
+            "accepted_worst_db", "answers_within_tol", "answers_worst_db", "network_alone_median_db",
+            "network_alone_within_tol", "plain_sweeps_per_s", "batched_sweeps_per_s", "surrogate_sweeps_per_s",
+            "gain_vs_plain", "gain_vs_batched")
+    out = {k: rep[k] for k in keep}
+    out["free_parameters"] = ["stack", "eps_inf", "delta_eps"]
+    return out
 
 
 def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
@@ -333,6 +356,8 @@ def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
     sweeps = None
     if args.sweep_instances > 0 and args.sweep_steps > 0:
         sweeps = sweep_measure(args.sweep_instances, args.sweep_steps)
+        if args.surrogate_instances:
+            sweeps["surrogate"] = surrogate_measure(args.surrogate_instances)
 
     if ranks.rank == 0:
         line = {
@@ -447,6 +472,7 @@ def main() -> None:
     ap.add_argument("--cells", default="", help="via-transition grid 'nx,ny,nz' (smaller profiling cases)")
     ap.add_argument("--sweep-instances", type=int, default=64, help="batched-sweep instances (0: skip)")
     ap.add_argument("--sweep-steps", type=int, default=2000, help="time steps per sweep instance")
+    ap.add_argument("--surrogate-instances", type=int, default=384, help="surrogate sweep instances (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
