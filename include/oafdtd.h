@@ -277,6 +277,53 @@ typedef struct oafdtd_energy_view {
 int oafdtd_energy_noalloc(const oafdtd_energy_view* view, double* out);
 
 /* ---------------------------------------------------------------------------------------------
+ * Native model compiler: the volume stages of compile_model (packages/oa-fdtd/src/oa_fdtd/
+ * model.py:501-768) on host threads, bit for bit equal to the NumPy stages it replaces:
+ * per-cell materials (model.py:272-296), the four-cell area-weighted edge average
+ * (_edge_average, model.py:300-321) with the static Debye term (model.py:534-537) and the
+ * lumped-port loading (model.py:610-647), the averaged-material table and uint16 index
+ * (model.py:688-722), and the Debye edge lists (_compile_ade, model.py:331-367). Host pointers;
+ * no GPU is needed. The caller builds the PEC masks (walls, PEC regions, conductors).
+ * ------------------------------------------------------------------------------------------- */
+typedef struct oafdtd_material_desc {
+  int32_t nx, ny, nz;
+  const double* cell_w[3];        /* storage cell weights, length n + 2 (zero on the ghosts) */
+  const double* centres[3];       /* cell centres, length n */
+  int32_t n_regions;              /* dielectric (non-PEC) regions, in the model's order */
+  const double* reg_lo;           /* (n_regions, 3) closed box, cells by centre */
+  const double* reg_hi;           /* (n_regions, 3) */
+  const double* reg_eps;          /* n_regions */
+  const double* reg_sig;          /* n_regions */
+  int32_t n_poles;                /* Debye relaxation times of the model (at most 8) */
+  const double* reg_strength;     /* (n_regions, n_poles) pole strengths of each region */
+  const double* static_fac;       /* n_poles: dt / (2 tau_p + dt) */
+  const uint8_t* pec[3];          /* per component, (nz+1, ny+1, nx+1), 1 = PEC edge */
+  int64_t n_loads;                /* lumped-port loading: sigma added to single edges, in order */
+  const int32_t* load_comp;
+  const int64_t* load_lattice;    /* (k * (ny+1) + j) * (nx+1) + i on the component's lattice */
+  const double* load_sig;
+  int32_t threads;                /* 0: one per hardware thread */
+} oafdtd_material_desc;
+
+typedef struct oafdtd_materials oafdtd_materials;
+
+/* Build; OAFDTD_E_TABLE when more than 65534 averaged materials. */
+int oafdtd_materials_build(const oafdtd_material_desc* desc, oafdtd_materials** out);
+
+/* Table entries including the PEC entry 0, and the dispersive edges per component. */
+int oafdtd_materials_sizes(const oafdtd_materials* m, int32_t* n_mat, int64_t* ade_n);
+
+/* Copy out: the three uint16 index arrays (nz+2, ny+2, pitch), the eps and sigma tables (n_mat),
+ * and per component the dispersive edges' storage flat indices (ade_n[c]) and their averaged
+ * pole strengths (n_poles, ade_n[c]); the lists of a component without dispersive edges may be
+ * NULL. */
+int oafdtd_materials_fetch(const oafdtd_materials* m, uint16_t* idx0, uint16_t* idx1, uint16_t* idx2, double* eps_tab,
+                           double* sig_tab, int64_t* flat0, int64_t* flat1, int64_t* flat2, double* del0, double* del1,
+                           double* del2);
+
+int oafdtd_materials_free(oafdtd_materials* m);
+
+/* ---------------------------------------------------------------------------------------------
  * Learned S-parameter surrogate: the kernels its training and inference run on. The reference
  * has no surrogate; these entry points extend the engine's sweep path (parameters -> S). All
  * pointers are device pointers; BF16 buffers are passed as void*; stream may be NULL. Nothing here

@@ -20,7 +20,10 @@ CSRC = PKG / "csrc"
 LIBDIR = PKG / "lib"
 LIBNAME = "liboafdtd.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
+# -fmad=false keeps the device arithmetic unfused; -ffp-contract=off does the same for host code
+# (GCC fuses multiply-add by default on Arm), which the native model compiler needs to equal NumPy
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+         "-Xcompiler", "-ffp-contract=off"]
 
 
 def nvcc() -> str:

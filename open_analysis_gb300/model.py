@@ -13,6 +13,12 @@ for bit (the fixtures under ``tests/golden`` pin this).
 
 Materials are never stored per cell on the device: every E edge carries a uint16 index into the
 table, and the kernels rebuild ``ca, cb`` from it.
+
+Two implementations of the volume stages (per-cell materials, edge averages, the table and
+index, the Debye edge lists) give the same arrays bit for bit: NumPy (``native=False``, the
+reference's stages restated) and the engine library's native compiler (``native=True``,
+``oafdtd_materials_build``: host threads, one uint16 region id per cell instead of float64
+volumes). ``compile_model`` uses the native one when the library is built.
 """
 
 from __future__ import annotations
@@ -524,34 +530,148 @@ def update_coefficients(eps_tab: FloatArray, sig_tab: FloatArray, dt: float) -> 
     return ca, cb
 
 
-def compile_model(model: Model, dtype: str = "float32") -> Compiled:
-    """Build the index arrays, tables, PML, channels and probes. Raises :class:`ModelError`."""
+def _native_library() -> Any:
+    """The engine library when it is built (it loads without a GPU), else None."""
+    try:
+        from open_analysis_gb300 import native as nat
+
+        return nat.load() if nat.library_path().exists() else None
+    except Exception:  # noqa: BLE001 - a missing or foreign library means the NumPy stages
+        return None
+
+
+def _native_materials(
+    model: Model,
+    g: Grid,
+    dt: float,
+    taus: FloatArray,
+    pec: list[npt.NDArray[np.bool_]],
+    loads: list[tuple[int, int, float]],
+    threads: int = 0,
+) -> tuple[list[npt.NDArray[np.uint16]], FloatArray, FloatArray, list[int], list[Any], list[FloatArray]]:
+    """The volume stages on the engine library's native compiler: index arrays, eps and sigma
+    tables, and per dispersive component its storage flat indices and averaged pole strengths."""
+    import ctypes as C
+
+    from open_analysis_gb300 import native as nat
+
+    lib = nat.load()
+    nx, ny, nz = g.n
+    regs = [r for r in model.regions if not r.pec]
+    n_poles = int(taus.size)
+    keep: list[Any] = []
+
+    def dp(a: Any) -> Any:
+        arr = np.ascontiguousarray(a, dtype=np.float64)
+        keep.append(arr)
+        return arr.ctypes.data_as(C.POINTER(C.c_double))
+
+    d = nat.MaterialDesc()
+    d.nx, d.ny, d.nz = nx, ny, nz
+    for a in range(3):
+        d.cell_w[a] = dp(g.cell_weights(a)[: g.n[a] + 2])
+        d.centres[a] = dp(g.centers(a))
+        m8 = np.ascontiguousarray(pec[a]).view(np.uint8)
+        keep.append(m8)
+        d.pec[a] = m8.ctypes.data_as(C.POINTER(C.c_uint8))
+    d.n_regions = len(regs)
+    d.reg_lo = dp([r.lo for r in regs] or [[0.0, 0.0, 0.0]])
+    d.reg_hi = dp([r.hi for r in regs] or [[0.0, 0.0, 0.0]])
+    d.reg_eps = dp([r.eps_r for r in regs] or [0.0])
+    d.reg_sig = dp([r.sigma for r in regs] or [0.0])
+    strength = np.zeros((max(1, len(regs)), max(1, n_poles)))
+    for ri, r in enumerate(regs):
+        by_tau = {round(t, 18): dv for dv, t in r.poles}
+        for pi, tau in enumerate(taus):
+            strength[ri, pi] = by_tau.get(round(float(tau), 18), 0.0)
+    d.n_poles = n_poles
+    d.reg_strength = dp(strength[:, :n_poles] if n_poles else strength)
+    d.static_fac = dp([dt / (2.0 * float(t) + dt) for t in taus] or [0.0])
+    comp = np.array([ld[0] for ld in loads] or [0], dtype=np.int32)
+    lat = np.array([ld[1] for ld in loads] or [0], dtype=np.int64)
+    sig = np.array([ld[2] for ld in loads] or [0.0], dtype=np.float64)
+    keep += [comp, lat, sig]
+    d.n_loads = len(loads)
+    d.load_comp = comp.ctypes.data_as(C.POINTER(C.c_int32))
+    d.load_lattice = lat.ctypes.data_as(C.POINTER(C.c_int64))
+    d.load_sig = sig.ctypes.data_as(C.POINTER(C.c_double))
+    d.threads = int(threads)
+    handle = C.c_void_p()
+    rc = lib.oafdtd_materials_build(C.byref(d), C.byref(handle))
+    if rc == nat.E_TABLE:
+        raise ModelError(
+            "FDTD_TOO_MANY_MATERIALS",
+            lib.oafdtd_last_error().decode(errors="replace"),
+            "Use fewer distinct materials or a more uniform grid.",
+        )
+    nat.check(rc, "oafdtd_materials_build")
+    try:
+        n_mat = C.c_int32()
+        ade_n = (C.c_int64 * 3)()
+        nat.check(lib.oafdtd_materials_sizes(handle, C.byref(n_mat), ade_n), "oafdtd_materials_sizes")
+        idx = [np.zeros(g.shape, dtype=np.uint16) for _ in range(3)]
+        eps_tab = np.zeros(n_mat.value)
+        sig_tab = np.zeros(n_mat.value)
+        flats = [np.zeros(int(ade_n[c]), dtype=np.int64) for c in range(3)]
+        dels = [np.zeros((n_poles, int(ade_n[c]))) for c in range(3)]
+        u16 = C.POINTER(C.c_uint16)
+        nat.check(
+            lib.oafdtd_materials_fetch(
+                handle,
+                *(a.ctypes.data_as(u16) for a in idx),
+                eps_tab.ctypes.data_as(C.POINTER(C.c_double)),
+                sig_tab.ctypes.data_as(C.POINTER(C.c_double)),
+                *(f.ctypes.data_as(C.POINTER(C.c_int64)) if f.size else None for f in flats),
+                *(x.ctypes.data_as(C.POINTER(C.c_double)) if x.size else None for x in dels),
+            ),
+            "oafdtd_materials_fetch",
+        )
+    finally:
+        lib.oafdtd_materials_free(handle)
+    comps = [c for c in range(3) if flats[c].size]
+    return idx, eps_tab, sig_tab, comps, [flats[c] for c in comps], [dels[c] for c in comps]
+
+
+def compile_model(model: Model, dtype: str = "float32", native: bool | None = None) -> Compiled:
+    """Build the index arrays, tables, PML, channels and probes. Raises :class:`ModelError`.
+
+    ``native``: run the volume stages on the engine library's native compiler (``True``), on
+    NumPy (``False``), or on the native compiler when the library is built (``None``); the
+    arrays are the same bit for bit."""
     del dtype  # the compiled arrays are float64 and uint16 whatever the engine precision
     g = model.grid
     nx, ny, nz = g.n
     if len(model.walls) != 6 or any(w not in WALL_KINDS for w in model.walls):
         raise ModelError("FDTD_BAD_WALLS", f"walls must be six of {WALL_KINDS}")
+    n_dielectric = sum(1 for r in model.regions if not r.pec)
+    if native is None:
+        # the native compiler numbers cells by region in uint16
+        native = _native_library() is not None and n_dielectric <= 65534
+    elif native and n_dielectric > 65534:
+        raise ModelError("FDTD_BAD_INPUT", "the native compiler takes at most 65534 dielectric regions")
     eps_min = min([1.0] + [r.eps_r for r in model.regions if not r.pec])
     dt = g.dt(model.courant, 299792458.0 / math.sqrt(eps_min))
     vacuum_only = not model.regions and not model.ports and not model.conductors
     taus = _pole_taus(model)
-    eps_c, sig_c, del_c = _cell_materials(model, taus)
 
     lattice = (nz + 1, ny + 1, nx + 1)
     edge_eps: list[FloatArray] = []
     edge_sig: list[FloatArray] = []
     edge_del: list[list[FloatArray]] = []
     pec: list[npt.NDArray[np.bool_]] = []
+    if not native:
+        eps_c, sig_c, del_c = _cell_materials(model, taus)
     for c in range(3):
-        if vacuum_only:
-            edge_eps.append(np.ones(lattice))
-            edge_sig.append(np.zeros(lattice))
-            edge_del.append([])
-        else:
-            e, s, *ds = _edge_average(g, c, [eps_c, sig_c, *del_c])
-            edge_eps.append(e)
-            edge_sig.append(s)
-            edge_del.append(ds)
+        if not native:
+            if vacuum_only:
+                edge_eps.append(np.ones(lattice))
+                edge_sig.append(np.zeros(lattice))
+                edge_del.append([])
+            else:
+                e, s, *ds = _edge_average(g, c, [eps_c, sig_c, *del_c])
+                edge_eps.append(e)
+                edge_sig.append(s)
+                edge_del.append(ds)
         real_edges = np.zeros(lattice, dtype=bool)
         (x0, x1), (y0, y1), (z0, z1) = g.valid("E", c)
         real_edges[z0 - 1 : z1 - 1, y0 - 1 : y1 - 1, x0 - 1 : x1 - 1] = True
@@ -562,11 +682,12 @@ def compile_model(model: Model, dtype: str = "float32") -> Compiled:
             "mode ports are not built by this compiler yet",
             "Use LumpedPort ports.",
         )
-    del eps_c, sig_c, del_c
-    # the static part of the Debye polarisation current joins eps: eps_inf + sum d_p dt/(2 tau+dt)
-    for c in range(3):
-        for pi, tau in enumerate(taus):
-            edge_eps[c] += edge_del[c][pi] * (dt / (2.0 * float(tau) + dt))
+    if not native:
+        del eps_c, sig_c, del_c
+        # the static part of the Debye polarisation current joins eps: eps_inf + sum d_p dt/(2 tau+dt)
+        for c in range(3):
+            for pi, tau in enumerate(taus):
+                edge_eps[c] += edge_del[c][pi] * (dt / (2.0 * float(tau) + dt))
     # tangential E on PEC and CPML outer walls
     for a in range(3):
         for side in (0, 1):
@@ -588,6 +709,7 @@ def compile_model(model: Model, dtype: str = "float32") -> Compiled:
     channels: list[dict[str, Any]] = []
     ports_info: list[dict[str, Any]] = []
     probes: list[dict[str, Any]] = []
+    loads: list[tuple[int, int, float]] = []
     sz, sy = g.shape[1] * g.shape[2], g.shape[2]
     for port in model.ports:
         assert isinstance(port, LumpedPort)
@@ -605,7 +727,11 @@ def compile_model(model: Model, dtype: str = "float32") -> Compiled:
         total_len = float(length.sum()) / (flat.size / n_series)
         total_area = float(area.sum()) / n_series
         sig_eq = total_len / (port.r_ohm * total_area)
-        edge_sig[a][k - 1, j - 1, i - 1] += sig_eq
+        if native:
+            lat = ((k - 1) * (ny + 1) + (j - 1)) * (nx + 1) + (i - 1)
+            loads += [(a, int(q), sig_eq) for q in lat]
+        else:
+            edge_sig[a][k - 1, j - 1, i - 1] += sig_eq
         ports_info.append(
             {
                 "name": port.name,
@@ -650,9 +776,24 @@ def compile_model(model: Model, dtype: str = "float32") -> Compiled:
             raise ModelError("FDTD_BAD_PROBE", f"probe {pr.name}: weight {pr.weight!r}")
         probes.append({"name": pr.name, "kind": pr.kind, "comp": pr.axis, "flat": flat, "weights": w})
 
-    idx, eps_tab, sig_tab = _material_table(g, edge_eps, edge_sig, pec)
-    ca_tab, cb_tab = update_coefficients(eps_tab, sig_tab, dt)
-    ade = _compile_ade(g, dt, taus, edge_del, pec, idx, cb_tab)
+    if native:
+        idx, eps_tab, sig_tab, comps, flats, dels = _native_materials(model, g, dt, taus, pec, loads)
+        ca_tab, cb_tab = update_coefficients(eps_tab, sig_tab, dt)
+        ade = None
+        if taus.size and comps:
+            tau = np.asarray(taus, dtype=np.float64)
+            ade = AdeData(
+                kp=(1.0 - 0.5 * dt / tau) / (1.0 + 0.5 * dt / tau),
+                tau=tau,
+                comp=comps,
+                flat=flats,
+                beta=[np.stack([EPS0 * dl[p] / (tau[p] + 0.5 * dt) for p in range(tau.size)]) for dl in dels],
+                cbe=[cb_tab[idx[c].ravel()[f]] for c, f in zip(comps, flats, strict=True)],
+            )
+    else:
+        idx, eps_tab, sig_tab = _material_table(g, edge_eps, edge_sig, pec)
+        ca_tab, cb_tab = update_coefficients(eps_tab, sig_tab, dt)
+        ade = _compile_ade(g, dt, taus, edge_del, pec, idx, cb_tab)
 
     for ch in channels:
         mat = idx[ch["comp"]].ravel()[ch["flat"]]

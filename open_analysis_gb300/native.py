@@ -130,6 +130,32 @@ class EnergyView(C.Structure):
     ]
 
 
+class MaterialDesc(C.Structure):
+    """``oafdtd_material_desc``: the native model compiler's input (host pointers)."""
+
+    _fields_ = [
+        ("nx", _i32),
+        ("ny", _i32),
+        ("nz", _i32),
+        ("cell_w", _pd * 3),
+        ("centres", _pd * 3),
+        ("n_regions", _i32),
+        ("reg_lo", _pd),
+        ("reg_hi", _pd),
+        ("reg_eps", _pd),
+        ("reg_sig", _pd),
+        ("n_poles", _i32),
+        ("reg_strength", _pd),
+        ("static_fac", _pd),
+        ("pec", C.POINTER(C.c_uint8) * 3),
+        ("n_loads", _i64),
+        ("load_comp", _pi32),
+        ("load_lattice", _pi64),
+        ("load_sig", _pd),
+        ("threads", _i32),
+    ]
+
+
 # every exported symbol with its argument types; tests check the library exports exactly these
 SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "oafdtd_abi_version": (_i32, []),
@@ -164,6 +190,11 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "oafdtd_graph_kernels": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "oafdtd_kernel_bytes": (C.c_int, [C.c_void_p, _pd, _i32]),
     "oafdtd_energy_noalloc": (C.c_int, [C.POINTER(EnergyView), _pd]),
+    # native model compiler (host pointers)
+    "oafdtd_materials_build": (C.c_int, [C.POINTER(MaterialDesc), C.POINTER(C.c_void_p)]),
+    "oafdtd_materials_sizes": (C.c_int, [C.c_void_p, _pi32, _pi64]),
+    "oafdtd_materials_fetch": (C.c_int, [C.c_void_p] + [C.POINTER(C.c_uint16)] * 3 + [_pd, _pd] + [_pi64] * 3 + [_pd] * 3),
+    "oafdtd_materials_free": (C.c_int, [C.c_void_p]),
     # surrogate kernels (device pointers as void*)
     "oafdtd_mlp_gemm": (
         C.c_int,
