@@ -117,7 +117,14 @@ class LumpedPort:
 
 @dataclass(frozen=True)
 class ModePort:
-    """Quasi-TEM mode port on a plane (interface type; the compiler does not build it yet)."""
+    """Quasi-TEM mode port on a plane (``open_analysis_gb300.modes``).
+
+    The plane ``axis = position`` is cut by the in-plane rectangle ``lo .. hi`` (the two other
+    axes in ascending order). The mode comes from a 2-D electrostatic solve with ``signals`` as the
+    signal conductors (rectangles in the same axes); every other conductor, PEC region and PEC
+    wall is ground. Ports with the same rectangle and signals but different ``mode`` give the modes
+    of coupled conductors. The reference impedance is the modal one. ``direction`` +1: the
+    structure lies towards +axis from the plane."""
 
     name: str
     axis: int
@@ -644,11 +651,13 @@ def compile_model(model: Model, dtype: str = "float32", native: bool | None = No
     if len(model.walls) != 6 or any(w not in WALL_KINDS for w in model.walls):
         raise ModelError("FDTD_BAD_WALLS", f"walls must be six of {WALL_KINDS}")
     n_dielectric = sum(1 for r in model.regions if not r.pec)
+    has_modes = any(isinstance(p, ModePort) for p in model.ports) or bool(model.mode_probes)
     if native is None:
-        # the native compiler numbers cells by region in uint16
-        native = _native_library() is not None and n_dielectric <= 65534
-    elif native and n_dielectric > 65534:
-        raise ModelError("FDTD_BAD_INPUT", "the native compiler takes at most 65534 dielectric regions")
+        # the native compiler numbers cells by region in uint16; mode ports read the per-edge
+        # permittivity arrays of the NumPy stages
+        native = _native_library() is not None and n_dielectric <= 65534 and not has_modes
+    elif native and (n_dielectric > 65534 or has_modes):
+        raise ModelError("FDTD_BAD_INPUT", "the native compiler takes at most 65534 dielectric regions and no mode ports")
     eps_min = min([1.0] + [r.eps_r for r in model.regions if not r.pec])
     dt = g.dt(model.courant, 299792458.0 / math.sqrt(eps_min))
     vacuum_only = not model.regions and not model.ports and not model.conductors
@@ -676,12 +685,14 @@ def compile_model(model: Model, dtype: str = "float32", native: bool | None = No
         (x0, x1), (y0, y1), (z0, z1) = g.valid("E", c)
         real_edges[z0 - 1 : z1 - 1, y0 - 1 : y1 - 1, x0 - 1 : x1 - 1] = True
         pec.append(~real_edges)
-    if any(isinstance(p, ModePort) for p in model.ports) or model.mode_probes:
-        raise ModelError(
-            "FDTD_UNSUPPORTED",
-            "mode ports are not built by this compiler yet",
-            "Use LumpedPort ports.",
-        )
+    eps_mid: FloatArray | None = None
+    if has_modes:
+        # real relative permittivity of the cells at the band centre, for the plane solves
+        w_mid = 2.0 * np.pi * 0.5 * sum(model.band)
+        eps_mid = eps_c.copy()
+        for pi, tau in enumerate(taus):
+            eps_mid = eps_mid + del_c[pi] / (1.0 + (w_mid * float(tau)) ** 2)
+        eps_mid = eps_mid[1:-1, 1:-1, 1:-1]
     if not native:
         del eps_c, sig_c, del_c
         # the static part of the Debye polarisation current joins eps: eps_inf + sum d_p dt/(2 tau+dt)
@@ -711,7 +722,57 @@ def compile_model(model: Model, dtype: str = "float32", native: bool | None = No
     probes: list[dict[str, Any]] = []
     loads: list[tuple[int, int, float]] = []
     sz, sy = g.shape[1] * g.shape[2], g.shape[2]
+    mode_cache: dict[Any, Any] = {}
+
+    def mode_port(mp_: ModePort) -> dict[str, Any]:
+        from open_analysis_gb300.modes import build_mode_port, solve_port_modes
+
+        key = (mp_.axis, mp_.position, mp_.lo, mp_.hi, mp_.signals, mp_.direction)
+        try:
+            if key not in mode_cache:
+                assert eps_mid is not None
+                mode_cache[key] = solve_port_modes(model, g, mp_, eps_mid)
+            modes, geo = mode_cache[key]
+            return build_mode_port(g, mp_, modes, geo, edge_eps)
+        except ValueError as exc:
+            raise ModelError("FDTD_BAD_PORT", str(exc)) from exc
+
+    def mode_parts(mp_: ModePort, arr: dict[str, Any], load: bool) -> list[str]:
+        """One probe per field component of the plane (and the sheet's loading when ``load``)."""
+        parts: list[str] = []
+        start = 0
+        for comp_seg, count in zip(sorted({int(v) for v in arr["comp"]}), arr["split"], strict=True):
+            seg = slice(start, start + count)
+            start += count
+            fl = arr["flat"][seg]
+            if load:
+                kk, jj, ii = np.unravel_index(fl, g.shape)
+                edge_sig[comp_seg][kk - 1, jj - 1, ii - 1] += arr["sigma"][seg]
+            parts.append(f"V:{mp_.name}:{comp_seg}")
+            probes.append({"name": parts[-1], "kind": "E", "comp": comp_seg, "flat": fl, "weights": arr["weights"][seg]})
+        return parts
+
     for port in model.ports:
+        if isinstance(port, ModePort):
+            arr = mode_port(port)
+            parts = mode_parts(port, arr, load=True)
+            ports_info.append(
+                {
+                    "name": port.name,
+                    "axis": port.axis,
+                    "r_ohm": arr["z"],
+                    "sign": port.sign,
+                    "flat": arr["flat"],
+                    "channel": len(channels),
+                    "sig_e": arr["sigma"],
+                    "e_t": arr["template"],
+                    "probe_parts": parts,
+                    "eps_eff": arr["eps_eff"],
+                    "voltages": arr["voltages"],
+                }
+            )
+            channels.append({"comp": arr["comp"], "flat": arr["flat"], "port": len(ports_info) - 1, "sign": port.sign})
+            continue
         assert isinstance(port, LumpedPort)
         if port.r_ohm <= 0:
             raise ModelError("FDTD_BAD_PORT", f"port {port.name}: r_ohm must be positive")
@@ -755,6 +816,9 @@ def compile_model(model: Model, dtype: str = "float32", native: bool | None = No
                 "weights": length * area / total_area,
             }
         )
+    probe_sums: dict[str, list[str]] = {}
+    for mpb in model.mode_probes:
+        probe_sums[f"V:{mpb.name}"] = mode_parts(mpb, mode_port(mpb), load=False)
     for src in model.sources:
         flat, _ = g.points("E", src.axis, src.lo, src.hi)
         channels.append({"comp": src.axis, "flat": flat, "amp": src.amplitude})
@@ -796,10 +860,19 @@ def compile_model(model: Model, dtype: str = "float32", native: bool | None = No
         ade = _compile_ade(g, dt, taus, edge_del, pec, idx, cb_tab)
 
     for ch in channels:
-        mat = idx[ch["comp"]].ravel()[ch["flat"]]
+        if np.ndim(ch["comp"]) == 0:
+            mat = idx[ch["comp"]].ravel()[ch["flat"]]
+        else:
+            mat = np.zeros(ch["flat"].size, dtype=np.uint16)
+            for cc in np.unique(ch["comp"]):
+                on = ch["comp"] == cc
+                mat[on] = idx[int(cc)].ravel()[ch["flat"][on]]
         if "port" in ch:
             info = ports_info[ch["port"]]
-            ch["amps"] = ch["sign"] * cb_tab[mat] * info["sig_eq"] / info["total_len"]
+            if "sig_e" in info:  # mode port: the sheet's own loading times its template
+                ch["amps"] = ch["sign"] * cb_tab[mat] * info["sig_e"] * info["e_t"]
+            else:
+                ch["amps"] = ch["sign"] * cb_tab[mat] * info["sig_eq"] / info["total_len"]
         else:
             ch["amps"] = ch["amp"] * np.ones(ch["flat"].size)
         ch["waveform"] = model.waveform
@@ -821,5 +894,5 @@ def compile_model(model: Model, dtype: str = "float32", native: bool | None = No
         frequencies=np.asarray(model.frequencies, dtype=np.float64),
         ade=ade,
         sibc=sibc,
-        probe_sums={},
+        probe_sums=probe_sums,
     )

@@ -104,10 +104,38 @@ def microstrip(ns: Any, nx: int = 40, ny: int = 24, nz: int = 16, cpml: int = 6)
     return m
 
 
+def mode_stripline(ns: Any) -> Any:
+    """60x22x14 stripline: single-pole Debye fill between PEC z walls, PEC y walls (graded y),
+    CPML on x, a zero-thickness PEC strip, quasi-TEM mode ports at both strip ends (both driven,
+    batch of two) and three wave planes behind each port (mode probes)."""
+    h = 0.1e-3
+    nx, ny, nz = 60, 22, 14
+    g = ns.Grid(np.arange(nx + 1) * h, graded(ny * 0.1e-3, ny, 1.02), np.arange(nz + 1) * h)
+    m = ns.Model(
+        g,
+        ns.Waveform("gauss_mod", 10e9, 18e9),
+        np.linspace(1e9, 19e9, 7),
+        walls=("cpml", "cpml", "pec", "pec", "pec", "pec"),
+    )
+    m.cpml = ns.CpmlSpec(cells=4)
+    m.regions.append(ns.Region((-1.0, -1.0, -1.0), (1.0, 1.0, 1.0), eps_r=3.4, poles=((0.3, 8e-12),)))
+    ys = g.lines[1]
+    y0, y1, zc = float(ys[8]), float(ys[14]), 7 * h
+    x0, x1 = 6 * h, (nx - 6) * h
+    m.regions.append(ns.Region((x0, y0, zc), (x1, y1, zc), pec=True))
+    rect = ((float(ys[0]), 0.0), (float(ys[-1]), nz * h))
+    sig = (((y0, zc), (y1, zc)),)
+    m.ports.append(ns.ModePort("p1", 0, x0, rect[0], rect[1], sig, direction=1))
+    m.ports.append(ns.ModePort("p2", 0, x1, rect[0], rect[1], sig, direction=-1))
+    m.plane_sets = [ns.add_wave_planes(m, "p1", 3 * h), ns.add_wave_planes(m, "p2", 3 * h)]
+    return m
+
+
 CASES = {
     "mixed_walls": (mixed_walls, 40),
     "dispersive_copper": (dispersive_copper, 40),
     "microstrip": (microstrip, 60),
+    "mode_stripline": (mode_stripline, 60),
 }
 
 
@@ -115,7 +143,7 @@ def namespace(module_root: str) -> Any:
     """Problem types of ``open_analysis_gb300`` (``module_root="gb300"``) or of the reference
     package (``module_root="ref"``, importable only where the reference is present)."""
     if module_root == "gb300":
-        from open_analysis_gb300 import grid, model, pml
+        from open_analysis_gb300 import deembed, grid, model, pml
 
         return SimpleNamespace(
             Grid=grid.Grid,
@@ -123,14 +151,17 @@ def namespace(module_root: str) -> Any:
             Region=model.Region,
             Conductor=model.Conductor,
             LumpedPort=model.LumpedPort,
+            ModePort=model.ModePort,
             SoftSource=model.SoftSource,
             Probe=model.Probe,
             Waveform=model.Waveform,
             CpmlSpec=pml.CpmlSpec,
+            add_wave_planes=deembed.add_wave_planes,
         )
     from oa_fdtd import grid as rgrid  # type: ignore[import-not-found]
     from oa_fdtd import model as rmodel  # type: ignore[import-not-found]
     from oa_fdtd import pml as rpml  # type: ignore[import-not-found]
+    from oa_fdtd.ports import deembed as rdeembed  # type: ignore[import-not-found]
 
     return SimpleNamespace(
         Grid=rgrid.Grid,
@@ -138,8 +169,10 @@ def namespace(module_root: str) -> Any:
         Region=rmodel.Region,
         Conductor=rmodel.Conductor,
         LumpedPort=rmodel.LumpedPort,
+        ModePort=rmodel.ModePort,
         SoftSource=rmodel.SoftSource,
         Probe=rmodel.Probe,
         Waveform=rmodel.Waveform,
         CpmlSpec=rpml.CpmlSpec,
+        add_wave_planes=rdeembed.add_wave_planes,
     )

@@ -60,6 +60,15 @@ def compiled_fingerprint(c: Any) -> dict[str, Any]:
             _put(out, f"ade{n}.flat", np.asarray(fl, dtype=np.int64))
             _put(out, f"ade{n}.beta", be)
             _put(out, f"ade{n}.cbe", cbe)
+    for i, q in enumerate(c.ports):
+        if "sig_e" in q:  # mode port: impedance, loading and template
+            out[f"port{i}.z"] = np.float64(q["r_ohm"])
+            out[f"port{i}.eps_eff"] = np.float64(q["eps_eff"])
+            _put(out, f"port{i}.sig_e", np.asarray(q["sig_e"], dtype=np.float64))
+            _put(out, f"port{i}.e_t", np.asarray(q["e_t"], dtype=np.float64))
+            out[f"port{i}.parts"] = list(q["probe_parts"])
+    for name, parts in sorted(getattr(c, "probe_sums", {}).items()):
+        out[f"sum.{name}"] = list(parts)
     if c.sibc is not None:
         s = c.sibc
         for name in ("comp", "flat", "hcomp", "hflat", "hsign", "mat", "r0", "rp", "cp", "gp"):

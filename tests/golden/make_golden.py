@@ -43,6 +43,8 @@ def main(reference_root: str) -> None:
             eng.step(steps)
             for k, v in state_fingerprint(eng).items():
                 data[f"{dtype}.{k}"] = v
+        if hasattr(model, "plane_sets"):
+            wave_fixture(np, model, c, NumpyEngine, steps, data)
         if name == "mixed_walls":
             eng = NumpyEngine(c, "float32")
             eng.step(steps)
@@ -52,6 +54,29 @@ def main(reference_root: str) -> None:
         print(name, "steps", steps, "batch", c.batch, "keys", len(data))
     debye_fits(np)
     touchstone_files(np)
+
+
+def wave_fixture(np, model, c, engine_cls, steps, data):  # type: ignore[no-untyped-def]
+    """Mode-port case: the reference's port S-parameters and wave-plane S-parameters (with its
+    propagation constants) from its float64 run, the probe parts summed as its run loop does."""
+    from oa_fdtd.ports.deembed import wave_sparams  # type: ignore[import-not-found]
+    from oa_fdtd.run import port_voltage_factor  # type: ignore[import-not-found]
+
+    eng = engine_cls(c, "float64")
+    eng.step(steps)
+    probes = eng.results()
+    sums = {f"V:{q['name']}": q["probe_parts"] for q in c.ports if q.get("probe_parts")}
+    sums.update(c.probe_sums)
+    for nm, parts in sums.items():
+        probes[nm] = sum(probes.pop(q) for q in parts)
+    fac = port_voltage_factor(c.dt, model.frequencies)
+    probes = {k: v * fac for k, v in probes.items()}
+    port_r = np.array([float(q["r_ohm"]) for q in c.ports])
+    s_wave, gammas = wave_sparams(probes, model.plane_sets, port_r)
+    data["wave.s"] = s_wave
+    data["wave.gamma"] = np.stack(gammas)
+    for ps_i, ps in enumerate(model.plane_sets):
+        data[f"wave.planes{ps_i}"] = np.array([ps.spacing, ps.ref, ps.spacing_b if ps.spacing_b is not None else np.nan])
 
 
 # Djordjevic-Sarkar materials fitted by the reference's multi-pole Debye fit:

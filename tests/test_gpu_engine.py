@@ -125,7 +125,7 @@ def test_fields_match_oracle(case: str, dtype: str) -> None:
     check_against_oracles(c, gpu, steps, dtype)
 
 
-@pytest.mark.parametrize("case", ["mixed_walls", "microstrip"])
+@pytest.mark.parametrize("case", ["mixed_walls", "microstrip", "mode_stripline"])
 def test_fields_match_reference_fixture(case: str) -> None:
     """The float32 fields' digests equal those of the reference's own NumPy engine."""
     ref = load(str(GOLDEN / f"{case}.npz"))
