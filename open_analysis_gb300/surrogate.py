@@ -636,7 +636,7 @@ class Ensemble:
     (:func:`line_factor`), each column less its mean, all columns over one common scale (so that
     the loss weighs absolute errors in S alike)."""
 
-    def __init__(self, g: ViaGrid, members: int = 4, width: int = 512, depth: int = 6, batch: int = 256, seed: int = 0,
+    def __init__(self, g: ViaGrid, members: int = 8, width: int = 512, depth: int = 6, batch: int = 256, seed: int = 0,
                  act: str = "tanh", bag: float = 1.0) -> None:
         self.g = g
         self.bag = bag
@@ -761,7 +761,7 @@ def experiment(
     seed: int = 4096,
     fixed: dict[str, float] | None = None,
     split: tuple[float, float, float] = (0.8, 0.05, 0.05),
-    members: int = 4,
+    members: int = 8,
     width: int = 512,
     depth: int = 6,
     batch: int = 256,
@@ -883,7 +883,7 @@ def main(argv: Sequence[str] | None = None) -> int:
     ap.add_argument("--grid", choices=["full", "half"], default="half")
     ap.add_argument("--seed", type=int, default=4096)
     ap.add_argument("--epochs", type=int, default=3000)
-    ap.add_argument("--members", type=int, default=4)
+    ap.add_argument("--members", type=int, default=8)
     ap.add_argument("--bag", type=float, default=1.0)
     ap.add_argument("--quantile", type=float, default=1.0)
     ap.add_argument("--data", default="", help="reuse a dataset written by --save")
