@@ -259,6 +259,7 @@ def surrogate_measure(n: int) -> dict[str, Any]:
     keep = ("grid", "steps", "folds", "network", "activation", "members", "train_seconds", "tol_db", "accepted",
             "accepted_worst_db", "answers_within_tol", "answers_worst_db", "network_alone_median_db",
             "network_alone_within_tol", "plain_sweeps_per_s", "batched_sweeps_per_s", "surrogate_sweeps_per_s",
+            "network_sweeps_per_s",
             "gain_vs_plain", "gain_vs_batched")
     out = {k: rep[k] for k in keep}
     out["free_parameters"] = ["stack", "eps_inf", "delta_eps"]

@@ -829,6 +829,12 @@ def experiment(
     if not test.same_as(plain.s, slice(0, k)):
         raise RuntimeError("the plain engine and the batched engine disagree")
     plain_rate = k / (plain.seconds + plain.create_seconds)
+    # the network's own rate: every member on a large batch of new parameter points
+    probe = via_params(8192, seed + 1)
+    ens.raw(probe[:256])  # first call pays for allocations
+    t_net = time.perf_counter()
+    ens.raw(probe)
+    net_rate = probe.shape[0] / (time.perf_counter() - t_net)
     batched_rate = n / (data.seconds + data.create_seconds) if data.seconds else float("nan")
     sur_rate = len(test.s) / ans.seconds
     acc = ~ans.fdtd
@@ -866,6 +872,7 @@ def experiment(
         "plain_sweeps_per_s": plain_rate,
         "batched_sweeps_per_s": batched_rate,
         "surrogate_sweeps_per_s": sur_rate,
+        "network_sweeps_per_s": net_rate,
         "surrogate_seconds": {"predict": ans.predict_seconds, "fdtd": ans.fdtd_seconds, "create": ans.fdtd_create_seconds},
         "gain_vs_plain": sur_rate / plain_rate,
         "gain_vs_batched": sur_rate / batched_rate if batched_rate == batched_rate else None,
