@@ -879,9 +879,47 @@ def experiment(
     }
 
 
+GEMM_SHAPES = ((256, 512, 512), (4096, 512, 512), (65536, 512, 512), (65536, 1024, 512), (16384, 4096, 4096))
+
+
+def gemm_rates(shapes: Sequence[tuple[int, int, int]] = GEMM_SHAPES, reps: int = 20) -> list[dict[str, float]]:
+    """Time ``oafdtd_mlp_gemm`` (BF16 A (M x K) . B (K x N) + bias, tanh, BF16 out) with CUDA
+    events over ``reps`` launches after three warm-up launches, and check it against the FP32
+    product. Returns per shape the microseconds per launch, TFLOP/s and the largest error."""
+    torch = _torch()
+    lib = native.load()
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(0)
+    out = []
+    for m, n, k in shapes:
+        a = torch.randn(m, k, device="cuda", generator=gen).to(torch.bfloat16)
+        b = torch.randn(k, n, device="cuda", generator=gen).to(torch.bfloat16)
+        c = torch.empty(m, n, device="cuda", dtype=torch.bfloat16)
+        bias = torch.zeros(n, device="cuda")
+        s = int(torch.cuda.current_stream().cuda_stream)
+
+        def launch() -> None:
+            native.check(lib.oafdtd_mlp_gemm(a.data_ptr(), b.data_ptr(), None, c.data_ptr(), bias.data_ptr(), None,
+                                             m, n, k, k, n, n, 0, 0, 3, 0.0, s), "oafdtd_mlp_gemm")
+
+        for _ in range(3):
+            launch()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(reps):
+            launch()
+        t1.record()
+        torch.cuda.synchronize()
+        us = 1e3 * t0.elapsed_time(t1) / reps
+        err = float((c.float() - torch.tanh(a.float() @ b.float())).abs().max().item())
+        out.append({"m": m, "n": n, "k": k, "us": us, "tflops": 2.0 * m * n * k / us / 1e6, "max_err": err})
+    return out
+
+
 def main(argv: Sequence[str] | None = None) -> int:
     """``python -m open_analysis_gb300.surrogate [--n N] [--grid full|half] [--out report.json]
-    [--data dataset.npz] [--save dataset.npz]``: the surrogate experiment on via transitions."""
+    [--data dataset.npz] [--save dataset.npz]``: the surrogate experiment on via transitions;
+    ``--gemm-rates``: the GEMM's throughput by shape."""
     import argparse
     import json
 
@@ -896,7 +934,12 @@ def main(argv: Sequence[str] | None = None) -> int:
     ap.add_argument("--data", default="", help="reuse a dataset written by --save")
     ap.add_argument("--save", default="", help="write the generated dataset (npz)")
     ap.add_argument("--out", default="")
+    ap.add_argument("--gemm-rates", action="store_true", help="time the training GEMM by shape and exit")
     a = ap.parse_args(argv)
+    if a.gemm_rates:
+        for r in gemm_rates():
+            print(json.dumps(r))
+        return 0
     g = ViaGrid(span=560e-12) if a.grid == "full" else HALF
     data = Dataset.load(a.data) if a.data else None
     if data is None and a.save:
