@@ -222,13 +222,16 @@ def cpu_sample(c: Any, target_s: float) -> dict[str, Any]:
 def sweep_measure(n: int, steps: int) -> dict[str, Any]:
     """Batched against looped S-parameter sweeps over ``n`` seeded instances (2 ports, 128
     frequencies each), ``steps`` time steps each."""
-    from open_analysis_gb300.batch import compile_all, run_batched, run_looped
+    from open_analysis_gb300.batch import compile_all, run_batched, run_looped, tune_shape
     from open_analysis_gb300.structures import sweep_instances
 
     models = sweep_instances(n)
     compiled = compile_all(models)
-    batched = run_batched(models, compiled, steps)
-    looped = run_looped(models, compiled, steps)
+    t0 = time.perf_counter()
+    shape = tune_shape(compiled)
+    tune_s = time.perf_counter() - t0
+    batched = run_batched(models, compiled, steps, shape=shape)
+    looped = run_looped(models, compiled, steps, shape=shape)
     same = all(np.array_equal(a, b) for a, b in zip(batched.s, looped.s, strict=True))
     return {
         "metric": "S-parameter sweeps/s",
@@ -241,6 +244,8 @@ def sweep_measure(n: int, steps: int) -> dict[str, Any]:
         "batched_gcell_s": batched.cell_updates / batched.seconds / 1e9,
         "looped_gcell_s": looped.cell_updates / looped.seconds / 1e9,
         "identical_s": same,
+        "launch_shape": None if shape is None else {"tile_z": shape.tile_z, "variant": shape.variant,
+                                                    "tune_seconds": tune_s},
     }
 
 

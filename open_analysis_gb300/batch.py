@@ -7,8 +7,10 @@ small grids side by side instead of one small grid at a time; ``run_looped`` is 
 one instance after the other (``step`` synchronises). Both give the same S-parameters bit for
 bit (each instance's arithmetic does not depend on what runs beside it).
 
-The host compiles the instances in a ``spawn`` process pool before any CUDA call (NumPy
-compile of one instance takes ~0.1-0.4 s).
+The host compiles the instances in a ``spawn`` process pool before any CUDA call. The launch
+shape (planes per block, sweep variant) comes from the project's autotuner
+(:func:`open_analysis_gb300.autotune.tune`), run once per sweep on a scratch engine of the
+median-size instance (:func:`tune_shape`) and applied to every instance.
 """
 
 from __future__ import annotations
@@ -86,11 +88,41 @@ class SweepRun:
         return len(self.s) / self.seconds
 
 
-def _engines(compiled: Sequence[Compiled], steps: int, dtype: str) -> tuple[list[Any], float]:
+SWEEP_TILES = (4, 8, 16)
+
+
+def tune_shape(compiled: Sequence[Compiled], dtype: str = "float32") -> Any:
+    """The autotuner's launch shape for a sweep: TMA-staged sweeps with 4, 8 or 16 planes per
+    block, each timed for one 64-step chunk on a scratch engine of the median-size instance.
+    Returns the :class:`~open_analysis_gb300.autotune.TuneResult`, or None when no TMA shape is
+    available (the engines then keep their default)."""
+    from open_analysis_gb300.autotune import steps_needed, tune
     from open_analysis_gb300.engine import Gb300Engine
 
+    c = sorted(compiled, key=lambda x: x.grid.cells)[len(compiled) // 2]
+    eng = Gb300Engine(c, dtype, max_steps=steps_needed(1, SWEEP_TILES, (2,)))
+    try:
+        return tune(eng, chunks=1, tiles=SWEEP_TILES, variants=(2,))
+    except ValueError:  # every candidate refused
+        return None
+    finally:
+        eng.close()
+
+
+def _engines(compiled: Sequence[Compiled], steps: int, dtype: str, shape: Any = None) -> tuple[list[Any], float]:
+    from open_analysis_gb300.engine import Gb300Engine
+    from open_analysis_gb300.model import ModelError
+
     t0 = time.perf_counter()
-    engines = [Gb300Engine(c, dtype, max_steps=steps) for c in compiled]
+    engines = []
+    for c in compiled:
+        e = Gb300Engine(c, dtype, max_steps=steps)
+        if shape is not None:
+            try:
+                e.set_tuning(shape.tile_z, shape.variant)
+            except ModelError:  # this instance cannot take the shape: keep its default
+                pass
+        engines.append(e)
     return engines, time.perf_counter() - t0
 
 
@@ -104,13 +136,15 @@ def _finish(models, compiled, engines, steps, dtype, seconds, create):  # type: 
     return SweepRun(s, seconds + read, create, updates, {"readback_seconds": read})
 
 
-def run_batched(models: Sequence[Model], compiled: Sequence[Compiled], steps: int, dtype: str = "float32") -> SweepRun:
+def run_batched(models: Sequence[Model], compiled: Sequence[Compiled], steps: int, dtype: str = "float32",
+                shape: Any = None) -> SweepRun:
     """All instances at once: every engine's steps queued on its own stream, then waited on.
 
     The first 64-step chunk goes first on every engine (each captures its graph there), the
     rest after: capturing a graph while other engines' work is queued would wait for that work
-    and run the instances one after the other."""
-    engines, create = _engines(compiled, steps, dtype)
+    and run the instances one after the other. ``shape``: a launch shape from
+    :func:`tune_shape` (None: the engines' default)."""
+    engines, create = _engines(compiled, steps, dtype, shape)
     t0 = time.perf_counter()
     first = min(64, steps)
     for e in engines:
@@ -125,9 +159,10 @@ def run_batched(models: Sequence[Model], compiled: Sequence[Compiled], steps: in
     return _finish(models, compiled, engines, steps, dtype, time.perf_counter() - t0, create)
 
 
-def run_looped(models: Sequence[Model], compiled: Sequence[Compiled], steps: int, dtype: str = "float32") -> SweepRun:
+def run_looped(models: Sequence[Model], compiled: Sequence[Compiled], steps: int, dtype: str = "float32",
+               shape: Any = None) -> SweepRun:
     """The plain way: one instance after the other."""
-    engines, create = _engines(compiled, steps, dtype)
+    engines, create = _engines(compiled, steps, dtype, shape)
     t0 = time.perf_counter()
     for e in engines:
         e.step(steps)

@@ -244,17 +244,21 @@ def generate(
     workers: int = 8,
     dtype: str = "float32",
     batched: bool = True,
+    tune: bool = True,
 ) -> Dataset:
     """S11 and S21 of every instance from the GPU engine: ``chunk`` instances at a time through
     :func:`~open_analysis_gb300.batch.run_batched` (or ``run_looped`` with ``batched=False``),
-    the next chunk compiling in the process pool meanwhile."""
-    from open_analysis_gb300.batch import run_batched, run_looped
+    the next chunk compiling in the process pool meanwhile. With ``tune`` the launch shape comes
+    from the autotuner once (:func:`~open_analysis_gb300.batch.tune_shape`, counted with the
+    engine creation time)."""
+    from open_analysis_gb300.batch import run_batched, run_looped, tune_shape
 
     p = meshed(np.atleast_2d(np.asarray(params, dtype=np.float64)), g)
     n = p.shape[0]
     out = np.zeros((n, 2, g.n_freq), np.complex128)
     seconds = create = comp_wait = 0.0
     runner = run_batched if batched else run_looped
+    shape = None
     chunks = [list(range(a, min(a + chunk, n))) for a in range(0, n, chunk)]
     with ProcessPoolExecutor(max_workers=max(1, workers), mp_context=get_context("spawn")) as pool:
 
@@ -268,7 +272,11 @@ def generate(
             comp_wait += time.perf_counter() - t0
             pending = submit(chunks[ci + 1]) if ci + 1 < len(chunks) else []
             models = [via_instance(p[i], g) for i in idx]
-            run = runner(models, compiled, steps, dtype)
+            if shape is None and tune:
+                t_tune = time.perf_counter()
+                shape = tune_shape(compiled, dtype)
+                create += time.perf_counter() - t_tune
+            run = runner(models, compiled, steps, dtype, shape)
             seconds += run.seconds
             create += run.create_seconds
             for k, i in enumerate(idx):
@@ -745,7 +753,7 @@ def surrogate_sweep(ens: Ensemble, params: npt.ArrayLike, g: ViaGrid = ViaGrid()
     fb = pred.bound_db > tol_db
     fsec = fcreate = 0.0
     if fb.any():
-        d = generate(p[fb], g, steps, chunk=chunk)
+        d = generate(p[fb], g, steps, chunk=chunk, tune=False)
         out[fb] = d.s
         fsec, fcreate = d.seconds, d.create_seconds
     return SweepAnswer(out, fb, pred.seconds, fsec, fcreate)
@@ -825,7 +833,8 @@ def experiment(
         raise RuntimeError("the FDTD fallback did not reproduce the engine's own S-parameters")
     err_db = db_error(ans.s, test.s, axis=(1, 2))
     k = min(plain_sample, len(test.s))
-    plain = generate(test.params[:k], g, steps, chunk=chunk, workers=workers, batched=False)
+    # the fallback above and this loop both run the engines' default launch shape
+    plain = generate(test.params[:k], g, steps, chunk=chunk, workers=workers, batched=False, tune=False)
     if not test.same_as(plain.s, slice(0, k)):
         raise RuntimeError("the plain engine and the batched engine disagree")
     plain_rate = k / (plain.seconds + plain.create_seconds)
