@@ -30,7 +30,7 @@ def test_instances_compile_with_debye_cpml_and_two_ports() -> None:
 
 @pytest.mark.gpu
 def test_batched_equals_looped_equals_run() -> None:
-    from open_analysis_gb300.batch import compile_all, run_batched, run_looped
+    from open_analysis_gb300.batch import SWEEP_TILES, compile_all, run_batched, run_looped, tune_shape
     from open_analysis_gb300.run import run, sparams
 
     params = sweep_params(6, seed=7)
@@ -38,8 +38,10 @@ def test_batched_equals_looped_equals_run() -> None:
     models = [line_instance(p, n_freq=16) for p in small]
     compiled = compile_all(models, workers=1)
     steps = 300
-    a = run_batched(models, compiled, steps)
-    b = run_looped(models, compiled, steps)
+    shape = tune_shape(compiled)
+    assert shape is not None and shape.tile_z in SWEEP_TILES and shape.variant == 2
+    a = run_batched(models, compiled, steps, shape=shape)
+    b = run_looped(models, compiled, steps)  # default shape: launch shapes do not change results
     for sa, sb in zip(a.s, b.s, strict=True):
         assert np.array_equal(sa, sb)
     one = run(models[0], engine="gb300", dtype="float32", end_db=None, max_steps=steps)
