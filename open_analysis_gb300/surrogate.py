@@ -753,7 +753,7 @@ def surrogate_sweep(ens: Ensemble, params: npt.ArrayLike, g: ViaGrid = ViaGrid()
     fb = pred.bound_db > tol_db
     fsec = fcreate = 0.0
     if fb.any():
-        d = generate(p[fb], g, steps, chunk=chunk, tune=False)
+        d = generate(p[fb], g, steps, chunk=chunk)
         out[fb] = d.s
         fsec, fcreate = d.seconds, d.create_seconds
     return SweepAnswer(out, fb, pred.seconds, fsec, fcreate)
@@ -833,8 +833,8 @@ def experiment(
         raise RuntimeError("the FDTD fallback did not reproduce the engine's own S-parameters")
     err_db = db_error(ans.s, test.s, axis=(1, 2))
     k = min(plain_sample, len(test.s))
-    # the fallback above and this loop both run the engines' default launch shape
-    plain = generate(test.params[:k], g, steps, chunk=chunk, workers=workers, batched=False, tune=False)
+    # the fallback above and this loop both take their launch shape from the autotuner
+    plain = generate(test.params[:k], g, steps, chunk=chunk, workers=workers, batched=False)
     if not test.same_as(plain.s, slice(0, k)):
         raise RuntimeError("the plain engine and the batched engine disagree")
     plain_rate = k / (plain.seconds + plain.create_seconds)
