@@ -363,9 +363,6 @@ int oafdtd_mlp_count(int32_t* counter, void* stream);
 int oafdtd_mlp_gather(const float* src, int32_t cols, const int32_t* idx, int32_t rows, float* dst32, void* dst16,
                       void* stream);
 
-/* FP32 -> BF16 conversion of n values. */
-int oafdtd_mlp_to_bf16(const float* x, void* y, int64_t n, void* stream);
-
 #ifdef __cplusplus
 }
 #endif

@@ -368,12 +368,6 @@ __global__ void gather_kernel(const float* src, int cols, const int* idx, int ro
   if (d16) d16[e] = __float2bfloat16(v);
 }
 
-// FP32 -> BF16.
-__global__ void to_bf16_kernel(const float* x, __nv_bfloat16* y, long long n) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) y[i] = __float2bfloat16(x[i]);
-}
-
 }  // namespace oafdtd
 
 // --------------------------------------------------------------------------------------- C ABI
@@ -447,13 +441,6 @@ int oafdtd_mlp_gather(const float* src, int32_t cols, const int32_t* idx, int32_
   const long long n = (long long)rows * cols;
   oafdtd::gather_kernel<<<(unsigned)((n + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
       src, cols, idx, rows, dst32, static_cast<__nv_bfloat16*>(dst16));
-  return cudaGetLastError() == cudaSuccess ? 0 : -3;
-}
-
-int oafdtd_mlp_to_bf16(const float* x, void* y, int64_t n, void* stream) {
-  if (!x || !y || n < 1) return -1;
-  oafdtd::to_bf16_kernel<<<(unsigned)((n + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-      x, static_cast<__nv_bfloat16*>(y), n);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 

@@ -208,7 +208,6 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     ),
     "oafdtd_mlp_count": (C.c_int, [C.c_void_p, C.c_void_p]),
     "oafdtd_mlp_gather": (C.c_int, [C.c_void_p, _i32, C.c_void_p, _i32, C.c_void_p, C.c_void_p, C.c_void_p]),
-    "oafdtd_mlp_to_bf16": (C.c_int, [C.c_void_p, C.c_void_p, _i64, C.c_void_p]),
 }
 
 _lock = threading.Lock()
