@@ -11,14 +11,16 @@ built on the engine and judged by it:
 * :func:`generate` — S11 and S21 at every DFT frequency of many instances from the engine's
   batched runner (:func:`open_analysis_gb300.batch.run_batched`), host compiles overlapped with
   the GPU in a ``spawn`` process pool.
-* :class:`Mlp` — the network (7 -> 512 x 6 -> 4 F outputs: S11 and S21, real and imaginary
-  parts) trained on the GPU by the engine library's own kernels: BF16 tensor-core GEMMs with FP32
-  accumulation and fused bias / ReLU / ReLU-derivative epilogues, the MSE gradient, bias sums and
-  Adam on FP32 master weights (``oafdtd_mlp_*`` in ``include/oafdtd.h``). One epoch of training
-  steps is captured once as a CUDA graph and replayed. PyTorch only owns the device buffers and
-  draws the epoch's shuffle.
-* :class:`Ensemble` — several independently initialised networks; their spread is the predicted
-  uncertainty, scaled by a factor calibrated against FDTD on a calibration fold.
+* :class:`Mlp` — the network (7 -> 512 x 6 tanh -> 4 F outputs: S11 and S21, real and
+  imaginary parts, with the TEM line propagation divided out, :func:`line_factor`) trained on the
+  GPU by the engine library's own kernels: BF16 tensor-core GEMMs with FP32 accumulation and fused
+  bias / activation / activation-derivative epilogues, the MSE gradient, bias sums and Adam on
+  FP32 master weights (``oafdtd_mlp_*`` in ``include/oafdtd.h``). One epoch of training steps is
+  captured once as a CUDA graph and replayed. PyTorch only owns the device buffers and draws the
+  epoch's shuffle.
+* :class:`Ensemble` — eight independently initialised networks trained side by side (early
+  stopping on a validation fold); their spread is the predicted uncertainty, scaled by a factor
+  calibrated against FDTD on a calibration fold; :meth:`Ensemble.save` / :meth:`Ensemble.load`.
 * :func:`surrogate_sweep` — answers a sweep: instances whose predicted error bound exceeds the
   tolerance (0.05 dB by default) are run by FDTD instead (the fallback), so every returned S is
   either FDTD's or predicted within the bound.
@@ -324,6 +326,7 @@ class Mlp:
         if act not in ACTS:
             raise ValueError(f"activation {act!r}: one of {sorted(ACTS)}")
         self.act, self.dact = ACTS[act]
+        self.act_name = act
         self.n_in = int(sizes[0])
         self.sizes = [_align(int(s), 8) for s in sizes]
         if self.sizes[1:] != [int(s) for s in sizes[1:]]:
@@ -714,6 +717,45 @@ class Ensemble:
         mean = stack.mean(axis=0)
         dev = np.sqrt((np.abs(stack - mean) ** 2).mean(axis=0))  # complex std per (n, 2, F)
         return mean, dev.reshape(dev.shape[0], -1).max(axis=1), sec
+
+    def save(self, path: str) -> None:
+        """Write the trained ensemble (grid, widths, activation, every member's FP32 weights,
+        the target scaling and the calibrated scale) to an npz file."""
+        g = self.g
+        np.savez_compressed(
+            path,
+            grid=np.array([g.nx, g.ny, g.nz, g.n_freq, g.cpml]),
+            cell=np.array([g.h, g.dz, g.delay_tau, g.span]),
+            sizes=np.array(self.sizes),
+            act=np.array(self.nets[0].act_name),
+            batch=np.array(self.nets[0].batch),
+            weights=np.stack([net.p32.detach().cpu().numpy() for net in self.nets]),
+            mu=self.mu,
+            sigma=np.array(self.sigma),
+            scale=np.array(self.scale),
+        )
+
+    @staticmethod
+    def load(path: str) -> Ensemble:
+        """An ensemble written by :meth:`save`, ready to predict (on the current CUDA device)."""
+        d = np.load(path)
+        nx, ny, nz, n_freq, cpml = (int(v) for v in d["grid"])
+        h, dz, delay_tau, span = (float(v) for v in d["cell"])
+        g = ViaGrid(nx=nx, ny=ny, nz=nz, h=h, dz=dz, n_freq=n_freq, cpml=cpml, delay_tau=delay_tau, span=span)
+        sizes = [int(v) for v in d["sizes"]]
+        act = str(d["act"])
+        w = d["weights"]
+        ens = Ensemble(g, members=w.shape[0], width=sizes[1], depth=len(sizes) - 2, batch=int(d["batch"]), act=act)
+        if ens.sizes != sizes:
+            raise ValueError(f"{path}: layer widths {sizes} are not an ensemble of this kind")
+        torch = ens.nets[0].torch
+        for net, flat in zip(ens.nets, w, strict=True):
+            if flat.size != net.n_params:
+                raise ValueError(f"{path}: {flat.size} weights where the network holds {net.n_params}")
+            net.p32.copy_(torch.from_numpy(flat.astype(np.float32)).to(net.dev))
+            net.p16.copy_(net.p32.to(torch.bfloat16))
+        ens.mu, ens.sigma, ens.scale = d["mu"], float(d["sigma"]), float(d["scale"])
+        return ens
 
     def calibrate(self, data: Dataset, quantile: float = 1.0) -> float:
         """Scale the spread so that it bounds the true error (FDTD's) on ``data``: the

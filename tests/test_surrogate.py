@@ -19,6 +19,7 @@ from open_analysis_gb300.surrogate import (
     meshed,
     rows_to_s,
     s_to_rows,
+    line_factor,
     scale_params,
     via_instance,
     via_params,
@@ -122,3 +123,19 @@ def test_via_instance_compiles_with_every_part() -> None:
         assert c.batch == 1 and len(c.ports) == 2
     with pytest.raises(ValueError):
         via_instance(p[0], ViaGrid(nz=60))  # the tallest stack and stub do not fit
+
+
+def test_line_factor_removes_the_tem_line() -> None:
+    g = ViaGrid()
+    p = meshed(via_params(5, seed=3), g)
+    f = line_factor(p, g)
+    assert f.shape == (5, 2, g.n_freq)
+    assert np.all(np.abs(f) >= 1.0)  # exp(+alpha L): dividing it out can only shrink errors
+    lossless = p.copy()
+    lossless[:, 5] = 0.0  # no Debye term: a pure phase
+    assert np.allclose(np.abs(line_factor(lossless, g)), 1.0, rtol=0, atol=1e-12)
+    # the S21 factor's phase is the TEM delay over both traces and the via
+    w = 2 * np.pi * np.linspace(0.1e9, 20e9, g.n_freq)
+    length = (g.nx // 2 - g.cpml - 4) * g.h + (g.nx - g.cpml - 4 - g.nx // 2) * g.h + lossless[:, 3:4]
+    want = w * np.sqrt(lossless[:, 4:5]) / 299792458.0 * length
+    assert np.allclose(np.unwrap(np.angle(line_factor(lossless, g)[:, 1]), axis=1), want, atol=1e-9)

@@ -160,3 +160,22 @@ def test_surrogate_gains_over_the_plain_engine() -> None:
     assert rep["network_alone_median_db"] <= TOL_DB
     assert rep["accepted"] >= 0.25
     assert rep["gain_vs_batched"] > 1.2 and rep["gain_vs_plain"] > rep["gain_vs_batched"]
+
+
+def test_ensemble_save_and_load_predict_the_same(tmp_path) -> None:  # type: ignore[no-untyped-def]
+    from open_analysis_gb300.surrogate import Dataset, Ensemble, ViaGrid, via_params
+
+    g = ViaGrid(nx=48, ny=48, nz=60, h=50e-6, dz=100e-6, n_freq=8, cpml=6, span=560e-12)
+    rng = np.random.default_rng(3)
+    p = via_params(96, seed=9)
+    s = (rng.standard_normal((96, 2, 8)) + 1j * rng.standard_normal((96, 2, 8))) * 0.1
+    ens = Ensemble(g, members=2, width=64, depth=2, batch=32, seed=4)
+    ens.fit(Dataset(p, s, np.linspace(0.1e9, 20e9, 8)), epochs=20)
+    ens.scale = 3.5
+    path = str(tmp_path / "ens.npz")
+    ens.save(path)
+    back = Ensemble.load(path)
+    a, b = ens.predict(p[:10]), back.predict(p[:10])
+    assert back.scale == 3.5 and back.sizes == ens.sizes
+    np.testing.assert_array_equal(a.s, b.s)
+    np.testing.assert_array_equal(a.bound_db, b.bound_db)
