@@ -31,7 +31,7 @@ from known_answers import (
 
 from open_analysis_gb300.grid import C0, EPS0, MU0, Grid
 from open_analysis_gb300.materials import fit_djordjevic_sarkar
-from open_analysis_gb300.model import LumpedPort, Model, Probe, SoftSource, Waveform, compile_model
+from open_analysis_gb300.model import Model, Probe, SoftSource, Waveform, compile_model
 from open_analysis_gb300.run import run, sparams
 from open_analysis_gb300.sibc import slab_surface_impedance
 from oracle.numpy_engine import OracleEngine

@@ -12,8 +12,6 @@
 
 from __future__ import annotations
 
-import time
-
 import numpy as np
 import pytest
 
