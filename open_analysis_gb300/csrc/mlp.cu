@@ -303,13 +303,28 @@ bool pipe_ok(const GemmArgs& g) {
          al(g.A, 16) && al(g.B, 16) && al(g.C32, 8) && al(g.C16, 4) && al(g.mask, 4);
 }
 
-// Column sums of an FP32 M x N matrix (bias gradients): one thread per column, fixed order.
-__global__ void colsum_kernel(const float* X, int M, int N, int ld, float* out) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= N) return;
+// Column sums of an FP32 M x N matrix (bias gradients). A block takes 32 columns; each of its 16
+// row lanes sums the rows lane, lane + 16, ... of one column (a warp reads 32 adjacent columns of
+// one row), then lane 0 adds the 16 partial sums in lane order: a fixed order, so the result is
+// the same on every run.
+constexpr int kSumCols = 32, kSumLanes = 16;
+
+__global__ void __launch_bounds__(kSumCols * kSumLanes) colsum_kernel(const float* X, int M, int N, int ld,
+                                                                      float* out) {
+  __shared__ float part[kSumLanes][kSumCols + 1];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int n = blockIdx.x * kSumCols + tx;
   float s = 0.f;
-  for (int m = 0; m < M; ++m) s += X[(long long)m * ld + n];
-  out[n] = s;
+  if (n < N)
+#pragma unroll 4
+    for (int m = ty; m < M; m += kSumLanes) s += X[(long long)m * ld + n];
+  part[ty][tx] = s;
+  __syncthreads();
+  if (ty == 0 && n < N) {
+    float t = 0.f;
+    for (int q = 0; q < kSumLanes; ++q) t += part[q][tx];
+    out[n] = t;
+  }
 }
 
 // Mean-squared-error gradient: G = (2 / (M N)) (Y - T), in FP32 and BF16; loss partials per row.
@@ -409,7 +424,9 @@ int oafdtd_mlp_gemm(const void* A, const void* B, float* C32, void* C16, const f
 
 int oafdtd_mlp_colsum(const float* X, int32_t M, int32_t N, int32_t ld, float* out, void* stream) {
   if (!X || !out || M < 1 || N < 1) return -1;
-  oafdtd::colsum_kernel<<<(N + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(X, M, N, ld, out);
+  const dim3 block(oafdtd::kSumCols, oafdtd::kSumLanes);
+  oafdtd::colsum_kernel<<<(N + oafdtd::kSumCols - 1) / oafdtd::kSumCols, block, 0, static_cast<cudaStream_t>(stream)>>>(
+      X, M, N, ld, out);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 
