@@ -241,7 +241,7 @@ class Dataset:
 def generate(
     params: npt.ArrayLike,
     g: ViaGrid = ViaGrid(),
-    steps: int = 3000,
+    steps: int | None = None,
     chunk: int = 32,
     workers: int = 8,
     dtype: str = "float32",
@@ -252,9 +252,10 @@ def generate(
     :func:`~open_analysis_gb300.batch.run_batched` (or ``run_looped`` with ``batched=False``),
     the next chunk compiling in the process pool meanwhile. With ``tune`` the launch shape comes
     from the autotuner once (:func:`~open_analysis_gb300.batch.tune_shape`, counted with the
-    engine creation time)."""
+    engine creation time). ``steps`` defaults to the grid's :attr:`ViaGrid.steps`."""
     from open_analysis_gb300.batch import run_batched, run_looped, tune_shape
 
+    steps = g.steps if steps is None else int(steps)
     p = meshed(np.atleast_2d(np.asarray(params, dtype=np.float64)), g)
     n = p.shape[0]
     out = np.zeros((n, 2, g.n_freq), np.complex128)
@@ -785,10 +786,11 @@ class SweepAnswer:
         return self.predict_seconds + self.fdtd_seconds + self.fdtd_create_seconds
 
 
-def surrogate_sweep(ens: Ensemble, params: npt.ArrayLike, g: ViaGrid = ViaGrid(), steps: int = 3000,
+def surrogate_sweep(ens: Ensemble, params: npt.ArrayLike, g: ViaGrid = ViaGrid(), steps: int | None = None,
                     tol_db: float = TOL_DB, chunk: int = 32) -> SweepAnswer:
     """Answer a sweep: the ensemble's prediction where its calibrated bound is within ``tol_db``,
-    the engine's batched FDTD everywhere else."""
+    the engine's batched FDTD everywhere else (``steps`` as the ensemble's data: by default the
+    grid's :attr:`ViaGrid.steps`)."""
     p = meshed(np.atleast_2d(np.asarray(params, np.float64)), g)
     pred = ens.predict(p)
     out = pred.s.copy()
