@@ -13,6 +13,11 @@ geometry where the workload calls for randomness.
   layers as surface-impedance copper (sigma 5.8e7 S/m), a via (0.3 mm drill as the 1.694 r
   square barrel, 0.5 mm pads, 0.8 mm antipads), 10-cell CPML, two lumped ports, 256 DFT
   frequencies 0.1-20 GHz.
+* :func:`large_board` — 1600 x 1200 x 160 cells of 20 um (307 M cells): an eight-layer stack of
+  single-pole Debye dielectrics (eps_inf 3.4-4.2 per layer, seeded), 12 routed traces and 40 vias
+  of surface-impedance copper at seeded positions, a PEC ground under the stack, 12-cell CPML,
+  eight lumped ports (trace ends to the ground) driven as a batch of eight, 512 DFT frequencies
+  0.05-40 GHz.
 * :func:`sweep_instances` — a seeded parameter sweep of microstrip and stripline instances with
   uneven grids (80-240 x 40-120 x 30-80 cells of 50 um), trace width 0.1-0.6 mm, substrate
   0.1-0.4 mm, single-pole Debye substrate (eps_inf 3.0-4.8, delta_eps 0.1-0.5, tau 2-20 ps),
@@ -141,6 +146,54 @@ def via_transition(
     # ports: top trace to the plane below it; bottom trace to the plane above it
     m.ports.append(LumpedPort("p1", 2, (x_p1, cy, z(planes[2] + 1)), (x_p1, cy, z(kt)), 50.0))
     m.ports.append(LumpedPort("p2", 2, (x_p2, cy, z(kb + 1)), (x_p2, cy, z(planes[0])), 50.0))
+    return m
+
+
+def large_board(nx: int = 1600, ny: int = 1200, nz: int = 160, h: float = 20e-6, seed: int = 2026,
+                n_freq: int = 512, cpml_cells: int = 12) -> Model:
+    """The large board region (defaults: 1600 x 1200 x 160 cells of 20 um). Eight dielectric
+    layers of ``(nz - 2 (cpml + 4)) / 8`` cells fill the middle of the z extent over a PEC ground;
+    traces run on the layer interfaces as two axis-aligned segments (an L) of 5 cells width, one
+    cell thick; vias are square barrels of 0.2-0.3 mm spanning two to five layers; the first eight
+    traces carry a lumped port (50 ohm) from their start down to the ground."""
+    rng = np.random.default_rng(seed)
+    g = Grid(uniform_lines(nx, h), uniform_lines(ny, h), uniform_lines(nz, h))
+    m = Model(
+        g,
+        Waveform("gauss_mod", 20.025e9, 39.95e9),
+        np.linspace(0.05e9, 40e9, n_freq),
+        walls=("cpml",) * 6,
+        cpml=CpmlSpec(cells=cpml_cells),
+        courant=0.95,
+    )
+    k0 = cpml_cells + 4
+    layer = (nz - 2 * k0) // 8
+    at = lambda k: k * h  # noqa: E731  (cell index -> coordinate, every axis)
+    big = 1.0
+    for n in range(8):
+        eps = float(rng.uniform(3.4, 4.2))
+        m.regions.append(Region((-big, -big, at(k0 + n * layer)), (big, big, at(k0 + (n + 1) * layer)), eps,
+                                poles=((0.3, 8e-12),)))
+    m.regions.append(Region((-big, -big, at(k0)), (big, big, at(k0)), pec=True))  # ground under the stack
+    cu = dict(sigma=5.8e7, thickness=18e-6)
+    margin = cpml_cells + 20
+    w = 5 * h
+    for t in range(12):
+        kz = k0 + layer * int(rng.integers(1, 8))  # on a layer interface
+        xa, xb = sorted(int(v) for v in rng.integers(margin, nx - margin, 2))
+        ya, yb = sorted(int(v) for v in rng.integers(margin, ny - margin, 2))
+        # an L: along x at ya from xa to xb, then along y at xb from ya to yb
+        m.conductors.append(Conductor((at(xa), at(ya), at(kz)), (at(xb), at(ya) + w, at(kz + 1)), **cu))
+        m.conductors.append(Conductor((at(xb) - w, at(ya), at(kz)), (at(xb), at(yb), at(kz + 1)), **cu))
+        if t < 8:
+            m.ports.append(LumpedPort(f"p{t + 1}", 2, (at(xa), at(ya) + 2 * h, at(k0)), (at(xa), at(ya) + 2 * h, at(kz)), 50.0))
+    for _ in range(40):
+        side = float(rng.uniform(0.2e-3, 0.3e-3)) * 0.5 / 0.5902
+        cx, cy = (int(v) * h for v in (rng.integers(margin, nx - margin), rng.integers(margin, ny - margin)))
+        a = int(rng.integers(0, 6))
+        b = min(8, a + int(rng.integers(2, 6)))
+        m.conductors.append(Conductor((cx - side / 2, cy - side / 2, at(k0 + a * layer)),
+                                      (cx + side / 2, cy + side / 2, at(k0 + b * layer)), **cu))
     return m
 
 
