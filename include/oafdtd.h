@@ -205,6 +205,14 @@ int oafdtd_step_half(oafdtd_engine* engine, int32_t which);
 int oafdtd_plane(oafdtd_engine* engine, int32_t comp, int32_t k, double* out);
 int oafdtd_set_plane(oafdtd_engine* engine, int32_t comp, int32_t k, const double* in);
 
+/* The same plane in the engine's own precision (real_bytes per value), device to device: dst / src
+ * is device memory holding (batch, ny+2, pitch) values, on this GPU or a peer. The copies run on
+ * the handle's stream and have finished when the call returns. For the halo exchange of a z-slab
+ * decomposition without a trip through host memory (NCCL send/recv or peer copies of the buffer);
+ * no counterpart in the reference. */
+int oafdtd_plane_device(oafdtd_engine* engine, int32_t comp, int32_t k, void* dst);
+int oafdtd_set_plane_device(oafdtd_engine* engine, int32_t comp, int32_t k, const void* src);
+
 /* Overwrites one field component from float64 values in the oafdtd_fields layout, rounded to
  * the field precision (restoring fields, or starting a check from a chosen state). The reference
  * engine has no counterpart. */

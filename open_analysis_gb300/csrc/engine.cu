@@ -57,6 +57,7 @@ struct EngineBase {
   virtual int snapshot(void* out, int64_t* bytes, const void* in) = 0;
   virtual int wait() = 0;
   virtual int plane(int comp, int k, double* out, const double* in) = 0;
+  virtual int plane_device(int comp, int k, void* dst, const void* src) = 0;
   virtual int kernel_times(double* out, int n) = 0;
   virtual int step_timed(int64_t n, double* ms) = 0;
   int64_t steps = 0;
@@ -170,6 +171,7 @@ struct Engine final : EngineBase {
   int launch_step(int off, cudaEvent_t* ev, bool capturing = false, int parts = 3);
   int step_half(int which) override;
   int plane(int comp, int k, double* out, const double* in) override;
+  int plane_device(int comp, int k, void* dst, const void* src) override;
   bool half_pending = false;  // an H half ran and its E half has not
   int capture();
 
@@ -1335,6 +1337,29 @@ int Engine<real>::plane(int comp, int k, double* out, const double* in) {
   return OAFDTD_OK;
 }
 
+// The same plane in the engine's own precision, device to device (dst or src is device memory
+// of (B, Y, X) elements, on this GPU or a peer): one copy per batch member on the engine's
+// stream, finished before the call returns.
+template <typename real>
+int Engine<real>::plane_device(int comp, int k, void* dst, const void* src) {
+  if (comp < 0 || comp > 5) return fail(OAFDTD_E_INVALID, "component must be 0..5");
+  if (k < 0 || k >= Z) return fail(OAFDTD_E_INVALID, "plane out of range");
+  OA_CUDA(cudaSetDevice(device));
+  real* f = comp < 3 ? sw.E[comp] : sw.H[comp - 3];
+  const size_t per = (size_t)X * Y;
+  for (int b = 0; b < B; ++b) {
+    real* field = f + (size_t)b * bs + (size_t)k * per;
+    if (src)
+      OA_CUDA(cudaMemcpyAsync(field, static_cast<const real*>(src) + b * per, per * sizeof(real), cudaMemcpyDefault,
+                              stream));
+    else
+      OA_CUDA(cudaMemcpyAsync(static_cast<real*>(dst) + b * per, field, per * sizeof(real), cudaMemcpyDefault,
+                              stream));
+  }
+  OA_CUDA(cudaStreamSynchronize(stream));
+  return OAFDTD_OK;
+}
+
 // Snapshot layout: a 32-byte header (magic, format version, total bytes, step count), then every
 // state buffer in registration order. out == in == nullptr: report the size only.
 constexpr uint64_t kSnapshotMagic = 0x3130504E53444641ull;  // "AFDSNP01" read little-endian
@@ -1550,6 +1575,16 @@ int oafdtd_plane(oafdtd_engine* engine, int32_t comp, int32_t k, double* out) {
 int oafdtd_set_plane(oafdtd_engine* engine, int32_t comp, int32_t k, const double* in) {
   if (!engine || !in) return fail(OAFDTD_E_INVALID, "null argument");
   return engine->impl->plane(comp, k, nullptr, in);
+}
+
+int oafdtd_plane_device(oafdtd_engine* engine, int32_t comp, int32_t k, void* dst) {
+  if (!engine || !dst) return fail(OAFDTD_E_INVALID, "null argument");
+  return engine->impl->plane_device(comp, k, dst, nullptr);
+}
+
+int oafdtd_set_plane_device(oafdtd_engine* engine, int32_t comp, int32_t k, const void* src) {
+  if (!engine || !src) return fail(OAFDTD_E_INVALID, "null argument");
+  return engine->impl->plane_device(comp, k, nullptr, src);
 }
 
 int oafdtd_set_field(oafdtd_engine* engine, int32_t comp, const double* in) {

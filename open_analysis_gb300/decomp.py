@@ -237,15 +237,36 @@ def _sum_dicts(parts: Sequence[dict[str, Any]]) -> dict[str, Any]:
     return out
 
 
+def _plane_buffers(engine: Any, comps: Sequence[int]) -> dict[int, Any]:
+    """One device buffer per component for a plane of ``engine`` (its precision and shape)."""
+    import torch
+
+    dtype = torch.float32 if engine.dtype == "float32" else torch.float64
+    shape = (engine.B, engine.shape[2], engine.shape[3])
+    return {comp: torch.empty(shape, dtype=dtype, device="cuda") for comp in comps}
+
+
 class LocalSlabs:
     """Every rank's engine in this process; boundary planes copied between them. ``factory``
     builds an engine from a ``Compiled`` (for example ``lambda c: Gb300Engine(c, "float32")``);
-    engines need ``half_h``, ``half_e``, ``plane``, ``set_plane`` and the engine protocol."""
+    engines need ``half_h``, ``half_e``, ``plane``, ``set_plane`` and the engine protocol.
+    ``device=True`` moves the planes device to device in the engines' own precision
+    (``plane_to_device`` / ``plane_from_device``) instead of through host float64."""
 
-    def __init__(self, c: Compiled, parts: int, factory: Callable[[Compiled], Any]) -> None:
+    def __init__(self, c: Compiled, parts: int, factory: Callable[[Compiled], Any], device: bool = False) -> None:
         self.c = c
         self.slabs = split_z(c, parts)
         self.engines = [factory(s.c) for s in self.slabs]
+        self.device = device
+        self._buf = _plane_buffers(self.engines[0], (HX, HY, EX, EY)) if device else {}
+
+    def _copy(self, comp: int, src: Any, k_src: int, dst: Any, k_dst: int) -> None:
+        if self.device:
+            buf = self._buf[comp]
+            src.plane_to_device(comp, k_src, buf.data_ptr())
+            dst.plane_from_device(comp, k_dst, buf.data_ptr())
+        else:
+            dst.set_plane(comp, k_dst, src.plane(comp, k_src))
 
     def step(self, n: int = 1) -> None:
         for _ in range(n):
@@ -254,13 +275,13 @@ class LocalSlabs:
             for r in range(len(self.slabs) - 1):  # H of the last owned plane up to the next slab
                 s, e, nxt = self.slabs[r], self.engines[r], self.engines[r + 1]
                 for comp in (HX, HY):
-                    nxt.set_plane(comp, 0, e.plane(comp, s.last_local))
+                    self._copy(comp, e, s.last_local, nxt, 0)
             for e in self.engines:
                 e.half_e()
             for r in range(1, len(self.slabs)):  # E of the first owned plane down to the previous
                 prev_s, prev, e = self.slabs[r - 1], self.engines[r - 1], self.engines[r]
                 for comp in (EX, EY):
-                    prev.set_plane(comp, prev_s.b - prev_s.z0, e.plane(comp, 1))
+                    self._copy(comp, e, 1, prev, prev_s.b - prev_s.z0)
 
     def results(self) -> dict[str, Any]:
         return _sum_dicts([e.results() for e in self.engines])
@@ -286,10 +307,15 @@ class LocalSlabs:
 
 class DistSlabs:
     """This process's rank of the decomposition; planes go to the neighbours through
-    ``torch.distributed`` point-to-point messages (host tensors), results are summed with
-    ``all_reduce``."""
+    ``torch.distributed`` point-to-point messages, results are summed with ``all_reduce``.
 
-    def __init__(self, c: Compiled, factory: Callable[[Compiled], Any]) -> None:
+    ``device=False``: host float64 tensors (any backend, ``gloo`` in the CPU tests).
+    ``device=True``: device tensors in the engine's precision, copied device to device out of and
+    into the engine (``plane_to_device`` / ``plane_from_device``), for the ``nccl`` backend with one
+    GPU per rank (``torch.cuda.set_device`` and ``native.set_device`` to the local rank before the
+    engine is built). The device mode needs two GPUs and is not run here."""
+
+    def __init__(self, c: Compiled, factory: Callable[[Compiled], Any], device: bool = False) -> None:
         import torch.distributed as dist
 
         self.dist = dist
@@ -298,6 +324,32 @@ class DistSlabs:
         self.slabs = split_z(c, self.world)
         self.slab = self.slabs[self.rank]
         self.engine = factory(self.slab.c)
+        self.device = device
+        if device:
+            self._send = _plane_buffers(self.engine, (HX, HY, EX, EY))
+            self._recv = _plane_buffers(self.engine, (HX, HY, EX, EY))
+
+    def _swap_device(self, send_to: int | None, send: list[tuple[int, int]], recv_from: int | None,
+                     recv: list[tuple[int, int]]) -> None:
+        """Planes ``(comp, k)`` of this engine to ``send_to``; planes from ``recv_from`` into
+        ``(comp, k)``: device buffers, one NCCL message each."""
+        import torch
+
+        e, ops = self.engine, []
+        if send_to is not None:
+            for comp, k in send:
+                e.plane_to_device(comp, k, self._send[comp].data_ptr())  # finished on return
+                ops.append(self.dist.P2POp(self.dist.isend, self._send[comp], send_to))
+        if recv_from is not None:
+            for comp, _ in recv:
+                ops.append(self.dist.P2POp(self.dist.irecv, self._recv[comp], recv_from))
+        if ops:
+            for req in self.dist.batch_isend_irecv(ops):
+                req.wait()
+        torch.cuda.synchronize()  # the received planes are complete before the engine reads them
+        if recv_from is not None:
+            for comp, k in recv:
+                e.plane_from_device(comp, k, self._recv[comp].data_ptr())
 
     def _swap(self, send_to: int | None, send: list[FloatArray], recv_from: int | None, n_recv: int) -> list[FloatArray]:
         import torch
@@ -321,6 +373,13 @@ class DistSlabs:
         r, w, s, e = self.rank, self.world, self.slab, self.engine
         up = r + 1 if r + 1 < w else None
         down = r - 1 if r > 0 else None
+        if self.device:
+            for _ in range(n):
+                e.half_h()
+                self._swap_device(up, [(HX, s.last_local), (HY, s.last_local)], down, [(HX, 0), (HY, 0)])
+                e.half_e()
+                self._swap_device(down, [(EX, 1), (EY, 1)], up, [(EX, s.b - s.z0), (EY, s.b - s.z0)])
+            return
         for _ in range(n):
             e.half_h()
             got = self._swap(up, [e.plane(HX, s.last_local), e.plane(HY, s.last_local)], down, 2)

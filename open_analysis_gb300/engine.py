@@ -294,6 +294,15 @@ class Gb300Engine:
         a = np.ascontiguousarray(np.broadcast_to(np.asarray(values, np.float64), (self.B, self.shape[2], self.shape[3])))
         native.check(self._lib.oafdtd_set_plane(self._h, int(comp), int(k), _ptr(a, C.c_double)), "set_plane")
 
+    def plane_to_device(self, comp: int, k: int, dst: int) -> None:
+        """Copy plane ``k`` of ``comp`` into device memory at address ``dst`` (``B x y x x``
+        values of the engine's precision, for example ``torch_tensor.data_ptr()``)."""
+        native.check(self._lib.oafdtd_plane_device(self._h, int(comp), int(k), C.c_void_p(int(dst))), "plane_device")
+
+    def plane_from_device(self, comp: int, k: int, src: int) -> None:
+        """Overwrite plane ``k`` of ``comp`` from device memory at address ``src``."""
+        native.check(self._lib.oafdtd_set_plane_device(self._h, int(comp), int(k), C.c_void_p(int(src))), "set_plane_device")
+
     def set_field(self, comp: int, values: FloatArray) -> None:
         """Overwrite one component (0..5 = Ex..Hz) with ``values`` of shape ``(B, z, y, x)``,
         rounded to the engine's precision. No counterpart in the reference engine."""

@@ -181,6 +181,8 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "oafdtd_wait": (C.c_int, [C.c_void_p]),
     "oafdtd_plane": (C.c_int, [C.c_void_p, _i32, _i32, _pd]),
     "oafdtd_set_plane": (C.c_int, [C.c_void_p, _i32, _i32, _pd]),
+    "oafdtd_plane_device": (C.c_int, [C.c_void_p, _i32, _i32, C.c_void_p]),
+    "oafdtd_set_plane_device": (C.c_int, [C.c_void_p, _i32, _i32, C.c_void_p]),
     "oafdtd_peak_bytes": (C.c_int, [C.c_void_p, _pi64]),
     "oafdtd_set_graph": (C.c_int, [C.c_void_p, _i32]),
     "oafdtd_set_tuning": (C.c_int, [C.c_void_p, _i32, _i32]),

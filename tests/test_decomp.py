@@ -158,8 +158,10 @@ def test_two_gloo_ranks_equal_single_domain() -> None:
 
 # ------------------------------------------------------------------------------- GPU slabs
 @pytest.mark.gpu
+@pytest.mark.parametrize("device", [False, True], ids=["host", "device"])
 @pytest.mark.parametrize("parts", [2, 3])
-def test_gpu_slabs_equal_single_engine(parts: int) -> None:
+def test_gpu_slabs_equal_single_engine(parts: int, device: bool) -> None:
+    """Sub-engines on one GPU, planes exchanged through host float64 or device to device."""
     from open_analysis_gb300.engine import Gb300Engine
 
     c = _via(cpml=6)
@@ -168,7 +170,7 @@ def test_gpu_slabs_equal_single_engine(parts: int) -> None:
     one = Gb300Engine(c, "float32", max_steps=256)
     for k, f in enumerate(fields):
         one.set_field(k, f)
-    local = LocalSlabs(c, parts, lambda sub: Gb300Engine(sub, "float32", max_steps=256))
+    local = LocalSlabs(c, parts, lambda sub: Gb300Engine(sub, "float32", max_steps=256), device=device)
     _scatter(local.slabs, local.engines, fields)
     one.step(20)
     local.step(20)
