@@ -70,8 +70,12 @@ struct oafdtd_materials {
   std::vector<Key> table;
   int pitch = 0;
   std::vector<uint16_t> idx[3];    // storage arrays (nz + 2, ny + 2, pitch)
-  std::vector<int64_t> ade_flat[3];
-  std::vector<double> ade_del[3];  // (n_poles, count) after finalisation
+  // Debye lists per worker and component, in worker (plane) order: [w * 3 + c]; fetch writes them
+  // straight into the caller's buffers
+  std::vector<std::vector<int64_t>> ade_flat;
+  std::vector<std::vector<double>> ade_del;  // (edge, pole) per worker
+  int64_t ade_n[3] = {0, 0, 0};
+  int threads = 1;
 };
 
 namespace {
@@ -222,22 +226,12 @@ int build(oafdtd_materials& m, int threads) {
         for (int64_t e = 0; e < plane; ++e) row[e] = lut[row[e]];
       }
   });
-  // Debye lists: worker lists in worker order = plane order = C order
-  for (int c = 0; c < 3; ++c) {
-    size_t count = 0;
-    for (int w = 0; w < threads; ++w) count += flat[(size_t)w * 3 + c].size();
-    m.ade_flat[c].reserve(count);
-    std::vector<double> rows((size_t)d.n_poles * count);
-    size_t at = 0;
-    for (int w = 0; w < threads; ++w) {
-      const auto& f = flat[(size_t)w * 3 + c];
-      const auto& dl = dels[(size_t)w * 3 + c];
-      m.ade_flat[c].insert(m.ade_flat[c].end(), f.begin(), f.end());
-      for (size_t e = 0; e < f.size(); ++e, ++at)
-        for (int pi = 0; pi < d.n_poles; ++pi) rows[(size_t)pi * count + at] = dl[e * d.n_poles + pi];
-    }
-    m.ade_del[c] = std::move(rows);
-  }
+  // Debye lists stay with their workers (worker order = plane order = C order)
+  m.threads = threads;
+  m.ade_flat = std::move(flat);
+  m.ade_del = std::move(dels);
+  for (int c = 0; c < 3; ++c)
+    for (int w = 0; w < threads; ++w) m.ade_n[c] += (int64_t)m.ade_flat[(size_t)w * 3 + c].size();
   return OAFDTD_OK;
 }
 
@@ -324,7 +318,7 @@ int oafdtd_materials_build(const oafdtd_material_desc* in, oafdtd_materials** ou
 int oafdtd_materials_sizes(const oafdtd_materials* m, int32_t* n_mat, int64_t* ade_n) {
   if (!m || !n_mat || !ade_n) return OAFDTD_E_INVALID;
   *n_mat = (int32_t)m->table.size() + 1;
-  for (int c = 0; c < 3; ++c) ade_n[c] = (int64_t)m->ade_flat[c].size();
+  for (int c = 0; c < 3; ++c) ade_n[c] = m->ade_n[c];
   return OAFDTD_OK;
 }
 
@@ -335,14 +329,26 @@ int oafdtd_materials_fetch(const oafdtd_materials* m, uint16_t* idx0, uint16_t* 
   uint16_t* idx[3] = {idx0, idx1, idx2};
   int64_t* flat[3] = {flat0, flat1, flat2};
   double* del[3] = {del0, del1, del2};
-  for (int c = 0; c < 3; ++c) {
-    std::memcpy(idx[c], m->idx[c].data(), m->idx[c].size() * sizeof(uint16_t));
-    if (!m->ade_flat[c].empty()) {
-      if (!flat[c] || !del[c]) return OAFDTD_E_INVALID;
-      std::memcpy(flat[c], m->ade_flat[c].data(), m->ade_flat[c].size() * sizeof(int64_t));
-      std::memcpy(del[c], m->ade_del[c].data(), m->ade_del[c].size() * sizeof(double));
-    }
-  }
+  for (int c = 0; c < 3; ++c)
+    if (m->ade_n[c] > 0 && (!flat[c] || !del[c])) return OAFDTD_E_INVALID;
+  const int P = m->d.n_poles, T = m->threads;
+  // each worker's segment goes to its own offset: the copies run side by side
+  std::vector<std::thread> pool;
+  for (int w = 0; w < T; ++w)
+    pool.emplace_back([&, w] {
+      for (int c = 0; c < 3; ++c) {
+        if (m->ade_n[c] == 0) continue;
+        int64_t at = 0;
+        for (int v = 0; v < w; ++v) at += (int64_t)m->ade_flat[(size_t)v * 3 + c].size();
+        const auto& f = m->ade_flat[(size_t)w * 3 + c];
+        const auto& dl = m->ade_del[(size_t)w * 3 + c];
+        std::memcpy(flat[c] + at, f.data(), f.size() * sizeof(int64_t));
+        for (size_t e = 0; e < f.size(); ++e)
+          for (int pi = 0; pi < P; ++pi) del[c][(size_t)pi * m->ade_n[c] + at + e] = dl[e * P + pi];
+      }
+    });
+  for (int c = 0; c < 3; ++c) std::memcpy(idx[c], m->idx[c].data(), m->idx[c].size() * sizeof(uint16_t));
+  for (auto& th : pool) th.join();
   eps_tab[0] = 0.0, sig_tab[0] = 0.0;
   for (size_t t = 0; t < m->table.size(); ++t) eps_tab[t + 1] = m->table[t].eps, sig_tab[t + 1] = m->table[t].sig;
   return OAFDTD_OK;
