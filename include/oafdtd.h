@@ -311,6 +311,9 @@ typedef struct oafdtd_material_desc {
   const int64_t* load_lattice;    /* (k * (ny+1) + j) * (nx+1) + i on the component's lattice */
   const double* load_sig;
   int32_t threads;                /* 0: one per hardware thread */
+  double dt;                      /* time step [s] (Debye coefficients) */
+  double eps0;                    /* the vacuum permittivity the caller's tables use [F/m] */
+  const double* taus;             /* n_poles relaxation times [s] */
 } oafdtd_material_desc;
 
 typedef struct oafdtd_materials oafdtd_materials;
@@ -322,12 +325,14 @@ int oafdtd_materials_build(const oafdtd_material_desc* desc, oafdtd_materials** 
 int oafdtd_materials_sizes(const oafdtd_materials* m, int32_t* n_mat, int64_t* ade_n);
 
 /* Copy out: the three uint16 index arrays (nz+2, ny+2, pitch), the eps and sigma tables (n_mat),
- * and per component the dispersive edges' storage flat indices (ade_n[c]) and their averaged
- * pole strengths (n_poles, ade_n[c]); the lists of a component without dispersive edges may be
- * NULL. */
-int oafdtd_materials_fetch(const oafdtd_materials* m, uint16_t* idx0, uint16_t* idx1, uint16_t* idx2, double* eps_tab,
-                           double* sig_tab, int64_t* flat0, int64_t* flat1, int64_t* flat2, double* del0, double* del1,
-                           double* del2);
+ * and per component the dispersive edges' storage flat indices (ade_n[c]), their Debye
+ * coefficients beta_p = eps0 d_p / (tau_p + dt / 2) (n_poles, ade_n[c]; d_p the averaged pole
+ * strength) and cbe = cb of their table entry (ade_n[c]; cb = dt / (eps0 eps) / (1 + sigma dt /
+ * (2 eps0 eps)) as model.py:723-726 writes it). The lists of a component without dispersive edges
+ * may be NULL. The handle's lists are released as they are copied: call it once. */
+int oafdtd_materials_fetch(oafdtd_materials* m, uint16_t* idx0, uint16_t* idx1, uint16_t* idx2, double* eps_tab,
+                           double* sig_tab, int64_t* flat0, int64_t* flat1, int64_t* flat2, double* beta0,
+                           double* beta1, double* beta2, double* cbe0, double* cbe1, double* cbe2);
 
 int oafdtd_materials_free(oafdtd_materials* m);
 

@@ -50,6 +50,8 @@ struct Desc {
   int n_regions = 0, n_poles = 0;
   std::vector<double> reg_eps, reg_sig, reg_del;  // per id (0 = vacuum), reg_del (id, pole)
   std::vector<double> static_fac;
+  double dt = 0.0, eps0 = 0.0;
+  std::vector<double> taus;
   const uint8_t* pec[3] = {nullptr, nullptr, nullptr};
   std::vector<std::vector<std::pair<int64_t, double>>> loads;  // per component, in order
 };
@@ -270,6 +272,14 @@ int oafdtd_materials_build(const oafdtd_material_desc* in, oafdtd_materials** ou
     for (int pi = 0; pi < d.n_poles; ++pi) d.reg_del.push_back(in->reg_strength[(size_t)r * d.n_poles + pi]);
   }
   d.static_fac.assign(in->static_fac, in->static_fac + d.n_poles);
+  d.dt = in->dt;
+  d.eps0 = in->eps0;
+  if (d.n_poles > 0 && !in->taus) {
+    delete m;
+    oafdtd::set_last_error("oafdtd_materials_build: Debye poles without relaxation times");
+    return OAFDTD_E_INVALID;
+  }
+  if (d.n_poles > 0) d.taus.assign(in->taus, in->taus + d.n_poles);
   // region ids: cells whose centre lies in the closed box; later regions overwrite earlier ones
   const int sx = d.n[0] + 2, sy = d.n[1] + 2, sz = d.n[2] + 2;
   d.region.assign((size_t)sx * sy * sz, 0);
@@ -318,39 +328,71 @@ int oafdtd_materials_build(const oafdtd_material_desc* in, oafdtd_materials** ou
 int oafdtd_materials_sizes(const oafdtd_materials* m, int32_t* n_mat, int64_t* ade_n) {
   if (!m || !n_mat || !ade_n) return OAFDTD_E_INVALID;
   *n_mat = (int32_t)m->table.size() + 1;
-  for (int c = 0; c < 3; ++c) ade_n[c] = m->ade_n[c];
+  for (int c = 0; c < 3; ++c) ade_n[c] = m->ade_n[c] < 0 ? -m->ade_n[c] - 1 : m->ade_n[c];
   return OAFDTD_OK;
 }
 
-int oafdtd_materials_fetch(const oafdtd_materials* m, uint16_t* idx0, uint16_t* idx1, uint16_t* idx2, double* eps_tab,
-                           double* sig_tab, int64_t* flat0, int64_t* flat1, int64_t* flat2, double* del0, double* del1,
-                           double* del2) {
+int oafdtd_materials_fetch(oafdtd_materials* m, uint16_t* idx0, uint16_t* idx1, uint16_t* idx2, double* eps_tab,
+                           double* sig_tab, int64_t* flat0, int64_t* flat1, int64_t* flat2, double* beta0,
+                           double* beta1, double* beta2, double* cbe0, double* cbe1, double* cbe2) {
   if (!m || !idx0 || !idx1 || !idx2 || !eps_tab || !sig_tab) return OAFDTD_E_INVALID;
   uint16_t* idx[3] = {idx0, idx1, idx2};
   int64_t* flat[3] = {flat0, flat1, flat2};
-  double* del[3] = {del0, del1, del2};
-  for (int c = 0; c < 3; ++c)
-    if (m->ade_n[c] > 0 && (!flat[c] || !del[c])) return OAFDTD_E_INVALID;
-  const int P = m->d.n_poles, T = m->threads;
-  // each worker's segment goes to its own offset: the copies run side by side
-  std::vector<std::thread> pool;
-  for (int w = 0; w < T; ++w)
-    pool.emplace_back([&, w] {
-      for (int c = 0; c < 3; ++c) {
-        if (m->ade_n[c] == 0) continue;
+  double* beta[3] = {beta0, beta1, beta2};
+  double* cbe[3] = {cbe0, cbe1, cbe2};
+  for (int c = 0; c < 3; ++c) {
+    if (m->ade_n[c] < 0) {
+      oafdtd::set_last_error("oafdtd_materials_fetch: the lists were fetched already");
+      return OAFDTD_E_INVALID;
+    }
+    if (m->ade_n[c] > 0 && (!flat[c] || !beta[c] || !cbe[c])) return OAFDTD_E_INVALID;
+  }
+  const Desc& d = m->d;
+  const int P = d.n_poles, T = m->threads;
+  // the tables, and cb of every entry in the operation order of the NumPy update_coefficients:
+  // ep = eps * eps0; loss = sigma * dt / (2 ep); cb = dt / ep / (1 + loss); the PEC entry 0
+  const size_t n_mat = m->table.size() + 1;
+  std::vector<double> cb(n_mat, 0.0);
+  eps_tab[0] = 0.0, sig_tab[0] = 0.0;
+  for (size_t t = 0; t < m->table.size(); ++t) {
+    const double eps = m->table[t].eps, sig = m->table[t].sig;
+    eps_tab[t + 1] = eps, sig_tab[t + 1] = sig;
+    if (eps > 0) {
+      const double ep = eps * d.eps0;
+      const double loss = sig * d.dt / (2.0 * ep);
+      cb[t + 1] = d.dt / ep / (1.0 + loss);
+    }
+  }
+  std::vector<double> denom(P);
+  for (int pi = 0; pi < P; ++pi) denom[pi] = d.taus[pi] + 0.5 * d.dt;
+  for (int c = 0; c < 3; ++c) std::memcpy(idx[c], m->idx[c].data(), m->idx[c].size() * sizeof(uint16_t));
+  // one component at a time: each worker's segment goes to its own offset (the copies run side by
+  // side), then that component's lists are released, so the lists and their copies never all
+  // coexist
+  for (int c = 0; c < 3; ++c) {
+    if (m->ade_n[c] == 0) continue;
+    std::vector<std::thread> pool;
+    for (int w = 0; w < T; ++w)
+      pool.emplace_back([&, w, c] {
         int64_t at = 0;
         for (int v = 0; v < w; ++v) at += (int64_t)m->ade_flat[(size_t)v * 3 + c].size();
         const auto& f = m->ade_flat[(size_t)w * 3 + c];
         const auto& dl = m->ade_del[(size_t)w * 3 + c];
         std::memcpy(flat[c] + at, f.data(), f.size() * sizeof(int64_t));
-        for (size_t e = 0; e < f.size(); ++e)
-          for (int pi = 0; pi < P; ++pi) del[c][(size_t)pi * m->ade_n[c] + at + e] = dl[e * P + pi];
-      }
-    });
-  for (int c = 0; c < 3; ++c) std::memcpy(idx[c], m->idx[c].data(), m->idx[c].size() * sizeof(uint16_t));
-  for (auto& th : pool) th.join();
-  eps_tab[0] = 0.0, sig_tab[0] = 0.0;
-  for (size_t t = 0; t < m->table.size(); ++t) eps_tab[t + 1] = m->table[t].eps, sig_tab[t + 1] = m->table[t].sig;
+        const uint16_t* ic = idx[c];
+        for (size_t e = 0; e < f.size(); ++e) {
+          cbe[c][at + e] = cb[ic[f[e]]];
+          for (int pi = 0; pi < P; ++pi)
+            beta[c][(size_t)pi * m->ade_n[c] + at + e] = d.eps0 * dl[e * P + pi] / denom[pi];
+        }
+      });
+    for (auto& th : pool) th.join();
+    for (int w = 0; w < T; ++w) {
+      std::vector<int64_t>().swap(m->ade_flat[(size_t)w * 3 + c]);
+      std::vector<double>().swap(m->ade_del[(size_t)w * 3 + c]);
+    }
+    m->ade_n[c] = -m->ade_n[c] - 1;  // fetched: the lists are gone
+  }
   return OAFDTD_OK;
 }
 

@@ -555,9 +555,10 @@ def _native_materials(
     pec: list[npt.NDArray[np.bool_]],
     loads: list[tuple[int, int, float]],
     threads: int = 0,
-) -> tuple[list[npt.NDArray[np.uint16]], FloatArray, FloatArray, list[int], list[Any], list[FloatArray]]:
+) -> tuple[list[npt.NDArray[np.uint16]], FloatArray, FloatArray, list[int], list[Any], list[FloatArray], list[FloatArray]]:
     """The volume stages on the engine library's native compiler: index arrays, eps and sigma
-    tables, and per dispersive component its storage flat indices and averaged pole strengths."""
+    tables, and per dispersive component its storage flat indices, Debye coefficients beta
+    ``(poles, n)`` and the ``cb`` of each edge."""
     import ctypes as C
 
     from open_analysis_gb300 import native as nat
@@ -603,6 +604,9 @@ def _native_materials(
     d.load_lattice = lat.ctypes.data_as(C.POINTER(C.c_int64))
     d.load_sig = sig.ctypes.data_as(C.POINTER(C.c_double))
     d.threads = int(threads)
+    d.dt = float(dt)
+    d.eps0 = float(EPS0)
+    d.taus = dp(taus if n_poles else [0.0])
     handle = C.c_void_p()
     rc = lib.oafdtd_materials_build(C.byref(d), C.byref(handle))
     if rc == nat.E_TABLE:
@@ -619,24 +623,28 @@ def _native_materials(
         idx = [np.zeros(g.shape, dtype=np.uint16) for _ in range(3)]
         eps_tab = np.zeros(n_mat.value)
         sig_tab = np.zeros(n_mat.value)
-        flats = [np.zeros(int(ade_n[c]), dtype=np.int64) for c in range(3)]
-        dels = [np.zeros((n_poles, int(ade_n[c]))) for c in range(3)]
+        flats = [np.empty(int(ade_n[c]), dtype=np.int64) for c in range(3)]
+        betas = [np.empty((n_poles, int(ade_n[c]))) for c in range(3)]
+        cbes = [np.empty(int(ade_n[c])) for c in range(3)]
         u16 = C.POINTER(C.c_uint16)
+        dpp = C.POINTER(C.c_double)
         nat.check(
             lib.oafdtd_materials_fetch(
                 handle,
                 *(a.ctypes.data_as(u16) for a in idx),
-                eps_tab.ctypes.data_as(C.POINTER(C.c_double)),
-                sig_tab.ctypes.data_as(C.POINTER(C.c_double)),
+                eps_tab.ctypes.data_as(dpp),
+                sig_tab.ctypes.data_as(dpp),
                 *(f.ctypes.data_as(C.POINTER(C.c_int64)) if f.size else None for f in flats),
-                *(x.ctypes.data_as(C.POINTER(C.c_double)) if x.size else None for x in dels),
+                *(x.ctypes.data_as(dpp) if x.size else None for x in betas),
+                *(x.ctypes.data_as(dpp) if x.size else None for x in cbes),
             ),
             "oafdtd_materials_fetch",
         )
     finally:
         lib.oafdtd_materials_free(handle)
     comps = [c for c in range(3) if flats[c].size]
-    return idx, eps_tab, sig_tab, comps, [flats[c] for c in comps], [dels[c] for c in comps]
+    return (idx, eps_tab, sig_tab, comps, [flats[c] for c in comps], [betas[c] for c in comps],
+            [cbes[c] for c in comps])
 
 
 def compile_model(model: Model, dtype: str = "float32", native: bool | None = None) -> Compiled:
@@ -841,19 +849,13 @@ def compile_model(model: Model, dtype: str = "float32", native: bool | None = No
         probes.append({"name": pr.name, "kind": pr.kind, "comp": pr.axis, "flat": flat, "weights": w})
 
     if native:
-        idx, eps_tab, sig_tab, comps, flats, dels = _native_materials(model, g, dt, taus, pec, loads)
+        idx, eps_tab, sig_tab, comps, flats, betas, cbes = _native_materials(model, g, dt, taus, pec, loads)
         ca_tab, cb_tab = update_coefficients(eps_tab, sig_tab, dt)
         ade = None
         if taus.size and comps:
             tau = np.asarray(taus, dtype=np.float64)
-            ade = AdeData(
-                kp=(1.0 - 0.5 * dt / tau) / (1.0 + 0.5 * dt / tau),
-                tau=tau,
-                comp=comps,
-                flat=flats,
-                beta=[np.stack([EPS0 * dl[p] / (tau[p] + 0.5 * dt) for p in range(tau.size)]) for dl in dels],
-                cbe=[cb_tab[idx[c].ravel()[f]] for c, f in zip(comps, flats, strict=True)],
-            )
+            ade = AdeData(kp=(1.0 - 0.5 * dt / tau) / (1.0 + 0.5 * dt / tau), tau=tau, comp=comps, flat=flats,
+                          beta=betas, cbe=cbes)
     else:
         idx, eps_tab, sig_tab = _material_table(g, edge_eps, edge_sig, pec)
         ca_tab, cb_tab = update_coefficients(eps_tab, sig_tab, dt)

@@ -153,6 +153,9 @@ class MaterialDesc(C.Structure):
         ("load_lattice", _pi64),
         ("load_sig", _pd),
         ("threads", _i32),
+        ("dt", _d),
+        ("eps0", _d),
+        ("taus", _pd),
     ]
 
 
@@ -195,7 +198,7 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     # native model compiler (host pointers)
     "oafdtd_materials_build": (C.c_int, [C.POINTER(MaterialDesc), C.POINTER(C.c_void_p)]),
     "oafdtd_materials_sizes": (C.c_int, [C.c_void_p, _pi32, _pi64]),
-    "oafdtd_materials_fetch": (C.c_int, [C.c_void_p] + [C.POINTER(C.c_uint16)] * 3 + [_pd, _pd] + [_pi64] * 3 + [_pd] * 3),
+    "oafdtd_materials_fetch": (C.c_int, [C.c_void_p] + [C.POINTER(C.c_uint16)] * 3 + [_pd, _pd] + [_pi64] * 3 + [_pd] * 6),
     "oafdtd_materials_free": (C.c_int, [C.c_void_p]),
     # surrogate kernels (device pointers as void*)
     "oafdtd_mlp_gemm": (

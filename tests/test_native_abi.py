@@ -130,7 +130,7 @@ int main(void) {
   d.nx = NX; d.ny = NY; d.nz = NZ;
   for (int a = 0; a < 3; ++a) { d.cell_w[a] = w[a]; d.centres[a] = c[a]; d.pec[a] = pec[a]; }
   d.n_regions = 1; d.reg_lo = lo; d.reg_hi = hi; d.reg_eps = &eps; d.reg_sig = &sig;
-  d.n_poles = 0; d.threads = 2;
+  d.n_poles = 0; d.threads = 2; d.dt = 1e-12; d.eps0 = 8.854e-12;
   oafdtd_materials* m = NULL;
   if (oafdtd_materials_build(&d, &m) != 0) { printf("build failed %s\n", oafdtd_last_error()); return 1; }
   int32_t nmat; int64_t ade[3];
@@ -140,7 +140,7 @@ int main(void) {
   uint16_t* idx[3];
   for (int a = 0; a < 3; ++a) idx[a] = calloc(st, 2);
   double et[16], stab[16];
-  oafdtd_materials_fetch(m, idx[0], idx[1], idx[2], et, stab, NULL, NULL, NULL, NULL, NULL, NULL);
+  oafdtd_materials_fetch(m, idx[0], idx[1], idx[2], et, stab, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL);
   oafdtd_materials_free(m);
   long zeros = 0, max_id = 0;
   for (int k = 1; k <= NZ + 1; ++k)
