@@ -237,13 +237,14 @@ def _sum_dicts(parts: Sequence[dict[str, Any]]) -> dict[str, Any]:
     return out
 
 
-def _plane_buffers(engine: Any, comps: Sequence[int]) -> dict[int, Any]:
-    """One device buffer per component for a plane of ``engine`` (its precision and shape)."""
+def _plane_buffers(engine: Any, comps: Sequence[int], device: str = "cuda") -> dict[int, Any]:
+    """One buffer per component for a plane of ``engine`` (its precision and shape), on
+    ``device`` (the GPU; ``"cpu"`` only for the host tests of the exchange logic)."""
     import torch
 
     dtype = torch.float32 if engine.dtype == "float32" else torch.float64
     shape = (engine.B, engine.shape[2], engine.shape[3])
-    return {comp: torch.empty(shape, dtype=dtype, device="cuda") for comp in comps}
+    return {comp: torch.empty(shape, dtype=dtype, device=device) for comp in comps}
 
 
 class LocalSlabs:
@@ -315,7 +316,8 @@ class DistSlabs:
     GPU per rank (``torch.cuda.set_device`` and ``native.set_device`` to the local rank before the
     engine is built). The device mode needs two GPUs and is not run here."""
 
-    def __init__(self, c: Compiled, factory: Callable[[Compiled], Any], device: bool = False) -> None:
+    def __init__(self, c: Compiled, factory: Callable[[Compiled], Any], device: bool = False,
+                 buffer_device: str = "cuda") -> None:
         import torch.distributed as dist
 
         self.dist = dist
@@ -325,9 +327,10 @@ class DistSlabs:
         self.slab = self.slabs[self.rank]
         self.engine = factory(self.slab.c)
         self.device = device
+        self._on_gpu = buffer_device.startswith("cuda")
         if device:
-            self._send = _plane_buffers(self.engine, (HX, HY, EX, EY))
-            self._recv = _plane_buffers(self.engine, (HX, HY, EX, EY))
+            self._send = _plane_buffers(self.engine, (HX, HY, EX, EY), buffer_device)
+            self._recv = _plane_buffers(self.engine, (HX, HY, EX, EY), buffer_device)
 
     def _swap_device(self, send_to: int | None, send: list[tuple[int, int]], recv_from: int | None,
                      recv: list[tuple[int, int]]) -> None:
@@ -346,7 +349,8 @@ class DistSlabs:
         if ops:
             for req in self.dist.batch_isend_irecv(ops):
                 req.wait()
-        torch.cuda.synchronize()  # the received planes are complete before the engine reads them
+        if self._on_gpu:
+            torch.cuda.synchronize()  # the received planes are complete before the engine reads them
         if recv_from is not None:
             for comp, k in recv:
                 e.plane_from_device(comp, k, self._recv[comp].data_ptr())

@@ -109,7 +109,30 @@ def _free_port() -> int:
         return int(s.getsockname()[1])
 
 
-def _rank_main(rank: int, world: int, port: int, out) -> None:  # type: ignore[no-untyped-def]
+class _PointerPlanes(OracleEngine):
+    """The oracle with the device-plane entry points of ``Gb300Engine`` over host memory: the
+    plane is written to / read from the buffer at an address, in the engine's precision."""
+
+    def __init__(self, c, dtype):  # type: ignore[no-untyped-def]
+        super().__init__(c, dtype)
+        self.B = self.E[0].shape[0]
+        self.shape = self.E[0].shape
+
+    def _view(self, addr: int):  # type: ignore[no-untyped-def]
+        import ctypes
+
+        n = self.B * self.shape[2] * self.shape[3]
+        ctype = ctypes.c_float if np.dtype(self.dtype) == np.float32 else ctypes.c_double
+        return np.ctypeslib.as_array((ctype * n).from_address(addr)).reshape(self.B, self.shape[2], self.shape[3])
+
+    def plane_to_device(self, comp: int, k: int, dst: int) -> None:
+        self._view(dst)[...] = (self.E + self.H)[comp][:, k]
+
+    def plane_from_device(self, comp: int, k: int, src: int) -> None:
+        (self.E + self.H)[comp][:, k] = self._view(src)
+
+
+def _rank_main(rank: int, world: int, port: int, out, device: bool = False) -> None:  # type: ignore[no-untyped-def]
     import torch.distributed as dist
 
     from open_analysis_gb300.decomp import DistSlabs
@@ -117,7 +140,10 @@ def _rank_main(rank: int, world: int, port: int, out) -> None:  # type: ignore[n
     dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
     try:
         c = _via()
-        run = DistSlabs(c, lambda sub: OracleEngine(sub, "float32"))
+        if device:  # the device-buffer exchange (NCCL's form) with host buffers under gloo
+            run = DistSlabs(c, lambda sub: _PointerPlanes(sub, "float32"), device=True, buffer_device="cpu")
+        else:
+            run = DistSlabs(c, lambda sub: OracleEngine(sub, "float32"))
         ref = OracleEngine(c, "float32")
         fields = _random_fields(ref)
         s, e = run.slab, run.engine
@@ -141,13 +167,14 @@ def _rank_main(rank: int, world: int, port: int, out) -> None:  # type: ignore[n
         dist.destroy_process_group()
 
 
-def test_two_gloo_ranks_equal_single_domain() -> None:
+@pytest.mark.parametrize("device", [False, True], ids=["host", "device-buffers"])
+def test_two_gloo_ranks_equal_single_domain(device: bool) -> None:
     import torch.multiprocessing as mp
 
     ctx = mp.get_context("spawn")
     out = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, out)) for r in range(2)]
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, out, device)) for r in range(2)]
     for p in procs:
         p.start()
     got = dict(out.get(timeout=300) for _ in procs)
