@@ -95,9 +95,11 @@ def write_wire(
     directory: Path, stem: str, model: Model, s_nnf: np.ndarray, res: RunResult, wall_build_s: float, wall_run_s: float
 ) -> dict[str, str]:
     """The worker's files in ``directory``: ``ports.npz`` (freqs, s (F, N, N), z0, names),
-    ``run.json`` and a Touchstone file. Returns their paths."""
+    ``run.json`` and a Touchstone file. Returns their paths. ``z0`` is the run's port resistances
+    (the lumped ports' R, the mode ports' modal impedance), as the reference's adapter takes it
+    (``adapter/sim.py:194``)."""
     names = [p.name for p in model.ports]
-    z0 = np.array([float(getattr(p, "r_ohm", 50.0)) for p in model.ports])
+    z0 = np.asarray(res.port_r, dtype=np.float64)
     s_fnn = np.moveaxis(np.asarray(s_nnf), -1, 0)
     freqs = np.asarray(model.frequencies, dtype=np.float64)
     directory.mkdir(parents=True, exist_ok=True)

@@ -88,3 +88,21 @@ def test_job_on_the_gpu_matches_the_oracle(tmp_path: Path) -> None:
     assert gpu["engine"] == "gb300" and gpu["steps"] == cpu["steps"]
     s_gpu, s_cpu = np.load(gpu["output"])["s"], np.load(cpu["output"])["s"]
     assert np.abs(s_gpu - s_cpu).max() < 1e-9  # the same float32 fields; DFT rounding only
+
+
+def test_wire_files_carry_the_modal_impedance(tmp_path: Path) -> None:
+    """Mode ports: the worker's z0 is the modal impedance of each port (the run's port_r)."""
+    import sys
+
+    sys.path.insert(0, str(GOLDEN.parent))
+    from cases import CASES, namespace
+
+    from open_analysis_gb300.jobs import write_wire
+    from open_analysis_gb300.run import run, sparams
+
+    m = CASES["mode_stripline"][0](namespace("gb300"))
+    res = run(m, engine=OracleEngine, dtype="float32", max_steps=64, end_db=None)
+    paths = write_wire(tmp_path, "modes", m, sparams(m, res), res, 0.0, 0.0)
+    wire = np.load(paths["wire"])
+    assert np.array_equal(wire["z0"], res.port_r) and abs(wire["z0"][0] - 55.77) < 0.01
+    assert "R 55.77" in Path(paths["touchstone"]).read_text() or "55.77" in Path(paths["touchstone"]).read_text()
