@@ -54,6 +54,7 @@ def main(reference_root: str) -> None:
         print(name, "steps", steps, "batch", c.batch, "keys", len(data))
     debye_fits(np)
     touchstone_files(np)
+    tail_fits(np)
 
 
 def wave_fixture(np, model, c, engine_cls, steps, data):  # type: ignore[no-untyped-def]
@@ -77,6 +78,38 @@ def wave_fixture(np, model, c, engine_cls, steps, data):  # type: ignore[no-unty
     data["wave.gamma"] = np.stack(gammas)
     for ps_i, ps in enumerate(model.plane_sets):
         data[f"wave.planes{ps_i}"] = np.array([ps.spacing, ps.ref, ps.spacing_b if ps.spacing_b is not None else np.nan])
+
+
+def tail_series(np):  # type: ignore[no-untyped-def]
+    """Synthetic probe series for the matrix-pencil tail: (name, y, dt, t_first, f_band)."""
+    dt = 1e-12
+    n = 9000
+    t = 1e-9 + np.arange(n) * dt
+    two = 0.8 * np.exp(-t / 0.9e-9) * np.cos(2 * np.pi * 7.1e9 * t + 0.3) + 0.35 * np.exp(-t / 0.6e-9) * np.sin(
+        2 * np.pi * 12.4e9 * t)
+    grow = two + 1e-3 * np.exp(t / 3e-9) * np.cos(2 * np.pi * 45e9 * t)  # growing, out of the band
+    quiet = 1e-14 * np.cos(2 * np.pi * 5e9 * t) + np.where(t < 1.2e-9, 1.0, 0.0)  # tail below noise
+    return [("two_modes", two, dt, 1e-9, 20e9), ("growing_out_of_band", grow, dt, 1e-9, 20e9),
+            ("below_noise", quiet, dt, 1e-9, 20e9)]
+
+
+def tail_fits(np):  # type: ignore[no-untyped-def]
+    """The reference's matrix-pencil tail fits and their DFT continuations on synthetic series."""
+    from oa_fdtd.tail import extrapolate_dft, fit_tail  # type: ignore[import-not-found]
+
+    out = {}
+    freqs = np.linspace(1e9, 20e9, 12)
+    for name, y, dt, t0, fb in tail_series(np):
+        fit = fit_tail(y, dt, t0, f_band=fb)
+        out[f"{name}.none"] = np.array(fit is None)
+        if fit is None:
+            continue
+        out[f"{name}.s"] = fit.s
+        out[f"{name}.c"] = fit.c
+        out[f"{name}.meta"] = np.array([fit.t_ref, fit.n_dropped, fit.residual])
+        out[f"{name}.dft"] = extrapolate_dft(fit, dt, t0 + y.size * dt, freqs)
+    np.savez(HERE / "tail_fits.npz", **out)
+    print("tail fits", len(out))
 
 
 # Djordjevic-Sarkar materials fitted by the reference's multi-pole Debye fit:
