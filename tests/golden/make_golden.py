@@ -55,6 +55,7 @@ def main(reference_root: str) -> None:
     debye_fits(np)
     touchstone_files(np)
     tail_fits(np)
+    run_loops(np)
 
 
 def wave_fixture(np, model, c, engine_cls, steps, data):  # type: ignore[no-untyped-def]
@@ -110,6 +111,34 @@ def tail_fits(np):  # type: ignore[no-untyped-def]
         out[f"{name}.dft"] = extrapolate_dft(fit, dt, t0 + y.size * dt, freqs)
     np.savez(HERE / "tail_fits.npz", **out)
     print("tail fits", len(out))
+
+
+RUNS = {
+    # case: run() keyword arguments (float64 NumPy engine)
+    "microstrip": {"max_steps": 6000, "end_db": -40.0},
+    "mode_stripline": {"max_steps": 1500, "end_db": -60.0, "tail": True},
+}
+
+
+def run_loops(np):  # type: ignore[no-untyped-def]
+    """The reference's own run loop (engine "numpy", float64) on two cases: the step count, why it
+    stopped, the energy level, the S-parameters, and the tail continuation where it applies."""
+    from cases import CASES, namespace  # type: ignore[import-not-found]
+    from oa_fdtd.run import run, sparams  # type: ignore[import-not-found]
+
+    out = {}
+    for name, kw in RUNS.items():
+        m = CASES[name][0](namespace("ref"))
+        res = run(m, engine="numpy", dtype="float64", **kw)
+        out[f"{name}.steps"] = np.array(res.steps)
+        out[f"{name}.stopped_by"] = np.array(res.stopped_by)
+        out[f"{name}.energy_db"] = np.array(res.energy_db)
+        out[f"{name}.s"] = sparams(m, res)
+        for k, v in sorted((res.tail or {}).items()):
+            if isinstance(v, (int, float, bool)) or (isinstance(v, np.ndarray) and v.dtype.kind in "biufc"):
+                out[f"{name}.tail.{k}"] = np.asarray(v)
+    np.savez(HERE / "run_loops.npz", **out)
+    print("run loops", sorted(out))
 
 
 # Djordjevic-Sarkar materials fitted by the reference's multi-pole Debye fit:
