@@ -124,7 +124,8 @@ def run_loops(np):  # type: ignore[no-untyped-def]
     """The reference's own run loop (engine "numpy", float64) on two cases: the step count, why it
     stopped, the energy level, the S-parameters, and the tail continuation where it applies."""
     from cases import CASES, namespace  # type: ignore[import-not-found]
-    from oa_fdtd.run import run, sparams  # type: ignore[import-not-found]
+    from oa_fdtd.ports.deembed import wave_sparams  # type: ignore[import-not-found]
+    from oa_fdtd.run import port_voltage_factor, run, sparams  # type: ignore[import-not-found]
 
     out = {}
     for name, kw in RUNS.items():
@@ -134,6 +135,12 @@ def run_loops(np):  # type: ignore[no-untyped-def]
         out[f"{name}.stopped_by"] = np.array(res.stopped_by)
         out[f"{name}.energy_db"] = np.array(res.energy_db)
         out[f"{name}.s"] = sparams(m, res)
+        if hasattr(m, "plane_sets"):  # wave planes with the port S fallback and gamma smoothing
+            fac = port_voltage_factor(res.dt, m.frequencies)
+            probes = {k: v * fac for k, v in res.probes.items()}
+            sw, gam = wave_sparams(probes, m.plane_sets, res.port_r, s_port=out[f"{name}.s"], freqs=m.frequencies)
+            out[f"{name}.wave_s"] = sw
+            out[f"{name}.wave_gamma"] = np.stack(gam)
         for k, v in sorted((res.tail or {}).items()):
             if isinstance(v, (int, float, bool)) or (isinstance(v, np.ndarray) and v.dtype.kind in "biufc"):
                 out[f"{name}.tail.{k}"] = np.asarray(v)

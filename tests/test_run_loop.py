@@ -37,6 +37,15 @@ def test_run_loop_matches_the_reference(case: str) -> None:
     fin = np.isfinite(want)
     assert np.array_equal(np.isfinite(s), fin)
     assert np.abs(s[fin] - want[fin]).max() <= 1e-10 * max(1.0, np.abs(want[fin]).max())
+    if f"{case}.wave_s" in ref.files:  # wave planes with the port S fallback and gamma smoothing
+        from open_analysis_gb300.deembed import wave_sparams
+        from open_analysis_gb300.run import port_voltage_factor
+
+        fac = port_voltage_factor(res.dt, m.frequencies)
+        probes = {k: v * fac for k, v in res.probes.items()}
+        sw, gam = wave_sparams(probes, m.plane_sets, res.port_r, s_port=s, freqs=m.frequencies)
+        np.testing.assert_allclose(np.stack(gam), ref[f"{case}.wave_gamma"], rtol=1e-8)
+        np.testing.assert_allclose(sw, ref[f"{case}.wave_s"], rtol=1e-8, atol=1e-10)
     for key in [k for k in ref.files if k.startswith(f"{case}.tail.")]:
         got = (res.tail or {})[key.rsplit(".", 1)[1]]
         np.testing.assert_allclose(np.asarray(got, dtype=np.float64), ref[key].astype(np.float64), rtol=1e-6, err_msg=key)
