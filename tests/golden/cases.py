@@ -139,6 +139,37 @@ CASES = {
 }
 
 
+def job_dict() -> dict[str, Any]:
+    """An engine-level job in the reference's CLI format using every key it reads: graded grid
+    lines, walls with CPML and PMC, a CPML spec, the Courant number, a lossy dielectric and a PEC
+    region, two lumped ports (one with a sign), a soft source, E and H probes with each weight."""
+    x = graded(0.012, 18, 1.02).tolist()
+    y = graded(0.010, 14, 1.0).tolist()
+    z = graded(0.006, 12, 0.98).tolist()
+    return {
+        "grid": {"x": x, "y": y, "z": z},
+        "waveform": {"kind": "gauss_mod", "f0": 8e9, "bandwidth": 12e9},
+        "frequencies": np.linspace(2e9, 14e9, 5).tolist(),
+        "walls": ["cpml", "cpml", "pmc", "pmc", "pec", "cpml"],
+        "cpml": {"cells": 4, "m": 3.0, "kappa_max": 4.0},
+        "courant": 0.9,
+        "regions": [
+            {"lo": [-1, -1, 0.0], "hi": [1, 1, 0.002], "eps_r": 3.7, "sigma": 0.01},
+            {"lo": [0.004, 0.003, 0.002], "hi": [0.008, 0.007, 0.002], "pec": True},
+        ],
+        "ports": [
+            {"name": "a", "axis": 2, "lo": [0.004, 0.005, 0.0], "hi": [0.004, 0.005, 0.002], "r_ohm": 50.0},
+            {"name": "b", "axis": 2, "lo": [0.008, 0.005, 0.0], "hi": [0.008, 0.005, 0.002], "r_ohm": 35.0, "sign": -1.0},
+        ],
+        "sources": [{"name": "s", "axis": 1, "lo": [0.006, 0.005, 0.003], "hi": [0.006, 0.005, 0.003], "amplitude": 0.5}],
+        "probes": [
+            {"name": "e_line", "kind": "E", "axis": 2, "lo": [0.006, 0.005, 0.0], "hi": [0.006, 0.005, 0.002], "weight": "line"},
+            {"name": "h_mean", "kind": "H", "axis": 0, "lo": [0.005, 0.004, 0.003], "hi": [0.007, 0.006, 0.003], "weight": "mean"},
+            {"name": "e_sum", "kind": "E", "axis": 0, "lo": [0.006, 0.005, 0.004], "hi": [0.006, 0.005, 0.004]},
+        ],
+    }
+
+
 def namespace(module_root: str) -> Any:
     """Problem types of ``open_analysis_gb300`` (``module_root="gb300"``) or of the reference
     package (``module_root="ref"``, importable only where the reference is present)."""

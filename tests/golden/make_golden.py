@@ -56,6 +56,7 @@ def main(reference_root: str) -> None:
     touchstone_files(np)
     tail_fits(np)
     run_loops(np)
+    job_parse(np)
 
 
 def wave_fixture(np, model, c, engine_cls, steps, data):  # type: ignore[no-untyped-def]
@@ -111,6 +112,19 @@ def tail_fits(np):  # type: ignore[no-untyped-def]
         out[f"{name}.dft"] = extrapolate_dft(fit, dt, t0 + y.size * dt, freqs)
     np.savez(HERE / "tail_fits.npz", **out)
     print("tail fits", len(out))
+
+
+def job_parse(np):  # type: ignore[no-untyped-def]
+    """The reference's CLI job parser and compiler on ``cases.job_dict()``: the compiled
+    fingerprint."""
+    from cases import job_dict  # type: ignore[import-not-found]
+    from fingerprint import compiled_fingerprint, save  # type: ignore[import-not-found]
+    from oa_fdtd.cli import model_from_job  # type: ignore[import-not-found]
+    from oa_fdtd.model import compile_model  # type: ignore[import-not-found]
+
+    c = compile_model(model_from_job(job_dict()), "float32")
+    save(str(HERE / "job_parse.npz"), compiled_fingerprint(c))
+    print("job parse", c.grid.n)
 
 
 RUNS = {

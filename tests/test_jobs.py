@@ -106,3 +106,19 @@ def test_wire_files_carry_the_modal_impedance(tmp_path: Path) -> None:
     wire = np.load(paths["wire"])
     assert np.array_equal(wire["z0"], res.port_r) and abs(wire["z0"][0] - 55.77) < 0.01
     assert "R 55.77" in Path(paths["touchstone"]).read_text() or "55.77" in Path(paths["touchstone"]).read_text()
+
+
+def test_job_parser_matches_the_reference_cli() -> None:
+    """``model_from_job`` on a job using every key of the reference's format compiles to the
+    reference's arrays bit for bit (fixture from the reference's ``oa_fdtd.cli.model_from_job``)."""
+    import sys
+
+    sys.path.insert(0, str(GOLDEN.parent))
+    from cases import job_dict
+    from fingerprint import compare_compiled, compiled_fingerprint, load
+
+    from open_analysis_gb300.model import compile_model
+
+    ref = load(str(GOLDEN.parent / "job_parse.npz"))
+    mine = compiled_fingerprint(compile_model(model_from_job(job_dict()), "float32"))
+    assert compare_compiled(ref, mine) == []
