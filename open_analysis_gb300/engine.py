@@ -22,20 +22,76 @@ FloatArray = npt.NDArray[np.float64]
 CHUNK = 64
 
 
-def estimate_bytes(c: Any, itemsize: int) -> int:
-    """Device bytes of a problem: fields, the index, CPML psi, ADE and SIBC state, plus 5 %
-    (the reference's estimate, ``engine.py:29-40``, which the run driver checks before creating
-    the engine)."""
-    cells = int(np.prod(c.grid.shape))
-    psi = sum(int(np.prod(k.shape)) for k in c.pml.corrections) * c.batch * itemsize
-    extra = 0
+def estimate_bytes(c: Any, itemsize: int, max_steps: int = 200_000, record_series: bool = False) -> int:
+    """Device bytes ``Gb300Engine`` allocates for a compiled problem: the role of the reference's
+    ``estimate_bytes`` (``engine.py:29-40``), which the run driver checks against free device
+    memory before it builds the engine, counted from this engine's own buffers.
+
+    * six field arrays ``(B, Z, Y, X)`` twice (the fused sweep, the default wherever the grid has
+      an interior free of CPML cells, reads one set and writes the other) and the three uint16
+      index arrays ``(Z, Y, X)``;
+    * dense Debye currents ``(P, B, nk, Y, X)`` per component over the z range ``nk`` of its
+      dispersive edges;
+    * one CPML psi array per correction: the slab width on its derivative axis, the full storage
+      extent on the other two, per batch member;
+    * surface impedance: a packed record per edge (32 bytes in float32, 48 in float64),
+      ``J_prev (B, n)`` and ``v (P, B, n)``;
+    * the edge list of injection targets and deferred Debye edges with their saved ``E^n``, the
+      sampled wave table ``(channels, max_steps)``, the probe lists, the DFT accumulators
+      ``(probes, B, F)`` complex128 and, when recording, the series ``(probes, B, max_steps)``;
+    * the one-dimensional metrics, CPML coefficients, energy weights and partial sums, which are
+      small; a fixed 1 MiB covers them and the per-allocation minimums.
+    """
+    g = c.grid
+    Z, Y, X = g.shape
+    B = int(c.batch)
+    bs = Z * Y * X
+    rb = int(itemsize)
+    total = 2 * 6 * bs * B * rb + 3 * bs * 2
+    ade_flat: list[np.ndarray] = [np.zeros(0, np.int64)] * 3
     if c.ade is not None:
-        ne = sum(f.size for f in c.ade.flat)
-        extra += ne * (c.ade.tau.size * (c.batch + 1) + c.batch + 2) * itemsize
+        P = int(c.ade.tau.size)
+        for comp, flat in zip(c.ade.comp, c.ade.flat, strict=True):
+            fl = np.asarray(flat, np.int64)
+            if fl.size == 0:
+                continue
+            ade_flat[int(comp)] = fl
+            k = fl // (Y * X)
+            total += P * B * int(k.max() - k.min() + 1) * Y * X * rb
+    for corr in c.pml.corrections:
+        ext = [X, Y, Z]
+        ext[corr.a] = corr.box[corr.a][1] - corr.box[corr.a][0]
+        total += B * ext[0] * ext[1] * ext[2] * rb
+    none = np.zeros(0, np.int64)
+    sibc_t = [none] * 3  # per component: surface-impedance edges and injection targets
+    inj_t: list[list[np.ndarray]] = [[], [], []]
     if c.sibc is not None:
-        ne = c.sibc.flat.size
-        extra += ne * (c.batch * (1 + c.sibc.cp.size) * itemsize + 2 * (4 + 8 + itemsize))
-    return int((cells * (6 * itemsize * c.batch + 6) + psi + extra) * 1.05)
+        s = c.sibc
+        n_s = int(s.flat.size)
+        total += n_s * (32 if rb == 4 else 48) + B * n_s * rb * (1 + int(s.cp.size))
+        sibc_t = [np.asarray(s.flat, np.int64)[np.asarray(s.comp) == cc] for cc in range(3)]
+    n_inj = 0
+    for ch in c.channels:
+        fl = np.asarray(ch["flat"], np.int64)
+        comp = np.broadcast_to(np.asarray(ch["comp"]), fl.shape)
+        n_inj += fl.size
+        for cc in range(3):
+            inj_t[cc].append(fl[comp == cc])
+    inj_edges = n_def = 0
+    for cc in range(3):
+        inj = np.unique(np.concatenate(inj_t[cc] or [none]))
+        inj_edges += inj.size
+        n_def += int(np.isin(ade_flat[cc], np.concatenate([sibc_t[cc], inj])).sum())
+    n_list = inj_edges + n_def
+    total += n_list * (1 + 8 + 3 * 4) + n_inj * (4 + 8) + n_def * (8 + 1 + B * rb)
+    n_chan = len(c.channels)
+    total += n_chan * max_steps * 8 + B * n_chan * 8
+    n_probe = len(c.probes)
+    total += sum(np.asarray(q["flat"]).size for q in c.probes) * 16 + n_probe * 16
+    total += n_probe * B * int(c.frequencies.size) * 16
+    if record_series:
+        total += n_probe * B * max_steps * 8
+    return int(total + (1 << 20))
 
 
 def wave_table(c: Any, max_steps: int) -> FloatArray:
@@ -56,6 +112,122 @@ def wave_table(c: Any, max_steps: int) -> FloatArray:
 
 def _ptr(a: np.ndarray, ctype: Any) -> Any:
     return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def describe(c: Any, dtype: str = "float32", max_steps: int = 200_000,
+             record_series: bool = False) -> tuple[native.Problem, list[Any]]:
+    """The ``oafdtd_problem`` descriptor of a compiled problem: the ``Compiled`` arrays
+    (``oa_fdtd/model.py:246-269``) flattened into the plain pointers and sizes of the C ABI, with
+    the host buffers they point into (keep them alive until ``oafdtd_create`` returns). It reads
+    only the attributes the reference's ``Compiled`` has, so a problem compiled by the reference
+    goes through unchanged."""
+    g = c.grid
+    keep: list[Any] = []
+
+    def arr(a: Any, dt: Any) -> np.ndarray:
+        out = np.ascontiguousarray(np.asarray(a, dtype=dt))
+        keep.append(out)
+        return out
+
+    p = native.Problem()
+    p.abi_version = native.ABI_VERSION
+    p.real_bytes = 4 if dtype == "float32" else 8
+    p.nx, p.ny, p.nz = g.n
+    p.pitch = g.pitch
+    p.batch = c.batch
+    p.dt = float(c.dt)
+    p.dtmu = float(c.dt / MU0)
+    for ci in range(3):
+        p.idx[ci] = _ptr(arr(c.idx[ci], np.uint16), C.c_uint16)
+    p.n_mat = int(c.eps_tab.size)
+    p.ca_tab = _ptr(arr(c.ca_tab, np.float64), C.c_double)
+    p.cb_tab = _ptr(arr(c.cb_tab, np.float64), C.c_double)
+    p.eps_tab = _ptr(arr(c.eps_tab, np.float64), C.c_double)
+    for a in range(3):
+        p.inv_primal[a] = _ptr(arr(g.inv_primal(a), np.float64), C.c_double)
+        p.inv_dual[a] = _ptr(arr(g.inv_dual(a), np.float64), C.c_double)
+        p.node_w[a] = _ptr(arr(g.node_weights(a), np.float64), C.c_double)
+        p.cell_w[a] = _ptr(arr(g.cell_weights(a), np.float64), C.c_double)
+    p.pmc_mask = sum(1 << k for k in range(6) if c.walls[k] == "pmc")
+    corr = c.pml.corrections
+    p.n_corr = len(corr)
+    if corr:
+        cs = (native.Correction * len(corr))()
+        for n, k in enumerate(corr):
+            cs[n].kind = 0 if k.kind == "E" else 1
+            cs[n].c, cs[n].a, cs[n].b = k.c, k.a, k.b
+            cs[n].sign = float(k.sign)
+            for ax in range(3):
+                cs[n].lo[ax], cs[n].hi[ax] = k.box[ax]
+        keep.append(cs)
+        p.corr = C.cast(cs, C.POINTER(native.Correction))
+    for a, co in c.pml.coeffs.items():
+        for t, name in enumerate(("eb", "ec", "ek", "hb", "hc", "hk")):
+            p.pml[a][t] = _ptr(arr(getattr(co, name), np.float64), C.c_double)
+    # sources
+    chans = c.channels
+    p.n_chan = len(chans)
+    p.max_steps = max_steps
+    p.wave = _ptr(arr(wave_table(c, max_steps) if chans else np.zeros(1), np.float64), C.c_double)
+    p.drive = _ptr(arr(c.drive, np.float64), C.c_double)
+    comp, flat, amp, chan = [], [], [], []
+    for ci, ch in enumerate(chans):
+        fl = np.asarray(ch["flat"], dtype=np.int64)
+        comp.append(np.broadcast_to(np.asarray(ch["comp"], np.int32), fl.shape))
+        flat.append(fl)
+        amp.append(np.asarray(ch["amps"], np.float64))
+        chan.append(np.full(fl.size, ci, np.int32))
+    cat = (lambda v, dt: np.concatenate(v).astype(dt) if v else np.zeros(0, dt))
+    inj_comp, inj_flat = cat(comp, np.int32), cat(flat, np.int64)
+    p.n_inj = int(inj_flat.size)
+    p.inj_comp = _ptr(arr(inj_comp, np.int32), C.c_int32)
+    p.inj_flat = _ptr(arr(inj_flat, np.int64), C.c_int64)
+    p.inj_amp = _ptr(arr(cat(amp, np.float64), np.float64), C.c_double)
+    p.inj_chan = _ptr(arr(cat(chan, np.int32), np.int32), C.c_int32)
+    # probes
+    probes = c.probes
+    p.n_probe = len(probes)
+    sizes = [np.asarray(q["flat"]).size for q in probes]
+    p.probe_kind = _ptr(arr([0 if q["kind"] == "E" else 1 for q in probes] or [0], np.int32), C.c_int32)
+    p.probe_comp = _ptr(arr([int(q["comp"]) for q in probes] or [0], np.int32), C.c_int32)
+    p.probe_off = _ptr(arr(np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64), np.int64), C.c_int64)
+    p.probe_flat = _ptr(
+        arr(cat([np.asarray(q["flat"], np.int64) for q in probes], np.int64), np.int64), C.c_int64
+    )
+    p.probe_w = _ptr(
+        arr(cat([np.asarray(q["weights"], np.float64) for q in probes], np.float64), np.float64),
+        C.c_double,
+    )
+    p.n_freq = int(c.frequencies.size)
+    p.omega = _ptr(arr(2.0 * np.pi * c.frequencies, np.float64), C.c_double)
+    p.record_series = int(record_series)
+    # Debye ADE
+    if c.ade is not None:
+        a = c.ade
+        p.ade_poles = int(a.tau.size)
+        p.ade_kp = _ptr(arr(a.kp, np.float64), C.c_double)
+        for comp_, fl, be, cbe in zip(a.comp, a.flat, a.beta, a.cbe, strict=True):
+            p.ade_n[comp_] = int(np.asarray(fl).size)
+            p.ade_flat[comp_] = _ptr(arr(fl, np.int64), C.c_int64)
+            p.ade_beta[comp_] = _ptr(arr(be, np.float64), C.c_double)
+            p.ade_cbe[comp_] = _ptr(arr(cbe, np.float64), C.c_double)
+    # surface impedance
+    if c.sibc is not None:
+        s = c.sibc
+        p.sibc_n = int(s.flat.size)
+        p.sibc_poles = int(s.cp.size)
+        p.sibc_nmat = int(s.r0.size)
+        p.sibc_comp = _ptr(arr(s.comp, np.int32), C.c_int32)
+        p.sibc_flat = _ptr(arr(s.flat, np.int64), C.c_int64)
+        p.sibc_hcomp = _ptr(arr(s.hcomp, np.int32), C.c_int32)
+        p.sibc_hflat = _ptr(arr(s.hflat, np.int64), C.c_int64)
+        p.sibc_hsign = _ptr(arr(s.hsign, np.float64), C.c_double)
+        p.sibc_mat = _ptr(arr(s.mat, np.int32), C.c_int32)
+        p.sibc_r0 = _ptr(arr(s.r0, np.float64), C.c_double)
+        p.sibc_rp = _ptr(arr(s.rp, np.float64), C.c_double)
+        p.sibc_cp = _ptr(arr(s.cp, np.float64), C.c_double)
+        p.sibc_gp = _ptr(arr(s.gp, np.float64), C.c_double)
+    return p, keep
 
 
 class Gb300Engine:
@@ -80,124 +252,16 @@ class Gb300Engine:
         self.max_steps = int(max_steps)
         self._lib = native.load()
         self._h = C.c_void_p()
-        self._keep: list[np.ndarray] = []
         g = c.grid
         self.B = c.batch
         self.shape = (self.B, *g.shape)
-        prob = self._problem()
-        self.h2d_bytes = int(sum(a.nbytes for a in self._keep))  # host buffers the library copies
+        prob, keep = describe(c, self.dtype, self.max_steps, self.record_series)
+        # host buffers the library copies
+        self.h2d_bytes = int(sum(a.nbytes for a in keep if isinstance(a, np.ndarray)))
         native.check(self._lib.oafdtd_create(C.byref(prob), C.byref(self._h)), "create")
-        self._keep.clear()
+        del keep
         self.set_graph(use_graph)
         self._probes = list(c.probes)
-
-    # ------------------------------------------------------------------ descriptor
-    def _arr(self, a: Any, dtype: Any) -> np.ndarray:
-        out = np.ascontiguousarray(np.asarray(a, dtype=dtype))
-        self._keep.append(out)
-        return out
-
-    def _problem(self) -> native.Problem:
-        c, g = self.c, self.c.grid
-        p = native.Problem()
-        p.abi_version = native.ABI_VERSION
-        p.real_bytes = 4 if self.dtype == "float32" else 8
-        p.nx, p.ny, p.nz = g.n
-        p.pitch = g.pitch
-        p.batch = self.B
-        p.dt = float(c.dt)
-        p.dtmu = float(c.dt / MU0)
-        for ci in range(3):
-            p.idx[ci] = _ptr(self._arr(c.idx[ci], np.uint16), C.c_uint16)
-        p.n_mat = int(c.eps_tab.size)
-        p.ca_tab = _ptr(self._arr(c.ca_tab, np.float64), C.c_double)
-        p.cb_tab = _ptr(self._arr(c.cb_tab, np.float64), C.c_double)
-        p.eps_tab = _ptr(self._arr(c.eps_tab, np.float64), C.c_double)
-        for a in range(3):
-            p.inv_primal[a] = _ptr(self._arr(g.inv_primal(a), np.float64), C.c_double)
-            p.inv_dual[a] = _ptr(self._arr(g.inv_dual(a), np.float64), C.c_double)
-            p.node_w[a] = _ptr(self._arr(g.node_weights(a), np.float64), C.c_double)
-            p.cell_w[a] = _ptr(self._arr(g.cell_weights(a), np.float64), C.c_double)
-        p.pmc_mask = sum(1 << k for k in range(6) if c.walls[k] == "pmc")
-        corr = c.pml.corrections
-        p.n_corr = len(corr)
-        if corr:
-            arr = (native.Correction * len(corr))()
-            for n, k in enumerate(corr):
-                arr[n].kind = 0 if k.kind == "E" else 1
-                arr[n].c, arr[n].a, arr[n].b = k.c, k.a, k.b
-                arr[n].sign = float(k.sign)
-                for ax in range(3):
-                    arr[n].lo[ax], arr[n].hi[ax] = k.box[ax]
-            self._corr = arr
-            p.corr = C.cast(arr, C.POINTER(native.Correction))
-        for a, co in c.pml.coeffs.items():
-            for t, name in enumerate(("eb", "ec", "ek", "hb", "hc", "hk")):
-                p.pml[a][t] = _ptr(self._arr(getattr(co, name), np.float64), C.c_double)
-        # sources
-        chans = c.channels
-        p.n_chan = len(chans)
-        p.max_steps = self.max_steps
-        p.wave = _ptr(self._arr(wave_table(c, self.max_steps) if chans else np.zeros(1), np.float64), C.c_double)
-        p.drive = _ptr(self._arr(c.drive, np.float64), C.c_double)
-        comp, flat, amp, chan = [], [], [], []
-        for ci, ch in enumerate(chans):
-            fl = np.asarray(ch["flat"], dtype=np.int64)
-            comp.append(np.broadcast_to(np.asarray(ch["comp"], np.int32), fl.shape))
-            flat.append(fl)
-            amp.append(np.asarray(ch["amps"], np.float64))
-            chan.append(np.full(fl.size, ci, np.int32))
-        cat = (lambda v, dt: np.concatenate(v).astype(dt) if v else np.zeros(0, dt))
-        inj_comp, inj_flat = cat(comp, np.int32), cat(flat, np.int64)
-        p.n_inj = int(inj_flat.size)
-        p.inj_comp = _ptr(self._arr(inj_comp, np.int32), C.c_int32)
-        p.inj_flat = _ptr(self._arr(inj_flat, np.int64), C.c_int64)
-        p.inj_amp = _ptr(self._arr(cat(amp, np.float64), np.float64), C.c_double)
-        p.inj_chan = _ptr(self._arr(cat(chan, np.int32), np.int32), C.c_int32)
-        # probes
-        probes = c.probes
-        p.n_probe = len(probes)
-        sizes = [np.asarray(q["flat"]).size for q in probes]
-        p.probe_kind = _ptr(self._arr([0 if q["kind"] == "E" else 1 for q in probes] or [0], np.int32), C.c_int32)
-        p.probe_comp = _ptr(self._arr([int(q["comp"]) for q in probes] or [0], np.int32), C.c_int32)
-        p.probe_off = _ptr(self._arr(np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64), np.int64), C.c_int64)
-        p.probe_flat = _ptr(
-            self._arr(cat([np.asarray(q["flat"], np.int64) for q in probes], np.int64), np.int64), C.c_int64
-        )
-        p.probe_w = _ptr(
-            self._arr(cat([np.asarray(q["weights"], np.float64) for q in probes], np.float64), np.float64),
-            C.c_double,
-        )
-        p.n_freq = int(c.frequencies.size)
-        p.omega = _ptr(self._arr(2.0 * np.pi * c.frequencies, np.float64), C.c_double)
-        p.record_series = int(self.record_series)
-        # Debye ADE
-        if c.ade is not None:
-            a = c.ade
-            p.ade_poles = int(a.tau.size)
-            p.ade_kp = _ptr(self._arr(a.kp, np.float64), C.c_double)
-            for comp_, fl, be, cbe in zip(a.comp, a.flat, a.beta, a.cbe, strict=True):
-                p.ade_n[comp_] = int(np.asarray(fl).size)
-                p.ade_flat[comp_] = _ptr(self._arr(fl, np.int64), C.c_int64)
-                p.ade_beta[comp_] = _ptr(self._arr(be, np.float64), C.c_double)
-                p.ade_cbe[comp_] = _ptr(self._arr(cbe, np.float64), C.c_double)
-        # surface impedance
-        if c.sibc is not None:
-            s = c.sibc
-            p.sibc_n = int(s.flat.size)
-            p.sibc_poles = int(s.cp.size)
-            p.sibc_nmat = int(s.r0.size)
-            p.sibc_comp = _ptr(self._arr(s.comp, np.int32), C.c_int32)
-            p.sibc_flat = _ptr(self._arr(s.flat, np.int64), C.c_int64)
-            p.sibc_hcomp = _ptr(self._arr(s.hcomp, np.int32), C.c_int32)
-            p.sibc_hflat = _ptr(self._arr(s.hflat, np.int64), C.c_int64)
-            p.sibc_hsign = _ptr(self._arr(s.hsign, np.float64), C.c_double)
-            p.sibc_mat = _ptr(self._arr(s.mat, np.int32), C.c_int32)
-            p.sibc_r0 = _ptr(self._arr(s.r0, np.float64), C.c_double)
-            p.sibc_rp = _ptr(self._arr(s.rp, np.float64), C.c_double)
-            p.sibc_cp = _ptr(self._arr(s.cp, np.float64), C.c_double)
-            p.sibc_gp = _ptr(self._arr(s.gp, np.float64), C.c_double)
-        return p
 
     # ------------------------------------------------------------------ protocol
     @property
@@ -319,14 +383,14 @@ class Gb300Engine:
         native.check(self._lib.oafdtd_set_graph(self._h, int(bool(on))), "set_graph")
 
     def set_tuning(self, tile_z: int = 0, variant: int = -1) -> None:
-        """Planes marched per block (0 keeps) and the sweep variant (2 staged by TMA, 1 staged
-        by cp.async, 0 register marching, -1 keeps)."""
+        """Planes marched per block (0 keeps) and the sweep variant (3 the fused H + E sweep of
+        the interior, 2 staged by TMA, 1 staged by cp.async, 0 register marching, -1 keeps)."""
         native.check(self._lib.oafdtd_set_tuning(self._h, int(tile_z), int(variant)), "set_tuning")
 
     def set_profiling(self, on: bool) -> None:
         native.check(self._lib.oafdtd_set_profiling(self._h, int(bool(on))), "set_profiling")
 
-    KERNELS = ("h_sweep", "h_slab", "ghosts", "pre_e", "e_sweep", "e_slab", "edges", "probe_e", "step")
+    KERNELS = ("h_sweep", "h_slab", "ghosts", "pre_e", "e_sweep", "e_slab", "edges", "probe_e", "fused", "step")
 
     def kernel_bytes(self) -> dict[str, float]:
         """Algorithmic DRAM bytes per time step of each kernel class (keys of ``kernel_times``;

@@ -87,7 +87,7 @@ def make_engine(
     from open_analysis_gb300.engine import Gb300Engine, estimate_bytes
 
     info = native.device_info()
-    need = estimate_bytes(c, np.dtype(dtype).itemsize)
+    need = estimate_bytes(c, np.dtype(dtype).itemsize, max_steps=max_steps, record_series=record_series)
     budget = _budget_bytes(info["total_bytes"])
     if need > budget:
         raise AccelError(

@@ -1,8 +1,12 @@
 """Generate the golden fixtures from the reference implementation itself.
 
-Run in a checkout that has the reference next to it (not needed anywhere else):
+Run in a checkout that has the reference's source tree at hand (not needed anywhere else):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference root> [part ...]
+
+where the parts are any of ``cases debye touchstone tail runs jobs workloads compiled`` (all of
+them by default; ``workloads`` runs the reference's NumPy engine on the full-size workloads of
+``workloads.py`` and takes about an hour on one host thread; ``workloads:<name>`` runs one).
 
 For every problem in ``cases.CASES`` it builds the model from the reference's own classes,
 compiles it with the reference's ``compile_model`` and steps the reference's ``NumpyEngine`` in
@@ -20,7 +24,10 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 
 
-def main(reference_root: str) -> None:
+PARTS = ("cases", "debye", "touchstone", "tail", "runs", "jobs", "workloads", "compiled")
+
+
+def main(reference_root: str, parts: tuple[str, ...] = PARTS) -> None:
     root = Path(reference_root)
     sys.path.insert(0, str(root / "packages" / "oa-fdtd" / "src"))
     sys.path.insert(0, str(root / "packages" / "oa-accel" / "src"))
@@ -33,6 +40,27 @@ def main(reference_root: str) -> None:
     from oa_fdtd.reference import NumpyEngine  # type: ignore[import-not-found]
 
     ns = namespace("ref")
+    if "cases" in parts:
+        cases(np, ns, CASES, compile_model, NumpyEngine, compiled_fingerprint, state_fingerprint, save)
+    if "debye" in parts:
+        debye_fits(np)
+    if "touchstone" in parts:
+        touchstone_files(np)
+    if "tail" in parts:
+        tail_fits(np)
+    if "runs" in parts:
+        run_loops(np)
+    if "jobs" in parts:
+        job_parse(np)
+    picked = tuple(p.split(":", 1)[1] for p in parts if p.startswith("workloads:"))
+    if "workloads" in parts or picked:
+        workload_fixtures(np, ns, picked)
+    if "compiled" in parts:
+        reference_compiled(np, ns)
+
+
+def cases(np, ns, CASES, compile_model, NumpyEngine, compiled_fingerprint, state_fingerprint, save):  # type: ignore[no-untyped-def]
+    """Every problem of ``cases.CASES``: compiled arrays, float32 and float64 engine states."""
     for name, (builder, steps) in CASES.items():
         model = builder(ns)
         c = compile_model(model, "float32")
@@ -52,11 +80,84 @@ def main(reference_root: str) -> None:
                 data[f"full.{comp}"] = np.ascontiguousarray(arr)
         save(str(HERE / f"{name}.npz"), data)
         print(name, "steps", steps, "batch", c.batch, "keys", len(data))
-    debye_fits(np)
-    touchstone_files(np)
-    tail_fits(np)
-    run_loops(np)
-    job_parse(np)
+
+
+SAMPLES = 4096  # float64 field values kept per component for the error against the FP64 oracle
+
+
+def workload_fixtures(np, ns, only=()):  # type: ignore[no-untyped-def]
+    """The benchmark workloads of ``workloads.py`` built from the reference's classes, compiled by
+    its ``compile_model`` and stepped by its ``NumpyEngine`` in float32 and float64 (from the
+    seeded fields where the workload has a seed). Stored per workload: the compiled arrays'
+    fingerprint, the float32 state (field digests, DFTs, energy), the float64 DFTs and energy,
+    each float32 field's rel-L2 distance from the float64 one, float64 values at seeded sample
+    points, and for the port workload without a seed the S-parameters of the float32 engine
+    (through the reference's ``sparams``) and of the reference's own ``run()`` in float64."""
+    import time
+
+    from fingerprint import compiled_fingerprint, save, state_fingerprint  # type: ignore[import-not-found]
+    from oa_fdtd.model import compile_model  # type: ignore[import-not-found]
+    from oa_fdtd.reference import NumpyEngine  # type: ignore[import-not-found]
+    from oa_fdtd.run import RunResult, run, source_spectrum, sparams  # type: ignore[import-not-found]
+    from workloads import NAMES, convert, sample_index, seeded_values, workloads  # type: ignore[import-not-found]
+
+    for name, w in workloads().items():
+        if only and name not in only:
+            continue
+        t0 = time.perf_counter()
+        model = convert(w["model"](), ns)
+        c = compile_model(model, "float32")
+        data = compiled_fingerprint(c)
+        steps, seed = w["steps"], w["seed"]
+        data["steps"], data["seed"] = steps, -1 if seed is None else seed
+        eng = {}
+        for dtype in ("float32", "float64"):
+            e = NumpyEngine(c, dtype)
+            if seed is not None:
+                for k, arr in enumerate(e.E + e.H):
+                    arr[...] = seeded_values(arr.shape, seed, k)
+            e.step(steps)
+            eng[dtype] = e
+            print(name, dtype, f"{time.perf_counter() - t0:.0f} s", flush=True)
+        f32, f64 = eng["float32"], eng["float64"]
+        for k, v in state_fingerprint(f32).items():
+            data[f"float32.{k}"] = v
+        data["float64.energy"] = np.float64(f64.energy())
+        for pname, v in f64.results().items():
+            data[f"float64.dft.{pname}"] = np.asarray(v, np.complex128)
+        idx = sample_index(f32.E[0].size, SAMPLES, 99)
+        data["sample.index"] = idx
+        for k, (a32, a64) in enumerate(zip(f32.E + f32.H, f64.E + f64.H, strict=True)):
+            diff = np.linalg.norm((a32.astype(np.float64) - a64).ravel())
+            data[f"rel64.{NAMES[k]}"] = float(diff / max(np.linalg.norm(a64.ravel()), 1e-300))
+            data[f"float64.sample.{NAMES[k]}"] = np.ascontiguousarray(a64.reshape(-1)[idx])
+        if seed is None and model.ports:
+            port_r = np.array([float(q["r_ohm"]) for q in c.ports])
+            res = RunResult(probes=f32.results(), source_dft=source_spectrum(c, steps), steps=steps, dt=c.dt,
+                            engine="numpy", dtype="float32", stopped_by="max_steps", energy_db=0.0, peak_bytes=0,
+                            port_r=port_r)
+            data["float32.s"] = sparams(model, res)
+            r64 = run(model, engine="numpy", dtype="float64", end_db=None, max_steps=steps)
+            data["float64.s"] = sparams(model, r64)
+        save(str(HERE / f"workload_{name}.npz"), data)
+        print(name, "done", f"{time.perf_counter() - t0:.0f} s", flush=True)
+
+
+COMPILED_CASES = ("dispersive_copper", "mode_stripline")
+
+
+def reference_compiled(np, ns):  # type: ignore[no-untyped-def]
+    """The reference's own ``Compiled`` of two cases, stored with ``compiled_io.dump`` (the
+    waveform sampled for the first 128 steps), so the GPU engine can be fed the reference's
+    objects on a host without the reference."""
+    from cases import CASES  # type: ignore[import-not-found]
+    from compiled_io import dump  # type: ignore[import-not-found]
+    from oa_fdtd.model import compile_model  # type: ignore[import-not-found]
+
+    for name in COMPILED_CASES:
+        c = compile_model(CASES[name][0](ns), "float32")
+        np.savez_compressed(HERE / f"ref_compiled_{name}.npz", **dump(c, 128))
+        print("reference compiled", name)
 
 
 def wave_fixture(np, model, c, engine_cls, steps, data):  # type: ignore[no-untyped-def]
@@ -216,4 +317,6 @@ def debye_fits(np):  # type: ignore[no-untyped-def]
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) < 2:
+        raise SystemExit("usage: make_golden.py <reference root> [part ...]; parts: " + " ".join(PARTS))
+    main(sys.argv[1], tuple(sys.argv[2:]) or PARTS)

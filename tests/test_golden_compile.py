@@ -58,3 +58,21 @@ def test_full_fields_fixture_consistent() -> None:
 
     for comp in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz"):
         assert digest(ref[f"full.{comp}"]) == ref[f"float32.field.{comp}.sha"]
+
+
+@pytest.mark.parametrize("native", [True, False], ids=["native", "numpy"])
+@pytest.mark.parametrize("name", ["microstrip_120x60x40", "via_transition_400x400x120", "large_board_200x150x80"])
+def test_compiler_matches_reference_on_the_workloads(name: str, native: bool) -> None:
+    """The benchmark workloads (the configured microstrip, the full-size via transition, the
+    large-board structure on a reduced grid) compile to the reference's arrays bit for bit."""
+    from workloads import workloads
+
+    from open_analysis_gb300.model import _native_library
+
+    if native and _native_library() is None:
+        pytest.skip("library not built")
+    ref = load(str(GOLDEN / f"workload_{name}.npz"))
+    c = compile_model(workloads()[name]["model"](), "float32", native=native)
+    skip = ("float32.", "float64.", "rel64.", "sample.", "steps", "seed")
+    ref_c = {k: v for k, v in ref.items() if not k.startswith(skip)}
+    assert compare_compiled(ref_c, compiled_fingerprint(c)) == []
