@@ -21,13 +21,14 @@ from collections.abc import Sequence
 from concurrent.futures import ProcessPoolExecutor
 from dataclasses import dataclass, field
 from multiprocessing import get_context
+from pathlib import Path
 from typing import Any
 
 import numpy as np
 import numpy.typing as npt
 
-from open_analysis_gb300.model import Compiled, Model, compile_model
-from open_analysis_gb300.run import RunResult, source_spectrum, sparams
+from open_analysis_gb300.model import Compiled, ModePort, Model, compile_model
+from open_analysis_gb300.run import RunResult, port_voltage_factor, source_spectrum, sparams
 
 ComplexArray = npt.NDArray[np.complex128]
 
@@ -72,6 +73,23 @@ def collect(model: Model, c: Compiled, eng: Any, steps: int, dtype: str) -> RunR
     )
 
 
+def instance_sparams(model: Model, res: RunResult) -> ComplexArray:
+    """S-parameters of one instance as the worker reports them (``adapter/sim.py:184-198``): the
+    port S, or, where every port is a mode port and the model has wave planes
+    (``deembed.add_wave_planes``), the wave-plane S (``deembed.wave_sparams``, the port voltages
+    mapped by the port voltage factor) with the port S where the planes are ill-conditioned."""
+    s_port = sparams(model, res)
+    planes = getattr(model, "plane_sets", None)
+    if not planes or not model.ports or not all(isinstance(p, ModePort) for p in model.ports):
+        return s_port
+    from open_analysis_gb300.deembed import wave_sparams
+
+    fac = port_voltage_factor(res.dt, model.frequencies)
+    probes = {k: v * fac for k, v in res.probes.items()}
+    s_wave, _ = wave_sparams(probes, planes, res.port_r, s_port=s_port, freqs=model.frequencies)
+    return s_wave
+
+
 @dataclass
 class SweepRun:
     """S-parameters of every instance (``(N, N, F)`` each), the time of the stepping and of the
@@ -92,17 +110,18 @@ SWEEP_TILES = (4, 8, 16)
 
 
 def tune_shape(compiled: Sequence[Compiled], dtype: str = "float32") -> Any:
-    """The autotuner's launch shape for a sweep: TMA-staged sweeps with 4, 8 or 16 planes per
-    block, each timed for one 64-step chunk on a scratch engine of the median-size instance.
+    """The autotuner's launch shape for a sweep: the fused or the TMA-staged sweeps with 4, 8 or
+    16 planes per block, each timed for one 64-step chunk on a scratch engine of the median-size
+    instance.
     Returns the :class:`~open_analysis_gb300.autotune.TuneResult`, or None when no TMA shape is
     available (the engines then keep their default)."""
     from open_analysis_gb300.autotune import steps_needed, tune
     from open_analysis_gb300.engine import Gb300Engine
 
     c = sorted(compiled, key=lambda x: x.grid.cells)[len(compiled) // 2]
-    eng = Gb300Engine(c, dtype, max_steps=steps_needed(1, SWEEP_TILES, (2,)))
+    eng = Gb300Engine(c, dtype, max_steps=steps_needed(1, SWEEP_TILES, (3, 2)))
     try:
-        return tune(eng, chunks=1, tiles=SWEEP_TILES, variants=(2,))
+        return tune(eng, chunks=1, tiles=SWEEP_TILES, variants=(3, 2))
     except ValueError:  # every candidate refused
         return None
     finally:
@@ -126,24 +145,41 @@ def _engines(compiled: Sequence[Compiled], steps: int, dtype: str, shape: Any = 
     return engines, time.perf_counter() - t0
 
 
-def _finish(models, compiled, engines, steps, dtype, seconds, create):  # type: ignore[no-untyped-def]
+def finish_sweep(models: Sequence[Model], compiled: Sequence[Compiled], engines: Sequence[Any], steps: int,
+                 dtype: str, seconds: float, create: float, wire_dir: str | Path | None = None) -> SweepRun:
+    """Read every instance's results back (``instance_sparams``), close the engines and, with
+    ``wire_dir``, write each instance's worker files (``ports.npz`` with ``(F, N, N)`` S,
+    ``run.json``, Touchstone; ``adapter/worker.py:47-52``) into ``wire_dir/instance_<n>``."""
     t0 = time.perf_counter()
-    s = [sparams(m, collect(m, c, e, steps, dtype)) for m, c, e in zip(models, compiled, engines, strict=True)]
+    results = [collect(m, c, e, steps, dtype) for m, c, e in zip(models, compiled, engines, strict=True)]
+    s = [instance_sparams(m, r) for m, r in zip(models, results, strict=True)]
     read = time.perf_counter() - t0
     for e in engines:
-        e.close()
+        close = getattr(e, "close", None)
+        if close is not None:
+            close()
     updates = float(sum(c.grid.cells * c.batch for c in compiled)) * steps
-    return SweepRun(s, seconds + read, create, updates, {"readback_seconds": read})
+    extra: dict[str, Any] = {"readback_seconds": read}
+    if wire_dir is not None:
+        from open_analysis_gb300.jobs import write_wire
+
+        share = (seconds + read) / max(len(models), 1)
+        extra["wire"] = [
+            write_wire(Path(wire_dir) / f"instance_{n:03d}", "sweep", m, sn, r, 0.0, share)
+            for n, (m, sn, r) in enumerate(zip(models, s, results, strict=True))
+        ]
+    return SweepRun(s, seconds + read, create, updates, extra)
 
 
 def run_batched(models: Sequence[Model], compiled: Sequence[Compiled], steps: int, dtype: str = "float32",
-                shape: Any = None) -> SweepRun:
+                shape: Any = None, wire_dir: str | Path | None = None) -> SweepRun:
     """All instances at once: every engine's steps queued on its own stream, then waited on.
 
     The first 64-step chunk goes first on every engine (each captures its graph there), the
     rest after: capturing a graph while other engines' work is queued would wait for that work
     and run the instances one after the other. ``shape``: a launch shape from
-    :func:`tune_shape` (None: the engines' default)."""
+    :func:`tune_shape` (None: the engines' default). ``wire_dir``: write each instance's worker
+    files there (:func:`finish_sweep`)."""
     engines, create = _engines(compiled, steps, dtype, shape)
     t0 = time.perf_counter()
     first = min(64, steps)
@@ -156,14 +192,14 @@ def run_batched(models: Sequence[Model], compiled: Sequence[Compiled], steps: in
             e.step_async(steps - first)
         for e in engines:
             e.wait()
-    return _finish(models, compiled, engines, steps, dtype, time.perf_counter() - t0, create)
+    return finish_sweep(models, compiled, engines, steps, dtype, time.perf_counter() - t0, create, wire_dir)
 
 
 def run_looped(models: Sequence[Model], compiled: Sequence[Compiled], steps: int, dtype: str = "float32",
-               shape: Any = None) -> SweepRun:
+               shape: Any = None, wire_dir: str | Path | None = None) -> SweepRun:
     """The plain way: one instance after the other."""
     engines, create = _engines(compiled, steps, dtype, shape)
     t0 = time.perf_counter()
     for e in engines:
         e.step(steps)
-    return _finish(models, compiled, engines, steps, dtype, time.perf_counter() - t0, create)
+    return finish_sweep(models, compiled, engines, steps, dtype, time.perf_counter() - t0, create, wire_dir)

@@ -39,7 +39,7 @@ def test_batched_equals_looped_equals_run() -> None:
     compiled = compile_all(models, workers=1)
     steps = 300
     shape = tune_shape(compiled)
-    assert shape is not None and shape.tile_z in SWEEP_TILES and shape.variant == 2
+    assert shape is not None and shape.tile_z in SWEEP_TILES and shape.variant in (2, 3)
     a = run_batched(models, compiled, steps, shape=shape)
     b = run_looped(models, compiled, steps)  # default shape: launch shapes do not change results
     for sa, sb in zip(a.s, b.s, strict=True):
@@ -47,3 +47,78 @@ def test_batched_equals_looped_equals_run() -> None:
     one = run(models[0], engine="gb300", dtype="float32", end_db=None, max_steps=steps)
     assert np.array_equal(sparams(models[0], one), a.s[0])
     assert a.cell_updates == b.cell_updates > 0
+
+
+def _mode_sweep(n: int = 3) -> list:  # type: ignore[type-arg]
+    """Mode-port striplines with wave planes (the ``mode_stripline`` case), the fill's eps_inf
+    varied per instance."""
+    from dataclasses import replace
+
+    from cases import CASES, namespace
+
+    out = []
+    for i in range(n):
+        m = CASES["mode_stripline"][0](namespace("gb300"))
+        m.regions[0] = replace(m.regions[0], eps_r=3.0 + 0.4 * i)
+        out.append(m)
+    return out
+
+
+def test_sweep_results_use_wave_planes_and_write_worker_files(tmp_path) -> None:  # type: ignore[no-untyped-def]
+    """On the oracle: a sweep instance with mode ports and wave planes reports the wave-plane S
+    (the worker's choice, ``adapter/sim.py:184-198``), and each instance's ``ports.npz``,
+    ``run.json`` and Touchstone file carry that S as the adapter reads it."""
+    import json
+
+    from open_analysis_gb300.batch import collect, finish_sweep, instance_sparams
+    from open_analysis_gb300.deembed import wave_sparams
+    from open_analysis_gb300.run import port_voltage_factor, sparams
+    from oracle.numpy_engine import OracleEngine
+
+    models = _mode_sweep(2)
+    compiled = [compile_model_f32(m) for m in models]
+    steps = 300
+    engines = []
+    for c in compiled:
+        e = OracleEngine(c, "float32")
+        e.step(steps)
+        engines.append(e)
+    res = [collect(m, c, e, steps, "float32") for m, c, e in zip(models, compiled, engines, strict=True)]
+    run = finish_sweep(models, compiled, engines, steps, "float32", 1.0, 0.0, wire_dir=tmp_path)
+    for m, r, s in zip(models, res, run.s, strict=True):
+        s_port = sparams(m, r)
+        fac = port_voltage_factor(r.dt, m.frequencies)
+        want, _ = wave_sparams({k: v * fac for k, v in r.probes.items()}, m.plane_sets, r.port_r, s_port=s_port,
+                               freqs=m.frequencies)
+        assert np.array_equal(s, want) and np.array_equal(instance_sparams(m, r), want)
+        assert not np.array_equal(s, s_port)
+    for n, files in enumerate(run.extra["wire"]):
+        with np.load(files["wire"]) as z:
+            assert np.array_equal(z["s"], np.moveaxis(run.s[n], -1, 0))
+            assert np.array_equal(z["freqs"], models[n].frequencies)
+            assert list(z["names"]) == [p.name for p in models[n].ports]
+        meta = json.loads(open(files["run_json"]).read())
+        assert meta["steps"] == steps and meta["port_names"] == ["p1", "p2"]
+        assert files["touchstone"].endswith(".s2p")
+
+
+def compile_model_f32(m):  # type: ignore[no-untyped-def]
+    from open_analysis_gb300.model import compile_model
+
+    return compile_model(m, "float32")
+
+
+@pytest.mark.gpu
+def test_batched_mode_port_sweep_equals_looped(tmp_path) -> None:  # type: ignore[no-untyped-def]
+    """Wave planes on the batched path: batched = looped bit for bit, wire files included."""
+    from open_analysis_gb300.batch import compile_all, run_batched, run_looped
+
+    models = _mode_sweep(3)
+    compiled = compile_all(models, workers=1)
+    a = run_batched(models, compiled, 400, wire_dir=tmp_path / "batched")
+    b = run_looped(models, compiled, 400, wire_dir=tmp_path / "looped")
+    for sa, sb in zip(a.s, b.s, strict=True):
+        assert np.array_equal(sa, sb)
+    for fa, fb in zip(a.extra["wire"], b.extra["wire"], strict=True):
+        with np.load(fa["wire"]) as za, np.load(fb["wire"]) as zb:
+            assert np.array_equal(za["s"], zb["s"])
