@@ -1,21 +1,28 @@
 // Field energy without any device allocation.
 //
-// Some callers cannot allocate device memory: code running inside a captured CUDA graph region
-// or another runtime's stream-ordered pool, plugins whose host application owns every
-// allocation, and budgets that forbid growth after start-up. This entry point computes the same
-// energy as oafdtd_energy from field arrays the caller already holds on the device, with its
-// per-plane partial sums in a file-scope device array instead of a cudaMalloc'd buffer.
+// Some callers cannot allocate device memory: a plugin whose host application owns every device
+// allocation (it hands the library only buffers it made itself and counts every byte), and
+// services that reserve their device memory at start-up and must not grow it afterwards. This
+// entry point computes the same energy as oafdtd_energy from field arrays the caller already holds
+// on the device, with its per-plane partial sums in a file-scope device array instead of a
+// cudaMalloc'd buffer.
 //
 // Limits and sharing:
 //  * the scratch holds kMaxPartials doubles (512 KiB) on every GPU that loads the library, for
 //    the life of the process; a problem needs 6 * batch * (nz + 2) partials and is rejected with
 //    OAFDTD_E_INVALID beyond that;
-//  * every call shares the one array: calls that overlap on the GPU (different streams, threads)
-//    race and must be serialised by the caller. Each call writes every partial it later reads,
-//    so nothing needs clearing between calls;
-//  * the first call on a device looks the array's device address up (cudaGetSymbolAddress, with
-//    that device current) and caches it; make that first call before any stream capture.
-
+//  * every call in the process shares the one array, whatever stream it is given: calls that
+//    overlap on the GPU (different streams or threads) race and must be serialised by the caller.
+//    Each call writes every partial it later reads, so nothing needs clearing between calls;
+//  * the call is synchronous: it copies the six component sums to the host and synchronises the
+//    caller's stream before it returns. It therefore cannot run on a stream that is being captured
+//    (or on the legacy default stream while another stream captures in global mode); it checks
+//    and returns OAFDTD_E_INVALID there, before it launches anything;
+//  * the first call in a device's context looks the array's device address up
+//    (cudaGetSymbolAddress, with that device current) and caches it, keyed by the context's
+//    unique id, so a context that was reset and created again looks it up anew. That first
+//    lookup may load the library's module on the device (with lazy loading), which the driver
+//    backs with memory for the module's code and this array.
 #include <mutex>
 #include <string>
 
@@ -34,7 +41,36 @@ constexpr double kEps0 = 1.0 / (4e-7 * 3.14159265358979323846 * 299792458.0 * 29
 constexpr double kMu0 = 4e-7 * 3.14159265358979323846;
 
 std::mutex g_scratch_mu;
-double* g_scratch_ptr[kMaxDevices] = {};
+struct ScratchSlot {
+  unsigned long long ctx_id;  // unique id of the context the address belongs to (0: none)
+  double* ptr;
+};
+ScratchSlot g_scratch[kMaxDevices] = {};
+
+// Driver entry points for the current context and its process-unique id (CUDA 12.0 and later).
+using CtxGetCurrent = CUresult (*)(CUcontext*);
+using CtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+
+template <typename F>
+F driver_entry(const char* name) {
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult q{};
+  if (cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess)
+    return nullptr;
+  return reinterpret_cast<F>(p);
+}
+
+// Id of the context current on this thread; 0 when none is current or the driver cannot say.
+unsigned long long current_context_id() {
+  static const CtxGetCurrent get_current = driver_entry<CtxGetCurrent>("cuCtxGetCurrent");
+  static const CtxGetId get_id = driver_entry<CtxGetId>("cuCtxGetId");
+  if (get_current == nullptr || get_id == nullptr) return 0;
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 // One block per (component, batch member, z plane): weighted sum of the plane, fixed order.
 template <typename real>
@@ -85,21 +121,25 @@ int fail_static(int code, const std::string& msg) {
   return code;
 }
 
-// Device address of the scratch array on the current device, looked up once per device.
+// Device address of the scratch array in the current device's context, looked up once per
+// context (and on every call where the driver cannot name the context).
 int scratch_address(double** out) {
   int dev = 0;
   cudaError_t err = cudaGetDevice(&dev);
   if (err != cudaSuccess) return fail_static(OAFDTD_E_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(err));
   if (dev < 0 || dev >= kMaxDevices) return fail_static(OAFDTD_E_NODEVICE, "device index beyond the scratch table");
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (g_scratch_ptr[dev] == nullptr) {
+  const unsigned long long id = current_context_id();
+  ScratchSlot& slot = g_scratch[dev];
+  if (id == 0 || slot.ctx_id != id || slot.ptr == nullptr) {
     void* p = nullptr;
     err = cudaGetSymbolAddress(&p, g_energy_scratch);
     if (err != cudaSuccess)
       return fail_static(OAFDTD_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(err));
-    g_scratch_ptr[dev] = static_cast<double*>(p);
+    slot.ptr = static_cast<double*>(p);
+    slot.ctx_id = current_context_id();  // the lookup made the context current if it was not
   }
-  *out = g_scratch_ptr[dev];
+  *out = slot.ptr;
   return OAFDTD_OK;
 }
 
@@ -122,15 +162,24 @@ extern "C" int oafdtd_energy_noalloc(const oafdtd_energy_view* view, double* out
     return fail_static(OAFDTD_E_INVALID, "6 * batch * (nz + 2) = " + std::to_string(6 * per_comp) +
                                              " partial sums exceed the static scratch of " +
                                              std::to_string(kMaxPartials));
+  cudaStream_t s = static_cast<cudaStream_t>(v.stream);
+  // the call ends in a read-back and a synchronise, which a stream capture cannot hold
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t err = cudaStreamIsCapturing(s, &cap);
+  if (err != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+    if (err != cudaSuccess) cudaGetLastError();  // the query's error is not sticky: clear it
+    return fail_static(OAFDTD_E_INVALID,
+                       "oafdtd_energy_noalloc is synchronous and cannot run while its stream (or, for the legacy "
+                       "default stream, any stream in global mode) is being captured");
+  }
   double* scratch = nullptr;
   if (int rc = scratch_address(&scratch)) return rc;
-  cudaStream_t s = static_cast<cudaStream_t>(v.stream);
   dim3 grid((unsigned)per_comp, 6);
   if (v.real_bytes == 4)
     plane_energy_kernel<float><<<grid, 256, 0, s>>>(v, scratch);
   else
     plane_energy_kernel<double><<<grid, 256, 0, s>>>(v, scratch);
-  cudaError_t err = cudaGetLastError();
+  err = cudaGetLastError();
   if (err != cudaSuccess) return fail_static(OAFDTD_E_CUDA, std::string("energy kernel: ") + cudaGetErrorString(err));
   double* sums = scratch + kMaxPartials;
   plane_energy_sum_kernel<<<1, 32, 0, s>>>(scratch, (int)per_comp, sums);

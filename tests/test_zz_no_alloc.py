@@ -1,11 +1,11 @@
 """The field energy without device allocation, through the C ABI, against the engine's own
-energy entry point.
+energy entry point and the CPU oracle.
 
 ``oafdtd_energy_noalloc`` serves callers that cannot allocate device memory (a plugin whose host
-application owns every allocation, code that must not grow a memory pool while a graph region is
-open): it takes fields already on the device and keeps its partial sums in a fixed device array
-compiled into the library. This file runs last so that a failure here leaves every other test's
-result in place.
+application owns every device allocation, a service that reserves its device memory at start-up
+and may not grow it): it takes fields already on the device and keeps its partial sums in a fixed
+device array compiled into the library. This file runs last so that a failure here leaves every
+other test's result in place.
 """
 
 from __future__ import annotations
@@ -14,6 +14,7 @@ import ctypes as C
 
 import numpy as np
 import pytest
+
 
 @pytest.mark.gpu
 def test_energy_noalloc_matches_engine_energy_on_two_calls() -> None:
@@ -49,17 +50,39 @@ def test_energy_noalloc_matches_engine_energy_on_two_calls() -> None:
         view.cell_w[a] = on_device(g.cell_weights(a))
     view.eps_tab = on_device(np.asarray(c.eps_tab, dtype=np.float64))
     view.stream = None
+    from oracle.numpy_engine import OracleEngine
+
+    oracle = OracleEngine(c, "float32", pole_sum="loop")
+    free = []
     for steps in (30, 45):  # two calls in a row, on different fields
         eng.step(steps)
+        oracle.step(steps)
         for k in range(6):
             view.field[k] = on_device(eng.field(k).astype(np.float32))
         torch.cuda.synchronize()
+        before = torch.cuda.mem_get_info()[0]
         out = C.c_double()
         rc = lib.oafdtd_energy_noalloc(C.byref(view), C.byref(out))
         assert rc == native.OK, lib.oafdtd_last_error().decode()
+        free.append((before, torch.cuda.mem_get_info()[0]))
         want = eng.energy()
         assert want > 0
         assert abs(out.value - want) <= 1e-12 * want, (out.value, want)
+        want_cpu = oracle.energy()
+        assert abs(out.value - want_cpu) <= 1e-10 * want_cpu, (out.value, want_cpu)
+    # the second call (its device's set-up done by the first) leaves free device memory as it was
+    assert free[1][0] == free[1][1], free
+    # on a stream that is being captured the synchronous call is refused, and the capture survives
+    s = torch.cuda.Stream()
+    view.stream = s.cuda_stream
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=s):
+        rc = lib.oafdtd_energy_noalloc(C.byref(view), C.byref(C.c_double()))
+        y = keep[-1] * 2.0
+    assert rc == native.E_INVALID and b"captured" in lib.oafdtd_last_error()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(y, keep[-1] * 2.0)
 
 
 def test_energy_noalloc_rejects_oversized_problems() -> None:
