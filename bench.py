@@ -55,7 +55,6 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 CHUNK = 64
-WORKLOAD = "via_transition_400x400x120"
 
 
 # ---------------------------------------------------------------------------- distributed plumbing
@@ -180,7 +179,9 @@ def profiled_traffic(kernel: str) -> float | None:
 
 
 # ---------------------------------------------------------------------------- arms
-def build_problem(args: argparse.Namespace) -> tuple[Any, Any]:
+def build_problem(args: argparse.Namespace, native: bool | None = None) -> tuple[Any, Any]:
+    """The workload's model and its compiled arrays. ``native=False`` compiles with the NumPy
+    stages only (bit for bit the same arrays), so no engine library is loaded."""
     from open_analysis_gb300.model import compile_model
     from open_analysis_gb300.structures import large_board, microstrip, via_transition
 
@@ -193,7 +194,24 @@ def build_problem(args: argparse.Namespace) -> tuple[Any, Any]:
         m = via_transition(nx=nx, ny=ny, nz=nz)
     else:
         m = via_transition()
-    return m, compile_model(m, "float32")
+    return m, compile_model(m, "float32", native=native)
+
+
+def workload_config(args: argparse.Namespace, c: Any, world: int) -> dict[str, Any]:
+    """The workload keys both arms print (the launch shape and the time steps per bench step are
+    reported beside them: they describe how an arm steps, not what it computes)."""
+    nx, ny, nz = c.grid.n
+    names = {"microstrip": f"microstrip_{nx}x{ny}x{nz}", "large_board": f"large_board_{nx}x{ny}x{nz}"}
+    return {
+        "workload": names.get(args.workload, f"via_transition_{nx}x{ny}x{nz}"),
+        "cells": [nx, ny, nz],
+        "batch": c.batch,
+        "dft_frequencies": int(c.frequencies.size),
+        "ade_poles": 0 if c.ade is None else int(c.ade.tau.size),
+        "sibc_edges": 0 if c.sibc is None else int(c.sibc.flat.size),
+        "l2": "inputs larger than L2 (fields 6 x batch x 4 B per storage cell), no flush",
+        "parallelism": f"replicas{world}",
+    }
 
 
 def cpu_sample(c: Any, target_s: float) -> dict[str, Any]:
@@ -330,7 +348,8 @@ def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
     graph_kernels = eng.graph_kernels()
     peak, peak_kind = measured_peak()
     achieved = kb[dominant] / (ktimes[dominant] / 1e3) / 1e9
-    step_bytes = all_bytes["step"]
+    step_bytes = all_bytes["step"]  # what the launch shape in use must move per time step
+    model_bytes = eng.model_bytes()  # the separate sweeps' traffic model (72 + 6 / B B per cell-update)
     eng.close()
 
     # e2e through the public API with host buffers
@@ -381,19 +400,9 @@ def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
             "vs_baseline": None,
             "dtype": "f32",
             "data": "synthetic",
-            "config": {
-                "workload": {"microstrip": "microstrip_120x60x40", "large_board": f"large_board_{nx}x{ny}x{nz}"}.get(
-                    args.workload, f"via_transition_{nx}x{ny}x{nz}"),
-                "cells": [nx, ny, nz],
-                "batch": c.batch,
-                "time_steps_per_step": CHUNK,
-                "dft_frequencies": int(c.frequencies.size),
-                "ade_poles": 0 if c.ade is None else int(c.ade.tau.size),
-                "sibc_edges": 0 if c.sibc is None else int(c.sibc.flat.size),
-                "l2": "inputs larger than L2 (fields 6 x batch x 4 B per storage cell), no flush",
-                "parallelism": f"replicas{ranks.world}",
-                "tiles": tiles,
-            },
+            "config": workload_config(args, c, ranks.world),
+            "time_steps_per_step": CHUNK,
+            "tiles": tiles,
             "roofline": {
                 "bound": "hbm",
                 "kernel": dominant,
@@ -406,8 +415,13 @@ def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
                 "traffic": profiled_traffic(dominant) if args.workload == "via_transition" else None,
                 "kernel_ms": ktimes,
                 "algorithmic_bytes_per_launch": kb,
-                # the whole time step of the timed region (sweeps overlapped with slab kernels)
-                "step_frac": step_bytes / (total_ms / (args.steps * CHUNK) / 1e3) / 1e9 / peak,
+                # the whole time step of the timed region: the traffic model of the separate
+                # sweeps (Gcell-updates/s x bytes per cell-update) over the measured peak, and the
+                # bytes the launch shape in use moves (less with the fused sweep)
+                "step_frac": model_bytes / (total_ms / (args.steps * CHUNK) / 1e3) / 1e9 / peak,
+                "step_moved_frac": step_bytes / (total_ms / (args.steps * CHUNK) / 1e3) / 1e9 / peak,
+                "step_bytes_model": model_bytes,
+                "step_bytes_moved": step_bytes,
             },
             "e2e": e2e,
             "gpu_launches": graph_kernels * args.steps,
@@ -423,7 +437,8 @@ def run_reference(args: argparse.Namespace, ranks: Ranks) -> None:
         return
     from oracle.numpy_engine import OracleEngine
 
-    _, c = build_problem(args)
+    # the NumPy stages of the compiler: the reference arm maps no library of this package
+    _, c = build_problem(args, native=False)
     nx, ny, nz = c.grid.n
     eng = OracleEngine(c, "float32")
     for _ in range(args.warmup):
@@ -454,9 +469,8 @@ def run_reference(args: argparse.Namespace, ranks: Ranks) -> None:
                 "vs_baseline": None,
                 "dtype": "f32",
                 "data": "synthetic",
-                "config": {"workload": {"microstrip": "microstrip_120x60x40", "large_board": f"large_board_{nx}x{ny}x{nz}"}.get(
-                               args.workload, WORKLOAD),
-                           "cells": [nx, ny, nz], "batch": c.batch},
+                "config": workload_config(args, c, ranks.world),
+                "time_steps_per_step": 1,
                 "cpu_baseline": {"value": value, "unit": "Gcell-updates/s", "cores": 1, "kind": "port",
                                  "sample": sample},
                 "e2e": {"value": value, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0,
@@ -479,10 +493,11 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--tile-z", type=int, default=0, help="planes per block")
-    ap.add_argument("--variant", type=int, default=-1, help="1 staged sweeps, 0 register marching")
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="3 fused interior sweep, 2 TMA-staged, 1 cp.async-staged, 0 register marching")
     ap.add_argument("--cells", default="", help="via-transition grid 'nx,ny,nz' (smaller profiling cases)")
     ap.add_argument("--sweep-instances", type=int, default=64, help="batched-sweep instances (0: skip)")
-    ap.add_argument("--sweep-steps", type=int, default=2000, help="time steps per sweep instance")
+    ap.add_argument("--sweep-steps", type=int, default=8000, help="time steps per sweep instance")
     ap.add_argument("--surrogate-instances", type=int, default=384, help="surrogate sweep instances (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":

@@ -226,25 +226,30 @@ int oafdtd_peak_bytes(const oafdtd_engine* engine, int64_t* out);
 int oafdtd_set_graph(oafdtd_engine* engine, int32_t use_graph);
 
 /* Launch shape of the sweeps: z planes marched per block (tile_z, 0 keeps the current value) and
- * the sweep variant (2 stages the planes through shared memory with TMA tensor copies, the
- * default where the driver encodes the descriptors; 1 stages them with cp.async; 0 marches them
- * in registers; -1 keeps it). Variant 2 without descriptors is OAFDTD_E_INVALID. The autotuner
- * sets these. A staged sweep whose copies do not arrive within its bounded wait makes the step
- * return OAFDTD_E_TIMEOUT. */
+ * the sweep variant (3: the fused sweep, which updates H and E of the interior in one z-march and
+ * runs the rest as variant 2; it keeps two buffers per field, reading the current ones and writing
+ * the others, and is the default where the interior is not empty and the device has room for them;
+ * 2 stages the planes through shared memory with TMA tensor copies, the default otherwise where
+ * the driver encodes the descriptors; 1 stages them with cp.async; 0 marches them in registers;
+ * -1 keeps it). Variants 2 and 3 without descriptors, and 3 without an interior, are
+ * OAFDTD_E_INVALID. The autotuner sets these. A staged sweep whose copies do not arrive within its
+ * bounded wait makes the step return OAFDTD_E_TIMEOUT. */
 int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_z, int32_t variant);
 
 /* Average device time per step of each kernel class over the last oafdtd_step call, measured
  * with CUDA events when profiling is on (oafdtd_set_profiling). Writes up to n values in the
- * order: h_sweep (interior, staged), h_slab (CPML slabs, or everything in variant 0), ghosts,
- * pre_e, e_sweep, e_slab, edges, probe_e, whole step. */
+ * order: h_sweep (interior, staged; in variant 3 the z-slab planes), h_slab (CPML slabs, or
+ * everything in variant 0), ghosts, pre_e, e_sweep, e_slab, edges, probe_e, fused (the fused
+ * sweep of variant 3), whole step. */
 int oafdtd_set_profiling(oafdtd_engine* engine, int32_t on);
 int oafdtd_kernel_times(oafdtd_engine* engine, double* out_ms, int32_t n);
 
 /* Algorithmic DRAM bytes per time step of each kernel class under the current sweep variant, in
  * the order of oafdtd_kernel_times, then their sum; up to n values. The traffic model: 9 field
- * values per grid cell and batch member for each sweep (E also its three uint16 indices per
- * cell and the Debye currents), psi read+write per CPML cell, the surface-impedance state per
- * edge. A diagnostic of this library; the reference has no counterpart. */
+ * values per grid cell and batch member for each separate sweep (E also its three uint16 indices
+ * per cell and the Debye currents), 12 for the fused sweep (E and H read once and written once),
+ * psi read+write per CPML cell, the surface-impedance state per edge. A diagnostic of this
+ * library; the reference has no counterpart. */
 int oafdtd_kernel_bytes(oafdtd_engine* engine, double* out, int32_t n);
 
 /* Kernel launches in one replay of the captured 64-step graph (0 before the first capture). A
@@ -252,7 +257,9 @@ int oafdtd_kernel_bytes(oafdtd_engine* engine, double* out, int32_t n);
 int oafdtd_graph_kernels(oafdtd_engine* engine, int64_t* out);
 
 /* Algorithmic DRAM bytes of one time step (all batch members) under the traffic model of the
- * engine: fields, index, CPML psi, ADE J, SIBC state. Used for the roofline report. */
+ * separate sweeps (72 + 6 / B bytes per plain float32 cell-update, plus CPML psi, Debye J and SIBC
+ * state), whatever the variant moves: the figure the roofline fraction of the step is quoted
+ * against. */
 int oafdtd_model_bytes(const oafdtd_engine* engine, double* out);
 
 /* Field arrays already resident on the device, described for oafdtd_energy_noalloc: the six
@@ -273,14 +280,18 @@ typedef struct oafdtd_energy_view {
 
 /* Field energy 1/2 sum eps E^2 V + 1/2 mu0 sum H^2 V (float64, written to the host double *out)
  * of device-resident fields, without allocating any device memory: no cudaMalloc, cudaFree or
- * allocating library call. For callers that cannot allocate on the device, such as a plugin
- * whose host application owns every allocation or code that must not grow the memory pool while
- * a graph region is open. This entry point has no counterpart in the reference.
+ * allocating library call. For callers that cannot allocate on the device, such as a plugin whose
+ * host application owns every device allocation, or a service that reserves its device memory at
+ * start-up and must not grow it afterwards. This entry point has no counterpart in the reference.
  * Its partial sums live in a fixed device array of 65536 doubles (512 KiB, held on every GPU that
  * loads the library until the process exits): a problem with 6 * batch * (nz + 2) > 65536 is
- * rejected with OAFDTD_E_INVALID. All calls share that array, so calls that overlap on the GPU
- * race; serialise them. The first call on a device looks the array's address up for that device
- * (make it before any stream capture). Same formula as oafdtd_energy; the summation order
+ * rejected with OAFDTD_E_INVALID. Every call in the process shares that one array, whatever stream
+ * it is given, so calls that overlap on the GPU race; serialise them. The call is synchronous: it
+ * returns after a device-to-host copy of the result and a synchronise of its stream, so it cannot
+ * be issued while that stream is being captured (nor on the legacy default stream while another
+ * stream captures in global mode); it returns OAFDTD_E_INVALID there without launching anything.
+ * The first call in a device's context looks the array's address up for that context, which may
+ * load the library's module on the device. Same formula as oafdtd_energy; the summation order
  * differs (per-plane partial sums), so results agree to float64 rounding. */
 int oafdtd_energy_noalloc(const oafdtd_energy_view* view, double* out);
 

@@ -1,9 +1,10 @@
 """Launch-shape autotuner for the sweeps.
 
 Each block of a sweep marches ``tile_z`` planes; longer marches amortise the pipeline prologue
-and the carried-plane reload, shorter ones expose more blocks. Three sweep variants exist (planes
-staged through shared memory by TMA tensor copies or by cp.async, or marched in registers). The best point depends on the grid and
-the batch. :func:`tune` times each candidate on the
+and the carried-plane reload, shorter ones expose more blocks. Four sweep variants exist: the
+fused H + E sweep of the interior (3), planes staged through shared memory by TMA tensor copies
+(2) or by cp.async (1), or marched in registers (0). The best point depends on the grid and the
+batch. :func:`tune` times each candidate on the
 engine itself with CUDA events (a few 64-step chunks after one warm-up chunk, which also captures
 the graph of that shape) and leaves the fastest shape set on the engine. Timing steps advance
 the engine: tune a scratch engine of the same problem, or account for the steps taken.
@@ -15,7 +16,8 @@ from dataclasses import dataclass
 from typing import Any
 
 TILES = (4, 8, 16, 24, 32, 64)
-VARIANTS = (2, 1, 0)  # staged by TMA, staged by cp.async, register marching
+FUSED_TILES = (8, 16, 32, 64, 128)  # the fused sweep recomputes one plane per march: longer ones
+VARIANTS = (3, 2, 1, 0)  # fused, staged by TMA, staged by cp.async, register marching
 
 
 @dataclass(frozen=True)
@@ -27,13 +29,19 @@ class TuneResult:
 
 
 def _candidates(tiles: tuple[int, ...], variants: tuple[int, ...]) -> list[tuple[int, int]]:
-    # variant 0 runs the slab kernel alone, whose march does not depend on the tile
-    return [(tz, v) for v in variants for tz in (tiles if v != 0 else tiles[:1])]
+    # variant 0 runs the slab kernel alone, whose march does not depend on the tile; the fused
+    # sweep takes its own, longer marches unless the caller gives tiles
+    out = []
+    for v in variants:
+        vt = tiles[:1] if v == 0 else (FUSED_TILES if v == 3 and tiles == TILES else tiles)
+        out.extend((tz, v) for tz in vt)
+    return out
 
 
 def tune(engine: Any, chunks: int = 2, tiles: tuple[int, ...] = TILES, variants: tuple[int, ...] = VARIANTS) -> TuneResult:
     """Time every (tile, variant); needs ``(1 + chunks) * 64`` steps each. A variant the engine
-    refuses (TMA staging where the driver encoded no descriptors) is skipped."""
+    refuses (TMA staging where the driver encoded no descriptors, the fused sweep where the
+    interior is empty) is skipped."""
     from open_analysis_gb300.model import ModelError
 
     table: dict[tuple[int, int], float] = {}

@@ -78,4 +78,112 @@ __device__ __noinline__ real ade_cell(real e, real e0, real cbe, real beta0, int
   return en;
 }
 
+// ---------------------------------------------------------------------------- E update of a quad
+// A z-term correction of one quad: psi <- b psi + c d; F <- F + (sign k)(ek d + psi), with the
+// plane's coefficients and psi staged in shared memory, for the cells of the correction box; the
+// updated psi row goes back to global memory.
+template <typename real>
+struct ZTerm {
+  const real* sm;  // staged psi of the quad
+  real* g;         // psi of the quad in global memory
+  real eb, ec, ek, sign;
+  int lo0, hi0;
+  bool on;         // the row and plane lie in the correction box
+};
+
+template <typename real>
+__device__ __forceinline__ ZTerm<real> z_term(const SweepArgs<real>& a, const CpmlTerm<real>& T, int sd,
+                                              const real* sm, int b, int k, int j, int i0, int kind) {
+  ZTerm<real> z;
+  z.on = false;
+  if (sd < 0) return z;
+  const CpmlSide<real>& s = sd == 0 ? T.side[0] : T.side[1];
+  z.on = j >= s.lo[1] && j < s.hi[1] && k >= s.lo[2] && k < s.hi[2];
+  if (!z.on) return z;
+  const int w = s.hi[2] - s.lo[2];
+  z.sm = sm;
+  z.g = s.psi + ((((long long)b * w + (k - s.lo[2])) * a.Y + j) * a.X + i0);
+  const real* const* co = kind == 0 ? a.pe[2] : a.ph[2];
+  z.eb = __ldg(co[0] + k);
+  z.ec = __ldg(co[1] + k);
+  z.ek = __ldg(co[2] + k);
+  z.sign = T.sign;
+  z.lo0 = s.lo[0];
+  z.hi0 = s.hi[0];
+  return z;
+}
+
+template <typename real>
+__device__ __forceinline__ void z_apply(const ZTerm<real>& z, Quad<real>& f, const real (&d)[4], const real (&kf)[4],
+                                        int i0) {
+  if (!z.on) return;
+  Quad<real> ps = ld4(z.sm);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const int i = i0 + e;
+    if (i < z.lo0 || i >= z.hi0) continue;
+    real p = ps.v[e] * z.eb;
+    p = p + z.ec * d[e];
+    ps.v[e] = p;
+    const real upd = z.ek * d[e] + p;
+    f.v[e] = f.v[e] + (z.sign * kf[e]) * upd;
+  }
+  st4(z.g, ps);
+}
+
+// Bulk update, z correction (z sweeps) and the Debye update of one E component on one quad, in
+// the reference's order. d0/d1 are the derivatives along the component's two axes in ascending
+// order; the reference's term order is (d0, -d1) when first_plus, else (d1, -d0). j4 holds the
+// prefetched Debye current (P = 1).
+template <typename real, bool kZ, bool kMulti>
+__device__ __forceinline__ void e_apply(const SweepArgs<real>& a, int c, real* __restrict__ E, long long p,
+                                        const Quad<real>& e_old, const uint16_t* m, const real (&d0)[4],
+                                        const real (&d1)[4], bool first_plus, const Quad<real>& j4in,
+                                        const ZTerm<real>& zt, int i0, int j, int k, int b) {
+  const int X = a.X, Y = a.Y, nx = a.nx;
+  Quad<real> e4 = e_old;
+  Coef<real> cf[4];
+  real kf[4];
+  bool valid[4];
+  bool disp = false;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const int i = i0 + e;
+    cf[e] = a.coef[m[e]];
+    kf[e] = cf[e].cb;
+    valid[e] = i >= 1 && i <= nx + 1;
+    const real acc = first_plus ? d0[e] + (-d1[e]) : d1[e] + (-d0[e]);
+    if (valid[e]) e4.v[e] = cf[e].ca * e4.v[e] + cf[e].cb * acc;
+    disp |= valid[e] && m[e] >= a.ade_lo && m[e] < a.ade_hi;
+  }
+  if constexpr (kZ) z_apply(zt, e4, d1, kf, i0);
+  if (disp) {
+    const long long jstride = (long long)a.B * a.jnk[c] * Y * X;
+    const long long jq = (((long long)b * a.jnk[c] + (k - a.jk0[c])) * Y + j) * X + i0;
+    real* J = a.J[c];
+    if constexpr (!kMulti) {
+      Quad<real> j4 = j4in;
+      const real onekp = a.ade_onekp[0], kp = a.ade_kp[0];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        if (!(valid[e] && m[e] >= a.ade_lo && m[e] < a.ade_hi)) continue;
+        const real jt = (real)0.5 * (onekp * j4.v[e]);
+        const real en = e4.v[e] - cf[e].cbe * jt;
+        const real de = en - e_old.v[e];
+        j4.v[e] = kp * j4.v[e] + cf[e].beta0 * de;
+        e4.v[e] = en;
+      }
+      st4(J + jq, j4);
+    } else {
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        if (!(valid[e] && m[e] >= a.ade_lo && m[e] < a.ade_hi)) continue;
+        e4.v[e] = ade_cell(e4.v[e], e_old.v[e], cf[e].cbe, cf[e].beta0, m[e], J, jq + e, jstride, a.ade_kp,
+                           a.ade_onekp, a.ade_beta, a.ade_P);
+      }
+    }
+  }
+  st4(E + p, e4);
+}
+
 }  // namespace oafdtd

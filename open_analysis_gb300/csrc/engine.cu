@@ -60,18 +60,24 @@ struct EngineBase {
   virtual int plane_device(int comp, int k, void* dst, const void* src) = 0;
   virtual int kernel_times(double* out, int n) = 0;
   virtual int step_timed(int64_t n, double* ms) = 0;
+  // Switches the sweep variant (0..3); the fused variant allocates the second field buffers.
+  virtual int set_variant(int v) = 0;
   int64_t steps = 0;
   int64_t bytes = 0;
   int use_graph = 1;
   int profiling = 0;
   int tile_z = 16;
-  int staged = 2;     // 2: sweeps staged by TMA; 1: staged by cp.async; 0: register marching
+  // 3: fused H + E sweep of the interior (two buffers per field), the rest as 2; 2: sweeps
+  // staged by TMA; 1: staged by cp.async; 0: register marching
+  int staged = 2;
   bool tma_ok = false;  // the TMA descriptors were encoded (variant 2 available)
+  bool fused_ok = false;  // the fused box is not empty and its descriptors were encoded
   bool graph_dirty = false;  // launch shape or profiling changed: the graph is re-captured
   int64_t graph_kernels = 0;  // kernel nodes of the current captured 64-step graph (0: none)
-  // kernel classes: h_sweep, h_slab, ghosts, pre_e, e_sweep, e_slab, edges, probe_e
-  static constexpr int kClasses = 8;
-  double class_bytes[2][kClasses] = {};  // algorithmic bytes per step and class ([staged?][class])
+  // kernel classes: h_sweep, h_slab, ghosts, pre_e, e_sweep, e_slab, edges, probe_e, fused
+  static constexpr int kClasses = 9;
+  // algorithmic bytes per step and class: [0] variant 0, [1] variants 1 and 2, [2] variant 3
+  double class_bytes[3][kClasses] = {};
   double model_bytes = 0.0;
 };
 
@@ -88,11 +94,22 @@ struct Engine final : EngineBase {
   std::vector<void*> allocs;
   int nx = 0, ny = 0, nz = 0, X = 0, Y = 0, Z = 0, B = 0;
   long long bs = 0;
+  // Field buffers [buffer][E0..E2, H0..H2]. Buffer 1 exists once the fused variant has run:
+  // it then reads the current buffers and writes the other ones, and cur[] (E, H) swaps.
+  real* fbuf[2][6] = {};
+  int cur[2] = {0, 0};
+  bool two_buffers = false;
+  oafdtd::Span3 fused_box{};              // the fused sweep's box (variant 3)
+  oafdtd::Span3 zin_fused[2][2]{};        // z-slab planes over its x-y extent
+  oafdtd::Span3 slab_fused[2][6]{};       // the slab boxes around it
+  int n_slab_fused[2] = {0, 0};
+  int graph_parity = 0;                   // cur[0] at the start of the captured chunk
   int pmc_mask = 0;
   int max_steps = 0;
   int n_probe = 0, n_freq = 0, record_series = 0;
   oafdtd::SweepArgs<real> sw{};
-  oafdtd::SweepMaps maps{};
+  oafdtd::SweepMaps maps_p[2]{};  // staged-sweep descriptors of a step starting in buffer 0 / 1
+  oafdtd::FusedMaps fmaps[2]{};   // fused-sweep descriptors of a step starting in buffer 0 / 1
   int* status = nullptr;  // device status word of the bounded waits
   oafdtd::EdgeArgs<real> ed{};
   oafdtd::SibcArgs<real> sb{};
@@ -180,13 +197,21 @@ struct Engine final : EngineBase {
   int snapshot(void* out, int64_t* bytes, const void* in) override;
   int wait() override;
   int check_status();
-  // The sweep regions of the current variant: interior + slab boxes, or the slab kernel alone.
-  void use_regions() {
-    sw.staged = staged;
+  // The sweep regions of variant rv: the fused box with the z-slab and slab boxes around it (3),
+  // the staged interior with its z-slab and slab boxes (1, 2), or the slab kernel alone (0).
+  void use_regions(int rv) {
+    sw.staged = rv == 3 ? 2 : rv;
+    sw.fused = rv == 3 ? fused_box : oafdtd::Span3{0, 0, 0, 0, 0, 0};
     for (int kind = 0; kind < 2; ++kind) {
       for (int zr = 0; zr < 2; ++zr)
         for (int cc = 0; cc < 2; ++cc) sw.zsd[kind][zr][cc] = zsd[kind][zr][cc];
-      if (staged) {
+      if (rv == 3) {
+        sw.inner[kind] = oafdtd::Span3{0, 0, 0, 0, 0, 0};
+        sw.zin[kind][0] = zin_fused[kind][0];
+        sw.zin[kind][1] = zin_fused[kind][1];
+        sw.n_slab[kind] = n_slab_fused[kind];
+        for (int n = 0; n < 6; ++n) sw.slab[kind][n] = slab_fused[kind][n];
+      } else if (rv) {
         sw.inner[kind] = inner_staged[kind];
         sw.zin[kind][0] = zin_staged[kind][0];
         sw.zin[kind][1] = zin_staged[kind][1];
@@ -200,6 +225,31 @@ struct Engine final : EngineBase {
       }
     }
   }
+  // Pointers of a step that starts with E in buffer pe and H in buffer ph. In place (variants
+  // 0-2) the step writes the buffers it reads; the fused variant writes the other ones.
+  void bind(int pe, int ph) {
+    const bool pp = staged == 3;
+    for (int c = 0; c < 3; ++c) {
+      sw.E[c] = fbuf[pe][c];
+      sw.H[c] = fbuf[ph][3 + c];
+      sw.Eo[c] = fbuf[pp ? 1 - pe : pe][c];
+      sw.Ho[c] = fbuf[pp ? 1 - ph : ph][3 + c];
+      ed.E[c] = sw.Eo[c];
+      ed.H[c] = sw.Ho[c];
+      sb.E[c] = sw.Eo[c];
+      sb.H[c] = sw.Ho[c];
+      pr.E[c] = sw.E[c];
+      pr.F[c] = sw.Eo[c];
+      pr.F[3 + c] = sw.Ho[c];
+    }
+  }
+  // The current buffer of one component (0..2 E, 3..5 H).
+  real* field(int comp) { return fbuf[cur[comp < 3 ? 0 : 1]][comp]; }
+  // Encodes the TMA descriptors of a step starting in each buffer for the current variant.
+  int encode_maps();
+  // Copies the current fields into the other buffers (both then hold the same state).
+  int sync_buffers();
+  int set_variant(int v) override;
   int energy(double* out) override;
   int dft(double* out) override;
   int series(double* out) override;
@@ -212,7 +262,7 @@ struct Engine final : EngineBase {
   // read only the other field): forked onto `side` and joined back, inside the graph as well.
   cudaStream_t side = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
-  int sweep_pair(int kind, cudaEvent_t* ev, int slot, unsigned rec);
+  int sweep_pair(int kind, cudaEvent_t* ev, int slot, unsigned rec, const oafdtd::SweepMaps& mp);
 };
 
 // Build phase timer: with OAFDTD_TIMING set in the environment, oafdtd_create prints the
@@ -270,6 +320,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
   OA_CUDA(oafdtd::preload_kernels<real>());
   OA_CUDA(oafdtd::preload_staged<real>());
   OA_CUDA(oafdtd::preload_slab<real>());
+  OA_CUDA(oafdtd::preload_fused<real>());
   OA_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   OA_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
   OA_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
@@ -285,11 +336,10 @@ int Engine<real>::build(const oafdtd_problem& p) {
     if (rc) return rc;
     rc = alloc(&h, (size_t)bs * B);
     if (rc) return rc;
-    keep_state(e, (size_t)bs * B);
-    keep_state(h, (size_t)bs * B);
-    sw.E[c] = e;
-    sw.H[c] = h;
+    fbuf[0][c] = e;
+    fbuf[0][3 + c] = h;
   }
+  bind(0, 0);
 
   timer.mark("fields");
   // ---- Debye ADE: per-edge coefficient rows and the set of dispersive edges
@@ -770,17 +820,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
     ed.n_chan = p.n_chan;
     ed.max_steps = p.max_steps;
   }
-  for (int c = 0; c < 3; ++c) {
-    ed.E[c] = sw.E[c];
-    ed.H[c] = sw.H[c];
-    sb.E[c] = sw.E[c];
-    sb.H[c] = sw.H[c];
-    pr.E[c] = sw.E[c];
-    pr.F[c] = sw.E[c];
-    pr.F[3 + c] = sw.H[c];
-    en.F[c] = sw.E[c];
-    en.F[3 + c] = sw.H[c];
-  }
+  bind(0, 0);
   ed.bs = pr.bs = sb.bs = bs;
   sb.B = B;
   ed.X = X;
@@ -879,6 +919,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
   {
     const int Q = X / 4;
     whole = oafdtd::Span3{0, Q, 1, ny + 2, 1, nz + 2};
+    int lo_h[3] = {0, 1, 1};  // the first H cell past the low CPML slabs, per axis
     for (int kind = 0; kind < 2; ++kind) {
       int lo[3] = {0, 1, 1}, hi[3] = {X, ny + 2, nz + 2};
       for (int c = 0; c < 3; ++c)
@@ -922,13 +963,49 @@ int Engine<real>::build(const oafdtd_problem& p) {
       for (const oafdtd::Span3& bx : boxes)
         if (bx.q1 > bx.q0 && bx.j1 > bx.j0 && bx.k1 > bx.k0) slab_staged[kind][n++] = bx;
       n_slab_staged[kind] = n;
+      if (kind == 1)
+        for (int ax = 0; ax < 3; ++ax) lo_h[ax] = lo[ax];
     }
-    use_regions();
+    // The fused box: inside both interiors; its first cell on each axis one past the first H
+    // cell without corrections and past index 1 (the halo cells the fused sweep recomputes are
+    // then plain H cells, no ghosts); its last cell below the wall node n + 1 (no PMC mirror
+    // planes inside); the x origin an even quad (16-byte TMA boxes, as the staged sweeps).
+    {
+      const oafdtd::Span3& e = inner_staged[0];
+      const oafdtd::Span3& h = inner_staged[1];
+      int q0 = std::max(std::max(e.q0, h.q0), std::max((lo_h[0] + 4) / 4, 2));
+      q0 += q0 & 1;
+      const int q1 = std::min(std::min(e.q1, h.q1), (nx + 1) / 4);
+      const int j0 = std::max(std::max(e.j0, h.j0), std::max(lo_h[1] + 1, 2));
+      const int j1 = std::min(std::min(e.j1, h.j1), ny + 1);
+      const int k0 = std::max(std::max(e.k0, h.k0), std::max(lo_h[2] + 1, 2));
+      const int k1 = std::min(std::min(e.k1, h.k1), nz + 1);
+      if (q1 > q0 && j1 > j0 && k1 > k0) {
+        fused_box = oafdtd::Span3{q0, q1, j0, j1, k0, k1};
+        for (int kind = 0; kind < 2; ++kind) {
+          zin_fused[kind][0] = oafdtd::Span3{q0, q1, j0, j1, 1, k0};
+          zin_fused[kind][1] = oafdtd::Span3{q0, q1, j0, j1, k1, nz + 2};
+          const oafdtd::Span3 boxes[4] = {{0, Q, 1, j0, 1, nz + 2},
+                                          {0, Q, j1, ny + 2, 1, nz + 2},
+                                          {0, q0, j0, j1, 1, nz + 2},
+                                          {q1, Q, j0, j1, 1, nz + 2}};
+          int n = 0;
+          for (const oafdtd::Span3& bx : boxes)
+            if (bx.q1 > bx.q0 && bx.j1 > bx.j0 && bx.k1 > bx.k0) slab_fused[kind][n++] = bx;
+          n_slab_fused[kind] = n;
+        }
+      }
+    }
+    use_regions(staged);
     std::string why;
-    tma_ok = oafdtd::encode_sweep_maps<real>(sw, &maps, &why);
+    tma_ok = oafdtd::encode_sweep_maps<real>(sw, &maps_p[0], &why);
     if (!tma_ok && staged == 2) {
       staged = 1;
-      use_regions();
+      use_regions(staged);
+    }
+    if (tma_ok && fused_box.k1 > fused_box.k0) {
+      oafdtd::FusedMaps probe{};
+      fused_ok = oafdtd::encode_fused_maps<real>(sw, &probe, &why);
     }
   }
   timer.mark("regions_maps");
@@ -936,8 +1013,10 @@ int Engine<real>::build(const oafdtd_problem& p) {
   // Sweeps: read 3 source components, read-modify-write 3 updated ones (9 values) per grid cell
   // and member; E also the three uint16 indices per cell and J read+write (2 P values) per
   // dispersive edge; psi read+write per correction cell, in the class of the kernel that applies
-  // it. Edges: surface-impedance v_p and J_prev read+write, two H samples and the E write per
-  // edge.
+  // it. The fused sweep: read E and H, write E and H (12 values) per cell and member, the indices
+  // and J. Edges: surface-impedance v_p and J_prev read+write, two H samples and the E write per
+  // edge. The step's model bytes are those of the separate sweeps (72 + 6 / B bytes per plain
+  // cell-update in float32), whatever the variant moves.
   {
     const double rb = sizeof(real);
     auto cells_in = [&](const oafdtd::Span3& s) {
@@ -946,68 +1025,96 @@ int Engine<real>::build(const oafdtd_problem& p) {
       const double z = std::max(0, std::min(s.k1, nz + 1) - std::max(s.k0, 1));
       return x * y * z;
     };
-    // the staged kernels' share of a kind: the interior and the two z-slab boxes
-    auto staged_cells = [&](int kind) {
-      return cells_in(inner_staged[kind]) + cells_in(zin_staged[kind][0]) + cells_in(zin_staged[kind][1]);
-    };
-    const double cells = (double)nx * ny * nz;
-    double psi[2] = {0.0, 0.0}, psi_st[2] = {0.0, 0.0};
-    for (int n = 0; n < p.n_corr; ++n) {
-      const oafdtd_correction& k = p.corr[n];
-      const double per = (double)B * 2.0 * rb;
-      psi[k.kind] += (double)(k.hi[0] - k.lo[0]) * (k.hi[1] - k.lo[1]) * (k.hi[2] - k.lo[2]) * per;
-      for (int zr = 0; zr < 2; ++zr) {  // the part inside a staged z-slab box
-        const oafdtd::Span3& z = zin_staged[k.kind][zr];
+    // psi bytes of one kind's corrections inside a box (all of them for the whole domain)
+    auto psi_in = [&](int kind, const oafdtd::Span3& z) {
+      double out = 0.0;
+      for (int n = 0; n < p.n_corr; ++n) {
+        const oafdtd_correction& k = p.corr[n];
+        if (k.kind != kind) continue;
         const double x = std::max(0, std::min(4 * z.q1, (int)k.hi[0]) - std::max(4 * z.q0, (int)k.lo[0]));
         const double y = std::max(0, std::min(z.j1, (int)k.hi[1]) - std::max(z.j0, (int)k.lo[1]));
         const double zz = std::max(0, std::min(z.k1, (int)k.hi[2]) - std::max(z.k0, (int)k.lo[2]));
-        psi_st[k.kind] += x * y * zz * per;
+        out += x * y * zz * (double)B * 2.0 * rb;
       }
-    }
-    // Debye edges: all, deferred, and those in the staged E boxes (index entries in the
-    // dispersive range, counted over the boxes' rows)
+      return out;
+    };
+    // Debye current bytes of the dispersive (not deferred) edges inside a box
     const double jv = (double)B * P * 2.0 * rb;
+    auto j_in = [&](const oafdtd::Span3& bx) {
+      double n_in = 0.0;
+      if (ade_hi <= ade_lo || bx.q1 <= bx.q0 || bx.j1 <= bx.j0 || bx.k1 <= bx.k0) return 0.0;
+      for (int c = 0; c < 3; ++c) {
+        std::vector<long long> part(kMaxParts, 0);
+        const int nj = bx.j1 - bx.j0;
+        parallel_parts((long long)(bx.k1 - bx.k0) * nj, [&](long long b0, long long e0, int t) {
+          long long n = 0;
+          for (long long r = b0; r < e0; ++r) {
+            const uint16_t* row = host_mat[c].data() + ((long long)(bx.k0 + r / nj) * Y + bx.j0 + r % nj) * X;
+            for (int i = 4 * bx.q0; i < 4 * bx.q1; ++i) n += row[i] >= ade_lo && row[i] < ade_hi;
+          }
+          part[t] = n;
+        });
+        for (long long n : part) n_in += (double)n;
+      }
+      return n_in * jv;
+    };
+    const oafdtd::Span3 all{0, X / 4, 0, Y, 0, Z};
+    const double cells = (double)nx * ny * nz;
     double n_all = 0.0, n_def = 0.0;
     for (int c = 0; c < 3; ++c)
       for (const AdeEdge& ae : ade_edges[c]) (ae.defer ? n_def : n_all) += 1.0;
-    double n_in = 0.0;
-    if (ade_hi > ade_lo) {
-      const oafdtd::Span3 boxes[3] = {inner_staged[0], zin_staged[0][0], zin_staged[0][1]};
-      for (int c = 0; c < 3; ++c)
-        for (const oafdtd::Span3& bx : boxes) {
-          if (bx.q1 <= bx.q0 || bx.j1 <= bx.j0 || bx.k1 <= bx.k0) continue;
-          std::vector<long long> part(kMaxParts, 0);
-          const int nj = bx.j1 - bx.j0;
-          parallel_parts((long long)(bx.k1 - bx.k0) * nj, [&](long long b0, long long e0, int t) {
-            long long n = 0;
-            for (long long r = b0; r < e0; ++r) {
-              const uint16_t* row = host_mat[c].data() + ((long long)(bx.k0 + r / nj) * Y + bx.j0 + r % nj) * X;
-              for (int i = 4 * bx.q0; i < 4 * bx.q1; ++i) n += row[i] >= ade_lo && row[i] < ade_hi;
-            }
-            part[t] = n;
-          });
-          for (long long n : part) n_in += (double)n;
-        }
-    }
-    const double j_all = n_all * jv, j_def = n_def * jv, j_in = n_in * jv;
-    const double h_in = staged_cells(1), e_in = staged_cells(0);
-    const double per_h = B * 9.0 * rb, per_e = B * 9.0 * rb + 6.0;
+    const double j_all = n_all * jv, j_def = n_def * jv;
+    const double psi_all[2] = {psi_in(0, all), psi_in(1, all)};
+    const double per_h = B * 9.0 * rb, per_e = B * 9.0 * rb + 6.0, per_f = B * 12.0 * rb + 6.0;
     const double edges = (double)p.sibc_n * B * (2.0 * rb * (1 + p.sibc_poles) + 3.0 * rb) + j_def;
-    // classes: h_sweep, h_slab, ghosts, pre_e, e_sweep, e_slab, edges, probe_e
-    double* st = class_bytes[1];
-    st[0] = h_in * per_h + psi_st[1];
-    st[1] = (cells - h_in) * per_h + psi[1] - psi_st[1];
-    st[4] = e_in * per_e + j_in + psi_st[0];
-    st[5] = (cells - e_in) * per_e + psi[0] - psi_st[0] + (j_all - j_in);
-    st[6] = edges;
-    double* sl = class_bytes[0];
-    sl[1] = cells * per_h + psi[1];
-    sl[5] = cells * per_e + psi[0] + j_all;
-    sl[6] = edges;
-    model_bytes = 0.0;
-    for (int k = 0; k < kClasses; ++k) model_bytes += st[k];
+    // classes: h_sweep, h_slab, ghosts, pre_e, e_sweep, e_slab, edges, probe_e, fused
+    {  // variants 1 and 2: staged interior and z-slab boxes, slab boxes around them
+      double* st = class_bytes[1];
+      const double hc = cells_in(inner_staged[1]) + cells_in(zin_staged[1][0]) + cells_in(zin_staged[1][1]);
+      const double ec = cells_in(inner_staged[0]) + cells_in(zin_staged[0][0]) + cells_in(zin_staged[0][1]);
+      const double hp = psi_in(1, zin_staged[1][0]) + psi_in(1, zin_staged[1][1]);
+      const double ep = psi_in(0, zin_staged[0][0]) + psi_in(0, zin_staged[0][1]);
+      const double ej = j_in(inner_staged[0]) + j_in(zin_staged[0][0]) + j_in(zin_staged[0][1]);
+      st[0] = hc * per_h + hp;
+      st[1] = (cells - hc) * per_h + psi_all[1] - hp;
+      st[4] = ec * per_e + ej + ep;
+      st[5] = (cells - ec) * per_e + psi_all[0] - ep + (j_all - ej);
+      st[6] = edges;
+      model_bytes = 0.0;
+      for (int k = 0; k < kClasses; ++k) model_bytes += st[k];
+    }
+    {  // variant 0: the slab kernel alone
+      double* sl = class_bytes[0];
+      sl[1] = cells * per_h + psi_all[1];
+      sl[5] = cells * per_e + psi_all[0] + j_all;
+      sl[6] = edges;
+    }
+    if (fused_box.k1 > fused_box.k0) {  // variant 3: the fused box, z-slab and slab boxes around it
+      double* fu = class_bytes[2];
+      const double fc = cells_in(fused_box);
+      const double fj = j_in(fused_box);
+      const double hz = cells_in(zin_fused[1][0]) + cells_in(zin_fused[1][1]);
+      const double ez = cells_in(zin_fused[0][0]) + cells_in(zin_fused[0][1]);
+      const double hp = psi_in(1, zin_fused[1][0]) + psi_in(1, zin_fused[1][1]);
+      const double ep = psi_in(0, zin_fused[0][0]) + psi_in(0, zin_fused[0][1]);
+      const double ej = j_in(zin_fused[0][0]) + j_in(zin_fused[0][1]);
+      fu[8] = fc * per_f + fj;
+      fu[0] = hz * per_h + hp;
+      fu[1] = (cells - fc - hz) * per_h + psi_all[1] - hp;
+      fu[4] = ez * per_e + ej + ep;
+      fu[5] = (cells - fc - ez) * per_e + psi_all[0] - ep + (j_all - fj - ej);
+      fu[6] = edges;
+    }
   }
   timer.mark("traffic_model");
+  // The fused sweep is the default where it applies and the device has room for the second
+  // field buffers; otherwise the staged sweeps run in place.
+  if (fused_ok && staged == 2) {
+    size_t free_b = 0, total_b = 0;
+    OA_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    if ((double)free_b > 1.05 * 6.0 * (double)bs * B * sizeof(real))
+      if (int rc = set_variant(3)) return rc;
+  }
   OA_CUDA(cudaStreamSynchronize(stream));
   timer.mark("device_sync");
   return OAFDTD_OK;
@@ -1018,7 +1125,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
 // other between the class events ev[slot], ev[slot + 1], ev[slot + 2]; otherwise the slab kernel
 // is forked onto the side stream and joined back.
 template <typename real>
-int Engine<real>::sweep_pair(int kind, cudaEvent_t* ev, int slot, unsigned rec) {
+int Engine<real>::sweep_pair(int kind, cudaEvent_t* ev, int slot, unsigned rec, const oafdtd::SweepMaps& mp) {
   const char* names[2][2] = {{"e_sweep: ", "e_slab: "}, {"h_sweep: ", "h_slab: "}};
   const bool fork = ev == nullptr && sw.staged;
   cudaError_t err;
@@ -1028,14 +1135,14 @@ int Engine<real>::sweep_pair(int kind, cudaEvent_t* ev, int slot, unsigned rec) 
     err = oafdtd::launch_slab<real>(sw, kind, side);
     if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string(names[kind][1]) + cudaGetErrorString(err));
     OA_CUDA(cudaEventRecord(join_ev, side));
-    err = oafdtd::launch_staged_sweep<real>(sw, maps, stream, kind == 1);
+    err = oafdtd::launch_staged_sweep<real>(sw, mp, stream, kind == 1);
     if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string(names[kind][0]) + cudaGetErrorString(err));
     OA_CUDA(cudaStreamWaitEvent(stream, join_ev, 0));
     return OAFDTD_OK;
   }
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[slot], stream, rec));
   if (sw.staged) {
-    err = oafdtd::launch_staged_sweep<real>(sw, maps, stream, kind == 1);
+    err = oafdtd::launch_staged_sweep<real>(sw, mp, stream, kind == 1);
     if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string(names[kind][0]) + cudaGetErrorString(err));
   }
   if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[slot + 1], stream, rec));
@@ -1045,15 +1152,46 @@ int Engine<real>::sweep_pair(int kind, cudaEvent_t* ev, int slot, unsigned rec) 
   return OAFDTD_OK;
 }
 
+// One time step (parts 3) or one half of it (1: H, 2: E), from the current buffers. Profiling
+// records the class events of the step: ev[9] at its start, ev[0..8] after the fused sweep,
+// h_sweep, h_slab, ghosts, pre_e, e_sweep, e_slab, edges and probe_e. In the fused variant the
+// H part outside the fused box runs beside the fused sweep, on the side stream, and the buffers
+// swap after the step (after each half for the halves, which run the separate sweeps).
 template <typename real>
 int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing, int parts) {
   cudaError_t err;
   // inside a stream capture an event record becomes a graph node only with the external flag
   const unsigned rec = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+  const int p = cur[0];
+  const bool fused = staged == 3 && parts == 3;
+  use_regions(fused ? 3 : (staged == 3 ? 2 : staged));
+  bind(p, p);
+  const oafdtd::SweepMaps& mp = maps_p[p];
+  if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[9], stream, rec));
+  if (fused) {
+    if (ev) {
+      err = oafdtd::launch_fused_sweep<real>(sw, fmaps[p], stream);
+      if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("fused: ") + cudaGetErrorString(err));
+      if (int rc = sweep_pair(1, ev, 0, rec, mp)) return rc;
+    } else {
+      // the H cells outside the fused box read only the current buffers: beside the fused sweep
+      OA_CUDA(cudaEventRecord(fork_ev, stream));
+      OA_CUDA(cudaStreamWaitEvent(side, fork_ev, 0));
+      err = oafdtd::launch_staged_sweep<real>(sw, mp, side, true);
+      if (err == cudaSuccess) err = oafdtd::launch_slab<real>(sw, 1, side);
+      if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("h_sweep: ") + cudaGetErrorString(err));
+      OA_CUDA(cudaEventRecord(join_ev, side));
+      err = oafdtd::launch_fused_sweep<real>(sw, fmaps[p], stream);
+      if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("fused: ") + cudaGetErrorString(err));
+      OA_CUDA(cudaStreamWaitEvent(stream, join_ev, 0));
+    }
+  } else if (parts & 1) {
+    if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[0], stream, rec));
+    if (int rc = sweep_pair(1, ev, 0, rec, mp)) return rc;
+  }
   if (parts & 1) {
-    if (int rc = sweep_pair(1, ev, 0, rec)) return rc;
     if (pmc_mask) {
-      err = oafdtd::launch_ghosts<real>(sw.H, pmc_mask, nx, ny, nz, X, Y, B, stream);
+      err = oafdtd::launch_ghosts<real>(sw.Ho, pmc_mask, nx, ny, nz, X, Y, B, stream);
       if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("ghosts: ") + cudaGetErrorString(err));
     }
     if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[3], stream, rec));
@@ -1061,7 +1199,7 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing, int part
     if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("pre_e: ") + cudaGetErrorString(err));
   }
   if (parts & 2) {
-    if (int rc = sweep_pair(0, ev, 4, rec)) return rc;
+    if (int rc = sweep_pair(0, ev, 4, rec, mp)) return rc;
     err = oafdtd::launch_sibc<real>(sb, stream);
     if (err == cudaSuccess) err = oafdtd::launch_edges<real>(ed, off, stream);
     if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("edges: ") + cudaGetErrorString(err));
@@ -1069,6 +1207,10 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing, int part
     err = oafdtd::launch_probe_e<real>(pr, off, stream);
     if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("probe_e: ") + cudaGetErrorString(err));
     if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[8], stream, rec));
+  }
+  if (staged == 3) {  // the other buffers now hold the newer field(s)
+    if (parts & 1) cur[1] ^= 1;
+    if (parts & 2) cur[0] ^= 1;
   }
   return OAFDTD_OK;
 }
@@ -1082,6 +1224,10 @@ int Engine<real>::capture() {
   graph_ready = false;
   graph_kernels = 0;
   cudaGraph_t graph = nullptr;
+  // a capture launches nothing: the buffer state it walks through is put back afterwards (a whole
+  // chunk is an even number of steps, so a replay leaves the buffers where it found them)
+  const int cur0[2] = {cur[0], cur[1]};
+  graph_parity = cur[0];
   OA_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
   int rc = OAFDTD_OK;
   for (int o = 0; o < oafdtd::kChunk && rc == OAFDTD_OK; ++o)
@@ -1090,6 +1236,8 @@ int Engine<real>::capture() {
     cudaError_t err = oafdtd::launch_bump(step_base, oafdtd::kChunk, stream);
     if (err != cudaSuccess) rc = fail(OAFDTD_E_CUDA, cudaGetErrorString(err));
   }
+  cur[0] = cur0[0];
+  cur[1] = cur0[1];
   cudaError_t err = cudaStreamEndCapture(stream, &graph);
   if (rc != OAFDTD_OK) {
     if (graph) cudaGraphDestroy(graph);
@@ -1156,7 +1304,6 @@ int Engine<real>::enqueue(int64_t n) {
     graph_ready = false;
   }
   sw.tile_z = tile_z;
-  use_regions();
   if (profiling) {
     for (double& v : prof_ms) v = 0.0;
     prof_steps = 0;
@@ -1166,7 +1313,7 @@ int Engine<real>::enqueue(int64_t n) {
     const int64_t start = steps;
     const int take = (int)std::min<int64_t>(n - done, oafdtd::kChunk - start % oafdtd::kChunk);
     if (use_graph && take == oafdtd::kChunk) {
-      if (!graph_ready) {
+      if (!graph_ready || (staged == 3 && graph_parity != cur[0])) {
         int rc = capture();
         if (rc) return rc;
       }
@@ -1181,15 +1328,17 @@ int Engine<real>::enqueue(int64_t n) {
     }
     if (profiling) {
       OA_CUDA(cudaStreamSynchronize(stream));
+      // class k < 8: ev[k] to ev[k + 1]; the fused sweep: ev[9] to ev[0]; the step: ev[9] to ev[8]
       for (int o = 0; o < take; ++o) {
         cudaEvent_t* ev = &events[(size_t)o * (kClasses + 1)];
-        for (int k = 0; k < kClasses; ++k) {
-          float ms = 0.f;
+        float ms = 0.f;
+        for (int k = 0; k < 8; ++k) {
           OA_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
           prof_ms[k] += ms;
         }
-        float ms = 0.f;
-        OA_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[kClasses]));
+        OA_CUDA(cudaEventElapsedTime(&ms, ev[9], ev[0]));
+        prof_ms[8] += ms;
+        OA_CUDA(cudaEventElapsedTime(&ms, ev[9], ev[8]));
         prof_ms[kClasses] += ms;
       }
       prof_steps += take;
@@ -1234,6 +1383,7 @@ int Engine<real>::kernel_times(double* out, int n) {
 template <typename real>
 int Engine<real>::energy(double* out) {
   OA_CUDA(cudaSetDevice(device));
+  for (int cc = 0; cc < 6; ++cc) en.F[cc] = field(cc);
   cudaError_t err = oafdtd::launch_energy<real>(en, energy_partial, oafdtd::kEnergyBlocks, energy_out, stream);
   if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, cudaGetErrorString(err));
   double parts[6];
@@ -1276,7 +1426,7 @@ template <typename real>
 int Engine<real>::fields(int comp, double* out) {
   if (comp < 0 || comp > 5) return fail(OAFDTD_E_INVALID, "component must be 0..5");
   OA_CUDA(cudaSetDevice(device));
-  const real* src = comp < 3 ? sw.E[comp] : sw.H[comp - 3];
+  const real* src = field(comp);
   const size_t count = (size_t)bs * B;
   std::vector<real> tmp(count);
   OA_CUDA(cudaMemcpyAsync(tmp.data(), src, count * sizeof(real), cudaMemcpyDeviceToHost, stream));
@@ -1295,7 +1445,6 @@ int Engine<real>::step_half(int which) {
     if (half_pending) return fail(OAFDTD_E_INVALID, "an H half is already pending");
     if (steps + 1 > max_steps) return fail(OAFDTD_E_RANGE, "step count exceeds max_steps (wave table length)");
     sw.tile_z = tile_z;
-    use_regions();
     if (int rc = launch_step(0, nullptr, false, 1)) return rc;
     half_pending = true;
   } else {
@@ -1318,14 +1467,15 @@ int Engine<real>::plane(int comp, int k, double* out, const double* in) {
   if (comp < 0 || comp > 5) return fail(OAFDTD_E_INVALID, "component must be 0..5");
   if (k < 0 || k >= Z) return fail(OAFDTD_E_INVALID, "plane out of range");
   OA_CUDA(cudaSetDevice(device));
-  real* f = comp < 3 ? sw.E[comp] : sw.H[comp - 3];
+  real* f = field(comp);
   const size_t per = (size_t)X * Y;
   std::vector<real> tmp(per * B);
-  if (in) {
+  if (in) {  // written to both buffers: the plane is the same state in either
     for (size_t q = 0; q < tmp.size(); ++q) tmp[q] = (real)in[q];
-    for (int b = 0; b < B; ++b)
-      OA_CUDA(cudaMemcpyAsync(f + (size_t)b * bs + (size_t)k * per, tmp.data() + b * per, per * sizeof(real),
-                              cudaMemcpyHostToDevice, stream));
+    for (int buf = 0; buf < (two_buffers ? 2 : 1); ++buf)
+      for (int b = 0; b < B; ++b)
+        OA_CUDA(cudaMemcpyAsync(fbuf[buf][comp] + (size_t)b * bs + (size_t)k * per, tmp.data() + b * per,
+                                per * sizeof(real), cudaMemcpyHostToDevice, stream));
     OA_CUDA(cudaStreamSynchronize(stream));
   } else {
     for (int b = 0; b < B; ++b)
@@ -1345,28 +1495,32 @@ int Engine<real>::plane_device(int comp, int k, void* dst, const void* src) {
   if (comp < 0 || comp > 5) return fail(OAFDTD_E_INVALID, "component must be 0..5");
   if (k < 0 || k >= Z) return fail(OAFDTD_E_INVALID, "plane out of range");
   OA_CUDA(cudaSetDevice(device));
-  real* f = comp < 3 ? sw.E[comp] : sw.H[comp - 3];
   const size_t per = (size_t)X * Y;
   for (int b = 0; b < B; ++b) {
-    real* field = f + (size_t)b * bs + (size_t)k * per;
-    if (src)
-      OA_CUDA(cudaMemcpyAsync(field, static_cast<const real*>(src) + b * per, per * sizeof(real), cudaMemcpyDefault,
-                              stream));
-    else
-      OA_CUDA(cudaMemcpyAsync(static_cast<real*>(dst) + b * per, field, per * sizeof(real), cudaMemcpyDefault,
-                              stream));
+    if (src) {  // written to both buffers, as oafdtd_set_plane
+      for (int buf = 0; buf < (two_buffers ? 2 : 1); ++buf)
+        OA_CUDA(cudaMemcpyAsync(fbuf[buf][comp] + (size_t)b * bs + (size_t)k * per,
+                                static_cast<const real*>(src) + b * per, per * sizeof(real), cudaMemcpyDefault,
+                                stream));
+    } else {
+      OA_CUDA(cudaMemcpyAsync(static_cast<real*>(dst) + b * per, field(comp) + (size_t)b * bs + (size_t)k * per,
+                              per * sizeof(real), cudaMemcpyDefault, stream));
+    }
   }
   OA_CUDA(cudaStreamSynchronize(stream));
   return OAFDTD_OK;
 }
 
-// Snapshot layout: a 32-byte header (magic, format version, total bytes, step count), then every
-// state buffer in registration order. out == in == nullptr: report the size only.
+// Snapshot layout: a 32-byte header (magic, format version, total bytes, step count), the six
+// current field arrays (E0..E2, H0..H2), then every other state buffer in registration order.
+// out == in == nullptr: report the size only. A restore writes the fields into both buffers.
 constexpr uint64_t kSnapshotMagic = 0x3130504E53444641ull;  // "AFDSNP01" read little-endian
+constexpr uint64_t kSnapshotVersion = 2;
 
 template <typename real>
 int Engine<real>::snapshot(void* out, int64_t* bytes, const void* in) {
-  uint64_t total = 32;
+  const size_t fbytes = (size_t)bs * B * sizeof(real);
+  uint64_t total = 32 + 6 * (uint64_t)fbytes;
   for (const auto& sb_ : state_bufs) total += sb_.second;
   if (bytes) *bytes = (int64_t)total;
   if (!out && !in) return OAFDTD_OK;
@@ -1374,9 +1528,11 @@ int Engine<real>::snapshot(void* out, int64_t* bytes, const void* in) {
   OA_CUDA(cudaSetDevice(device));
   if (out) {
     unsigned char* o = static_cast<unsigned char*>(out);
-    const uint64_t head[4] = {kSnapshotMagic, 1, total, (uint64_t)steps};
+    const uint64_t head[4] = {kSnapshotMagic, kSnapshotVersion, total, (uint64_t)steps};
     std::memcpy(o, head, sizeof(head));
     size_t at = 32;
+    for (int comp = 0; comp < 6; ++comp, at += fbytes)
+      OA_CUDA(cudaMemcpyAsync(o + at, field(comp), fbytes, cudaMemcpyDeviceToHost, stream));
     for (const auto& sb_ : state_bufs) {
       OA_CUDA(cudaMemcpyAsync(o + at, sb_.first, sb_.second, cudaMemcpyDeviceToHost, stream));
       at += sb_.second;
@@ -1387,10 +1543,13 @@ int Engine<real>::snapshot(void* out, int64_t* bytes, const void* in) {
   const unsigned char* i = static_cast<const unsigned char*>(in);
   uint64_t head[4];
   std::memcpy(head, i, sizeof(head));
-  if (head[0] != kSnapshotMagic || head[1] != 1) return fail(OAFDTD_E_INVALID, "not a snapshot of this format");
+  if (head[0] != kSnapshotMagic || head[1] != kSnapshotVersion) return fail(OAFDTD_E_INVALID, "not a snapshot of this format");
   if (head[2] != total) return fail(OAFDTD_E_INVALID, "the snapshot was taken of another problem or configuration");
   if ((int64_t)head[3] > max_steps) return fail(OAFDTD_E_RANGE, "the snapshot's step count exceeds max_steps");
   size_t at = 32;
+  for (int comp = 0; comp < 6; ++comp, at += fbytes)
+    for (int buf = 0; buf < (two_buffers ? 2 : 1); ++buf)
+      OA_CUDA(cudaMemcpyAsync(fbuf[buf][comp], i + at, fbytes, cudaMemcpyHostToDevice, stream));
   for (const auto& sb_ : state_bufs) {
     OA_CUDA(cudaMemcpyAsync(sb_.first, i + at, sb_.second, cudaMemcpyHostToDevice, stream));
     at += sb_.second;
@@ -1404,11 +1563,62 @@ template <typename real>
 int Engine<real>::set_field(int comp, const double* in) {
   if (comp < 0 || comp > 5) return fail(OAFDTD_E_INVALID, "component must be 0..5");
   OA_CUDA(cudaSetDevice(device));
-  real* dst = comp < 3 ? sw.E[comp] : sw.H[comp - 3];
   const size_t count = (size_t)bs * B;
   std::vector<real> tmp(count);
   for (size_t k = 0; k < count; ++k) tmp[k] = (real)in[k];
-  OA_CUDA(cudaMemcpyAsync(dst, tmp.data(), count * sizeof(real), cudaMemcpyHostToDevice, stream));
+  for (int buf = 0; buf < (two_buffers ? 2 : 1); ++buf)  // the same state in both buffers
+    OA_CUDA(cudaMemcpyAsync(fbuf[buf][comp], tmp.data(), count * sizeof(real), cudaMemcpyHostToDevice, stream));
+  OA_CUDA(cudaStreamSynchronize(stream));
+  return OAFDTD_OK;
+}
+
+template <typename real>
+int Engine<real>::sync_buffers() {
+  if (!two_buffers) return OAFDTD_OK;
+  OA_CUDA(cudaSetDevice(device));
+  for (int comp = 0; comp < 6; ++comp) {
+    const int c = cur[comp < 3 ? 0 : 1];
+    OA_CUDA(cudaMemcpyAsync(fbuf[1 - c][comp], fbuf[c][comp], (size_t)bs * B * sizeof(real), cudaMemcpyDeviceToDevice,
+                            stream));
+  }
+  return OAFDTD_OK;
+}
+
+template <typename real>
+int Engine<real>::encode_maps() {
+  std::string why;
+  const int n = two_buffers ? 2 : 1;
+  for (int p = 0; p < n; ++p) {
+    bind(p, p);
+    sw.staged = staged == 3 ? 2 : staged;
+    if (tma_ok && !oafdtd::encode_sweep_maps<real>(sw, &maps_p[p], &why)) return fail(OAFDTD_E_CUDA, why);
+    if (staged == 3 && !oafdtd::encode_fused_maps<real>(sw, &fmaps[p], &why)) return fail(OAFDTD_E_CUDA, why);
+  }
+  bind(cur[0], cur[0]);
+  return OAFDTD_OK;
+}
+
+// Variant 3 allocates the second field buffers (once) and copies the current fields into them:
+// cells no sweep writes (ghosts, the padding of the rows) must hold the same values in both.
+template <typename real>
+int Engine<real>::set_variant(int v) {
+  if (v < 0 || v > 3) return fail(OAFDTD_E_INVALID, "variant must be 0..3");
+  if (half_pending) return fail(OAFDTD_E_INVALID, "an H half is pending: finish the step with the E half");
+  if (v >= 2 && !tma_ok)
+    return fail(OAFDTD_E_INVALID, "variants 2 and 3 need TMA descriptors, which the driver did not encode");
+  if (v == 3 && !fused_ok)
+    return fail(OAFDTD_E_INVALID, "variant 3 needs a fused box (an interior free of CPML cells) and its descriptors");
+  OA_CUDA(cudaSetDevice(device));
+  if (v == 3 && !two_buffers) {
+    for (int comp = 0; comp < 6; ++comp)
+      if (int rc = alloc(&fbuf[1][comp], (size_t)bs * B)) return rc;
+    two_buffers = true;
+  }
+  // leaving the fused variant with the newer fields in buffer 1: stay there, in place
+  if (v == 3 && staged != 3)
+    if (int rc = sync_buffers()) return rc;
+  staged = v;
+  if (int rc = encode_maps()) return rc;
   OA_CUDA(cudaStreamSynchronize(stream));
   return OAFDTD_OK;
 }
@@ -1607,11 +1817,10 @@ int oafdtd_set_graph(oafdtd_engine* engine, int32_t use_graph) {
 int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_z, int32_t variant) {
   if (!engine) return fail(OAFDTD_E_INVALID, "null engine");
   if (tile_z < 0 || tile_z > 4096) return fail(OAFDTD_E_INVALID, "tile_z must be 0..4096 planes");
-  if (variant < -1 || variant > 2) return fail(OAFDTD_E_INVALID, "variant must be -1, 0, 1 or 2");
-  if (variant == 2 && !engine->impl->tma_ok)
-    return fail(OAFDTD_E_INVALID, "variant 2 needs TMA descriptors, which the driver did not encode");
+  if (variant < -1 || variant > 3) return fail(OAFDTD_E_INVALID, "variant must be -1, 0, 1, 2 or 3");
+  if (variant >= 0 && variant != engine->impl->staged)
+    if (int rc = engine->impl->set_variant(variant)) return rc;
   if (tile_z) engine->impl->tile_z = tile_z;
-  if (variant >= 0) engine->impl->staged = variant;
   engine->impl->graph_dirty = true;  // a new launch shape needs a new graph
   return OAFDTD_OK;
 }
@@ -1625,7 +1834,7 @@ int oafdtd_graph_kernels(oafdtd_engine* engine, int64_t* out) {
 int oafdtd_kernel_bytes(oafdtd_engine* engine, double* out, int32_t n) {
   if (!engine || !out || n < 0) return fail(OAFDTD_E_INVALID, "null argument");
   EngineBase& e = *engine->impl;
-  const double* cls = e.class_bytes[e.staged ? 1 : 0];
+  const double* cls = e.class_bytes[e.staged == 3 ? 2 : (e.staged ? 1 : 0)];
   double total = 0.0;
   for (int k = 0; k < EngineBase::kClasses; ++k) {
     if (k < n) out[k] = cls[k];

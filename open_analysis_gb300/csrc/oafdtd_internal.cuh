@@ -55,10 +55,16 @@ struct __align__(4 * sizeof(real)) Coef {
   real ca, cb, cbe, beta0;
 };
 
+// Field pointers of a time step. The H sweeps read E (E^n) and H (H^{n-1/2}) and write Ho
+// (H^{n+1/2}); the E sweeps read Ho (H^{n+1/2}) and E (E^n) and write Eo (E^{n+1}). In place,
+// Eo == E and Ho == H; with two buffers per field (the fused sweep), E and H are the current
+// buffers and Eo, Ho the other ones, and the engine swaps them after each step.
 template <typename real>
 struct SweepArgs {
   real* E[3];
   real* H[3];
+  real* Eo[3];
+  real* Ho[3];
   const uint16_t* mat[3];
   const Coef<real>* coef;   // [entry]; entries [ade_lo, ade_hi) are dispersive, then deferred ones
   int ade_lo, ade_hi;
@@ -81,13 +87,15 @@ struct SweepArgs {
   long long bs;             // Z * Y * X
   int B;
   int tile_z;       // planes marched per block by the staged sweeps
-  int staged;       // 2: staged by TMA tensor copies; 1: staged by cp.async; 0: slab kernel only
+  int staged;       // 3: fused H + E sweep of the interior, the rest as 2; 2: staged by TMA
+                    // tensor copies; 1: staged by cp.async; 0: slab kernel only
   int* status;      // device status word: bit 0 set when a bounded wait of a sweep gave up
   // Per kind ([0] E, [1] H): the interior box, which holds no CPML correction cell and is swept
   // by the staged kernels; the z-slab planes over the interior's x-y extent ([low, high]), swept
   // by the staged kernels with their z corrections; and up to six disjoint boxes covering the rest
   // of the update domain, marched by the slab kernel (bulk update, corrections, Debye update).
   Span3 inner[2];
+  Span3 fused;       // the box both fields of which the fused sweep updates (variant 3)
   Span3 zin[2][2];
   int zsd[2][2][2];  // [kind][low/high][component 0/1]: side of the z-term psi, -1 if none
   Span3 slab[2][6];
@@ -96,7 +104,9 @@ struct SweepArgs {
 
 // TMA descriptors of the staged sweeps: per component, the field arrays as 4-D tensors
 // (x, y, z, batch) with a wide box (132 x 9: the tile plus its one-quad / one-row halo) and a
-// tile box (128 x 8), and the material index arrays (x, y, z) with a 128 x 8 box.
+// tile box (128 x 8), and the material index arrays (x, y, z) with a 128 x 8 box. E wide and
+// E tile describe E (the H sweep's source, the E sweep's old values), H tile describes H (the H
+// sweep's old values) and H wide describes Ho (the E sweep's source).
 struct SweepMaps {
   CUtensorMap e_wide[3], e_tile[3];
   CUtensorMap h_wide[3], h_tile[3];
@@ -104,6 +114,15 @@ struct SweepMaps {
   // z-term psi of the two components that have one (E: Ex, Ey; H: Hx, Hy) as (x, y, z', batch)
   // tensors with a tile box: [kind][component][low/high]
   CUtensorMap psi_z[2][2][2];
+};
+
+// TMA descriptors of the fused sweep, on the current buffers: E with a one-quad and one-row halo
+// on every side (136 x 10), H with a halo on the low sides (132 x 9), and the material index
+// (128 x 8).
+struct FusedMaps {
+  CUtensorMap e_halo[3];
+  CUtensorMap h_halo[3];
+  CUtensorMap mat[3];
 };
 
 constexpr int kStatusWaitTimeout = 1;
@@ -231,6 +250,18 @@ cudaError_t launch_energy(const EnergyArgs<real>& a, double* partial, int nblock
 cudaError_t launch_bump(long long* step_base, int n, cudaStream_t s);
 template <typename real>
 cudaError_t launch_staged_sweep(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_t s, bool h);
+// The fused H + E sweep of a.fused (variant 3, two buffers per field).
+template <typename real>
+cudaError_t launch_fused_sweep(const SweepArgs<real>& a, const FusedMaps& m, cudaStream_t s);
+template <typename real>
+bool encode_fused_maps(const SweepArgs<real>& a, FusedMaps* m, std::string* why);
+template <typename real>
+cudaError_t preload_fused();
+// One tiled TMA descriptor (dims and box innermost first, strides in bytes of dims 1..rank-1,
+// no interleave or swizzle, zero fill); false with a message when the driver's encoder is missing
+// or rejects it.
+bool encode_tensor_map(CUtensorMap* m, CUtensorMapDataType dt, int rank, const void* base, const cuuint64_t* dims,
+                       const cuuint64_t* strides, const cuuint32_t* box, const char* what, std::string* why);
 // Encodes the TMA descriptors of the staged sweeps for the fields and indices in a; false (with
 // a message) when the driver entry point is missing or rejects a descriptor.
 template <typename real>

@@ -179,10 +179,11 @@ __device__ __forceinline__ void slab_e_column(const SweepArgs<real>& a, const Sl
   const int X = a.X, Y = a.Y, Z = a.nz + 2, nx = a.nx, b = w.b, j = w.j, i0 = w.i0;
   const long long sz = (long long)X * Y;
   const long long base = (long long)b * a.bs;
-  const real* Hx = a.H[0] + base;
-  const real* Hy = a.H[1] + base;
-  const real* Hz = a.H[2] + base;
-  real* E = a.E[C] + base;
+  const real* Hx = a.Ho[0] + base;  // H^{n+1/2}
+  const real* Hy = a.Ho[1] + base;
+  const real* Hz = a.Ho[2] + base;
+  const real* E = a.E[C] + base;     // E^n
+  real* Eo = a.Eo[C] + base;         // E^{n+1}
   const Quad<real> idx4 = ld4(a.idd[0] + i0);
   const real idy = a.idd[1][j];
   long long q = (long long)w.k0 * sz + (long long)j * X + i0;  // offset within one member
@@ -281,7 +282,7 @@ __device__ __forceinline__ void slab_e_column(const SweepArgs<real>& a, const Sl
       }
     }
     // ---- stores
-    st4(E + q, e4);
+    st4(Eo + q, e4);
     if (!kMulti && disp) st4(a.J[C] + jindex(a, C, b, k, j, i0), j4);
     psi_store<real>(a.ecorr[C][0], ps[0], b, k, j, i0, X, Y, Z);
     psi_store<real>(a.ecorr[C][1], ps[1], b, k, j, i0, X, Y, Z);
@@ -318,7 +319,8 @@ __device__ __forceinline__ void slab_h_column(const SweepArgs<real>& a, const Sl
   const real* Ex = a.E[0] + base;
   const real* Ey = a.E[1] + base;
   const real* Ez = a.E[2] + base;
-  real* H = a.H[C] + base;
+  const real* H = a.H[C] + base;  // H^{n-1/2}
+  real* Ho = a.Ho[C] + base;      // H^{n+1/2}
   const Quad<real> ipx = ld4(a.ip[0] + i0);
   const real ipy = a.ip[1][j];
   const bool right = i0 + 4 < X;  // the x + 1 neighbour of element 3 is in the row
@@ -382,7 +384,7 @@ __device__ __forceinline__ void slab_h_column(const SweepArgs<real>& a, const Sl
     psi_apply<real>(a.hcorr[C][0], ps[0], a.ph, h, d0, kf, k, j, i0);
     psi_apply<real>(a.hcorr[C][1], ps[1], a.ph, h, d1, kf, k, j, i0);
     // ---- stores
-    st4(H + q, h);
+    st4(Ho + q, h);
     psi_store<real>(a.hcorr[C][0], ps[0], b, k, j, i0, X, Y, Z);
     psi_store<real>(a.hcorr[C][1], ps[1], b, k, j, i0, X, Y, Z);
     if (C != 2) sc = s2;

@@ -24,7 +24,7 @@
 #include <mutex>
 #include <type_traits>
 
-#include "device_common.cuh"
+#include "tma.cuh"
 
 namespace oafdtd {
 
@@ -32,102 +32,6 @@ constexpr int kTQ = 32;       // quads per tile row (128 cells)
 constexpr int kTY = 8;        // rows per tile
 constexpr int kTW = 4 * kTQ;  // tile width in cells
 constexpr int kHW = kTW + 4;  // staged width with a one-quad halo
-
-// One staged array: rows x width, dense (the layout a TMA box lands in), 128-byte aligned.
-template <typename T, int R, int W>
-struct alignas(128) Box {
-  T v[R][W];
-};
-
-// ------------------------------------------------------------------------------ TMA + mbarrier
-__device__ __forceinline__ unsigned smem_addr(const void* p) {
-  return static_cast<unsigned>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ unsigned long long global_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
-  return t;
-}
-constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s: far above any plane's copy time
-constexpr unsigned long long kDrainNs = 100000000ull;  // 0.1 s per copy still in flight at abort
-constexpr unsigned kWaitPolls = 1u << 28;              // hard cap on polls whatever the timer says
-
-// Waits for the phase of the given parity; false when the time or poll limit ran out.
-__device__ __noinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, unsigned long long limit_ns) {
-  const unsigned long long t0 = global_ns();
-  for (unsigned n = 0; n < kWaitPolls; ++n) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((n & 63u) == 63u && global_ns() - t0 > limit_ns) return false;
-  }
-  return false;
-}
-__device__ __forceinline__ void tma_load4(void* dst, const CUtensorMap* map, unsigned long long* bar, int x, int y,
-                                          int z, int w) {
-  asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(smem_addr(dst)),
-      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_addr(bar))
-      : "memory");
-}
-__device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* map, unsigned long long* bar, int x, int y,
-                                          int z) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(smem_addr(dst)),
-      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
-      : "memory");
-}
-__device__ __forceinline__ void prefetch_map(const CUtensorMap* map) {
-  asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<unsigned long long>(map)) : "memory");
-}
-// Barrier setup of the block's leader, made visible to the TMA unit before the first copy.
-template <int S>
-__device__ __forceinline__ void mbar_setup(unsigned long long* bar) {
-#pragma unroll
-  for (int s = 0; s < S; ++s) mbar_init(&bar[s], 1);
-  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-}
-// Orders the block's reads of a slot (generic proxy) before the TMA writes that refill it.
-__device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-}
-
-// Plane t of a block's march uses slot t % S in phase (t / S) & 1.
-template <int S>
-__device__ __forceinline__ bool wait_plane(unsigned long long* bar, int t) {
-  return mbar_wait(&bar[t % S], (unsigned)((t / S) & 1), kWaitNs);
-}
-
-// A wait gave up: the leader records it and waits (bounded) for the planes [t, issued) it has
-// issued and not yet seen arrive, so no copy lands after the block has exited.
-template <int S>
-__device__ __noinline__ void abort_march(unsigned long long* bar, int t, int issued, int* status, bool leader) {
-  if (!leader) return;
-  if (status) atomicOr(status, kStatusWaitTimeout);
-  for (int p = t; p < issued; ++p) mbar_wait(&bar[p % S], (unsigned)((p / S) & 1), kDrainNs);
-}
-
-__device__ __forceinline__ unsigned char* align_smem(unsigned char* raw) {
-  return raw + ((128u - (smem_addr(raw) & 127u)) & 127u);
-}
 
 // ------------------------------------------------------------------------------------- blocks
 // Stages per kernel: three planes in flight, two for the E sweep with z corrections (its slot is
@@ -174,58 +78,6 @@ __device__ __forceinline__ BlockSpan block_span(const SweepArgs<real>& a, int ki
   s.y0 = s.box.j0 + (int)blockIdx.y * kTY;
   s.empty = s.k1 <= s.k0 || s.x0 >= 4 * s.box.q1 || s.y0 >= s.box.j1;
   return s;
-}
-
-// A z-term correction of one quad: psi <- b psi + c d; F <- F + (sign k)(ek d + psi), with the
-// plane's coefficients and psi staged in shared memory, for the cells of the correction box; the
-// updated psi row goes back to global memory.
-template <typename real>
-struct ZTerm {
-  const real* sm;  // staged psi of the quad
-  real* g;         // psi of the quad in global memory
-  real eb, ec, ek, sign;
-  int lo0, hi0;
-  bool on;         // the row and plane lie in the correction box
-};
-
-template <typename real>
-__device__ __forceinline__ ZTerm<real> z_term(const SweepArgs<real>& a, const CpmlTerm<real>& T, int sd,
-                                              const real* sm, int b, int k, int j, int i0, int kind) {
-  ZTerm<real> z;
-  z.on = false;
-  if (sd < 0) return z;
-  const CpmlSide<real>& s = sd == 0 ? T.side[0] : T.side[1];
-  z.on = j >= s.lo[1] && j < s.hi[1] && k >= s.lo[2] && k < s.hi[2];
-  if (!z.on) return z;
-  const int w = s.hi[2] - s.lo[2];
-  z.sm = sm;
-  z.g = s.psi + ((((long long)b * w + (k - s.lo[2])) * a.Y + j) * a.X + i0);
-  const real* const* co = kind == 0 ? a.pe[2] : a.ph[2];
-  z.eb = __ldg(co[0] + k);
-  z.ec = __ldg(co[1] + k);
-  z.ek = __ldg(co[2] + k);
-  z.sign = T.sign;
-  z.lo0 = s.lo[0];
-  z.hi0 = s.hi[0];
-  return z;
-}
-
-template <typename real>
-__device__ __forceinline__ void z_apply(const ZTerm<real>& z, Quad<real>& f, const real (&d)[4], const real (&kf)[4],
-                                        int i0) {
-  if (!z.on) return;
-  Quad<real> ps = ld4(z.sm);
-#pragma unroll
-  for (int e = 0; e < 4; ++e) {
-    const int i = i0 + e;
-    if (i < z.lo0 || i >= z.hi0) continue;
-    real p = ps.v[e] * z.eb;
-    p = p + z.ec * d[e];
-    ps.v[e] = p;
-    const real upd = z.ek * d[e] + p;
-    f.v[e] = f.v[e] + (z.sign * kf[e]) * upd;
-  }
-  st4(z.g, ps);
 }
 
 // psi tile copies of one plane of a z sweep (cp.async variant): [component][row][quad]
@@ -414,7 +266,7 @@ __global__ void __launch_bounds__(256, 2)
         if constexpr (kZ)
           z_apply(z_term(a, a.hcorr[0][1], a.zsd[1][zr][0], &cur.z.p[0].v[ty][4 * tx], b, k, j, i0, 1), h, d1, kf,
                   i0);
-        st4(a.H[0] + p, h);
+        st4(a.Ho[0] + p, h);
       }
       if (kin) {  // Hy: cell along x (1..nx), node along y (1..ny+1), cell along z
         const Quad<real> ex1 = ld4(&nxt.e[0].v[ty][4 * tx]);
@@ -431,7 +283,7 @@ __global__ void __launch_bounds__(256, 2)
         if constexpr (kZ)
           z_apply(z_term(a, a.hcorr[1][1], a.zsd[1][zr][1], &cur.z.p[1].v[ty][4 * tx], b, k, j, i0, 1), h, d1, kf,
                   i0);
-        st4(a.H[1] + p, h);
+        st4(a.Ho[1] + p, h);
       }
       if (j <= ny) {  // Hz: cell along x and y, node along z (1..nz+1)
         const Quad<real> exy = ld4(&cur.e[0].v[ty + 1][4 * tx]);
@@ -444,7 +296,7 @@ __global__ void __launch_bounds__(256, 2)
           const real d1 = (exy.v[e] - ex.v[e]) * ipy;  // axis y
           if (i >= 1 && i <= nx) h.v[e] = h.v[e] + dtmu * ((-d0) + d1);
         }
-        st4(a.H[2] + p, h);
+        st4(a.Ho[2] + p, h);
       }
     }
     __syncthreads();  // every thread is done with the slot of plane k
@@ -491,7 +343,7 @@ __device__ __forceinline__ void e_stage(const SweepArgs<real>& a, ESlot<real, kZ
       const int c = t / CQ / (kHW / 4) / (kTY + 1);
       const int x = x0 - 4 + 4 * q, y = y0 - 1 + r;
       if (x < 0 || x >= X || y >= Y) continue;
-      cp_async16(&s.h[c].v[r][4 * q] + part * EL, a.H[c] + base + (long long)y * X + x + part * EL);
+      cp_async16(&s.h[c].v[r][4 * q] + part * EL, a.Ho[c] + base + (long long)y * X + x + part * EL);
     } else if (t < hcount + ecount) {
       const int u = t - hcount;
       const int part = u % CQ, q = (u / CQ) % (kTW / 4), r = (u / CQ / (kTW / 4)) % kTY;
@@ -523,61 +375,6 @@ __device__ __forceinline__ void e_issue(const SweepArgs<real>& a, const SweepMap
     tma_load3(&s.m[c], &tm.mat[c], bar, x0, y0, k);
   }
   if constexpr (kZ) z_issue(a, tm, s.z, bar, 0, zr, b, k, x0, y0);
-}
-
-// Bulk update, z correction (z sweeps) and the Debye update of one E component on one quad, in
-// the reference's order. d0/d1 are the derivatives along the component's two axes in ascending
-// order; the reference's term order is (d0, -d1) when first_plus, else (d1, -d0). j4 holds the
-// prefetched Debye current (P = 1).
-template <typename real, bool kZ, bool kMulti>
-__device__ __forceinline__ void e_apply(const SweepArgs<real>& a, int c, real* __restrict__ E, long long p,
-                                        const Quad<real>& e_old, const uint16_t* m, const real (&d0)[4],
-                                        const real (&d1)[4], bool first_plus, const Quad<real>& j4in,
-                                        const ZTerm<real>& zt, int i0, int j, int k, int b) {
-  const int X = a.X, Y = a.Y, nx = a.nx;
-  Quad<real> e4 = e_old;
-  Coef<real> cf[4];
-  real kf[4];
-  bool valid[4];
-  bool disp = false;
-#pragma unroll
-  for (int e = 0; e < 4; ++e) {
-    const int i = i0 + e;
-    cf[e] = a.coef[m[e]];
-    kf[e] = cf[e].cb;
-    valid[e] = i >= 1 && i <= nx + 1;
-    const real acc = first_plus ? d0[e] + (-d1[e]) : d1[e] + (-d0[e]);
-    if (valid[e]) e4.v[e] = cf[e].ca * e4.v[e] + cf[e].cb * acc;
-    disp |= valid[e] && m[e] >= a.ade_lo && m[e] < a.ade_hi;
-  }
-  if constexpr (kZ) z_apply(zt, e4, d1, kf, i0);
-  if (disp) {
-    const long long jstride = (long long)a.B * a.jnk[c] * Y * X;
-    const long long jq = (((long long)b * a.jnk[c] + (k - a.jk0[c])) * Y + j) * X + i0;
-    real* J = a.J[c];
-    if constexpr (!kMulti) {
-      Quad<real> j4 = j4in;
-      const real onekp = a.ade_onekp[0], kp = a.ade_kp[0];
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        if (!(valid[e] && m[e] >= a.ade_lo && m[e] < a.ade_hi)) continue;
-        const real jt = (real)0.5 * (onekp * j4.v[e]);
-        const real en = e4.v[e] - cf[e].cbe * jt;
-        const real de = en - e_old.v[e];
-        j4.v[e] = kp * j4.v[e] + cf[e].beta0 * de;
-        e4.v[e] = en;
-      }
-      st4(J + jq, j4);
-    } else {
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        if (!(valid[e] && m[e] >= a.ade_lo && m[e] < a.ade_hi)) continue;
-        e4.v[e] = ade_cell(e4.v[e], e_old.v[e], cf[e].cbe, cf[e].beta0, m[e], J, jq + e, jstride, a.ade_kp,
-                           a.ade_onekp, a.ade_beta, a.ade_P);
-      }
-    }
-  }
-  st4(E + p, e4);
 }
 
 // Debye currents of plane k for the three components (single-pole runs only; zero elsewhere).
@@ -616,8 +413,8 @@ __global__ void __launch_bounds__(256, 2)
   Quad<real> hx_m{}, hy_m{};  // H at plane k - 1, carried
   if (live) {
     const long long p = base + (long long)(k0 - 1) * X * Y + (long long)j * X + i0;
-    hx_m = ld4(a.H[0] + p);
-    hy_m = ld4(a.H[1] + p);
+    hx_m = ld4(a.Ho[0] + p);
+    hy_m = ld4(a.Ho[1] + p);
   }
   Quad<real> jcur[3];
   j_prefetch(a, jcur, k0, j, i0, b, live);
@@ -676,7 +473,7 @@ __global__ void __launch_bounds__(256, 2)
         d0[e] = (hz.v[e] - hzy.v[e]) * idy;
         d1[e] = (hy.v[e] - hy_m.v[e]) * idz;
       }
-      e_apply<real, kZ, kMulti>(a, 0, a.E[0] + base, q, ld4(&cur.e[0].v[ty][4 * tx]), &cur.m[0].v[ty][4 * tx], d0, d1,
+      e_apply<real, kZ, kMulti>(a, 0, a.Eo[0] + base, q, ld4(&cur.e[0].v[ty][4 * tx]), &cur.m[0].v[ty][4 * tx], d0, d1,
                         true, jcur[0], zt[0], i0, j, k, b);
       // Ey: terms (a = z, +Hx) then (a = x, -Hz); d0 is the x term, d1 the z term
 #pragma unroll
@@ -685,7 +482,7 @@ __global__ void __launch_bounds__(256, 2)
         d0[e] = (hz.v[e] - hzl) * idx4.v[e];
         d1[e] = (hx.v[e] - hx_m.v[e]) * idz;
       }
-      e_apply<real, kZ, kMulti>(a, 1, a.E[1] + base, q, ld4(&cur.e[1].v[ty][4 * tx]), &cur.m[1].v[ty][4 * tx], d0, d1,
+      e_apply<real, kZ, kMulti>(a, 1, a.Eo[1] + base, q, ld4(&cur.e[1].v[ty][4 * tx]), &cur.m[1].v[ty][4 * tx], d0, d1,
                         false, jcur[1], zt[1], i0, j, k, b);
       // Ez: terms (a = x, +Hy) then (a = y, -Hx); no z term
 #pragma unroll
@@ -696,7 +493,7 @@ __global__ void __launch_bounds__(256, 2)
       }
       ZTerm<real> none;
       none.on = false;
-      e_apply<real, false, kMulti>(a, 2, a.E[2] + base, q, ld4(&cur.e[2].v[ty][4 * tx]), &cur.m[2].v[ty][4 * tx], d0, d1,
+      e_apply<real, false, kMulti>(a, 2, a.Eo[2] + base, q, ld4(&cur.e[2].v[ty][4 * tx]), &cur.m[2].v[ty][4 * tx], d0, d1,
                            true, jcur[2], none, i0, j, k, b);
       hx_m = hx;
       hy_m = hy;
@@ -773,13 +570,11 @@ cudaError_t launch_staged_sweep(const SweepArgs<real>& a, const SweepMaps& m, cu
 }
 
 // ------------------------------------------------------------------------------- descriptors
-namespace {
-
 using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-EncodeTiled encoder() {
+static EncodeTiled encoder() {
   static EncodeTiled fn = nullptr;
   static std::once_flag once;
   std::call_once(once, [] {
@@ -794,8 +589,13 @@ EncodeTiled encoder() {
 }
 
 // dims/box innermost first; strides in bytes for dims 1..rank-1.
-bool encode(EncodeTiled f, CUtensorMap* m, CUtensorMapDataType dt, int rank, const void* base, const cuuint64_t* dims,
-            const cuuint64_t* strides, const cuuint32_t* box, const char* what, std::string* why) {
+bool encode_tensor_map(CUtensorMap* m, CUtensorMapDataType dt, int rank, const void* base, const cuuint64_t* dims,
+                       const cuuint64_t* strides, const cuuint32_t* box, const char* what, std::string* why) {
+  const EncodeTiled f = encoder();
+  if (f == nullptr) {
+    *why = "the driver does not provide cuTensorMapEncodeTiled";
+    return false;
+  }
   const cuuint32_t ones[4] = {1, 1, 1, 1};
   const CUresult r = f(m, dt, (cuuint32_t)rank, const_cast<void*>(base), dims, strides, box, ones,
                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -807,15 +607,9 @@ bool encode(EncodeTiled f, CUtensorMap* m, CUtensorMapDataType dt, int rank, con
   return true;
 }
 
-}  // namespace
 
 template <typename real>
 bool encode_sweep_maps(const SweepArgs<real>& a, SweepMaps* m, std::string* why) {
-  const EncodeTiled f = encoder();
-  if (f == nullptr) {
-    *why = "the driver does not provide cuTensorMapEncodeTiled";
-    return false;
-  }
   const CUtensorMapDataType dt = sizeof(real) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
   const cuuint64_t X = (cuuint64_t)a.X, Y = (cuuint64_t)a.Y, Z = (cuuint64_t)a.nz + 2, B = (cuuint64_t)a.B;
   const cuuint64_t dims[4] = {X, Y, Z, B};
@@ -826,11 +620,11 @@ bool encode_sweep_maps(const SweepArgs<real>& a, SweepMaps* m, std::string* why)
   const cuuint64_t mdims[3] = {X, Y, Z};
   const cuuint64_t mstrides[2] = {X * 2, X * Y * 2};
   for (int c = 0; c < 3; ++c) {
-    if (!encode(f, &m->e_wide[c], dt, 4, a.E[c], dims, strides, wide, "E wide", why) ||
-        !encode(f, &m->e_tile[c], dt, 4, a.E[c], dims, strides, tile, "E tile", why) ||
-        !encode(f, &m->h_wide[c], dt, 4, a.H[c], dims, strides, wide, "H wide", why) ||
-        !encode(f, &m->h_tile[c], dt, 4, a.H[c], dims, strides, tile, "H tile", why) ||
-        !encode(f, &m->mat[c], CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, a.mat[c], mdims, mstrides, tile, "mat", why))
+    if (!encode_tensor_map(&m->e_wide[c], dt, 4, a.E[c], dims, strides, wide, "E wide", why) ||
+        !encode_tensor_map(&m->e_tile[c], dt, 4, a.E[c], dims, strides, tile, "E tile", why) ||
+        !encode_tensor_map(&m->h_wide[c], dt, 4, a.Ho[c], dims, strides, wide, "H wide", why) ||
+        !encode_tensor_map(&m->h_tile[c], dt, 4, a.H[c], dims, strides, tile, "H tile", why) ||
+        !encode_tensor_map(&m->mat[c], CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, a.mat[c], mdims, mstrides, tile, "mat", why))
       return false;
   }
   for (int kind = 0; kind < 2; ++kind)
@@ -842,7 +636,7 @@ bool encode_sweep_maps(const SweepArgs<real>& a, SweepMaps* m, std::string* why)
         const cuuint64_t w = (cuuint64_t)(s.hi[2] - s.lo[2]);
         const cuuint64_t pdims[4] = {X, Y, w, B};
         const cuuint64_t pstrides[3] = {X * rs, X * Y * rs, X * Y * w * rs};
-        if (!encode(f, &m->psi_z[kind][cc][zr], dt, 4, s.psi, pdims, pstrides, tile, "psi", why)) return false;
+        if (!encode_tensor_map(&m->psi_z[kind][cc][zr], dt, 4, s.psi, pdims, pstrides, tile, "psi", why)) return false;
       }
   return true;
 }

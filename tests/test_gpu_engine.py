@@ -209,7 +209,7 @@ def test_kernel_profile_and_model_bytes() -> None:
     assert eng.model_bytes() > 0
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 @pytest.mark.parametrize("tile_z", [3, 32])
 def test_launch_shapes_match_oracle(variant: int, tile_z: int) -> None:
     """Every sweep variant and z tiling gives the oracle's float32 fields bit for bit."""
@@ -231,7 +231,7 @@ def test_variants_agree_across_x_tiles(cpml_cells: int) -> None:
     c = compile_model(via_transition(nx=150, ny=24, nz=24, n_freq=8, cpml_cells=cpml_cells), "float32")
     assert c.grid.shape[2] > 128 and _ade_in_cpml(c)
     fields = {}
-    for variant in (0, 1, 2):
+    for variant in (0, 1, 2, 3):
         gpu = _engine(c)
         gpu.set_tuning(5, variant)
         gpu.step(40)
@@ -242,6 +242,25 @@ def test_variants_agree_across_x_tiles(cpml_cells: int) -> None:
     for k in range(6):
         assert np.array_equal(fields[2][k], fields[1][k]), NAMES[k]
         assert np.array_equal(fields[2][k], fields[0][k]), NAMES[k]
+        assert np.array_equal(fields[2][k], fields[3][k]), NAMES[k]
+
+
+def test_fused_variant_switches_mid_run_bit_for_bit() -> None:
+    """The fused sweep (two buffers per field) against the oracle across variant switches and odd
+    step counts: 70 steps fused (one graph chunk, six eager steps), 51 in place, 64 fused again,
+    then 3 eager steps; the benchmark structure at 150 x 48 x 40 with 10-cell CPML."""
+    from open_analysis_gb300.structures import via_transition
+
+    c = compile_model(via_transition(nx=150, ny=48, nz=40, n_freq=8), "float32")
+    gpu = _engine(c)
+    gpu.set_tuning(8, 3)
+    gpu.step(70)
+    gpu.set_tuning(8, 2)
+    gpu.step(51)
+    gpu.set_tuning(16, 3)
+    gpu.step(64)
+    gpu.step(3)
+    check_against_oracles(c, gpu, 188)
 
 
 def test_via_transition_small_matches_oracle() -> None:
