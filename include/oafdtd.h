@@ -379,6 +379,22 @@ int oafdtd_mlp_mse_grad(const float* Y, const float* T, int32_t M, int32_t N, fl
 int oafdtd_mlp_adam(float* w, void* w16, const float* grad, float* m1, float* m2, int64_t n, const float* lr,
                     float b1, float b2, float eps, const int32_t* step, void* stream);
 
+/* C = act(A . B^T + bias) with A row-major M x K and B row-major N x K (both K-contiguous), BF16
+ * operands, FP32 accumulation, the epilogues of oafdtd_mlp_gemm (ldc for C32, C16 and mask). Shapes
+ * with M and N multiples of 128, K a multiple of 64 and 16-byte aligned rows run on the fifth-
+ * generation tensor cores (tcgen05.mma, accumulator in tensor memory, operand tiles by TMA tensor
+ * copies); other shapes on the mma.sync kernel. C16T (BF16, nullable) receives the result
+ * transposed, N x M with leading dimension ldct (the next layer's weight gradient reads it
+ * K-contiguous); off the tcgen05 shapes it needs C16 as well. status (device int32, nullable):
+ * bit 0 is set when a bounded wait of the tcgen05 kernel gave up (that launch's C is not written). */
+int oafdtd_mlp_gemm_tn(const void* A, const void* B, float* C32, void* C16, void* C16T, const float* bias,
+                       const void* mask, int32_t M, int32_t N, int32_t K, int32_t lda, int32_t ldb, int32_t ldc,
+                       int32_t ldct, int32_t act, float beta, int32_t* status, void* stream);
+
+/* dst (cols x rows, leading dimension ldd) = src^T (rows x cols, leading dimension lds), BF16. */
+int oafdtd_mlp_transpose(const void* src, int32_t rows, int32_t cols, int32_t lds, void* dst, int32_t ldd,
+                         void* stream);
+
 /* *counter += 1 on the device (the Adam step number inside a captured training step). */
 int oafdtd_mlp_count(int32_t* counter, void* stream);
 

@@ -383,10 +383,72 @@ __global__ void gather_kernel(const float* src, int cols, const int* idx, int ro
   if (d16) d16[e] = __float2bfloat16(v);
 }
 
+// dst (cols x rows, leading dimension ldd) = src^T (rows x cols, leading dimension lds), BF16,
+// through 32 x 32 shared tiles (both sides coalesced).
+__global__ void transpose16_kernel(const __nv_bfloat16* src, int rows, int cols, int lds, __nv_bfloat16* dst,
+                                   int ldd) {
+  __shared__ __nv_bfloat16 t[32][33];
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int r = r0 + y, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) t[y][threadIdx.x] = src[(long long)r * lds + c];
+  }
+  __syncthreads();
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int c = c0 + y, r = r0 + threadIdx.x;
+    if (r < rows && c < cols) dst[(long long)c * ldd + r] = t[threadIdx.x][y];
+  }
+}
+
 }  // namespace oafdtd
 
 // --------------------------------------------------------------------------------------- C ABI
 extern "C" {
+
+int oafdtd_mlp_transpose(const void* src, int32_t rows, int32_t cols, int32_t lds, void* dst, int32_t ldd,
+                         void* stream) {
+  if (!src || !dst || rows < 1 || cols < 1 || lds < cols || ldd < rows) {
+    oafdtd::set_last_error("oafdtd_mlp_transpose: bad arguments");
+    return -1;
+  }
+  const dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
+  oafdtd::transpose16_kernel<<<grid, block, 0, static_cast<cudaStream_t>(stream)>>>(
+      static_cast<const __nv_bfloat16*>(src), rows, cols, lds, static_cast<__nv_bfloat16*>(dst), ldd);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+int oafdtd_mlp_gemm(const void* A, const void* B, float* C32, void* C16, const float* bias, const void* mask,
+                    int32_t M, int32_t N, int32_t K, int32_t lda, int32_t ldb, int32_t ldc, int32_t ta, int32_t tb,
+                    int32_t act, float beta, void* stream);
+
+int oafdtd_mlp_gemm_tn(const void* A, const void* B, float* C32, void* C16, void* C16T, const float* bias,
+                       const void* mask, int32_t M, int32_t N, int32_t K, int32_t lda, int32_t ldb, int32_t ldc,
+                       int32_t ldct, int32_t act, float beta, int32_t* status, void* stream) {
+  if (!A || !B || (!C32 && !C16 && !C16T) || M < 1 || N < 1 || K < 1 || act < 0 || act > 4 ||
+      ((act == 2 || act == 4) && !mask) || (C16T && ldct < M)) {
+    oafdtd::set_last_error("oafdtd_mlp_gemm_tn: bad arguments");
+    return -1;
+  }
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (oafdtd::umma_shape_ok(M, N, K, lda, ldb, A, B)) {
+    std::string why;
+    const cudaError_t err = oafdtd::launch_umma_gemm(A, B, C32, C16, C16T, bias, mask, M, N, K, lda, ldb, ldc, ldct,
+                                                     act, beta, status, s, &why);
+    if (err != cudaSuccess) {
+      oafdtd::set_last_error(std::string("oafdtd_mlp_gemm_tn: ") + (why.empty() ? cudaGetErrorString(err) : why));
+      return err == cudaErrorInvalidValue ? -1 : -3;
+    }
+    return 0;
+  }
+  // other shapes: the mma.sync kernel, then the transposed copy from the BF16 result
+  if (C16T && !C16) {
+    oafdtd::set_last_error("oafdtd_mlp_gemm_tn: a transposed result off the tcgen05 shapes needs C16 as well");
+    return -1;
+  }
+  int rc = oafdtd_mlp_gemm(A, B, C32, C16, bias, mask, M, N, K, lda, ldb, ldc, 0, 1, act, beta, stream);
+  if (rc == 0 && C16T) rc = oafdtd_mlp_transpose(C16, M, N, ldc, C16T, ldct, stream);
+  return rc;
+}
 
 int oafdtd_mlp_gemm(const void* A, const void* B, float* C32, void* C16, const float* bias, const void* mask,
                     int32_t M, int32_t N, int32_t K, int32_t lda, int32_t ldb, int32_t ldc, int32_t ta, int32_t tb,

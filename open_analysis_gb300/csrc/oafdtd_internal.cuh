@@ -261,7 +261,16 @@ cudaError_t preload_fused();
 // no interleave or swizzle, zero fill); false with a message when the driver's encoder is missing
 // or rejects it.
 bool encode_tensor_map(CUtensorMap* m, CUtensorMapDataType dt, int rank, const void* base, const cuuint64_t* dims,
-                       const cuuint64_t* strides, const cuuint32_t* box, const char* what, std::string* why);
+                       const cuuint64_t* strides, const cuuint32_t* box, const char* what, std::string* why,
+                       CUtensorMapSwizzle swizzle = CU_TENSOR_MAP_SWIZZLE_NONE);
+// The tcgen05 GEMM of the surrogate (umma.cu): C = A . B^T for row-major A (M x K) and B (N x K);
+// umma_shape_ok tells whether a shape and its operands suit it (M, N multiples of 128, K of 64,
+// 16-byte aligned rows).
+bool umma_shape_ok(int M, int N, int K, int lda, int ldb, const void* A, const void* B);
+cudaError_t launch_umma_gemm(const void* A, const void* B, float* C32, void* C16, void* C16T, const float* bias,
+                             const void* mask, int M, int N, int K, int lda, int ldb, int ldc, int ldct, int act,
+                             float beta, int* status, cudaStream_t s, std::string* why);
+cudaError_t preload_umma();
 // Encodes the TMA descriptors of the staged sweeps for the fields and indices in a; false (with
 // a message) when the driver entry point is missing or rejects a descriptor.
 template <typename real>

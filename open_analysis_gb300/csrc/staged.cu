@@ -590,7 +590,8 @@ static EncodeTiled encoder() {
 
 // dims/box innermost first; strides in bytes for dims 1..rank-1.
 bool encode_tensor_map(CUtensorMap* m, CUtensorMapDataType dt, int rank, const void* base, const cuuint64_t* dims,
-                       const cuuint64_t* strides, const cuuint32_t* box, const char* what, std::string* why) {
+                       const cuuint64_t* strides, const cuuint32_t* box, const char* what, std::string* why,
+                       CUtensorMapSwizzle swizzle) {
   const EncodeTiled f = encoder();
   if (f == nullptr) {
     *why = "the driver does not provide cuTensorMapEncodeTiled";
@@ -598,7 +599,7 @@ bool encode_tensor_map(CUtensorMap* m, CUtensorMapDataType dt, int rank, const v
   }
   const cuuint32_t ones[4] = {1, 1, 1, 1};
   const CUresult r = f(m, dt, (cuuint32_t)rank, const_cast<void*>(base), dims, strides, box, ones,
-                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
     *why = std::string("cuTensorMapEncodeTiled(") + what + ") returned " + std::to_string((int)r);

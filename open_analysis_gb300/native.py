@@ -213,6 +213,11 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     ),
     "oafdtd_mlp_count": (C.c_int, [C.c_void_p, C.c_void_p]),
     "oafdtd_mlp_gather": (C.c_int, [C.c_void_p, _i32, C.c_void_p, _i32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "oafdtd_mlp_gemm_tn": (
+        C.c_int,
+        [C.c_void_p] * 7 + [_i32] * 8 + [C.c_float, C.c_void_p, C.c_void_p],
+    ),
+    "oafdtd_mlp_transpose": (C.c_int, [C.c_void_p, _i32, _i32, _i32, C.c_void_p, _i32, C.c_void_p]),
 }
 
 _lock = threading.Lock()

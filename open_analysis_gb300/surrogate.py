@@ -313,12 +313,15 @@ def cosine_lr(epoch: int, epochs: int, lr: float, lr_end: float) -> float:
 
 
 class Mlp:
-    """A ReLU network ``sizes[0] -> ... -> sizes[-1]`` on the GPU, trained and evaluated by the
-    engine library's kernels. Weights ``W[l]`` are ``(fan_in, fan_out)`` FP32 masters with BF16
-    copies the GEMMs read; all weights and biases live in one flat buffer so one Adam launch
-    updates them all. Every width is padded to a multiple of 8 (the input with zero columns, so
-    the extra weights see zero inputs and zero gradients), which keeps every GEMM on the
-    pipelined tensor-core path."""
+    """A tanh (or ReLU) network ``sizes[0] -> ... -> sizes[-1]`` on the GPU, trained and evaluated
+    by the engine library's kernels. Weights ``W[l]`` are ``(fan_in, fan_out)`` FP32 masters with
+    BF16 copies and transposed BF16 copies the GEMMs read; all weights and biases live in one flat
+    buffer so one Adam launch updates them all. Every GEMM is C = A . B^T with both operands
+    K-contiguous (``oafdtd_mlp_gemm_tn``): the forward reads the transposed weights, the weight
+    gradients the transposed activations and output gradients, which the epilogues and a small
+    transpose kernel write; shapes with M and N multiples of 128 and K of 64 (batch 256, widths
+    of 512) run on the tcgen05 tensor cores. Every width is padded to a multiple of 8 (the input
+    with zero columns, so the extra weights see zero inputs and zero gradients)."""
 
     def __init__(self, sizes: Sequence[int], batch: int = 256, seed: int = 0, device: int = 0, act: str = "tanh") -> None:
         torch = _torch()
@@ -356,6 +359,11 @@ class Mlp:
         f32, bf = torch.float32, torch.bfloat16
         self.p32 = torch.from_numpy(flat).to(self.dev)
         self.p16 = self.p32.to(bf)
+        # every layer's BF16 weights also transposed, (fan_out, fan_in): the forward GEMM reads its
+        # B operand K-contiguous, the layout the tcgen05 kernel takes
+        self.p16T = torch.zeros_like(self.p16)
+        self.status = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        self._refresh_t(self._stream())
         self.grad = torch.zeros(off, dtype=f32, device=self.dev)
         self.m1 = torch.zeros_like(self.grad)
         self.m2 = torch.zeros_like(self.grad)
@@ -378,6 +386,9 @@ class Mlp:
         wo = self.layout[l][0]
         t = self.p16 if half else self.p32
         return t.data_ptr() + wo * t.element_size()
+
+    def _wT(self, l: int) -> int:
+        return self.p16T.data_ptr() + self.layout[l][0] * self.p16T.element_size()
 
     def _b(self, l: int) -> int:
         return self.p32.data_ptr() + self.layout[l][3] * 4
@@ -405,21 +416,44 @@ class Mlp:
             flat[bo : bo + n] = np.asarray(bl, np.float32)
         self.p32.copy_(self.torch.from_numpy(flat).to(self.dev))
         self.p16.copy_(self.p32.to(self.torch.bfloat16))
+        self._refresh_t(self._stream())
+
+    def load_flat(self, flat32: Any) -> None:
+        """Set every weight and bias from a flat FP32 device tensor in this network's layout (its
+        BF16 and transposed BF16 copies follow)."""
+        self.p32.copy_(flat32)
+        self.p16.copy_(self.p32.to(self.torch.bfloat16))
+        self._refresh_t(self._stream())
 
     # ---- kernels
+    def _refresh_t(self, s: int) -> None:
+        """The transposed BF16 weights from the current BF16 weights."""
+        for l, (_, a, b, _) in enumerate(self.layout):
+            native.check(self.lib.oafdtd_mlp_transpose(self._w(l), a, b, b, self._wT(l), a, s), "transpose")
+
+    def _gemm_tn(self, a: int, b: int, c32: int, c16: int, c16t: int, bias: int, mask: int, m: int, n: int, k: int,
+                 lda: int, ldb: int, ldc: int, ldct: int, act: int, s: int) -> None:
+        """C (m x n) = A (m x k) . B^T with B (n x k): tcgen05 on the shapes that allow it."""
+        native.check(self.lib.oafdtd_mlp_gemm_tn(a, b, c32 or None, c16 or None, c16t or None, bias or None,
+                                                 mask or None, m, n, k, lda, ldb, ldc, ldct, act, 0.0,
+                                                 self.status.data_ptr(), s), "oafdtd_mlp_gemm_tn")
+
     def _gemm(self, a: int, b: int, c32: int, c16: int, bias: int, mask: int, m: int, n: int, k: int,
               lda: int, ldb: int, ldc: int, ta: int, tb: int, act: int, s: int) -> None:
         native.check(self.lib.oafdtd_mlp_gemm(a, b, c32 or None, c16 or None, bias or None, mask or None,
                                               m, n, k, lda, ldb, ldc, ta, tb, act, 0.0, s), "oafdtd_mlp_gemm")
 
-    def _forward(self, x16: int, acts: list[Any], y32: int, m: int, s: int) -> None:
-        """acts[l] (BF16, m x sizes[l+1]) for the hidden layers; y32 the FP32 output."""
+    def _forward(self, x16: int, acts: list[Any], y32: int, m: int, s: int, acts_t: list[Any] | None = None) -> None:
+        """acts[l] (BF16, m x sizes[l+1]) for the hidden layers, and transposed into acts_t[l]
+        (sizes[l+1] x m) when given (training: the weight gradients read them); y32 the FP32
+        output. Each layer is X . W = X . (W^T)^T on the transposed weights."""
         inp = x16
         n_layers = len(self.layout)
         for l, (_, a, b, _) in enumerate(self.layout):
             last = l == n_layers - 1
-            self._gemm(inp, self._w(l), y32 if last else 0, 0 if last else acts[l].data_ptr(), self._b(l), 0,
-                       m, b, a, a, b, b, 0, 0, 0 if last else self.act, s)
+            ct = 0 if last or acts_t is None else acts_t[l].data_ptr()
+            self._gemm_tn(inp, self._wT(l), y32 if last else 0, 0 if last else acts[l].data_ptr(), ct, self._b(l), 0,
+                          m, b, a, a, a, b, m, 0 if last else self.act, s)
             if not last:
                 inp = acts[l].data_ptr()
 
@@ -429,7 +463,11 @@ class Mlp:
         out = self.sizes[-1]
         return {
             "x16": torch.zeros((m, self.sizes[0]), dtype=bf, device=self.dev),
+            "x16T": torch.zeros((self.sizes[0], m), dtype=bf, device=self.dev),
             "acts": [torch.zeros((m, b), dtype=bf, device=self.dev) for b in self.sizes[1:-1]],
+            "actsT": [torch.zeros((b, m), dtype=bf, device=self.dev) for b in self.sizes[1:-1]],
+            "g16T": torch.zeros((out, m), dtype=bf, device=self.dev),
+            "dz16T": [torch.zeros((b, m), dtype=bf, device=self.dev) for b in self.sizes[1:-1]],
             "y": torch.zeros((m, out), dtype=f32, device=self.dev),
             "t": torch.zeros((m, out), dtype=f32, device=self.dev),
             "g32": torch.zeros((m, out), dtype=f32, device=self.dev),
@@ -445,19 +483,25 @@ class Mlp:
         out = self.sizes[-1]
         native.check(lib.oafdtd_mlp_mse_grad(y.data_ptr(), t.data_ptr(), m, out, buf["g32"].data_ptr(),
                                              buf["g16"].data_ptr(), buf["row_loss"].data_ptr(), s), "mse_grad")
-        g32, g16 = buf["g32"].data_ptr(), buf["g16"].data_ptr()
+        g32, g16, gT = buf["g32"].data_ptr(), buf["g16"].data_ptr(), buf["g16T"].data_ptr()
+        native.check(lib.oafdtd_mlp_transpose(g16, m, out, out, gT, m, s), "transpose")
+        native.check(lib.oafdtd_mlp_transpose(buf["x16"].data_ptr(), m, self.sizes[0], self.sizes[0],
+                                              buf["x16T"].data_ptr(), m, s), "transpose")
         for l in range(len(self.layout) - 1, -1, -1):
             _, a, b, _ = self.layout[l]
             inp = buf["x16"].data_ptr() if l == 0 else buf["acts"][l - 1].data_ptr()
-            # dW = inp^T . g  (a x b)
-            self._gemm(inp, g16, self._gw(l), 0, 0, 0, a, b, m, a, b, b, 1, 0, 0, s)
+            inp_t = buf["x16T"].data_ptr() if l == 0 else buf["actsT"][l - 1].data_ptr()
+            # dW = inp^T . g = (inp^T) . (g^T)^T  (a x b), from the transposed activations and g
+            self._gemm_tn(inp_t, gT, self._gw(l), 0, 0, 0, 0, a, b, m, m, m, b, a, 0, s)
             native.check(lib.oafdtd_mlp_colsum(g32, m, b, b, self._gb(l), s), "colsum")
             if l == 0:
                 break
-            # dZ[l-1] = (g . W^T) times the activation's derivative at the layer input  (m x a)
+            # dZ[l-1] = (g . W^T) times the activation's derivative at the layer input  (m x a);
+            # W (a x b) is the B operand (N x K) as stored; the transposed dZ feeds layer l-1's dW
             dz32, dz16 = buf["dz32"][l - 1].data_ptr(), buf["dz16"][l - 1].data_ptr()
-            self._gemm(g16, self._w(l), dz32, dz16, 0, inp, m, a, b, b, b, a, 0, 1, self.dact, s)
-            g32, g16 = dz32, dz16
+            dzt = buf["dz16T"][l - 1].data_ptr()
+            self._gemm_tn(g16, self._w(l), dz32, dz16, dzt, 0, inp, m, a, b, b, b, a, m, self.dact, s)
+            g32, g16, gT = dz32, dz16, dzt
 
     def gradients(self, x: npt.ArrayLike, t: npt.ArrayLike) -> tuple[float, FloatArray]:
         """Loss and the flat gradient buffer for one batch given on the host (checks and tests)."""
@@ -469,9 +513,10 @@ class Mlp:
         buf["x16"].copy_(torch.from_numpy(x).to(self.dev).to(torch.bfloat16))
         buf["t"].copy_(torch.from_numpy(t).to(self.dev))
         s = self._stream()
-        self._forward(buf["x16"].data_ptr(), buf["acts"], buf["y"].data_ptr(), m, s)
+        self._forward(buf["x16"].data_ptr(), buf["acts"], buf["y"].data_ptr(), m, s, buf["actsT"])
         self._backward(buf, m, s)
         torch.cuda.synchronize(self.dev)
+        self.check_status()
         loss = float(buf["row_loss"].sum().item()) / (m * self.sizes[-1])
         return loss, self.grad.detach().cpu().numpy().astype(np.float64)
 
@@ -488,6 +533,15 @@ class Mlp:
         native.check(self.lib.oafdtd_mlp_adam(self.p32.data_ptr(), self.p16.data_ptr(), self.grad.data_ptr(),
                                               self.m1.data_ptr(), self.m2.data_ptr(), self.n_params,
                                               self.lr.data_ptr(), b1, b2, eps, self.step_no.data_ptr(), s), "adam")
+        self._refresh_t(s)
+
+    def check_status(self) -> None:
+        """Raise when a bounded wait of a tcgen05 GEMM gave up since the last check (its result
+        was not written); clears the word."""
+        if int(self.status.item()) != 0:
+            self.status.zero_()
+            raise AccelError(ErrorInfo("ACCEL_TIMEOUT", "a tensor-core GEMM gave up waiting for its operands",
+                                       "surrogate"))
 
     # ---- training
     def _train_step(self, tr: dict[str, Any], j: int, s: int) -> None:
@@ -496,12 +550,13 @@ class Mlp:
         buf = tr["buf"]
         native.check(lib.oafdtd_mlp_gather(tr["x"].data_ptr(), self.sizes[0], idx, m, None, buf["x16"].data_ptr(), s), "gather")
         native.check(lib.oafdtd_mlp_gather(tr["t"].data_ptr(), self.sizes[-1], idx, m, buf["t"].data_ptr(), None, s), "gather")
-        self._forward(buf["x16"].data_ptr(), buf["acts"], buf["y"].data_ptr(), m, s)
+        self._forward(buf["x16"].data_ptr(), buf["acts"], buf["y"].data_ptr(), m, s, buf["actsT"])
         self._backward(buf, m, s)
         native.check(lib.oafdtd_mlp_count(self.step_no.data_ptr(), s), "count")
         native.check(lib.oafdtd_mlp_adam(self.p32.data_ptr(), self.p16.data_ptr(), self.grad.data_ptr(),
                                          self.m1.data_ptr(), self.m2.data_ptr(), self.n_params, self.lr.data_ptr(),
                                          0.9, 0.999, 1e-8, self.step_no.data_ptr(), s), "adam")
+        self._refresh_t(s)
 
     def prepare(self, x: npt.ArrayLike, t: npt.ArrayLike, graph: bool = True) -> None:
         """Upload the training set ``x (n, n_in)`` -> ``t (n, sizes[-1])`` (both already scaled)
@@ -574,6 +629,7 @@ class Mlp:
             if log_every and (e % log_every == 0 or e == epochs - 1):
                 losses.append(self.last_loss())
         self.torch.cuda.synchronize(self.dev)
+        self.check_status()
         return losses
 
     def predict(self, x: npt.ArrayLike, chunk: int = 4096) -> FloatArray:
@@ -590,6 +646,7 @@ class Mlp:
             y = torch.empty((m, self.sizes[-1]), dtype=torch.float32, device=self.dev)
             self._forward(x16.data_ptr(), acts, y.data_ptr(), m, s)
             out[a : a + m] = y.cpu().numpy()
+        self.check_status()
         return out
 
 
@@ -702,8 +759,7 @@ class Ensemble:
         for k, net in enumerate(self.nets):
             net.stream.synchronize()
             if keep[k] is not None:
-                net.p32.copy_(keep[k])
-                net.p16.copy_(keep[k].to(net.torch.bfloat16))
+                net.load_flat(keep[k])
         self.val_scores = best
         self.train_seconds = time.perf_counter() - t0
         return logs
@@ -753,8 +809,7 @@ class Ensemble:
         for net, flat in zip(ens.nets, w, strict=True):
             if flat.size != net.n_params:
                 raise ValueError(f"{path}: {flat.size} weights where the network holds {net.n_params}")
-            net.p32.copy_(torch.from_numpy(flat.astype(np.float32)).to(net.dev))
-            net.p16.copy_(net.p32.to(torch.bfloat16))
+            net.load_flat(torch.from_numpy(flat.astype(np.float32)).to(net.dev))
         ens.mu, ens.sigma, ens.scale = d["mu"], float(d["sigma"]), float(d["scale"])
         return ens
 
@@ -935,10 +990,12 @@ def experiment(
 GEMM_SHAPES = ((256, 512, 512), (4096, 512, 512), (65536, 512, 512), (65536, 1024, 512), (16384, 4096, 4096))
 
 
-def gemm_rates(shapes: Sequence[tuple[int, int, int]] = GEMM_SHAPES, reps: int = 20) -> list[dict[str, float]]:
-    """Time ``oafdtd_mlp_gemm`` (BF16 A (M x K) . B (K x N) + bias, tanh, BF16 out) with CUDA
-    events over ``reps`` launches after three warm-up launches, and check it against the FP32
-    product. Returns per shape the microseconds per launch, TFLOP/s and the largest error."""
+def gemm_rates(shapes: Sequence[tuple[int, int, int]] = GEMM_SHAPES, reps: int = 20) -> list[dict[str, Any]]:
+    """Time the two GEMM kernels on BF16 A (M x K) and B + bias, tanh, BF16 out, with CUDA events
+    over ``reps`` launches after three warm-up launches, and check them against the FP32 product:
+    ``oafdtd_mlp_gemm`` (mma.sync, B as K x N) and ``oafdtd_mlp_gemm_tn`` (B as N x K; tcgen05
+    where the shape allows). Returns per shape and kernel the microseconds per launch, TFLOP/s
+    and the largest error."""
     torch = _torch()
     lib = native.load()
     gen = torch.Generator(device="cuda")
@@ -947,25 +1004,33 @@ def gemm_rates(shapes: Sequence[tuple[int, int, int]] = GEMM_SHAPES, reps: int =
     for m, n, k in shapes:
         a = torch.randn(m, k, device="cuda", generator=gen).to(torch.bfloat16)
         b = torch.randn(k, n, device="cuda", generator=gen).to(torch.bfloat16)
+        bt = b.t().contiguous()
         c = torch.empty(m, n, device="cuda", dtype=torch.bfloat16)
         bias = torch.zeros(n, device="cuda")
         s = int(torch.cuda.current_stream().cuda_stream)
 
-        def launch() -> None:
+        def mma_sync() -> None:
             native.check(lib.oafdtd_mlp_gemm(a.data_ptr(), b.data_ptr(), None, c.data_ptr(), bias.data_ptr(), None,
                                              m, n, k, k, n, n, 0, 0, 3, 0.0, s), "oafdtd_mlp_gemm")
 
-        for _ in range(3):
-            launch()
-        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        t0.record()
-        for _ in range(reps):
-            launch()
-        t1.record()
-        torch.cuda.synchronize()
-        us = 1e3 * t0.elapsed_time(t1) / reps
-        err = float((c.float() - torch.tanh(a.float() @ b.float())).abs().max().item())
-        out.append({"m": m, "n": n, "k": k, "us": us, "tflops": 2.0 * m * n * k / us / 1e6, "max_err": err})
+        def tcgen05() -> None:
+            native.check(lib.oafdtd_mlp_gemm_tn(a.data_ptr(), bt.data_ptr(), None, c.data_ptr(), None, bias.data_ptr(),
+                                                None, m, n, k, k, k, n, m, 3, 0.0, None, s), "oafdtd_mlp_gemm_tn")
+
+        want = torch.tanh(a.float() @ b.float())
+        for name, launch in (("mma_sync", mma_sync), ("gemm_tn", tcgen05)):
+            for _ in range(3):
+                launch()
+            t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0.record()
+            for _ in range(reps):
+                launch()
+            t1.record()
+            torch.cuda.synchronize()
+            us = 1e3 * t0.elapsed_time(t1) / reps
+            err = float((c.float() - want).abs().max().item())
+            out.append({"kernel": name, "m": m, "n": n, "k": k, "us": us, "tflops": 2.0 * m * n * k / us / 1e6,
+                        "max_err": err})
     return out
 
 

@@ -1,7 +1,11 @@
 """The surrogate's GPU kernels against the CPU oracle, and what the trained network gains.
 
 * GEMM: BF16 operands with FP32 accumulation against FP64 sums of the same BF16 values, every
-  transpose combination, ragged sizes, each epilogue.
+  transpose combination, ragged sizes, each epilogue; the same for the K-major entry point
+  (``oafdtd_mlp_gemm_tn``) on tcgen05 tile shapes and on ragged shapes it hands to the fallback,
+  with its transposed BF16 output; the transpose kernel.
+* One training batch at tcgen05 shapes (batch 256, widths 512): loss and gradients against the
+  oracle.
 * One training batch: loss and every weight and bias gradient against ``oracle/mlp_oracle.py``
   (rounded to BF16 where the GPU stores BF16), and against the exact FP64 network (stated).
 * Adam: one step against the oracle's.
@@ -76,6 +80,79 @@ def test_gemm_rejects_bad_arguments() -> None:
     assert lib.oafdtd_mlp_gemm(x.data_ptr(), x.data_ptr(), None, None, None, None, 4, 4, 4, 4, 4, 4, 0, 0, 0, 0.0, None) == -1
     y = torch.zeros(16, dtype=torch.float32, device="cuda")
     assert lib.oafdtd_mlp_gemm(x.data_ptr(), x.data_ptr(), y.data_ptr(), None, None, None, 4, 4, 4, 4, 4, 4, 0, 0, 2, 0.0, None) == -1
+
+
+# tcgen05 tiles (M, N multiples of 128, K of 64) and ragged shapes the fallback takes
+TN_SHAPES = [(256, 512, 512), (128, 128, 64), (256, 1024, 512), (384, 256, 192), (77, 134, 203), (256, 512, 8)]
+
+
+@pytest.mark.parametrize("shape", TN_SHAPES)
+@pytest.mark.parametrize("act", [0, 2, 3, 4])
+def test_gemm_tn_matches_fp64_sums_of_bf16_operands(shape: tuple[int, int, int], act: int) -> None:
+    """C = A . B^T with A (M x K) and B (N x K), both K-contiguous: FP32 C, BF16 C and its
+    transpose, each epilogue; the status word stays zero."""
+    lib = _lib()
+    rng = np.random.default_rng(1000 + act + shape[0] + shape[2])
+    m, n, k = shape
+    a = bf16_round(rng.standard_normal((m, k)))
+    b = bf16_round(rng.standard_normal((n, k)))
+    bias = rng.standard_normal(n).astype(np.float32)
+    mask = bf16_round(rng.standard_normal((m, n)))
+    ref = a @ b.T + bias
+    if act == 2:
+        ref = np.where(mask > 0, ref, 0)
+    if act == 3:
+        ref = np.tanh(ref)
+    if act == 4:
+        ref = ref * (1.0 - mask * mask)
+    da, db_ = _dev(a, torch.bfloat16), _dev(b, torch.bfloat16)
+    dbias, dmask = _dev(bias, torch.float32), _dev(mask, torch.bfloat16)
+    c32 = torch.zeros((m, n), dtype=torch.float32, device="cuda")
+    c16 = torch.zeros((m, n), dtype=torch.bfloat16, device="cuda")
+    c16t = torch.zeros((n, m), dtype=torch.bfloat16, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    rc = lib.oafdtd_mlp_gemm_tn(da.data_ptr(), db_.data_ptr(), c32.data_ptr(), c16.data_ptr(), c16t.data_ptr(),
+                                dbias.data_ptr(), dmask.data_ptr(), m, n, k, k, k, n, m, act, 0.0,
+                                status.data_ptr(), None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    got = c32.cpu().numpy().astype(np.float64)
+    scale = np.sqrt(k) * 4 * (1.0 if act != 4 else np.abs(mask).max() ** 2 + 1.0)
+    assert np.abs(got - ref).max() <= 2e-6 * scale
+    np.testing.assert_array_equal(c16.float().cpu().numpy(), bf16_round(got))
+    np.testing.assert_array_equal(c16t.float().cpu().numpy(), c16.float().cpu().numpy().T)
+
+
+def test_transpose16() -> None:
+    lib = _lib()
+    rng = np.random.default_rng(4)
+    for rows, cols in ((256, 512), (77, 134), (8, 1024)):
+        x = _dev(rng.standard_normal((rows, cols)), torch.bfloat16)
+        y = torch.zeros((cols, rows), dtype=torch.bfloat16, device="cuda")
+        assert lib.oafdtd_mlp_transpose(x.data_ptr(), rows, cols, cols, y.data_ptr(), rows, None) == 0
+        torch.cuda.synchronize()
+        assert torch.equal(y, x.t())
+
+
+def test_training_batch_on_tcgen05_shapes_matches_the_oracle() -> None:
+    """Batch 256 and hidden widths of 512: the forward, weight-gradient and input-gradient GEMMs
+    of the hidden layers run on tcgen05; loss and gradients against the oracle."""
+    from open_analysis_gb300.surrogate import Mlp
+
+    net = Mlp([7, 512, 512, 128], batch=256, seed=2, act="tanh")
+    w, b = net.weights()
+    rng = np.random.default_rng(8)
+    x = rng.uniform(-1, 1, (256, 7))
+    t = rng.standard_normal((256, 128))
+    loss, flat = net.gradients(x, t)
+    gw, gb = net.split(flat)
+    ref = loss_and_grads(w, b, net.pad(x), t.astype(np.float32), bf16=True, act="tanh")
+    assert abs(loss - ref.loss) <= 1e-5 * ref.loss
+    for l in range(len(w)):
+        for got, want in ((gw[l], ref.dw[l]), (gb[l], ref.db[l])):
+            rel = np.linalg.norm(got - want) / np.linalg.norm(want)
+            assert rel <= 5e-3, (l, rel)
 
 
 def _small_net(seed: int = 0, act: str = "tanh"):  # type: ignore[no-untyped-def]
