@@ -365,13 +365,16 @@ int oafdtd_mlp_gemm(const void* A, const void* B, float* C32, void* C16, const f
                     int32_t M, int32_t N, int32_t K, int32_t lda, int32_t ldb, int32_t ldc, int32_t ta, int32_t tb,
                     int32_t act, float beta, void* stream);
 
-/* out[n] = sum over m of X[m * ld + n] (FP32; bias gradients). */
-int oafdtd_mlp_colsum(const float* X, int32_t M, int32_t N, int32_t ld, float* out, void* stream);
+/* out[g * out_stride + n] = sum over m < M of X[g * x_stride + m * ld + n] for g < groups (FP32;
+ * bias gradients of every ensemble member in one launch). */
+int oafdtd_mlp_colsum(const float* X, int32_t M, int32_t N, int32_t ld, float* out, int32_t groups,
+                      int64_t x_stride, int64_t out_stride, void* stream);
 
-/* Mean squared error of Y against T (both M x N FP32): the gradient 2 (Y - T) / (M N) into G32
- * (FP32) and G16 (BF16), and the sum of squared errors of each row into row_loss[M]. */
+/* Mean squared error of Y against T (both M x N FP32, M = groups x rows of each group): the
+ * gradient 2 (Y - T) / ((M / groups) N) of each group's mean into G32 (FP32) and G16 (BF16), and
+ * the sum of squared errors of each row into row_loss[M]. */
 int oafdtd_mlp_mse_grad(const float* Y, const float* T, int32_t M, int32_t N, float* G32, void* G16,
-                        float* row_loss, void* stream);
+                        float* row_loss, int32_t groups, void* stream);
 
 /* One Adam step on n FP32 weights w (moments m1, m2), refreshing the BF16 copy w16 (nullable).
  * The learning rate is read from *lr (device float) and the step number for the bias corrections
@@ -379,21 +382,27 @@ int oafdtd_mlp_mse_grad(const float* Y, const float* T, int32_t M, int32_t N, fl
 int oafdtd_mlp_adam(float* w, void* w16, const float* grad, float* m1, float* m2, int64_t n, const float* lr,
                     float b1, float b2, float eps, const int32_t* step, void* stream);
 
-/* C = act(A . B^T + bias) with A row-major M x K and B row-major N x K (both K-contiguous), BF16
- * operands, FP32 accumulation, the epilogues of oafdtd_mlp_gemm (ldc for C32, C16 and mask). Shapes
- * with M and N multiples of 128, K a multiple of 64 and 16-byte aligned rows run on the fifth-
- * generation tensor cores (tcgen05.mma, accumulator in tensor memory, operand tiles by TMA tensor
- * copies); other shapes on the mma.sync kernel. C16T (BF16, nullable) receives the result
- * transposed, N x M with leading dimension ldct (the next layer's weight gradient reads it
- * K-contiguous); off the tcgen05 shapes it needs C16 as well. status (device int32, nullable):
- * bit 0 is set when a bounded wait of the tcgen05 kernel gave up (that launch's C is not written). */
+/* Grouped: C_g = act(A_g . B_g^T + bias_g) for g < groups, with A_g row-major M x K and B_g
+ * row-major N x K (both K-contiguous), BF16 operands, FP32 accumulation, the epilogues of
+ * oafdtd_mlp_gemm (ldc for C32, C16 and mask). Group g's operands start strideA, strideB, strideC
+ * (C32, C16 and mask), strideCT (C16T) and strideBias elements after group g - 1's (ignored for
+ * one group). Problems with M a multiple of 128, N and K multiples of 64, leading dimensions and
+ * strides multiples of 8, 16-byte aligned pointers and beta 0 run on the fifth-generation tensor
+ * cores (tcgen05.mma, accumulators in tensor memory, operand tiles and results moved by TMA tensor
+ * copies; one persistent launch for all groups); the others on the mma.sync kernel, one launch.
+ * C16T (BF16, nullable) receives the result transposed, N x M with leading dimension ldct (the next
+ * layer's weight gradient reads it K-contiguous); off the tcgen05 shapes it needs C16 as well.
+ * status (device int32, nullable): bit 0 is set when a bounded wait of the tcgen05 kernel gave up
+ * (that launch's C is then incomplete). */
 int oafdtd_mlp_gemm_tn(const void* A, const void* B, float* C32, void* C16, void* C16T, const float* bias,
                        const void* mask, int32_t M, int32_t N, int32_t K, int32_t lda, int32_t ldb, int32_t ldc,
-                       int32_t ldct, int32_t act, float beta, int32_t* status, void* stream);
+                       int32_t ldct, int32_t act, float beta, int32_t groups, int64_t strideA, int64_t strideB,
+                       int64_t strideC, int64_t strideCT, int64_t strideBias, int32_t* status, void* stream);
 
-/* dst (cols x rows, leading dimension ldd) = src^T (rows x cols, leading dimension lds), BF16. */
+/* dst_g (cols x rows, leading dimension ldd) = src_g^T (rows x cols, leading dimension lds), BF16,
+ * for g < groups, src_g and dst_g src_stride and dst_stride elements after group g - 1's. */
 int oafdtd_mlp_transpose(const void* src, int32_t rows, int32_t cols, int32_t lds, void* dst, int32_t ldd,
-                         void* stream);
+                         int32_t groups, int64_t src_stride, int64_t dst_stride, void* stream);
 
 /* *counter += 1 on the device (the Adam step number inside a captured training step). */
 int oafdtd_mlp_count(int32_t* counter, void* stream);

@@ -34,13 +34,30 @@ struct GemmArgs {
   // 1 - mask^2 (tanh derivative, mask = the stored tanh output)
   int M, N, K, lda, ldb, ldc, ta, tb, act;
   float beta;             // C32 = acc + beta * C32 (gradient accumulation); 0 overwrites
+  long long sA, sB, sC, sBias;  // elements between groups (blockIdx.z); the mask moves with C
 };
+
+// The arguments of group blockIdx.z.
+__device__ __forceinline__ GemmArgs at_group(const GemmArgs& g0) {
+  GemmArgs g = g0;
+  const long long z = blockIdx.z;
+  if (z) {
+    g.A += z * g.sA;
+    g.B += z * g.sB;
+    if (g.C32) g.C32 += z * g.sC;
+    if (g.C16) g.C16 += z * g.sC;
+    if (g.mask) g.mask += z * g.sC;
+    if (g.bias) g.bias += z * g.sBias;
+  }
+  return g;
+}
 
 __device__ __forceinline__ uint32_t pack2(const __nv_bfloat16* p) {
   return *reinterpret_cast<const uint32_t*>(p);
 }
 
-__global__ void __launch_bounds__(128) gemm_bf16_kernel(const GemmArgs g) {
+__global__ void __launch_bounds__(128) gemm_bf16_kernel(const GemmArgs g0) {
+  const GemmArgs g = at_group(g0);
   __shared__ __align__(16) __nv_bfloat16 As[kBM][kPadK];
   __shared__ __align__(16) __nv_bfloat16 Bs[kBN][kPadK];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -193,7 +210,8 @@ __device__ __forceinline__ void pipe_load(const GemmArgs& g, PipeSmem<TA, TB, BM
 }
 
 template <int TA, int TB, int BM>
-__global__ void __launch_bounds__(128) gemm_pipe_kernel(const GemmArgs g) {
+__global__ void __launch_bounds__(128) gemm_pipe_kernel(const GemmArgs g0) {
+  const GemmArgs g = at_group(g0);
   __shared__ __align__(128) PipeSmem<TA, TB, BM> sm;
   constexpr int MI = BM / 32;  // m16 tiles per warp (warp tile BM/2 x 32)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -289,8 +307,8 @@ __global__ void __launch_bounds__(128) gemm_pipe_kernel(const GemmArgs g) {
 }
 
 template <int BM>
-void launch_pipe(const GemmArgs& g, cudaStream_t s) {
-  const dim3 grid((g.N + kPipeBN - 1) / kPipeBN, (g.M + BM - 1) / BM);
+void launch_pipe(const GemmArgs& g, int groups, cudaStream_t s) {
+  const dim3 grid((g.N + kPipeBN - 1) / kPipeBN, (g.M + BM - 1) / BM, groups);
   if (g.ta && g.tb) gemm_pipe_kernel<1, 1, BM><<<grid, 128, 0, s>>>(g);
   else if (g.ta) gemm_pipe_kernel<1, 0, BM><<<grid, 128, 0, s>>>(g);
   else if (g.tb) gemm_pipe_kernel<0, 1, BM><<<grid, 128, 0, s>>>(g);
@@ -300,18 +318,20 @@ void launch_pipe(const GemmArgs& g, cudaStream_t s) {
 bool pipe_ok(const GemmArgs& g) {
   auto al = [](const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; };
   return g.M % 8 == 0 && g.N % 8 == 0 && g.K % 8 == 0 && g.lda % 8 == 0 && g.ldb % 8 == 0 && g.ldc % 2 == 0 &&
-         al(g.A, 16) && al(g.B, 16) && al(g.C32, 8) && al(g.C16, 4) && al(g.mask, 4);
+         g.sA % 8 == 0 && g.sB % 8 == 0 && g.sC % 2 == 0 && al(g.A, 16) && al(g.B, 16) && al(g.C32, 8) && al(g.C16, 4) && al(g.mask, 4);
 }
 
-// Column sums of an FP32 M x N matrix (bias gradients). A block takes 32 columns; each of its 16
-// row lanes sums the rows lane, lane + 16, ... of one column (a warp reads 32 adjacent columns of
-// one row), then lane 0 adds the 16 partial sums in lane order: a fixed order, so the result is
-// the same on every run.
+// Column sums of an FP32 M x N matrix (bias gradients), per group (blockIdx.y: X and out move by
+// xs and os elements). A block takes 32 columns; each of its 16 row lanes sums the rows lane,
+// lane + 16, ... of one column (a warp reads 32 adjacent columns of one row), then lane 0 adds the
+// 16 partial sums in lane order: a fixed order, so the result is the same on every run.
 constexpr int kSumCols = 32, kSumLanes = 16;
 
 __global__ void __launch_bounds__(kSumCols * kSumLanes) colsum_kernel(const float* X, int M, int N, int ld,
-                                                                      float* out) {
+                                                                      long long xs, float* out, long long os) {
   __shared__ float part[kSumLanes][kSumCols + 1];
+  X += blockIdx.y * xs;
+  out += blockIdx.y * os;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int n = blockIdx.x * kSumCols + tx;
   float s = 0.f;
@@ -327,12 +347,13 @@ __global__ void __launch_bounds__(kSumCols * kSumLanes) colsum_kernel(const floa
   }
 }
 
-// Mean-squared-error gradient: G = (2 / (M N)) (Y - T), in FP32 and BF16; loss partials per row.
-__global__ void mse_grad_kernel(const float* Y, const float* T, int M, int N, float* G32, __nv_bfloat16* G16,
+// Mean-squared-error gradient of each group's mean over its M_g rows: G = (2 / (M_g N)) (Y - T),
+// in FP32 and BF16; loss partials per row.
+__global__ void mse_grad_kernel(const float* Y, const float* T, int Mg, int N, float* G32, __nv_bfloat16* G16,
                                 float* row_loss) {
   const int m = blockIdx.x;
   float s = 0.f;
-  const float scale = 2.f / ((float)M * (float)N);
+  const float scale = 2.f / ((float)Mg * (float)N);
   for (int n = threadIdx.x; n < N; n += blockDim.x) {
     const long long o = (long long)m * N + n;
     const float d = Y[o] - T[o];
@@ -384,10 +405,12 @@ __global__ void gather_kernel(const float* src, int cols, const int* idx, int ro
 }
 
 // dst (cols x rows, leading dimension ldd) = src^T (rows x cols, leading dimension lds), BF16,
-// through 32 x 32 shared tiles (both sides coalesced).
-__global__ void transpose16_kernel(const __nv_bfloat16* src, int rows, int cols, int lds, __nv_bfloat16* dst,
-                                   int ldd) {
+// through 32 x 32 shared tiles (both sides coalesced); group blockIdx.z at ss / sd elements.
+__global__ void transpose16_kernel(const __nv_bfloat16* src, int rows, int cols, int lds, long long ss,
+                                   __nv_bfloat16* dst, int ldd, long long sd) {
   __shared__ __nv_bfloat16 t[32][33];
+  src += blockIdx.z * ss;
+  dst += blockIdx.z * sd;
   const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
   for (int y = threadIdx.y; y < 32; y += blockDim.y) {
     const int r = r0 + y, c = c0 + threadIdx.x;
@@ -400,53 +423,87 @@ __global__ void transpose16_kernel(const __nv_bfloat16* src, int rows, int cols,
   }
 }
 
+// One GEMM launch of `groups` problems (blockIdx.z): the pipelined kernel where the shape and
+// alignment allow, the scalar-staging kernel elsewhere. Returns 0 or -3 (launch error).
+int gemm_grouped(const GemmArgs& g, int groups, cudaStream_t s, const char* who) {
+  if (pipe_ok(g)) {
+    // 64-row tiles unless that leaves fewer than two blocks per SM on a 152-SM part
+    const long long tiles64 = (long long)((g.N + 63) / 64) * ((g.M + 63) / 64) * groups;
+    if (tiles64 < 304) launch_pipe<32>(g, groups, s);
+    else launch_pipe<64>(g, groups, s);
+  } else {
+    const dim3 grid((g.N + kBN - 1) / kBN, (g.M + kBM - 1) / kBM, groups);
+    gemm_bf16_kernel<<<grid, 128, 0, s>>>(g);
+  }
+  const cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) {
+    set_last_error(std::string(who) + ": " + cudaGetErrorString(err));
+    return -3;
+  }
+  return 0;
+}
+
 }  // namespace oafdtd
 
 // --------------------------------------------------------------------------------------- C ABI
 extern "C" {
 
 int oafdtd_mlp_transpose(const void* src, int32_t rows, int32_t cols, int32_t lds, void* dst, int32_t ldd,
-                         void* stream) {
-  if (!src || !dst || rows < 1 || cols < 1 || lds < cols || ldd < rows) {
+                         int32_t groups, int64_t src_stride, int64_t dst_stride, void* stream) {
+  if (!src || !dst || rows < 1 || cols < 1 || lds < cols || ldd < rows || groups < 1 || groups > 65535 ||
+      (groups > 1 && (src_stride < (int64_t)rows * lds || dst_stride < (int64_t)cols * ldd))) {
     oafdtd::set_last_error("oafdtd_mlp_transpose: bad arguments");
     return -1;
   }
-  const dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
+  const dim3 grid((cols + 31) / 32, (rows + 31) / 32, groups), block(32, 8);
   oafdtd::transpose16_kernel<<<grid, block, 0, static_cast<cudaStream_t>(stream)>>>(
-      static_cast<const __nv_bfloat16*>(src), rows, cols, lds, static_cast<__nv_bfloat16*>(dst), ldd);
+      static_cast<const __nv_bfloat16*>(src), rows, cols, lds, src_stride, static_cast<__nv_bfloat16*>(dst), ldd,
+      dst_stride);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 
-int oafdtd_mlp_gemm(const void* A, const void* B, float* C32, void* C16, const float* bias, const void* mask,
-                    int32_t M, int32_t N, int32_t K, int32_t lda, int32_t ldb, int32_t ldc, int32_t ta, int32_t tb,
-                    int32_t act, float beta, void* stream);
-
 int oafdtd_mlp_gemm_tn(const void* A, const void* B, float* C32, void* C16, void* C16T, const float* bias,
                        const void* mask, int32_t M, int32_t N, int32_t K, int32_t lda, int32_t ldb, int32_t ldc,
-                       int32_t ldct, int32_t act, float beta, int32_t* status, void* stream) {
+                       int32_t ldct, int32_t act, float beta, int32_t groups, int64_t strideA, int64_t strideB,
+                       int64_t strideC, int64_t strideCT, int64_t strideBias, int32_t* status, void* stream) {
+  const bool bad_strides = groups > 1 && (strideA < (int64_t)M * lda || strideB < (int64_t)N * ldb ||
+                                          ((C32 || C16 || mask) && strideC < (int64_t)M * ldc) ||
+                                          (C16T && strideCT < (int64_t)N * ldct) || (bias && strideBias < N));
   if (!A || !B || (!C32 && !C16 && !C16T) || M < 1 || N < 1 || K < 1 || act < 0 || act > 4 ||
-      ((act == 2 || act == 4) && !mask) || (C16T && ldct < M)) {
+      ((act == 2 || act == 4) && !mask) || (C16T && ldct < M) || lda < K || ldb < K ||
+      ((C32 || C16 || mask) && ldc < N) || groups < 1 || groups > 65535 || bad_strides) {
     oafdtd::set_last_error("oafdtd_mlp_gemm_tn: bad arguments");
     return -1;
   }
   const cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (oafdtd::umma_shape_ok(M, N, K, lda, ldb, A, B)) {
+  oafdtd::UmmaProblem p{A, B, C32, C16, C16T, bias, mask, M, N, K, lda, ldb, ldc, ldct, act, groups,
+                        strideA, strideB, strideC, strideCT, strideBias, beta, status};
+  if (oafdtd::umma_shape_ok(p)) {
     std::string why;
-    const cudaError_t err = oafdtd::launch_umma_gemm(A, B, C32, C16, C16T, bias, mask, M, N, K, lda, ldb, ldc, ldct,
-                                                     act, beta, status, s, &why);
+    const cudaError_t err = oafdtd::launch_umma_gemm(p, s, &why);
     if (err != cudaSuccess) {
       oafdtd::set_last_error(std::string("oafdtd_mlp_gemm_tn: ") + (why.empty() ? cudaGetErrorString(err) : why));
       return err == cudaErrorInvalidValue ? -1 : -3;
     }
     return 0;
   }
-  // other shapes: the mma.sync kernel, then the transposed copy from the BF16 result
+  // other shapes: the mma.sync kernels (B transposed), then the transposed copy of the BF16 result
   if (C16T && !C16) {
     oafdtd::set_last_error("oafdtd_mlp_gemm_tn: a transposed result off the tcgen05 shapes needs C16 as well");
     return -1;
   }
-  int rc = oafdtd_mlp_gemm(A, B, C32, C16, bias, mask, M, N, K, lda, ldb, ldc, 0, 1, act, beta, stream);
-  if (rc == 0 && C16T) rc = oafdtd_mlp_transpose(C16, M, N, ldc, C16T, ldct, stream);
+  oafdtd::GemmArgs g;
+  g.A = static_cast<const __nv_bfloat16*>(A);
+  g.B = static_cast<const __nv_bfloat16*>(B);
+  g.C32 = C32;
+  g.C16 = static_cast<__nv_bfloat16*>(C16);
+  g.bias = bias;
+  g.mask = static_cast<const __nv_bfloat16*>(mask);
+  g.M = M, g.N = N, g.K = K, g.lda = lda, g.ldb = ldb, g.ldc = ldc, g.ta = 0, g.tb = 1, g.act = act;
+  g.beta = beta;
+  g.sA = strideA, g.sB = strideB, g.sC = strideC, g.sBias = strideBias;
+  int rc = oafdtd::gemm_grouped(g, groups, s, "oafdtd_mlp_gemm_tn");
+  if (rc == 0 && C16T) rc = oafdtd_mlp_transpose(C16, M, N, ldc, C16T, ldct, groups, strideC, strideCT, stream);
   return rc;
 }
 
@@ -466,36 +523,25 @@ int oafdtd_mlp_gemm(const void* A, const void* B, float* C32, void* C16, const f
   g.mask = static_cast<const __nv_bfloat16*>(mask);
   g.M = M, g.N = N, g.K = K, g.lda = lda, g.ldb = ldb, g.ldc = ldc, g.ta = ta, g.tb = tb, g.act = act;
   g.beta = beta;
-  const cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (oafdtd::pipe_ok(g)) {
-    // 64-row tiles unless that leaves fewer than two blocks per SM on a 152-SM part
-    const long long tiles64 = (long long)((N + 63) / 64) * ((M + 63) / 64);
-    if (tiles64 < 304) oafdtd::launch_pipe<32>(g, s);
-    else oafdtd::launch_pipe<64>(g, s);
-  } else {
-    const dim3 grid((N + oafdtd::kBN - 1) / oafdtd::kBN, (M + oafdtd::kBM - 1) / oafdtd::kBM);
-    oafdtd::gemm_bf16_kernel<<<grid, 128, 0, s>>>(g);
-  }
-  const cudaError_t err = cudaGetLastError();
-  if (err != cudaSuccess) {
-    oafdtd::set_last_error(std::string("oafdtd_mlp_gemm: ") + cudaGetErrorString(err));
-    return -3;
-  }
-  return 0;
+  g.sA = g.sB = g.sC = g.sBias = 0;
+  return oafdtd::gemm_grouped(g, 1, static_cast<cudaStream_t>(stream), "oafdtd_mlp_gemm");
 }
 
-int oafdtd_mlp_colsum(const float* X, int32_t M, int32_t N, int32_t ld, float* out, void* stream) {
-  if (!X || !out || M < 1 || N < 1) return -1;
-  const dim3 block(oafdtd::kSumCols, oafdtd::kSumLanes);
-  oafdtd::colsum_kernel<<<(N + oafdtd::kSumCols - 1) / oafdtd::kSumCols, block, 0, static_cast<cudaStream_t>(stream)>>>(
-      X, M, N, ld, out);
+int oafdtd_mlp_colsum(const float* X, int32_t M, int32_t N, int32_t ld, float* out, int32_t groups,
+                      int64_t x_stride, int64_t out_stride, void* stream) {
+  if (!X || !out || M < 1 || N < 1 || ld < N || groups < 1 || groups > 65535 ||
+      (groups > 1 && (x_stride < (int64_t)M * ld || out_stride < N)))
+    return -1;
+  const dim3 block(oafdtd::kSumCols, oafdtd::kSumLanes), grid((N + oafdtd::kSumCols - 1) / oafdtd::kSumCols, groups);
+  oafdtd::colsum_kernel<<<grid, block, 0, static_cast<cudaStream_t>(stream)>>>(X, M, N, ld, x_stride, out,
+                                                                                out_stride);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 
 int oafdtd_mlp_mse_grad(const float* Y, const float* T, int32_t M, int32_t N, float* G32, void* G16,
-                        float* row_loss, void* stream) {
-  if (!Y || !T || !G32 || !G16 || !row_loss || M < 1 || N < 1) return -1;
-  oafdtd::mse_grad_kernel<<<M, 256, 0, static_cast<cudaStream_t>(stream)>>>(Y, T, M, N, G32,
+                        float* row_loss, int32_t groups, void* stream) {
+  if (!Y || !T || !G32 || !G16 || !row_loss || M < 1 || N < 1 || groups < 1 || M % groups != 0) return -1;
+  oafdtd::mse_grad_kernel<<<M, 256, 0, static_cast<cudaStream_t>(stream)>>>(Y, T, M / groups, N, G32,
                                                                               static_cast<__nv_bfloat16*>(G16), row_loss);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }

@@ -263,13 +263,25 @@ cudaError_t preload_fused();
 bool encode_tensor_map(CUtensorMap* m, CUtensorMapDataType dt, int rank, const void* base, const cuuint64_t* dims,
                        const cuuint64_t* strides, const cuuint32_t* box, const char* what, std::string* why,
                        CUtensorMapSwizzle swizzle = CU_TENSOR_MAP_SWIZZLE_NONE);
-// The tcgen05 GEMM of the surrogate (umma.cu): C = A . B^T for row-major A (M x K) and B (N x K);
-// umma_shape_ok tells whether a shape and its operands suit it (M, N multiples of 128, K of 64,
-// 16-byte aligned rows).
-bool umma_shape_ok(int M, int N, int K, int lda, int ldb, const void* A, const void* B);
-cudaError_t launch_umma_gemm(const void* A, const void* B, float* C32, void* C16, void* C16T, const float* bias,
-                             const void* mask, int M, int N, int K, int lda, int ldb, int ldc, int ldct, int act,
-                             float beta, int* status, cudaStream_t s, std::string* why);
+// The tcgen05 GEMM of the surrogate (umma.cu), grouped: C_g = A_g . B_g^T for row-major A_g
+// (M x K) and B_g (N x K), g < groups, each operand's groups a fixed number of elements apart.
+struct UmmaProblem {
+  const void* A;
+  const void* B;
+  float* C32;          // FP32 result (nullable), ldc
+  void* C16;           // BF16 result (nullable), ldc
+  void* C16T;          // BF16 result transposed, N x M (nullable), ldct
+  const float* bias;   // per column (nullable)
+  const void* mask;    // epilogues 2 and 4: BF16 in the layout of C
+  int M, N, K, lda, ldb, ldc, ldct, act, groups;
+  long long sA, sB, sC, sCT, sBias;  // elements between consecutive groups
+  float beta;
+  int* status;         // set nonzero when a bounded wait gave up (nullable)
+};
+// Whether a problem suits the kernel: M a multiple of 128, N of 64, K of 64; leading dimensions
+// and group strides multiples of 8 elements; 16-byte aligned operands; beta 0.
+bool umma_shape_ok(const UmmaProblem& p);
+cudaError_t launch_umma_gemm(const UmmaProblem& p, cudaStream_t s, std::string* why);
 cudaError_t preload_umma();
 // Encodes the TMA descriptors of the staged sweeps for the fields and indices in a; false (with
 // a message) when the driver entry point is missing or rejects a descriptor.

@@ -205,8 +205,8 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
         C.c_int,
         [C.c_void_p] * 6 + [_i32] * 9 + [C.c_float, C.c_void_p],
     ),
-    "oafdtd_mlp_colsum": (C.c_int, [C.c_void_p, _i32, _i32, _i32, C.c_void_p, C.c_void_p]),
-    "oafdtd_mlp_mse_grad": (C.c_int, [C.c_void_p, C.c_void_p, _i32, _i32] + [C.c_void_p] * 4),
+    "oafdtd_mlp_colsum": (C.c_int, [C.c_void_p, _i32, _i32, _i32, C.c_void_p, _i32, _i64, _i64, C.c_void_p]),
+    "oafdtd_mlp_mse_grad": (C.c_int, [C.c_void_p, C.c_void_p, _i32, _i32] + [C.c_void_p] * 3 + [_i32, C.c_void_p]),
     "oafdtd_mlp_adam": (
         C.c_int,
         [C.c_void_p] * 5 + [_i64, C.c_void_p] + [C.c_float] * 3 + [C.c_void_p, C.c_void_p],
@@ -215,9 +215,9 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "oafdtd_mlp_gather": (C.c_int, [C.c_void_p, _i32, C.c_void_p, _i32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "oafdtd_mlp_gemm_tn": (
         C.c_int,
-        [C.c_void_p] * 7 + [_i32] * 8 + [C.c_float, C.c_void_p, C.c_void_p],
+        [C.c_void_p] * 7 + [_i32] * 8 + [C.c_float, _i32] + [_i64] * 5 + [C.c_void_p, C.c_void_p],
     ),
-    "oafdtd_mlp_transpose": (C.c_int, [C.c_void_p, _i32, _i32, _i32, C.c_void_p, _i32, C.c_void_p]),
+    "oafdtd_mlp_transpose": (C.c_int, [C.c_void_p, _i32, _i32, _i32, C.c_void_p, _i32, _i32, _i64, _i64, C.c_void_p]),
 }
 
 _lock = threading.Lock()

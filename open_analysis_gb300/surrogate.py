@@ -313,31 +313,39 @@ def cosine_lr(epoch: int, epochs: int, lr: float, lr_end: float) -> float:
 
 
 class Mlp:
-    """A tanh (or ReLU) network ``sizes[0] -> ... -> sizes[-1]`` on the GPU, trained and evaluated
-    by the engine library's kernels. Weights ``W[l]`` are ``(fan_in, fan_out)`` FP32 masters with
-    BF16 copies and transposed BF16 copies the GEMMs read; all weights and biases live in one flat
-    buffer so one Adam launch updates them all. Every GEMM is C = A . B^T with both operands
+    """``members`` tanh (or ReLU) networks ``sizes[0] -> ... -> sizes[-1]`` of the same widths on the
+    GPU, trained side by side and evaluated by the engine library's kernels: every launch covers
+    all members (the GEMMs are grouped, one Adam launch updates every parameter). Member ``k`` is
+    initialised from seed ``seed + 101 k``.
+
+    Weights ``W[l]`` are ``(fan_in, fan_out)`` FP32 masters with BF16 copies and transposed BF16
+    copies the GEMMs read; a member's weights and biases live in one flat block of ``n_params``
+    floats, the members' blocks side by side. Every GEMM is C = A . B^T with both operands
     K-contiguous (``oafdtd_mlp_gemm_tn``): the forward reads the transposed weights, the weight
     gradients the transposed activations and output gradients, which the epilogues and a small
-    transpose kernel write; shapes with M and N multiples of 128 and K of 64 (batch 256, widths
-    of 512) run on the tcgen05 tensor cores. Every width is padded to a multiple of 8 (the input
-    with zero columns, so the extra weights see zero inputs and zero gradients)."""
+    transpose kernel write. Problems with M a multiple of 128 and N, K multiples of 64 (batch 256,
+    widths of 512) run on the tcgen05 tensor cores, all members in one persistent launch. Every
+    width is padded to a multiple of 8 (the input with zero columns, so the extra weights see zero
+    inputs and zero gradients)."""
 
-    def __init__(self, sizes: Sequence[int], batch: int = 256, seed: int = 0, device: int = 0, act: str = "tanh") -> None:
+    def __init__(self, sizes: Sequence[int], batch: int = 256, seed: int = 0, device: int = 0, act: str = "tanh",
+                 members: int = 1) -> None:
         torch = _torch()
         self.torch = torch
         self.lib = native.load()
         if act not in ACTS:
             raise ValueError(f"activation {act!r}: one of {sorted(ACTS)}")
+        if members < 1:
+            raise ValueError("an ensemble has at least one member")
         self.act, self.dact = ACTS[act]
         self.act_name = act
+        self.members = int(members)
         self.n_in = int(sizes[0])
         self.sizes = [_align(int(s), 8) for s in sizes]
         if self.sizes[1:] != [int(s) for s in sizes[1:]]:
             raise ValueError("hidden and output widths must be multiples of 8")
         self.batch = int(batch)
         self.dev = torch.device("cuda", device)
-        rng = np.random.default_rng(seed)
         self.layout: list[tuple[int, int, int, int]] = []  # (w offset, fan_in, fan_out, b offset)
         off = 0
         for a, b in zip(self.sizes[:-1], self.sizes[1:], strict=True):
@@ -346,25 +354,27 @@ class Mlp:
             self.layout.append((wo, a, b, off))
             off = _align(off + b)
         self.n_params = off
-        flat = np.zeros(off, np.float32)
+        flat = np.zeros((self.members, off), np.float32)
         n_layers = len(self.layout)
         gain = 2.0 if act == "relu" else 1.0  # He / Glorot-style variance per fan-in
-        for l, (wo, a, b, _) in enumerate(self.layout):
-            fan_in = self.n_in if l == 0 else a
-            std = math.sqrt(gain / fan_in) if l < n_layers - 1 else math.sqrt(1.0 / fan_in) * 0.5
-            w = (rng.standard_normal((a, b)) * std).astype(np.float32)
-            if l == 0:
-                w[self.n_in :] = 0.0
-            flat[wo : wo + a * b] = w.reshape(-1)
+        for k in range(self.members):
+            rng = np.random.default_rng(seed + 101 * k)
+            for l, (wo, a, b, _) in enumerate(self.layout):
+                fan_in = self.n_in if l == 0 else a
+                std = math.sqrt(gain / fan_in) if l < n_layers - 1 else math.sqrt(1.0 / fan_in) * 0.5
+                w = (rng.standard_normal((a, b)) * std).astype(np.float32)
+                if l == 0:
+                    w[self.n_in :] = 0.0
+                flat[k, wo : wo + a * b] = w.reshape(-1)
         f32, bf = torch.float32, torch.bfloat16
-        self.p32 = torch.from_numpy(flat).to(self.dev)
+        self.p32 = torch.from_numpy(flat.reshape(-1)).to(self.dev)
         self.p16 = self.p32.to(bf)
         # every layer's BF16 weights also transposed, (fan_out, fan_in): the forward GEMM reads its
         # B operand K-contiguous, the layout the tcgen05 kernel takes
         self.p16T = torch.zeros_like(self.p16)
         self.status = torch.zeros(1, dtype=torch.int32, device=self.dev)
         self._refresh_t(self._stream())
-        self.grad = torch.zeros(off, dtype=f32, device=self.dev)
+        self.grad = torch.zeros(self.members * off, dtype=f32, device=self.dev)
         self.m1 = torch.zeros_like(self.grad)
         self.m2 = torch.zeros_like(self.grad)
         self.step_no = torch.zeros(1, dtype=torch.int32, device=self.dev)
@@ -375,13 +385,13 @@ class Mlp:
         self.graph: Any = None
 
     def pad(self, x: npt.ArrayLike) -> npt.NDArray[np.float32]:
-        """Inputs ``(n, n_in)`` as ``(n, sizes[0])`` float32 with zero padding columns."""
+        """Inputs ``(..., n, n_in)`` as ``(..., n, sizes[0])`` float32 with zero padding columns."""
         x = np.asarray(x, np.float32)
-        out = np.zeros((x.shape[0], self.sizes[0]), np.float32)
-        out[:, : self.n_in] = x
+        out = np.zeros((*x.shape[:-1], self.sizes[0]), np.float32)
+        out[..., : self.n_in] = x
         return out
 
-    # ---- pointers
+    # ---- pointers (member 0; member k is k * n_params elements further on)
     def _w(self, l: int, half: bool = True) -> int:
         wo = self.layout[l][0]
         t = self.p16 if half else self.p32
@@ -402,113 +412,136 @@ class Mlp:
     def _stream(self) -> int:
         return int(self.torch.cuda.current_stream(self.dev).cuda_stream)
 
-    def weights(self) -> tuple[list[FloatArray], list[FloatArray]]:
-        """FP32 master weights and biases on the host (``W[l]`` is ``(fan_in, fan_out)``)."""
-        flat = self.p32.detach().cpu().numpy().astype(np.float64)
-        w = [flat[wo : wo + a * b].reshape(a, b) for wo, a, b, _ in self.layout]
-        bias = [flat[bo : bo + b] for _, _, b, bo in self.layout]
-        return w, bias
+    def flat(self, member: int = 0) -> Any:
+        """Member ``member``'s FP32 parameters (a view of the device buffer)."""
+        return self.p32[member * self.n_params : (member + 1) * self.n_params]
 
-    def set_weights(self, w: Sequence[FloatArray], b: Sequence[FloatArray]) -> None:
+    def weights(self, member: int = 0) -> tuple[list[FloatArray], list[FloatArray]]:
+        """A member's FP32 master weights and biases on the host (``W[l]`` is ``(fan_in, fan_out)``)."""
+        flat = self.flat(member).detach().cpu().numpy().astype(np.float64)
+        return self.split(flat)
+
+    def set_weights(self, w: Sequence[FloatArray], b: Sequence[FloatArray], member: int = 0) -> None:
         flat = np.zeros(self.n_params, np.float32)
         for (wo, a, n, bo), wl, bl in zip(self.layout, w, b, strict=True):
             flat[wo : wo + a * n] = np.asarray(wl, np.float32).reshape(-1)
             flat[bo : bo + n] = np.asarray(bl, np.float32)
-        self.p32.copy_(self.torch.from_numpy(flat).to(self.dev))
-        self.p16.copy_(self.p32.to(self.torch.bfloat16))
-        self._refresh_t(self._stream())
+        self.flat(member).copy_(self.torch.from_numpy(flat).to(self.dev))
+        self.load_flat(self.p32)
 
-    def load_flat(self, flat32: Any) -> None:
-        """Set every weight and bias from a flat FP32 device tensor in this network's layout (its
-        BF16 and transposed BF16 copies follow)."""
-        self.p32.copy_(flat32)
+    def load_flat(self, flat32: Any, member: int | None = None) -> None:
+        """Set the weights and biases from a flat FP32 device tensor: every member's (``member``
+        None, the whole buffer) or one member's block; the BF16 and transposed copies follow."""
+        if member is None:
+            if flat32.data_ptr() != self.p32.data_ptr():
+                self.p32.copy_(flat32)
+        else:
+            self.flat(member).copy_(flat32)
         self.p16.copy_(self.p32.to(self.torch.bfloat16))
         self._refresh_t(self._stream())
 
     # ---- kernels
     def _refresh_t(self, s: int) -> None:
-        """The transposed BF16 weights from the current BF16 weights."""
+        """The transposed BF16 weights from the current BF16 weights, every member."""
+        p = self.n_params
         for l, (_, a, b, _) in enumerate(self.layout):
-            native.check(self.lib.oafdtd_mlp_transpose(self._w(l), a, b, b, self._wT(l), a, s), "transpose")
+            native.check(self.lib.oafdtd_mlp_transpose(self._w(l), a, b, b, self._wT(l), a, self.members, p, p, s),
+                         "transpose")
 
     def _gemm_tn(self, a: int, b: int, c32: int, c16: int, c16t: int, bias: int, mask: int, m: int, n: int, k: int,
-                 lda: int, ldb: int, ldc: int, ldct: int, act: int, s: int) -> None:
-        """C (m x n) = A (m x k) . B^T with B (n x k): tcgen05 on the shapes that allow it."""
+                 lda: int, ldb: int, ldc: int, ldct: int, act: int, s: int, sa: int, sb: int, sc: int, sct: int,
+                 sbias: int) -> None:
+        """C_g (m x n) = A_g (m x k) . B_g^T with B_g (n x k) for every member g (the s* arguments:
+        elements between members)."""
         native.check(self.lib.oafdtd_mlp_gemm_tn(a, b, c32 or None, c16 or None, c16t or None, bias or None,
-                                                 mask or None, m, n, k, lda, ldb, ldc, ldct, act, 0.0,
-                                                 self.status.data_ptr(), s), "oafdtd_mlp_gemm_tn")
-
-    def _gemm(self, a: int, b: int, c32: int, c16: int, bias: int, mask: int, m: int, n: int, k: int,
-              lda: int, ldb: int, ldc: int, ta: int, tb: int, act: int, s: int) -> None:
-        native.check(self.lib.oafdtd_mlp_gemm(a, b, c32 or None, c16 or None, bias or None, mask or None,
-                                              m, n, k, lda, ldb, ldc, ta, tb, act, 0.0, s), "oafdtd_mlp_gemm")
+                                                 mask or None, m, n, k, lda, ldb, ldc, ldct, act, 0.0, self.members,
+                                                 sa, sb, sc, sct, sbias, self.status.data_ptr(), s),
+                     "oafdtd_mlp_gemm_tn")
 
     def _forward(self, x16: int, acts: list[Any], y32: int, m: int, s: int, acts_t: list[Any] | None = None) -> None:
-        """acts[l] (BF16, m x sizes[l+1]) for the hidden layers, and transposed into acts_t[l]
-        (sizes[l+1] x m) when given (training: the weight gradients read them); y32 the FP32
-        output. Each layer is X . W = X . (W^T)^T on the transposed weights."""
+        """acts[l] (BF16, members x m x sizes[l+1]) for the hidden layers, and transposed into
+        acts_t[l] (members x sizes[l+1] x m) when given (training: the weight gradients read
+        them); y32 the FP32 output (members x m x sizes[-1]). x16: members x m x sizes[0]. Each
+        layer is X . W = X . (W^T)^T on the transposed weights."""
         inp = x16
         n_layers = len(self.layout)
+        p = self.n_params
         for l, (_, a, b, _) in enumerate(self.layout):
             last = l == n_layers - 1
             ct = 0 if last or acts_t is None else acts_t[l].data_ptr()
             self._gemm_tn(inp, self._wT(l), y32 if last else 0, 0 if last else acts[l].data_ptr(), ct, self._b(l), 0,
-                          m, b, a, a, a, b, m, 0 if last else self.act, s)
+                          m, b, a, a, a, b, m, 0 if last else self.act, s, m * a, p, m * b, b * m, p)
             if not last:
                 inp = acts[l].data_ptr()
 
     def _buffers(self, m: int) -> dict[str, Any]:
         torch = self.torch
         bf, f32 = torch.bfloat16, torch.float32
-        out = self.sizes[-1]
+        g, out = self.members, self.sizes[-1]
+
+        def z(*shape: int, dt: Any = bf) -> Any:
+            return torch.zeros((g, *shape), dtype=dt, device=self.dev)
+
         return {
-            "x16": torch.zeros((m, self.sizes[0]), dtype=bf, device=self.dev),
-            "x16T": torch.zeros((self.sizes[0], m), dtype=bf, device=self.dev),
-            "acts": [torch.zeros((m, b), dtype=bf, device=self.dev) for b in self.sizes[1:-1]],
-            "actsT": [torch.zeros((b, m), dtype=bf, device=self.dev) for b in self.sizes[1:-1]],
-            "g16T": torch.zeros((out, m), dtype=bf, device=self.dev),
-            "dz16T": [torch.zeros((b, m), dtype=bf, device=self.dev) for b in self.sizes[1:-1]],
-            "y": torch.zeros((m, out), dtype=f32, device=self.dev),
-            "t": torch.zeros((m, out), dtype=f32, device=self.dev),
-            "g32": torch.zeros((m, out), dtype=f32, device=self.dev),
-            "g16": torch.zeros((m, out), dtype=bf, device=self.dev),
-            "dz32": [torch.zeros((m, b), dtype=f32, device=self.dev) for b in self.sizes[1:-1]],
-            "dz16": [torch.zeros((m, b), dtype=bf, device=self.dev) for b in self.sizes[1:-1]],
-            "row_loss": torch.zeros(m, dtype=f32, device=self.dev),
+            "x16": z(m, self.sizes[0]),
+            "x16T": z(self.sizes[0], m),
+            "acts": [z(m, b) for b in self.sizes[1:-1]],
+            "actsT": [z(b, m) for b in self.sizes[1:-1]],
+            "g16T": z(out, m),
+            "dz16T": [z(b, m) for b in self.sizes[1:-1]],
+            "y": z(m, out, dt=f32),
+            "t": z(m, out, dt=f32),
+            "g32": z(m, out, dt=f32),
+            "g16": z(m, out),
+            "dz32": [z(m, b, dt=f32) for b in self.sizes[1:-1]],
+            "dz16": [z(m, b) for b in self.sizes[1:-1]],
+            "row_loss": z(m, dt=f32),
         }
 
     def _backward(self, buf: dict[str, Any], m: int, s: int) -> None:
-        lib = self.lib
+        lib, g, p = self.lib, self.members, self.n_params
         y, t = buf["y"], buf["t"]
-        out = self.sizes[-1]
-        native.check(lib.oafdtd_mlp_mse_grad(y.data_ptr(), t.data_ptr(), m, out, buf["g32"].data_ptr(),
-                                             buf["g16"].data_ptr(), buf["row_loss"].data_ptr(), s), "mse_grad")
+        out, n_in = self.sizes[-1], self.sizes[0]
+        native.check(lib.oafdtd_mlp_mse_grad(y.data_ptr(), t.data_ptr(), g * m, out, buf["g32"].data_ptr(),
+                                             buf["g16"].data_ptr(), buf["row_loss"].data_ptr(), g, s), "mse_grad")
         g32, g16, gT = buf["g32"].data_ptr(), buf["g16"].data_ptr(), buf["g16T"].data_ptr()
-        native.check(lib.oafdtd_mlp_transpose(g16, m, out, out, gT, m, s), "transpose")
-        native.check(lib.oafdtd_mlp_transpose(buf["x16"].data_ptr(), m, self.sizes[0], self.sizes[0],
-                                              buf["x16T"].data_ptr(), m, s), "transpose")
+        native.check(lib.oafdtd_mlp_transpose(g16, m, out, out, gT, m, g, m * out, out * m, s), "transpose")
+        native.check(lib.oafdtd_mlp_transpose(buf["x16"].data_ptr(), m, n_in, n_in, buf["x16T"].data_ptr(), m, g,
+                                              m * n_in, n_in * m, s), "transpose")
         for l in range(len(self.layout) - 1, -1, -1):
             _, a, b, _ = self.layout[l]
             inp = buf["x16"].data_ptr() if l == 0 else buf["acts"][l - 1].data_ptr()
             inp_t = buf["x16T"].data_ptr() if l == 0 else buf["actsT"][l - 1].data_ptr()
             # dW = inp^T . g = (inp^T) . (g^T)^T  (a x b), from the transposed activations and g
-            self._gemm_tn(inp_t, gT, self._gw(l), 0, 0, 0, 0, a, b, m, m, m, b, a, 0, s)
-            native.check(lib.oafdtd_mlp_colsum(g32, m, b, b, self._gb(l), s), "colsum")
+            self._gemm_tn(inp_t, gT, self._gw(l), 0, 0, 0, 0, a, b, m, m, m, b, a, 0, s, a * m, b * m, p, 0, 0)
+            native.check(lib.oafdtd_mlp_colsum(g32, m, b, b, self._gb(l), g, m * b, p, s), "colsum")
             if l == 0:
                 break
             # dZ[l-1] = (g . W^T) times the activation's derivative at the layer input  (m x a);
             # W (a x b) is the B operand (N x K) as stored; the transposed dZ feeds layer l-1's dW
             dz32, dz16 = buf["dz32"][l - 1].data_ptr(), buf["dz16"][l - 1].data_ptr()
             dzt = buf["dz16T"][l - 1].data_ptr()
-            self._gemm_tn(g16, self._w(l), dz32, dz16, dzt, 0, inp, m, a, b, b, b, a, m, self.dact, s)
+            self._gemm_tn(g16, self._w(l), dz32, dz16, dzt, 0, inp, m, a, b, b, b, a, m, self.dact, s,
+                          m * b, p, m * a, a * m, 0)
             g32, g16, gT = dz32, dz16, dzt
 
-    def gradients(self, x: npt.ArrayLike, t: npt.ArrayLike) -> tuple[float, FloatArray]:
-        """Loss and the flat gradient buffer for one batch given on the host (checks and tests)."""
+    def _per_member(self, v: npt.ArrayLike) -> npt.NDArray[np.float32]:
+        """Host rows ``(m, c)`` for every member alike, or ``(members, m, c)`` per member."""
+        v = np.asarray(v, np.float32)
+        if v.ndim == 2:
+            v = np.broadcast_to(v, (self.members, *v.shape))
+        if v.shape[0] != self.members:
+            raise ValueError(f"{v.shape[0]} row sets for {self.members} members")
+        return np.ascontiguousarray(v)
+
+    def gradients(self, x: npt.ArrayLike, t: npt.ArrayLike) -> tuple[Any, FloatArray]:
+        """Loss and the flat gradient buffer for one batch given on the host (checks and tests):
+        ``x (m, n_in)`` and ``t (m, sizes[-1])`` for every member, or per member with a leading
+        member axis. One member: ``(loss, flat)``; more: ``(losses[members], flat[members, n_params])``."""
         torch = self.torch
-        x = self.pad(x)
-        t = np.asarray(t, np.float32)
-        m = x.shape[0]
+        x = self._per_member(self.pad(x))
+        t = self._per_member(t)
+        m = x.shape[1]
         buf = self._buffers(m)
         buf["x16"].copy_(torch.from_numpy(x).to(self.dev).to(torch.bfloat16))
         buf["t"].copy_(torch.from_numpy(t).to(self.dev))
@@ -517,27 +550,34 @@ class Mlp:
         self._backward(buf, m, s)
         torch.cuda.synchronize(self.dev)
         self.check_status()
-        loss = float(buf["row_loss"].sum().item()) / (m * self.sizes[-1])
-        return loss, self.grad.detach().cpu().numpy().astype(np.float64)
+        losses = buf["row_loss"].sum(dim=1).cpu().numpy().astype(np.float64) / (m * self.sizes[-1])
+        flat = self.grad.detach().cpu().numpy().astype(np.float64).reshape(self.members, self.n_params)
+        if self.members == 1:
+            return float(losses[0]), flat[0]
+        return losses, flat
 
     def split(self, flat: FloatArray) -> tuple[list[FloatArray], list[FloatArray]]:
-        """A flat buffer as per-layer ``(W, b)`` lists."""
+        """One member's flat buffer as per-layer ``(W, b)`` lists."""
         return ([flat[wo : wo + a * b].reshape(a, b) for wo, a, b, _ in self.layout],
                 [flat[bo : bo + b] for _, _, b, bo in self.layout])
 
-    def adam_step(self, lr: float, b1: float = 0.9, b2: float = 0.999, eps: float = 1e-8) -> None:
-        """One Adam step on the current gradient buffer (the step number moves on by one)."""
-        s = self._stream()
-        self.lr.fill_(lr)
-        native.check(self.lib.oafdtd_mlp_count(self.step_no.data_ptr(), s), "count")
-        native.check(self.lib.oafdtd_mlp_adam(self.p32.data_ptr(), self.p16.data_ptr(), self.grad.data_ptr(),
-                                              self.m1.data_ptr(), self.m2.data_ptr(), self.n_params,
-                                              self.lr.data_ptr(), b1, b2, eps, self.step_no.data_ptr(), s), "adam")
+    def _adam(self, s: int, b1: float = 0.9, b2: float = 0.999, eps: float = 1e-8) -> None:
+        lib = self.lib
+        native.check(lib.oafdtd_mlp_count(self.step_no.data_ptr(), s), "count")
+        native.check(lib.oafdtd_mlp_adam(self.p32.data_ptr(), self.p16.data_ptr(), self.grad.data_ptr(),
+                                         self.m1.data_ptr(), self.m2.data_ptr(), self.members * self.n_params,
+                                         self.lr.data_ptr(), b1, b2, eps, self.step_no.data_ptr(), s), "adam")
         self._refresh_t(s)
+
+    def adam_step(self, lr: float, b1: float = 0.9, b2: float = 0.999, eps: float = 1e-8) -> None:
+        """One Adam step of every member on the current gradient buffer (the step number moves on
+        by one)."""
+        self.lr.fill_(lr)
+        self._adam(self._stream(), b1, b2, eps)
 
     def check_status(self) -> None:
         """Raise when a bounded wait of a tcgen05 GEMM gave up since the last check (its result
-        was not written); clears the word."""
+        is incomplete); clears the word."""
         if int(self.status.item()) != 0:
             self.status.zero_()
             raise AccelError(ErrorInfo("ACCEL_TIMEOUT", "a tensor-core GEMM gave up waiting for its operands",
@@ -545,36 +585,42 @@ class Mlp:
 
     # ---- training
     def _train_step(self, tr: dict[str, Any], j: int, s: int) -> None:
-        lib, m = self.lib, self.batch
-        idx = tr["perm"].data_ptr() + j * m * 4
+        lib, m, g = self.lib, self.batch, self.members
+        idx = tr["perm"].data_ptr() + j * g * m * 4
         buf = tr["buf"]
-        native.check(lib.oafdtd_mlp_gather(tr["x"].data_ptr(), self.sizes[0], idx, m, None, buf["x16"].data_ptr(), s), "gather")
-        native.check(lib.oafdtd_mlp_gather(tr["t"].data_ptr(), self.sizes[-1], idx, m, buf["t"].data_ptr(), None, s), "gather")
+        native.check(lib.oafdtd_mlp_gather(tr["x"].data_ptr(), self.sizes[0], idx, g * m, None, buf["x16"].data_ptr(),
+                                           s), "gather")
+        native.check(lib.oafdtd_mlp_gather(tr["t"].data_ptr(), self.sizes[-1], idx, g * m, buf["t"].data_ptr(), None,
+                                           s), "gather")
         self._forward(buf["x16"].data_ptr(), buf["acts"], buf["y"].data_ptr(), m, s, buf["actsT"])
         self._backward(buf, m, s)
-        native.check(lib.oafdtd_mlp_count(self.step_no.data_ptr(), s), "count")
-        native.check(lib.oafdtd_mlp_adam(self.p32.data_ptr(), self.p16.data_ptr(), self.grad.data_ptr(),
-                                         self.m1.data_ptr(), self.m2.data_ptr(), self.n_params, self.lr.data_ptr(),
-                                         0.9, 0.999, 1e-8, self.step_no.data_ptr(), s), "adam")
-        self._refresh_t(s)
+        self._adam(s)
 
-    def prepare(self, x: npt.ArrayLike, t: npt.ArrayLike, graph: bool = True) -> None:
+    def prepare(self, x: npt.ArrayLike, t: npt.ArrayLike, graph: bool = True,
+                rows: Sequence[npt.ArrayLike] | None = None) -> None:
         """Upload the training set ``x (n, n_in)`` -> ``t (n, sizes[-1])`` (both already scaled)
-        and capture one epoch of training steps (``n // batch`` batches) as a CUDA graph."""
+        and capture one epoch of training steps as a CUDA graph. Every member draws its batches
+        from all rows, or from its own subset ``rows[k]`` (bagging); an epoch is as many batches
+        as the smallest subset holds."""
         torch = self.torch
         x = self.pad(x)
         t = np.asarray(t, np.float32)
         n = x.shape[0]
-        nb = n // self.batch
+        subsets = [np.arange(n)] * self.members if rows is None else [np.asarray(r, np.int64) for r in rows]
+        if len(subsets) != self.members:
+            raise ValueError(f"{len(subsets)} row subsets for {self.members} members")
+        nb = min(len(r) for r in subsets) // self.batch
         if nb < 1:
-            raise ValueError(f"{n} training rows are fewer than one batch of {self.batch}")
+            raise ValueError(f"{min(len(r) for r in subsets)} training rows are fewer than one batch of {self.batch}")
         self.stream = torch.cuda.Stream(self.dev)
         tr = {
             "n": n,
             "nb": nb,
             "x": torch.from_numpy(x).to(self.dev),
             "t": torch.from_numpy(t).to(self.dev),
-            "perm": torch.zeros(nb * self.batch, dtype=torch.int32, device=self.dev),
+            "rows": [torch.from_numpy(r.astype(np.int64)).to(self.dev) for r in subsets],
+            # batch j of member k: perm[j, k, :]
+            "perm": torch.zeros((nb, self.members, self.batch), dtype=torch.int32, device=self.dev),
             "buf": self._buffers(self.batch),
         }
         self._train = tr
@@ -596,34 +642,38 @@ class Mlp:
             self._train_step(tr, j, s)
 
     def run_epoch(self, lr: float) -> None:
-        """Queue one epoch on this network's stream: set the learning rate, draw the shuffle,
-        replay the captured steps. Returns without waiting."""
+        """Queue one epoch on this network's stream: set the learning rate, draw every member's
+        shuffle, replay the captured steps. Returns without waiting."""
         torch = self.torch
         tr = self._train
         assert tr is not None
+        nb, m = tr["nb"], self.batch
         with torch.cuda.stream(self.stream):
             self.lr.fill_(lr)
-            perm = torch.randperm(tr["n"], generator=self.gen, device=self.dev)
-            tr["perm"].copy_(perm[: tr["nb"] * self.batch].to(torch.int32))
+            for k, r in enumerate(tr["rows"]):
+                pick = r[torch.randperm(r.numel(), generator=self.gen, device=self.dev)[: nb * m]]
+                tr["perm"][:, k, :].copy_(pick.view(nb, m).to(torch.int32))
             if self.graph is not None:
                 self.graph.replay()
             else:
                 self._epoch()
 
-    def last_loss(self) -> float:
-        """Mean squared error of the last training batch (waits for this network's stream)."""
+    def last_loss(self) -> Any:
+        """Mean squared error of the last training batch, per member (a float for one member);
+        waits for this network's stream."""
         tr = self._train
         assert tr is not None
         self.stream.synchronize()
-        return float(tr["buf"]["row_loss"].sum().item()) / (self.batch * self.sizes[-1])
+        v = tr["buf"]["row_loss"].sum(dim=1).cpu().numpy().astype(np.float64) / (self.batch * self.sizes[-1])
+        return float(v[0]) if self.members == 1 else v
 
     def fit(self, x: npt.ArrayLike, t: npt.ArrayLike, epochs: int, lr: float = 1e-3, lr_end: float = 1e-5,
-            graph: bool = True, log_every: int = 0) -> list[float]:
+            graph: bool = True, log_every: int = 0, rows: Sequence[npt.ArrayLike] | None = None) -> list[Any]:
         """Train: Adam, batches of ``batch`` rows drawn without replacement each epoch, learning
         rate along a cosine from ``lr`` to ``lr_end`` (:func:`cosine_lr`). Returns the last
         batch's loss at every ``log_every``-th epoch."""
-        self.prepare(x, t, graph)
-        losses: list[float] = []
+        self.prepare(x, t, graph, rows)
+        losses: list[Any] = []
         for e in range(epochs):
             self.run_epoch(cosine_lr(e, epochs, lr, lr_end))
             if log_every and (e % log_every == 0 or e == epochs - 1):
@@ -633,21 +683,22 @@ class Mlp:
         return losses
 
     def predict(self, x: npt.ArrayLike, chunk: int = 4096) -> FloatArray:
-        """Outputs for ``x (n, sizes[0])`` (scaled inputs), FP32 on the GPU, float64 on return."""
+        """Outputs for ``x (n, n_in)`` (scaled inputs): ``(n, sizes[-1])`` for one member,
+        ``(members, n, sizes[-1])`` for more; FP32 on the GPU, float64 on return."""
         torch = self.torch
         x = self.pad(x)
-        n = x.shape[0]
-        out = np.zeros((n, self.sizes[-1]))
+        n, g = x.shape[0], self.members
+        out = np.zeros((g, n, self.sizes[-1]))
         s = self._stream()
         for a in range(0, n, chunk):
             m = min(chunk, n - a)
-            x16 = torch.from_numpy(x[a : a + m]).to(self.dev).to(torch.bfloat16)
-            acts = [torch.empty((m, b), dtype=torch.bfloat16, device=self.dev) for b in self.sizes[1:-1]]
-            y = torch.empty((m, self.sizes[-1]), dtype=torch.float32, device=self.dev)
+            x16 = torch.from_numpy(x[a : a + m]).to(self.dev).to(torch.bfloat16).expand(g, m, -1).contiguous()
+            acts = [torch.empty((g, m, b), dtype=torch.bfloat16, device=self.dev) for b in self.sizes[1:-1]]
+            y = torch.empty((g, m, self.sizes[-1]), dtype=torch.float32, device=self.dev)
             self._forward(x16.data_ptr(), acts, y.data_ptr(), m, s)
-            out[a : a + m] = y.cpu().numpy()
+            out[:, a : a + m] = y.cpu().numpy()
         self.check_status()
-        return out
+        return out[0] if g == 1 else out
 
 
 # ------------------------------------------------------------------------------------ ensemble
@@ -711,7 +762,7 @@ class Ensemble:
         self.bag = bag
         self.seed = seed
         self.sizes = [7] + [width] * depth + [4 * g.n_freq]
-        self.nets = [Mlp(self.sizes, batch, seed=seed + 101 * k, act=act) for k in range(members)]
+        self.net = Mlp(self.sizes, batch, seed=seed, act=act, members=members)
         self.mu = np.zeros(4 * g.n_freq)
         self.sigma = 1.0
         self.scale = 1.0
@@ -720,10 +771,10 @@ class Ensemble:
 
     def fit(self, data: Dataset, epochs: int = 2000, lr: float = 1e-3, lr_end: float = 1e-5,
             val: Dataset | None = None, checks: int = 30) -> list[list[float]]:
-        """Train every member on ``data``; the members run side by side, each on its own stream
-        replaying its own captured epoch. With ``val``, every member is scored on it ``checks``
-        times along the way and keeps the weights of its best score (early stopping). Returns
-        each member's training loss at those points."""
+        """Train every member on ``data``, side by side: one captured epoch covers all members
+        (grouped GEMMs). With ``val``, every member is scored on it ``checks`` times along the way
+        and keeps the weights of its best score (early stopping). Returns each member's training
+        loss at those points."""
         rows = s_to_rows(data.s * line_factor(data.params, self.g))
         self.mu = rows.mean(axis=0)
         self.sigma = float(np.sqrt(np.mean((rows - self.mu) ** 2))) + 1e-9
@@ -735,31 +786,32 @@ class Ensemble:
             tv = (s_to_rows(val.s * line_factor(val.params, self.g)) - self.mu) / self.sigma
         t0 = time.perf_counter()
         rng = np.random.default_rng(self.seed + 7)
-        for net in self.nets:
-            if self.bag < 1.0:
-                rows_k = np.sort(rng.choice(len(x), size=max(net.batch, int(self.bag * len(x))), replace=False))
-                net.prepare(x[rows_k], t[rows_k])
-            else:
-                net.prepare(x, t)
-        logs: list[list[float]] = [[] for _ in self.nets]
-        best = [math.inf] * len(self.nets)
-        keep: list[Any] = [None] * len(self.nets)
+        net, members = self.net, self.net.members
+        rows = None
+        if self.bag < 1.0:
+            size = max(net.batch, int(self.bag * len(x)))
+            rows = [np.sort(rng.choice(len(x), size=size, replace=False)) for _ in range(members)]
+        net.prepare(x, t, rows=rows)
+        logs: list[list[float]] = [[] for _ in range(members)]
+        best = [math.inf] * members
+        keep: list[Any] = [None] * members
         every = max(1, epochs // checks)
         for e in range(epochs):
-            rate = cosine_lr(e, epochs, lr, lr_end)
-            for net in self.nets:
-                net.run_epoch(rate)
+            net.run_epoch(cosine_lr(e, epochs, lr, lr_end))
             if (e + 1) % every == 0 or e == epochs - 1:
-                for k, net in enumerate(self.nets):
-                    logs[k].append(net.last_loss())  # waits for this member's stream
-                    if xv is not None:
-                        score = float(np.mean((net.predict(xv) - tv) ** 2))
+                losses = np.atleast_1d(net.last_loss())  # waits for the training stream
+                pred = net.predict(xv).reshape(members, *tv.shape) if xv is not None else None
+                for k in range(members):
+                    logs[k].append(float(losses[k]))
+                    if pred is not None:
+                        score = float(np.mean((pred[k] - tv) ** 2))
                         if score < best[k]:
-                            best[k], keep[k] = score, net.p32.clone()
-        for k, net in enumerate(self.nets):
-            net.stream.synchronize()
+                            best[k], keep[k] = score, net.flat(k).clone()
+        net.stream.synchronize()
+        for k in range(members):
             if keep[k] is not None:
-                net.load_flat(keep[k])
+                net.flat(k).copy_(keep[k])
+        net.load_flat(net.p32)
         self.val_scores = best
         self.train_seconds = time.perf_counter() - t0
         return logs
@@ -767,7 +819,7 @@ class Ensemble:
     def raw(self, params: npt.ArrayLike) -> tuple[ComplexArray, FloatArray, float]:
         t0 = time.perf_counter()
         x = scale_params(params)
-        ys = [net.predict(x) * self.sigma + self.mu for net in self.nets]
+        ys = self.net.predict(x).reshape(self.net.members, len(x), -1) * self.sigma + self.mu
         sec = time.perf_counter() - t0
         fac = line_factor(params, self.g)
         stack = np.stack([rows_to_s(y) / fac for y in ys])  # (members, n, 2, F)
@@ -784,9 +836,9 @@ class Ensemble:
             grid=np.array([g.nx, g.ny, g.nz, g.n_freq, g.cpml]),
             cell=np.array([g.h, g.dz, g.delay_tau, g.span]),
             sizes=np.array(self.sizes),
-            act=np.array(self.nets[0].act_name),
-            batch=np.array(self.nets[0].batch),
-            weights=np.stack([net.p32.detach().cpu().numpy() for net in self.nets]),
+            act=np.array(self.net.act_name),
+            batch=np.array(self.net.batch),
+            weights=self.net.p32.detach().cpu().numpy().reshape(self.net.members, self.net.n_params),
             mu=self.mu,
             sigma=np.array(self.sigma),
             scale=np.array(self.scale),
@@ -805,11 +857,10 @@ class Ensemble:
         ens = Ensemble(g, members=w.shape[0], width=sizes[1], depth=len(sizes) - 2, batch=int(d["batch"]), act=act)
         if ens.sizes != sizes:
             raise ValueError(f"{path}: layer widths {sizes} are not an ensemble of this kind")
-        torch = ens.nets[0].torch
-        for net, flat in zip(ens.nets, w, strict=True):
-            if flat.size != net.n_params:
-                raise ValueError(f"{path}: {flat.size} weights where the network holds {net.n_params}")
-            net.load_flat(torch.from_numpy(flat.astype(np.float32)).to(net.dev))
+        net = ens.net
+        if w.shape[1] != net.n_params:
+            raise ValueError(f"{path}: {w.shape[1]} weights a member where the network holds {net.n_params}")
+        net.load_flat(net.torch.from_numpy(w.reshape(-1).astype(np.float32)).to(net.dev))
         ens.mu, ens.sigma, ens.scale = d["mu"], float(d["sigma"]), float(d["scale"])
         return ens
 
@@ -987,37 +1038,42 @@ def experiment(
     }
 
 
-GEMM_SHAPES = ((256, 512, 512), (4096, 512, 512), (65536, 512, 512), (65536, 1024, 512), (16384, 4096, 4096))
+# (groups, M, N, K): one member's training GEMM, the 8-member ensemble's grouped one, and larger
+GEMM_SHAPES = ((1, 256, 512, 512), (8, 256, 512, 512), (8, 512, 512, 256), (1, 4096, 512, 512),
+               (1, 65536, 512, 512), (1, 65536, 1024, 512), (1, 16384, 4096, 4096))
 
 
-def gemm_rates(shapes: Sequence[tuple[int, int, int]] = GEMM_SHAPES, reps: int = 20) -> list[dict[str, Any]]:
-    """Time the two GEMM kernels on BF16 A (M x K) and B + bias, tanh, BF16 out, with CUDA events
-    over ``reps`` launches after three warm-up launches, and check them against the FP32 product:
-    ``oafdtd_mlp_gemm`` (mma.sync, B as K x N) and ``oafdtd_mlp_gemm_tn`` (B as N x K; tcgen05
-    where the shape allows). Returns per shape and kernel the microseconds per launch, TFLOP/s
-    and the largest error."""
+def gemm_rates(shapes: Sequence[tuple[int, int, int, int]] = GEMM_SHAPES, reps: int = 20) -> list[dict[str, Any]]:
+    """Time the two GEMM kernels on BF16 A (M x K) and B + bias, tanh, BF16 out, per group, with
+    CUDA events over ``reps`` launches after three warm-up launches, and check them against the
+    FP32 product: ``oafdtd_mlp_gemm`` (mma.sync, B as K x N, one launch per group) and
+    ``oafdtd_mlp_gemm_tn`` (B as N x K; tcgen05 where the shape allows, all groups in one launch).
+    Returns per shape and kernel the microseconds per call, TFLOP/s and the largest error."""
     torch = _torch()
     lib = native.load()
     gen = torch.Generator(device="cuda")
     gen.manual_seed(0)
     out = []
-    for m, n, k in shapes:
-        a = torch.randn(m, k, device="cuda", generator=gen).to(torch.bfloat16)
-        b = torch.randn(k, n, device="cuda", generator=gen).to(torch.bfloat16)
-        bt = b.t().contiguous()
-        c = torch.empty(m, n, device="cuda", dtype=torch.bfloat16)
-        bias = torch.zeros(n, device="cuda")
+    for groups, m, n, k in shapes:
+        a = torch.randn(groups, m, k, device="cuda", generator=gen).to(torch.bfloat16)
+        b = torch.randn(groups, k, n, device="cuda", generator=gen).to(torch.bfloat16)
+        bt = b.transpose(1, 2).contiguous()
+        c = torch.empty(groups, m, n, device="cuda", dtype=torch.bfloat16)
+        bias = torch.zeros(groups, n, device="cuda")
         s = int(torch.cuda.current_stream().cuda_stream)
 
         def mma_sync() -> None:
-            native.check(lib.oafdtd_mlp_gemm(a.data_ptr(), b.data_ptr(), None, c.data_ptr(), bias.data_ptr(), None,
-                                             m, n, k, k, n, n, 0, 0, 3, 0.0, s), "oafdtd_mlp_gemm")
+            for gi in range(groups):
+                native.check(lib.oafdtd_mlp_gemm(a[gi].data_ptr(), b[gi].data_ptr(), None, c[gi].data_ptr(),
+                                                 bias[gi].data_ptr(), None, m, n, k, k, n, n, 0, 0, 3, 0.0, s),
+                             "oafdtd_mlp_gemm")
 
         def tcgen05() -> None:
             native.check(lib.oafdtd_mlp_gemm_tn(a.data_ptr(), bt.data_ptr(), None, c.data_ptr(), None, bias.data_ptr(),
-                                                None, m, n, k, k, k, n, m, 3, 0.0, None, s), "oafdtd_mlp_gemm_tn")
+                                                None, m, n, k, k, k, n, m, 3, 0.0, groups, m * k, n * k, m * n, 0, n,
+                                                None, s), "oafdtd_mlp_gemm_tn")
 
-        want = torch.tanh(a.float() @ b.float())
+        want = torch.tanh(torch.bmm(a.float(), b.float()))
         for name, launch in (("mma_sync", mma_sync), ("gemm_tn", tcgen05)):
             for _ in range(3):
                 launch()
@@ -1029,8 +1085,8 @@ def gemm_rates(shapes: Sequence[tuple[int, int, int]] = GEMM_SHAPES, reps: int =
             torch.cuda.synchronize()
             us = 1e3 * t0.elapsed_time(t1) / reps
             err = float((c.float() - want).abs().max().item())
-            out.append({"kernel": name, "m": m, "n": n, "k": k, "us": us, "tflops": 2.0 * m * n * k / us / 1e6,
-                        "max_err": err})
+            out.append({"kernel": name, "groups": groups, "m": m, "n": n, "k": k, "us": us,
+                        "tflops": 2.0 * groups * m * n * k / us / 1e6, "max_err": err})
     return out
 
 

@@ -112,7 +112,7 @@ def test_gemm_tn_matches_fp64_sums_of_bf16_operands(shape: tuple[int, int, int],
     c16t = torch.zeros((n, m), dtype=torch.bfloat16, device="cuda")
     status = torch.zeros(1, dtype=torch.int32, device="cuda")
     rc = lib.oafdtd_mlp_gemm_tn(da.data_ptr(), db_.data_ptr(), c32.data_ptr(), c16.data_ptr(), c16t.data_ptr(),
-                                dbias.data_ptr(), dmask.data_ptr(), m, n, k, k, k, n, m, act, 0.0,
+                                dbias.data_ptr(), dmask.data_ptr(), m, n, k, k, k, n, m, act, 0.0, 1, 0, 0, 0, 0, 0,
                                 status.data_ptr(), None)
     assert rc == 0
     torch.cuda.synchronize()
@@ -130,9 +130,85 @@ def test_transpose16() -> None:
     for rows, cols in ((256, 512), (77, 134), (8, 1024)):
         x = _dev(rng.standard_normal((rows, cols)), torch.bfloat16)
         y = torch.zeros((cols, rows), dtype=torch.bfloat16, device="cuda")
-        assert lib.oafdtd_mlp_transpose(x.data_ptr(), rows, cols, cols, y.data_ptr(), rows, None) == 0
+        assert lib.oafdtd_mlp_transpose(x.data_ptr(), rows, cols, cols, y.data_ptr(), rows, 1, 0, 0, None) == 0
         torch.cuda.synchronize()
         assert torch.equal(y, x.t())
+    xs = _dev(rng.standard_normal((3, 64, 40)), torch.bfloat16)
+    ys = torch.zeros((3, 40, 64), dtype=torch.bfloat16, device="cuda")
+    assert lib.oafdtd_mlp_transpose(xs.data_ptr(), 64, 40, 40, ys.data_ptr(), 64, 3, 64 * 40, 40 * 64, None) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(ys, xs.transpose(1, 2))
+
+
+# (groups, M, N, K): 64-column tcgen05 tiles (few tiles), 128-column ones with several tiles per CTA
+# (512 tiles), and a ragged shape on the mma.sync kernels
+GROUPED = [(8, 256, 512, 512), (3, 128, 192, 128), (16, 512, 1024, 128), (4, 72, 40, 24)]
+
+
+@pytest.mark.parametrize("shape", GROUPED)
+@pytest.mark.parametrize("act", [3, 4])
+def test_grouped_gemm_tn_matches_each_group(shape: tuple[int, int, int, int], act: int) -> None:
+    """Every group of one grouped launch against its own FP64 product, with padding between the
+    groups' blocks (the strides are larger than the blocks) left untouched."""
+    lib = _lib()
+    groups, m, n, k = shape
+    rng = np.random.default_rng(77 + groups + act)
+    pad_a, pad_b, pad_c = 64, 128, 256  # elements between one group's block and the next
+    sa, sb, sc, sct, sbias = m * k + pad_a, n * k + pad_b, m * n + pad_c, n * m + pad_c, n + 64
+    a = bf16_round(rng.standard_normal((groups, sa)))
+    b = bf16_round(rng.standard_normal((groups, sb)))
+    bias = rng.standard_normal((groups, sbias)).astype(np.float32)
+    mask = bf16_round(rng.standard_normal((groups, sc)))
+    da, db_ = _dev(a, torch.bfloat16), _dev(b, torch.bfloat16)
+    dbias, dmask = _dev(bias, torch.float32), _dev(mask, torch.bfloat16)
+    c32 = torch.full((groups, sc), 7.0, dtype=torch.float32, device="cuda")
+    c16 = torch.full((groups, sc), 7.0, dtype=torch.bfloat16, device="cuda")
+    c16t = torch.full((groups, sct), 7.0, dtype=torch.bfloat16, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    rc = lib.oafdtd_mlp_gemm_tn(da.data_ptr(), db_.data_ptr(), c32.data_ptr(), c16.data_ptr(), c16t.data_ptr(),
+                                dbias.data_ptr(), dmask.data_ptr(), m, n, k, k, k, n, m, act, 0.0, groups, sa, sb, sc,
+                                sct, sbias, status.data_ptr(), None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    got32 = c32.cpu().numpy().astype(np.float64)
+    got16 = c16.float().cpu().numpy()
+    got16t = c16t.float().cpu().numpy()
+    for gi in range(groups):
+        ag = a[gi, : m * k].reshape(m, k)
+        bg = b[gi, : n * k].reshape(n, k)
+        ref = ag @ bg.T + bias[gi, :n]
+        mk = mask[gi, : m * n].reshape(m, n)
+        ref = np.tanh(ref) if act == 3 else ref * (1.0 - mk * mk)
+        scale = np.sqrt(k) * 4 * (1.0 if act != 4 else np.abs(mk).max() ** 2 + 1.0)
+        g32 = got32[gi, : m * n].reshape(m, n)
+        assert np.abs(g32 - ref).max() <= 2e-6 * scale, gi
+        np.testing.assert_array_equal(got16[gi, : m * n].reshape(m, n), bf16_round(g32))
+        np.testing.assert_array_equal(got16t[gi, : m * n].reshape(n, m), bf16_round(g32).T)
+        assert np.all(got32[gi, m * n :] == 7.0) and np.all(got16[gi, m * n :] == 7.0)
+        assert np.all(got16t[gi, m * n :] == 7.0)
+
+
+def test_grouped_training_batch_matches_the_oracle_per_member() -> None:
+    """Three members in one grouped network, each on its own batch: every member's loss and
+    gradients against the oracle run on that member's weights and rows alone."""
+    from open_analysis_gb300.surrogate import Mlp
+
+    net = Mlp([7, 512, 512, 128], batch=256, seed=5, act="tanh", members=3)
+    rng = np.random.default_rng(9)
+    x = rng.uniform(-1, 1, (3, 256, 7))
+    t = rng.standard_normal((3, 256, 128))
+    losses, flat = net.gradients(x, t)
+    assert flat.shape == (3, net.n_params)
+    for k in range(3):
+        w, b = net.weights(k)
+        ref = loss_and_grads(w, b, net.pad(x[k]), t[k].astype(np.float32), bf16=True, act="tanh")
+        assert abs(losses[k] - ref.loss) <= 1e-5 * ref.loss, k
+        gw, gb = net.split(flat[k])
+        for l in range(len(w)):
+            for got, want in ((gw[l], ref.dw[l]), (gb[l], ref.db[l])):
+                rel = np.linalg.norm(got - want) / np.linalg.norm(want)
+                assert rel <= 5e-3, (k, l, rel)
 
 
 def test_training_batch_on_tcgen05_shapes_matches_the_oracle() -> None:
