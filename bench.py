@@ -251,8 +251,10 @@ def sweep_measure(n: int, steps: int) -> dict[str, Any]:
     shape = tune_shape(compiled)
     tune_s = time.perf_counter() - t0
     batched = run_batched(models, compiled, steps, shape=shape)
+    streams = run_batched(models, compiled, steps, shape=shape, launch="streams")
     looped = run_looped(models, compiled, steps, shape=shape)
-    same = all(np.array_equal(a, b) for a, b in zip(batched.s, looped.s, strict=True))
+    same = all(np.array_equal(a, b) and np.array_equal(a, c)
+               for a, b, c in zip(batched.s, looped.s, streams.s, strict=True))
     return {
         "metric": "S-parameter sweeps/s",
         "instances": n,
@@ -260,9 +262,13 @@ def sweep_measure(n: int, steps: int) -> dict[str, Any]:
         "cells_total": int(sum(x.grid.cells for x in compiled)),
         "batched": batched.sweeps_per_s,
         "looped": looped.sweeps_per_s,
+        "streams": streams.sweeps_per_s,
         "batched_over_looped": batched.sweeps_per_s / looped.sweeps_per_s,
+        "batched_over_streams": batched.sweeps_per_s / streams.sweeps_per_s,
         "batched_gcell_s": batched.cell_updates / batched.seconds / 1e9,
         "looped_gcell_s": looped.cell_updates / looped.seconds / 1e9,
+        "streams_gcell_s": streams.cell_updates / streams.seconds / 1e9,
+        "batched_launch": {k: batched.extra[k] for k in ("graph_kernels_per_chunk", "native_batches")},
         "identical_s": same,
         "launch_shape": None if shape is None else {"tile_z": shape.tile_z, "variant": shape.variant,
                                                     "tune_seconds": tune_s},

@@ -120,6 +120,7 @@ typedef struct oafdtd_problem {
 } oafdtd_problem;
 
 typedef struct oafdtd_engine oafdtd_engine;
+typedef struct oafdtd_batch oafdtd_batch;
 
 /* Library ABI version (OAFDTD_ABI_VERSION). */
 int32_t oafdtd_abi_version(void);
@@ -192,6 +193,24 @@ int oafdtd_restore(oafdtd_engine* engine, const void* in);
 int oafdtd_step_async(oafdtd_engine* engine, int64_t n);
 int oafdtd_wait(oafdtd_engine* engine);
 
+/* A batched sweep: n engines of one precision, device and sweep variant, at the same step, stepped
+ * together. Every kernel class of a time step is then one launch over the blocks of all n engines
+ * (the same kernel bodies on each engine's own arguments, so each engine's fields, DFTs and
+ * S-parameters are bit for bit those of stepping it alone); whole 64-step chunks replay one
+ * captured graph for the whole batch. The engines stay owned by the caller and must outlive the
+ * batch; while it exists they are stepped through it only (OAFDTD_E_INVALID otherwise), and
+ * their observables (oafdtd_dft, oafdtd_energy, ...) stay available, ordered after the batch's
+ * work. oafdtd_batch_step_async queues n steps of every engine and returns; oafdtd_batch_wait
+ * synchronises and reports errors, including a bounded wait that gave up (OAFDTD_E_TIMEOUT).
+ * OAFDTD_E_RANGE past any engine's max_steps. Replaces looping the reference's engine over the
+ * instances of a sweep (one CupyEngine per problem, packages/oa-fdtd/src/oa_fdtd/engine.py:390-437). */
+int oafdtd_batch_create(oafdtd_engine* const* engines, int32_t n, oafdtd_batch** out);
+int oafdtd_batch_step_async(oafdtd_batch* batch, int64_t n);
+int oafdtd_batch_wait(oafdtd_batch* batch);
+/* Kernel launches in one replay of the batch's 64-step graph (0 before the first capture). */
+int oafdtd_batch_graph_kernels(const oafdtd_batch* batch, int64_t* out);
+int oafdtd_batch_destroy(oafdtd_batch* batch);
+
 /* One half of a time step, launched eagerly and synchronised: which 0 = the H half (H update,
  * CPML-H, PMC ghosts, H probes), 1 = the E half (E update, CPML-E, Debye, SIBC, injection, E
  * probes; advances the step counter). A z-slab decomposition exchanges boundary planes between
@@ -235,6 +254,8 @@ int oafdtd_set_graph(oafdtd_engine* engine, int32_t use_graph);
  * OAFDTD_E_INVALID. The autotuner sets these. A staged sweep whose copies do not arrive within its
  * bounded wait makes the step return OAFDTD_E_TIMEOUT. */
 int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_z, int32_t variant);
+/* The current launch shape: planes per block and sweep variant (as oafdtd_set_tuning takes them). */
+int oafdtd_get_tuning(const oafdtd_engine* engine, int32_t* tile_z, int32_t* variant);
 
 /* Average device time per step of each kernel class over the last oafdtd_step call, measured
  * with CUDA events when profiling is on (oafdtd_set_profiling). Writes up to n values in the

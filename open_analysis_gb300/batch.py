@@ -1,11 +1,14 @@
 """Batched parameter sweeps: many independent FDTD instances on one GPU at the same time.
 
 A sweep (the reference runs one problem at a time) is a list of models with different grids.
-Each instance gets its own engine, stream and captured 64-step graphs; ``run_batched`` queues all
-their steps (``Gb300Engine.step_async``) before waiting on any, so the GPU runs kernels of many
-small grids side by side instead of one small grid at a time; ``run_looped`` is the plain way,
-one instance after the other (``step`` synchronises). Both give the same S-parameters bit for
-bit (each instance's arithmetic does not depend on what runs beside it).
+Each instance gets its own engine (its own device state). ``run_batched`` steps them as one
+:class:`EngineBatch` (``oafdtd_batch_*``): every kernel class of a time step is a single launch
+over the blocks of all instances, each block finding its instance and its own arguments through
+a table, and whole 64-step chunks replay one captured graph for the whole sweep, so small grids
+fill the GPU together. ``run_looped`` is the plain way, one instance after the other.
+``run_batched(..., launch="streams")`` keeps the earlier form: every engine's own graphs queued
+on its own stream. All three give the same S-parameters bit for bit (the batched launches run the
+same kernel bodies on each instance's own arguments).
 
 The host compiles the instances in a ``spawn`` process pool before any CUDA call. The launch
 shape (planes per block, sweep variant) comes from the project's autotuner
@@ -171,28 +174,111 @@ def finish_sweep(models: Sequence[Model], compiled: Sequence[Compiled], engines:
     return SweepRun(s, seconds + read, create, updates, extra)
 
 
-def run_batched(models: Sequence[Model], compiled: Sequence[Compiled], steps: int, dtype: str = "float32",
-                shape: Any = None, wire_dir: str | Path | None = None) -> SweepRun:
-    """All instances at once: every engine's steps queued on its own stream, then waited on.
+class EngineBatch:
+    """Engines stepped as one (``oafdtd_batch_*``): engines of one sweep variant form one native
+    batch each (instances that could not take a sweep's launch shape may run another variant).
+    Every engine's results stay readable through the engine; the engines must outlive the batch
+    and are stepped only through it while it exists."""
 
-    The first 64-step chunk goes first on every engine (each captures its graph there), the
-    rest after: capturing a graph while other engines' work is queued would wait for that work
-    and run the instances one after the other. ``shape``: a launch shape from
-    :func:`tune_shape` (None: the engines' default). ``wire_dir``: write each instance's worker
-    files there (:func:`finish_sweep`)."""
-    engines, create = _engines(compiled, steps, dtype, shape)
-    t0 = time.perf_counter()
-    first = min(64, steps)
-    for e in engines:
-        e.step_async(first)
-    for e in engines:
-        e.wait()
-    if steps > first:
+    def __init__(self, engines: Sequence[Any]) -> None:
+        import ctypes as C
+
+        from open_analysis_gb300 import native
+
+        self._lib = native.load()
+        self._C = C
+        groups: dict[int, list[Any]] = {}
         for e in engines:
-            e.step_async(steps - first)
+            groups.setdefault(e.get_tuning()[1], []).append(e)
+        self.engines = list(engines)
+        self.handles: list[Any] = []
+        try:
+            for members in groups.values():
+                arr = (C.c_void_p * len(members))(*[m._h.value for m in members])
+                h = C.c_void_p()
+                native.check(self._lib.oafdtd_batch_create(arr, len(members), C.byref(h)), "batch_create")
+                self.handles.append(h)
+        except Exception:
+            self.close()
+            raise
+
+    def step_async(self, n: int) -> None:
+        from open_analysis_gb300 import native
+
+        for h in self.handles:
+            native.check(self._lib.oafdtd_batch_step_async(h, int(n)), "batch_step_async")
+
+    def wait(self) -> None:
+        from open_analysis_gb300 import native
+
+        for h in self.handles:
+            native.check(self._lib.oafdtd_batch_wait(h), "batch_wait")
+
+    def step(self, n: int) -> None:
+        self.step_async(n)
+        self.wait()
+
+    def graph_kernels(self) -> int:
+        """Kernel launches in one replay of the batches' 64-step graphs (0 before a capture)."""
+        from open_analysis_gb300 import native
+
+        total = 0
+        for h in self.handles:
+            out = self._C.c_int64()
+            native.check(self._lib.oafdtd_batch_graph_kernels(h, self._C.byref(out)), "batch_graph_kernels")
+            total += int(out.value)
+        return total
+
+    def close(self) -> None:
+        for h in self.handles:
+            if h:
+                self._lib.oafdtd_batch_destroy(h)
+        self.handles = []
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def run_batched(models: Sequence[Model], compiled: Sequence[Compiled], steps: int, dtype: str = "float32",
+                shape: Any = None, wire_dir: str | Path | None = None, launch: str = "batch") -> SweepRun:
+    """All instances at once. ``launch="batch"`` (the default): one :class:`EngineBatch`, every
+    kernel class one launch over all instances. ``launch="streams"``: every engine's steps queued
+    on its own stream, then waited on; the first 64-step chunk goes first on every engine (each
+    captures its graph there), the rest after, since capturing a graph while other engines' work
+    is queued would wait for that work. ``shape``: a launch shape from :func:`tune_shape` (None:
+    the engines' default). ``wire_dir``: write each instance's worker files there
+    (:func:`finish_sweep`)."""
+    if launch not in ("batch", "streams"):
+        raise ValueError(f"launch {launch!r}: 'batch' or 'streams'")
+    engines, create = _engines(compiled, steps, dtype, shape)
+    extra: dict[str, Any] = {"launch": launch}
+    if launch == "batch":
+        t_b = time.perf_counter()
+        batch = EngineBatch(engines)
+        create += time.perf_counter() - t_b
+        t0 = time.perf_counter()
+        batch.step(steps)
+        extra["graph_kernels_per_chunk"] = batch.graph_kernels()
+        extra["native_batches"] = len(batch.handles)
+        batch.close()
+    else:
+        t0 = time.perf_counter()
+        first = min(64, steps)
+        for e in engines:
+            e.step_async(first)
         for e in engines:
             e.wait()
-    return finish_sweep(models, compiled, engines, steps, dtype, time.perf_counter() - t0, create, wire_dir)
+        if steps > first:
+            for e in engines:
+                e.step_async(steps - first)
+            for e in engines:
+                e.wait()
+    run = finish_sweep(models, compiled, engines, steps, dtype, time.perf_counter() - t0, create, wire_dir)
+    run.extra.update(extra)
+    return run
 
 
 def run_looped(models: Sequence[Model], compiled: Sequence[Compiled], steps: int, dtype: str = "float32",

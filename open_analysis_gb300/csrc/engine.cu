@@ -1623,6 +1623,367 @@ int Engine<real>::set_variant(int v) {
   return OAFDTD_OK;
 }
 
+// ---------------------------------------------------------------------------- batched sweeps
+// Several engines of one precision and one sweep variant stepped as one: every kernel class of
+// the step is a single launch over the blocks of all engines (a BatchGrid maps each block to its
+// engine and to its block in that engine's own grid), with the engines' arguments in device
+// arrays, one set per field-buffer parity. The launches run in the order and on the streams of
+// Engine::launch_step, the same kernel bodies on the same arguments, so every engine's fields
+// come out bit for bit as when it steps alone. Kernel boundaries order the half steps of every
+// engine at once; nothing waits on the device. Whole 64-step chunks replay one captured graph.
+struct BatchBase {
+  virtual ~BatchBase() = default;
+  virtual int enqueue(int64_t n) = 0;
+  virtual int wait() = 0;
+  int64_t graph_kernels = 0;
+};
+
+template <typename real>
+struct Batch final : BatchBase {
+  struct Launch {
+    oafdtd::BatchGrid g{};
+    int blocks = 0;
+    int key = 0;  // kernel variant of the engines in this launch
+  };
+  std::vector<Engine<real>*> eng;
+  int device = 0, variant = 0;
+  cudaStream_t stream = nullptr, side = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr, done_ev = nullptr;
+  std::vector<cudaEvent_t> in_ev;
+  std::vector<void*> allocs;
+  oafdtd::SweepArgs<real>* d_sw[2] = {};
+  oafdtd::SweepMaps* d_mp[2] = {};
+  oafdtd::FusedMaps* d_fm[2] = {};
+  oafdtd::ProbeArgs<real>* d_pr[2] = {};
+  oafdtd::SibcArgs<real>* d_sb[2] = {};
+  oafdtd::EdgeArgs<real>* d_ed[2] = {};
+  oafdtd::SlabLaunch* d_slab[2] = {};  // per kind (the same for both parities)
+  long long** d_step_base = nullptr;
+  std::vector<oafdtd::SweepArgs<real>> h_sw[2];
+  std::vector<Launch> fused, h_inner, h_z, e_inner, e_z, slab_h, slab_e, pre_e, probe_e, edges, sibc;
+  bool tma = false;
+  cudaGraphExec_t graph[2] = {};
+
+  ~Batch() override {
+    for (cudaGraphExec_t g : graph)
+      if (g) cudaGraphExecDestroy(g);
+    for (void* q : allocs) cudaFree(q);
+    for (cudaEvent_t e : in_ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : {fork_ev, join_ev, done_ev})
+      if (e) cudaEventDestroy(e);
+    if (side) cudaStreamDestroy(side);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  template <typename T>
+  int upload(T** out, const T* host, size_t count) {
+    *out = nullptr;
+    void* q = nullptr;
+    OA_CUDA(cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T)));
+    allocs.push_back(q);
+    if (count) OA_CUDA(cudaMemcpy(q, host, count * sizeof(T), cudaMemcpyHostToDevice));
+    *out = static_cast<T*>(q);
+    return OAFDTD_OK;
+  }
+
+  // One launch per kernel variant over the engines' grids (x, y, z blocks; 1-D: x only).
+  int plan(const std::vector<dim3>& grids, const std::vector<int>& keys, std::vector<Launch>* out) {
+    out->clear();
+    const int n = (int)eng.size();
+    std::vector<int> done(n, 0);
+    for (int i = 0; i < n; ++i) {
+      const long long bi = (long long)grids[i].x * grids[i].y * grids[i].z;
+      if (done[i] || bi == 0) continue;
+      const int key = keys[i];
+      // every block of the launch: (engine, x, y, z), x fastest within the engine's grid
+      std::vector<int4> blk;
+      for (int k = i; k < n; ++k) {
+        const dim3 g = grids[k];
+        const long long bk = (long long)g.x * g.y * g.z;
+        if (done[k] || bk == 0 || keys[k] != key) continue;
+        done[k] = 1;
+        if ((long long)blk.size() + bk > 2147483647LL) return fail(OAFDTD_E_INVALID, "a batched launch exceeds 2^31 blocks");
+        for (unsigned z = 0; z < g.z; ++z)
+          for (unsigned y = 0; y < g.y; ++y)
+            for (unsigned x = 0; x < g.x; ++x) blk.push_back(make_int4(k, (int)x, (int)y, (int)z));
+      }
+      Launch L;
+      L.blocks = (int)blk.size();
+      L.key = key;
+      int4* d_blk;
+      if (int rc = upload(&d_blk, blk.data(), blk.size())) return rc;
+      L.g = oafdtd::BatchGrid{d_blk};
+      out->push_back(L);
+    }
+    return OAFDTD_OK;
+  }
+
+  int build(const std::vector<Engine<real>*>& engines) {
+    eng = engines;
+    const int n = (int)eng.size();
+    Engine<real>& e0 = *eng[0];
+    device = e0.device;
+    variant = e0.staged;
+    for (Engine<real>* e : eng) {
+      if (e->device != device) return fail(OAFDTD_E_INVALID, "the engines of a batch share one device");
+      if (e->staged != variant) return fail(OAFDTD_E_INVALID, "the engines of a batch run one sweep variant");
+      if (e->half_pending) return fail(OAFDTD_E_INVALID, "an engine has an H half pending");
+      if (e->profiling) return fail(OAFDTD_E_INVALID, "an engine of a batch is in profiling mode");
+      if (e->steps != e0.steps || e->cur[0] != e0.cur[0] || e->cur[1] != e0.cur[1])
+        return fail(OAFDTD_E_INVALID, "the engines of a batch start at the same step and buffers");
+    }
+    OA_CUDA(cudaSetDevice(device));
+    for (Engine<real>* e : eng) OA_CUDA(cudaStreamSynchronize(e->stream));
+    OA_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    OA_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    for (cudaEvent_t* ev : {&fork_ev, &join_ev, &done_ev}) OA_CUDA(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+    in_ev.assign(n, nullptr);
+    for (cudaEvent_t& ev : in_ev) OA_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    tma = variant >= 2;
+    const int rv = variant;
+    // the engines' arguments of a step starting in buffer p (in place: p = 0 only)
+    const int parities = variant == 3 ? 2 : 1;
+    std::vector<oafdtd::SweepMaps> mp(n);
+    std::vector<oafdtd::FusedMaps> fm(n);
+    std::vector<oafdtd::ProbeArgs<real>> pr(n);
+    std::vector<oafdtd::SibcArgs<real>> sb(n);
+    std::vector<oafdtd::EdgeArgs<real>> ed(n);
+    for (int p = 0; p < parities; ++p) {
+      h_sw[p].resize(n);
+      for (int i = 0; i < n; ++i) {
+        Engine<real>& e = *eng[i];
+        e.sw.tile_z = e.tile_z;
+        e.use_regions(rv);
+        e.bind(p, p);
+        h_sw[p][i] = e.sw;
+        mp[i] = e.maps_p[p];
+        fm[i] = e.fmaps[p];
+        pr[i] = e.pr;
+        sb[i] = e.sb;
+        ed[i] = e.ed;
+      }
+      if (int rc = upload(&d_sw[p], h_sw[p].data(), n)) return rc;
+      if (int rc = upload(&d_mp[p], mp.data(), n)) return rc;
+      if (int rc = upload(&d_fm[p], fm.data(), n)) return rc;
+      if (int rc = upload(&d_pr[p], pr.data(), n)) return rc;
+      if (int rc = upload(&d_sb[p], sb.data(), n)) return rc;
+      if (int rc = upload(&d_ed[p], ed.data(), n)) return rc;
+    }
+    for (Engine<real>* e : eng) e->bind(e->cur[0], e->cur[1]);
+    // launch geometry, from the parity-0 arguments (the boxes do not depend on the buffers)
+    const std::vector<oafdtd::SweepArgs<real>>& a = h_sw[0];
+    std::vector<dim3> g_fused(n), g_hi(n), g_hz(n), g_ei(n), g_ez(n), g_sh(n), g_se(n), g_pre(n), g_probe(n),
+        g_edge(n), g_sibc(n);
+    std::vector<int> k_pole(n), k_zero(n, 0), k_sibc(n);
+    std::vector<oafdtd::SlabLaunch> slabs[2];
+    slabs[0].resize(n);
+    slabs[1].resize(n);
+    for (int i = 0; i < n; ++i) {
+      cudaError_t err = cudaSuccess;
+      if (variant == 3 && (err = oafdtd::fused_grid(a[i], &g_fused[i])) != cudaSuccess)
+        return fail(OAFDTD_E_INVALID, "fused sweep geometry of a batched engine");
+      if (variant != 0) {
+        if ((err = oafdtd::staged_grids(a[i], 1, &g_hi[i], &g_hz[i])) != cudaSuccess ||
+            (err = oafdtd::staged_grids(a[i], 0, &g_ei[i], &g_ez[i])) != cudaSuccess)
+          return fail(OAFDTD_E_INVALID, "staged sweep geometry of a batched engine");
+      } else {
+        g_hi[i] = g_hz[i] = g_ei[i] = g_ez[i] = dim3(0, 0, 0);
+      }
+      if (variant != 3) g_fused[i] = dim3(0, 0, 0);
+      for (int kind = 0; kind < 2; ++kind) {
+        long long blocks = 0;
+        if (oafdtd::slab_plan(a[i], kind, &slabs[kind][i], &blocks) != cudaSuccess)
+          return fail(OAFDTD_E_INVALID, "slab geometry of a batched engine");
+        (kind == 0 ? g_se : g_sh)[i] = dim3((unsigned)blocks, 1, 1);
+      }
+      const Engine<real>& e = *eng[i];
+      g_pre[i] = dim3((unsigned)oafdtd::pre_e_blocks(e.pr), 1, 1);
+      g_probe[i] = dim3((unsigned)oafdtd::probe_e_blocks(e.pr), 1, 1);
+      g_edge[i] = dim3((unsigned)oafdtd::edge_blocks(e.ed), 1, 1);
+      g_sibc[i] = dim3((unsigned)oafdtd::sibc_blocks(e.sb), 1, 1);
+      k_pole[i] = a[i].ade_P > 1 ? 1 : 0;
+      k_sibc[i] = oafdtd::sibc_variant(e.sb);
+    }
+    for (int kind = 0; kind < 2; ++kind)
+      if (int rc = upload(&d_slab[kind], slabs[kind].data(), n)) return rc;
+    std::vector<long long*> bases(n);
+    for (int i = 0; i < n; ++i) bases[i] = eng[i]->step_base;
+    if (int rc = upload(&d_step_base, bases.data(), n)) return rc;
+    const std::pair<std::vector<dim3>*, std::pair<std::vector<int>*, std::vector<Launch>*>> plans[] = {
+        {&g_fused, {&k_pole, &fused}},  {&g_hi, {&k_zero, &h_inner}}, {&g_hz, {&k_zero, &h_z}},
+        {&g_ei, {&k_pole, &e_inner}},   {&g_ez, {&k_pole, &e_z}},     {&g_sh, {&k_zero, &slab_h}},
+        {&g_se, {&k_pole, &slab_e}},    {&g_pre, {&k_zero, &pre_e}},  {&g_probe, {&k_zero, &probe_e}},
+        {&g_edge, {&k_zero, &edges}},   {&g_sibc, {&k_sibc, &sibc}},
+    };
+    for (const auto& q : plans)
+      if (int rc = plan(*q.first, *q.second.first, q.second.second)) return rc;
+    return OAFDTD_OK;
+  }
+
+  int sweep_launches(const std::vector<Launch>& ls, bool h, bool z, int p, cudaStream_t s) {
+    for (const Launch& L : ls) {
+      const cudaError_t err =
+          oafdtd::launch_staged_batch<real>(d_sw[p], d_mp[p], L.g, L.blocks, h, tma, z, L.key != 0, s);
+      if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("batched sweep: ") + cudaGetErrorString(err));
+    }
+    return OAFDTD_OK;
+  }
+  int slab_launches(int kind, int p, cudaStream_t s) {
+    for (const Launch& L : kind == 0 ? slab_e : slab_h) {
+      const cudaError_t err =
+          oafdtd::launch_slab_batch<real>(d_sw[p], d_slab[kind], L.g, L.blocks, kind, L.key != 0, s);
+      if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("batched slab: ") + cudaGetErrorString(err));
+    }
+    return OAFDTD_OK;
+  }
+  // the staged sweep of one kind with its slab kernel beside it (Engine::sweep_pair)
+  int pair(int kind, int p) {
+    const bool h = kind == 1;
+    if (variant != 0) {
+      OA_CUDA(cudaEventRecord(fork_ev, stream));
+      OA_CUDA(cudaStreamWaitEvent(side, fork_ev, 0));
+      if (int rc = slab_launches(kind, p, side)) return rc;
+      OA_CUDA(cudaEventRecord(join_ev, side));
+      if (int rc = sweep_launches(h ? h_inner : e_inner, h, false, p, stream)) return rc;
+      if (int rc = sweep_launches(h ? h_z : e_z, h, true, p, stream)) return rc;
+      OA_CUDA(cudaStreamWaitEvent(stream, join_ev, 0));
+      return OAFDTD_OK;
+    }
+    return slab_launches(kind, p, stream);
+  }
+
+  // One time step of every engine, from buffers p (Engine::launch_step with parts 3).
+  int launch_step(int off, int p) {
+    cudaError_t err = cudaSuccess;
+    if (variant == 3) {
+      OA_CUDA(cudaEventRecord(fork_ev, stream));
+      OA_CUDA(cudaStreamWaitEvent(side, fork_ev, 0));
+      if (int rc = sweep_launches(h_inner, true, false, p, side)) return rc;
+      if (int rc = sweep_launches(h_z, true, true, p, side)) return rc;
+      if (int rc = slab_launches(1, p, side)) return rc;
+      OA_CUDA(cudaEventRecord(join_ev, side));
+      for (const Launch& L : fused)
+        if ((err = oafdtd::launch_fused_batch<real>(d_sw[p], d_fm[p], L.g, L.blocks, L.key != 0, stream)) != cudaSuccess)
+          return fail(OAFDTD_E_CUDA, std::string("batched fused sweep: ") + cudaGetErrorString(err));
+      OA_CUDA(cudaStreamWaitEvent(stream, join_ev, 0));
+    } else if (int rc = pair(1, p)) {
+      return rc;
+    }
+    for (size_t i = 0; i < eng.size(); ++i) {
+      const Engine<real>& e = *eng[i];
+      if (!e.pmc_mask) continue;
+      if ((err = oafdtd::launch_ghosts<real>(h_sw[p][i].Ho, e.pmc_mask, e.nx, e.ny, e.nz, e.X, e.Y, e.B, stream)) !=
+          cudaSuccess)
+        return fail(OAFDTD_E_CUDA, std::string("ghosts: ") + cudaGetErrorString(err));
+    }
+    for (const Launch& L : pre_e)
+      if ((err = oafdtd::launch_pre_e_batch<real>(d_pr[p], L.g, L.blocks, off, stream)) != cudaSuccess)
+        return fail(OAFDTD_E_CUDA, std::string("batched pre_e: ") + cudaGetErrorString(err));
+    if (int rc = pair(0, p)) return rc;
+    for (const Launch& L : sibc)
+      if ((err = oafdtd::launch_sibc_batch<real>(d_sb[p], L.g, L.blocks, L.key, stream)) != cudaSuccess)
+        return fail(OAFDTD_E_CUDA, std::string("batched sibc: ") + cudaGetErrorString(err));
+    for (const Launch& L : edges)
+      if ((err = oafdtd::launch_edges_batch<real>(d_ed[p], L.g, L.blocks, off, stream)) != cudaSuccess)
+        return fail(OAFDTD_E_CUDA, std::string("batched edges: ") + cudaGetErrorString(err));
+    for (const Launch& L : probe_e)
+      if ((err = oafdtd::launch_probe_e_batch<real>(d_pr[p], L.g, L.blocks, off, stream)) != cudaSuccess)
+        return fail(OAFDTD_E_CUDA, std::string("batched probe_e: ") + cudaGetErrorString(err));
+    return OAFDTD_OK;
+  }
+
+  int capture(int p) {
+    cudaGraph_t g = nullptr;
+    OA_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    int rc = OAFDTD_OK;
+    int q = p;
+    for (int o = 0; o < oafdtd::kChunk && rc == OAFDTD_OK; ++o) {
+      rc = launch_step(o, q);
+      if (variant == 3) q ^= 1;
+    }
+    if (rc == OAFDTD_OK) {
+      const cudaError_t err = oafdtd::launch_bump_batch(d_step_base, (int)eng.size(), oafdtd::kChunk, stream);
+      if (err != cudaSuccess) rc = fail(OAFDTD_E_CUDA, cudaGetErrorString(err));
+    }
+    const cudaError_t err = cudaStreamEndCapture(stream, &g);
+    if (rc != OAFDTD_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("batch capture: ") + cudaGetErrorString(err));
+    size_t nodes = 0;
+    int64_t kernels = 0;
+    if (cudaGraphGetNodes(g, nullptr, &nodes) == cudaSuccess && nodes) {
+      std::vector<cudaGraphNode_t> v(nodes);
+      if (cudaGraphGetNodes(g, v.data(), &nodes) == cudaSuccess)
+        for (cudaGraphNode_t nd : v) {
+          cudaGraphNodeType t;
+          if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++kernels;
+        }
+    }
+    const cudaError_t ierr = cudaGraphInstantiate(&graph[p], g, 0);
+    cudaGraphDestroy(g);
+    if (ierr != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("batch instantiate: ") + cudaGetErrorString(ierr));
+    graph_kernels = kernels;
+    return OAFDTD_OK;
+  }
+
+  int enqueue(int64_t n) override {
+    if (n < 0) return fail(OAFDTD_E_INVALID, "negative step count");
+    Engine<real>& e0 = *eng[0];
+    for (Engine<real>* e : eng) {
+      if (e->steps != e0.steps || e->cur[0] != e0.cur[0] || e->half_pending)
+        return fail(OAFDTD_E_INVALID, "an engine of the batch was stepped on its own");
+      if (e->steps + n > e->max_steps) return fail(OAFDTD_E_RANGE, "step count exceeds max_steps (wave table length)");
+    }
+    OA_CUDA(cudaSetDevice(device));
+    for (size_t i = 0; i < eng.size(); ++i) {
+      OA_CUDA(cudaEventRecord(in_ev[i], eng[i]->stream));
+      OA_CUDA(cudaStreamWaitEvent(stream, in_ev[i], 0));
+    }
+    int64_t done = 0;
+    while (done < n) {
+      const int64_t start = e0.steps;
+      const int take = (int)std::min<int64_t>(n - done, oafdtd::kChunk - start % oafdtd::kChunk);
+      const int p = variant == 3 ? e0.cur[0] : 0;
+      if (e0.use_graph && take == oafdtd::kChunk) {
+        if (!graph[p])
+          if (int rc = capture(p)) return rc;
+        OA_CUDA(cudaGraphLaunch(graph[p], stream));
+      } else {
+        int q = p;
+        for (int o = 0; o < take; ++o) {
+          if (int rc = launch_step(o, q)) return rc;
+          if (variant == 3) q ^= 1;
+        }
+        const cudaError_t err = oafdtd::launch_bump_batch(d_step_base, (int)eng.size(), take, stream);
+        if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, cudaGetErrorString(err));
+      }
+      for (Engine<real>* e : eng) {
+        e->steps += take;
+        if (variant == 3 && (take & 1)) {
+          e->cur[0] ^= 1;
+          e->cur[1] ^= 1;
+        }
+      }
+      done += take;
+    }
+    // later work on an engine's own stream follows the batch
+    OA_CUDA(cudaEventRecord(done_ev, stream));
+    for (Engine<real>* e : eng) OA_CUDA(cudaStreamWaitEvent(e->stream, done_ev, 0));
+    return OAFDTD_OK;
+  }
+
+  int wait() override {
+    OA_CUDA(cudaSetDevice(device));
+    OA_CUDA(cudaStreamSynchronize(stream));
+    OA_CUDA(cudaGetLastError());
+    for (Engine<real>* e : eng)
+      if (int rc = e->check_status()) return rc;
+    return OAFDTD_OK;
+  }
+};
+
 }  // namespace
 
 namespace oafdtd {
@@ -1631,6 +1992,10 @@ void set_last_error(const std::string& msg) { g_last_error = msg; }
 
 struct oafdtd_engine {
   std::unique_ptr<EngineBase> impl;
+};
+
+struct oafdtd_batch {
+  std::unique_ptr<BatchBase> impl;
 };
 
 extern "C" {
@@ -1822,6 +2187,61 @@ int oafdtd_set_tuning(oafdtd_engine* engine, int32_t tile_z, int32_t variant) {
     if (int rc = engine->impl->set_variant(variant)) return rc;
   if (tile_z) engine->impl->tile_z = tile_z;
   engine->impl->graph_dirty = true;  // a new launch shape needs a new graph
+  return OAFDTD_OK;
+}
+
+int oafdtd_get_tuning(const oafdtd_engine* engine, int32_t* tile_z, int32_t* variant) {
+  if (!engine || !tile_z || !variant) return fail(OAFDTD_E_INVALID, "null argument");
+  *tile_z = engine->impl->tile_z;
+  *variant = engine->impl->staged;
+  return OAFDTD_OK;
+}
+
+int oafdtd_batch_create(oafdtd_engine* const* engines, int32_t n, oafdtd_batch** out) {
+  if (!engines || !out || n < 1) return fail(OAFDTD_E_INVALID, "null argument or empty batch");
+  *out = nullptr;
+  std::vector<Engine<float>*> f32;
+  std::vector<Engine<double>*> f64;
+  for (int i = 0; i < n; ++i) {
+    if (!engines[i]) return fail(OAFDTD_E_INVALID, "null engine in the batch");
+    EngineBase* e = engines[i]->impl.get();
+    if (auto* ef = dynamic_cast<Engine<float>*>(e)) f32.push_back(ef);
+    else if (auto* ed = dynamic_cast<Engine<double>*>(e)) f64.push_back(ed);
+  }
+  if (!f32.empty() && !f64.empty()) return fail(OAFDTD_E_INVALID, "the engines of a batch share one precision");
+  std::unique_ptr<oafdtd_batch> b(new (std::nothrow) oafdtd_batch);
+  if (!b) return fail(OAFDTD_E_OOM, "host allocation");
+  if (!f32.empty()) {
+    auto* impl = new Batch<float>();
+    b->impl.reset(impl);
+    if (int rc = impl->build(f32)) return rc;
+  } else {
+    auto* impl = new Batch<double>();
+    b->impl.reset(impl);
+    if (int rc = impl->build(f64)) return rc;
+  }
+  *out = b.release();
+  return OAFDTD_OK;
+}
+
+int oafdtd_batch_step_async(oafdtd_batch* batch, int64_t n) {
+  if (!batch) return fail(OAFDTD_E_INVALID, "null batch");
+  return batch->impl->enqueue(n);
+}
+
+int oafdtd_batch_wait(oafdtd_batch* batch) {
+  if (!batch) return fail(OAFDTD_E_INVALID, "null batch");
+  return batch->impl->wait();
+}
+
+int oafdtd_batch_graph_kernels(const oafdtd_batch* batch, int64_t* out) {
+  if (!batch || !out) return fail(OAFDTD_E_INVALID, "null argument");
+  *out = batch->impl->graph_kernels;
+  return OAFDTD_OK;
+}
+
+int oafdtd_batch_destroy(oafdtd_batch* batch) {
+  delete batch;
   return OAFDTD_OK;
 }
 

@@ -89,9 +89,10 @@ __device__ __noinline__ void abort_fused(unsigned long long* bar_e, unsigned lon
   for (int u = h_seen; u < h_issued; ++u) mbar_wait(&bar_h[u % kSH], (unsigned)((u / kSH) & 1), kDrainNs);
 }
 
+// The sweep of block bid of the fused box (a plain launch passes blockIdx; a batched one the
+// block of its engine).
 template <typename real, bool kMulti>
-__global__ void __launch_bounds__(256, 2)
-    fused_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ FusedMaps tm) {
+__device__ __forceinline__ void fused_body(const SweepArgs<real>& a, const FusedMaps& tm, const uint3 bid) {
   extern __shared__ unsigned char smem_raw[];
   __shared__ unsigned long long bar_e[kSE], bar_h[kSH];
   FusedSmem<real>& sm = *reinterpret_cast<FusedSmem<real>*>(align_smem(smem_raw));
@@ -100,11 +101,11 @@ __global__ void __launch_bounds__(256, 2)
   const Span3 F = a.fused;
   const int nx = a.nx, ny = a.ny, nz = a.nz, X = a.X, Y = a.Y;
   const int nkc = (F.k1 - F.k0 + a.tile_z - 1) / a.tile_z;
-  const int b = (int)blockIdx.z / nkc;
-  const int kc0 = F.k0 + ((int)blockIdx.z % nkc) * a.tile_z;
+  const int b = (int)bid.z / nkc;
+  const int kc0 = F.k0 + ((int)bid.z % nkc) * a.tile_z;
   const int kc1 = min(kc0 + a.tile_z, F.k1);
-  const int x0 = 4 * (F.q0 + (int)blockIdx.x * kFQ);
-  const int y0 = F.j0 + (int)blockIdx.y * kFY;
+  const int x0 = 4 * (F.q0 + (int)bid.x * kFQ);
+  const int y0 = F.j0 + (int)bid.y * kFY;
   if (kc1 <= kc0 || x0 >= 4 * F.q1 || y0 >= F.j1) return;
   const int ks = kc0 - 1;            // the plane below the chunk: H only, for the carry
   const int n_planes = kc1 - ks;     // planes of the march, ks .. kc1 - 1
@@ -331,15 +332,52 @@ __global__ void __launch_bounds__(256, 2)
   }
 }
 
+template <typename real, bool kMulti>
+__global__ void __launch_bounds__(256, 2)
+    fused_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ FusedMaps tm) {
+  fused_body<real, kMulti>(a, tm, blockIdx);
+}
+
+// Several engines' fused sweeps in one launch: engine e's arguments at A[e] and M[e].
+template <typename real, bool kMulti>
+__global__ void __launch_bounds__(256, 2)
+    fused_batch_kernel(const SweepArgs<real>* __restrict__ A, const FusedMaps* __restrict__ M, const BatchGrid G) {
+  __shared__ __align__(16) unsigned char args[sizeof(SweepArgs<real>)];
+  int e;
+  const uint3 bid = G.block(&e);
+  fused_body<real, kMulti>(stage_args(A + e, args), M[e], bid);
+}
+
 }  // namespace
 
 template <typename real>
-cudaError_t launch_fused_sweep(const SweepArgs<real>& a, const FusedMaps& m, cudaStream_t s) {
+cudaError_t fused_grid(const SweepArgs<real>& a, dim3* grid) {
   const Span3 F = a.fused;
+  *grid = dim3(0, 0, 0);
   if (F.q1 <= F.q0 || F.j1 <= F.j0 || F.k1 <= F.k0) return cudaSuccess;
   if (F.q0 % 2 != 0 || F.q0 < 2 || F.j0 < 2 || F.k0 < 2 || F.k1 > a.nz + 1) return cudaErrorInvalidValue;
   const int nkc = (F.k1 - F.k0 + a.tile_z - 1) / a.tile_z;
-  const dim3 grid((F.q1 - F.q0 + kFQ - 1) / kFQ, (F.j1 - F.j0 + kFY - 1) / kFY, nkc * a.B);
+  *grid = dim3((F.q1 - F.q0 + kFQ - 1) / kFQ, (F.j1 - F.j0 + kFY - 1) / kFY, nkc * a.B);
+  return cudaSuccess;
+}
+
+template <typename real>
+cudaError_t launch_fused_batch(const SweepArgs<real>* A, const FusedMaps* M, const BatchGrid& G, int blocks,
+                               bool multi_pole, cudaStream_t s) {
+  if (blocks <= 0) return cudaSuccess;
+  const size_t bytes = sizeof(FusedSmem<real>) + 128;
+  auto kern = multi_pole ? fused_batch_kernel<real, true> : fused_batch_kernel<real, false>;
+  const cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (err != cudaSuccess) return err;
+  kern<<<blocks, dim3(kFQ, kFY), bytes, s>>>(A, M, G);
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_fused_sweep(const SweepArgs<real>& a, const FusedMaps& m, cudaStream_t s) {
+  dim3 grid;
+  if (const cudaError_t e = fused_grid(a, &grid)) return e;
+  if (grid.x == 0) return cudaSuccess;
   const dim3 block(kFQ, kFY);
   const size_t bytes = sizeof(FusedSmem<real>) + 128;
   auto kern = a.ade_P > 1 ? fused_kernel<real, true> : fused_kernel<real, false>;
@@ -375,7 +413,9 @@ template <typename real>
 cudaError_t preload_fused() {
   cudaFuncAttributes fa;
   const void* fns[] = {reinterpret_cast<const void*>(fused_kernel<real, false>),
-                       reinterpret_cast<const void*>(fused_kernel<real, true>)};
+                       reinterpret_cast<const void*>(fused_kernel<real, true>),
+                       reinterpret_cast<const void*>(fused_batch_kernel<real, false>),
+                       reinterpret_cast<const void*>(fused_batch_kernel<real, true>)};
   for (const void* f : fns) {
     const cudaError_t err = cudaFuncGetAttributes(&fa, f);
     if (err != cudaSuccess) return err;
@@ -388,6 +428,12 @@ static_assert((kEW * sizeof(float)) % 16 == 0 && (kHW * sizeof(float)) % 16 == 0
 static_assert(sizeof(FusedSmem<float>) + 128 <= 113 * 1024, "two fused blocks per SM in float32");
 static_assert(sizeof(FusedSmem<double>) + 128 <= 227 * 1024, "one fused block per SM in float64");
 
+template cudaError_t fused_grid<float>(const SweepArgs<float>&, dim3*);
+template cudaError_t fused_grid<double>(const SweepArgs<double>&, dim3*);
+template cudaError_t launch_fused_batch<float>(const SweepArgs<float>*, const FusedMaps*, const BatchGrid&, int, bool,
+                                               cudaStream_t);
+template cudaError_t launch_fused_batch<double>(const SweepArgs<double>*, const FusedMaps*, const BatchGrid&, int,
+                                                bool, cudaStream_t);
 template cudaError_t launch_fused_sweep<float>(const SweepArgs<float>&, const FusedMaps&, cudaStream_t);
 template cudaError_t launch_fused_sweep<double>(const SweepArgs<double>&, const FusedMaps&, cudaStream_t);
 template bool encode_fused_maps<float>(const SweepArgs<float>&, FusedMaps*, std::string*);

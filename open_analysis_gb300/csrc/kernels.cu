@@ -81,25 +81,54 @@ __device__ void probe_block(const ProbeArgs<real>& a, int pid, int b, long long 
 }
 
 template <typename real>
-__global__ void __launch_bounds__(256) pre_e_kernel(const __grid_constant__ ProbeArgs<real> a, int off) {
+__device__ __forceinline__ void pre_e_body(const ProbeArgs<real>& a, int off, int block) {
   const long long step = *a.step_base + off;
   const int nprobe_blocks = a.n_kind[1] * a.B;
-  if ((int)blockIdx.x < nprobe_blocks) {
-    const int pi = blockIdx.x / a.B, b = blockIdx.x % a.B;
+  if (block < nprobe_blocks) {
+    const int pi = block / a.B, b = block % a.B;
     probe_block(a, a.list[1][pi], b, step, 0.5);
     return;
   }
-  const int t = (blockIdx.x - nprobe_blocks) * blockDim.x + threadIdx.x;
+  const int t = (block - nprobe_blocks) * blockDim.x + threadIdx.x;
   if (t >= a.n_def) return;
   const real* E = a.E[a.def_comp[t]];
   for (int b = 0; b < a.B; ++b) a.eold[(long long)b * a.n_def + t] = E[(long long)b * a.bs + a.def_flat[t]];
 }
 
 template <typename real>
-__global__ void __launch_bounds__(256) probe_e_kernel(const __grid_constant__ ProbeArgs<real> a, int off) {
+__global__ void __launch_bounds__(256) pre_e_kernel(const __grid_constant__ ProbeArgs<real> a, int off) {
+  pre_e_body(a, off, (int)blockIdx.x);
+}
+
+template <typename real>
+__device__ __forceinline__ void probe_e_body(const ProbeArgs<real>& a, int off, int block) {
   const long long step = *a.step_base + off;
-  const int pi = blockIdx.x / a.B, b = blockIdx.x % a.B;
+  const int pi = block / a.B, b = block % a.B;
   probe_block(a, a.list[0][pi], b, step, 1.0);
+}
+
+template <typename real>
+__global__ void __launch_bounds__(256) probe_e_kernel(const __grid_constant__ ProbeArgs<real> a, int off) {
+  probe_e_body(a, off, (int)blockIdx.x);
+}
+
+// Several engines' deferred-E saves and H-probe DFTs, and E-probe DFTs, in one launch each.
+template <typename real>
+__global__ void __launch_bounds__(256) pre_e_batch_kernel(const ProbeArgs<real>* __restrict__ A, const BatchGrid G,
+                                                          int off) {
+  __shared__ __align__(16) unsigned char args[sizeof(ProbeArgs<real>)];
+  int e;
+  const uint3 bid = G.block(&e);
+  pre_e_body(stage_args(A + e, args), off, (int)bid.x);
+}
+
+template <typename real>
+__global__ void __launch_bounds__(256) probe_e_batch_kernel(const ProbeArgs<real>* __restrict__ A, const BatchGrid G,
+                                                            int off) {
+  __shared__ __align__(16) unsigned char args[sizeof(ProbeArgs<real>)];
+  int e;
+  const uint3 bid = G.block(&e);
+  probe_e_body(stage_args(A + e, args), off, (int)bid.x);
 }
 
 // ----------------------------------------------------------------------------- surface impedance
@@ -107,8 +136,8 @@ __global__ void __launch_bounds__(256) probe_e_kernel(const __grid_constant__ Pr
 // H samples (reference.py:129-150). One thread per edge handles every batch member; BB and PP
 // unroll the batch and pole loops so all loads of an edge are issued together.
 template <typename real, int BB, int PP>
-__global__ void __launch_bounds__(128) sibc_kernel(const __grid_constant__ SibcArgs<real> a) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void sibc_body(const SibcArgs<real>& a, int block) {
+  const int s = block * blockDim.x + threadIdx.x;
   if (s >= a.n) return;
   const SibcEdge<real> ed = a.edge[s];
   const real* __restrict__ alpha = a.alpha + (long long)ed.mat * PP;
@@ -147,10 +176,15 @@ __global__ void __launch_bounds__(128) sibc_kernel(const __grid_constant__ SibcA
   }
 }
 
+template <typename real, int BB, int PP>
+__global__ void __launch_bounds__(128) sibc_kernel(const __grid_constant__ SibcArgs<real> a) {
+  sibc_body<real, BB, PP>(a, (int)blockIdx.x);
+}
+
 // Any batch size and pole count (loops not unrolled).
 template <typename real>
-__global__ void __launch_bounds__(128) sibc_generic_kernel(const __grid_constant__ SibcArgs<real> a) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void sibc_generic_body(const SibcArgs<real>& a, int block) {
+  const int s = block * blockDim.x + threadIdx.x;
   if (s >= a.n) return;
   const SibcEdge<real> ed = a.edge[s];
   const int B = a.B, P = a.P;
@@ -176,6 +210,48 @@ __global__ void __launch_bounds__(128) sibc_generic_kernel(const __grid_constant
 }
 
 template <typename real>
+__global__ void __launch_bounds__(128) sibc_generic_kernel(const __grid_constant__ SibcArgs<real> a) {
+  sibc_generic_body(a, (int)blockIdx.x);
+}
+
+// Several engines' surface-impedance updates in one launch (engines of one kernel variant).
+template <typename real, int BB, int PP>
+__global__ void __launch_bounds__(128) sibc_batch_kernel(const SibcArgs<real>* __restrict__ A, const BatchGrid G) {
+  __shared__ __align__(16) unsigned char args[sizeof(SibcArgs<real>)];
+  int e;
+  const uint3 bid = G.block(&e);
+  const SibcArgs<real>& a = stage_args(A + e, args);
+  if constexpr (BB == 0)
+    sibc_generic_body(a, (int)bid.x);
+  else
+    sibc_body<real, BB, PP>(a, (int)bid.x);
+}
+
+template <typename real>
+int sibc_variant(const SibcArgs<real>& a) {
+  return a.P == 16 && (a.B == 1 || a.B == 2 || a.B == 4) ? a.B : 0;
+}
+
+template <typename real>
+int sibc_blocks(const SibcArgs<real>& a) {
+  return (int)((a.n + 127) / 128);
+}
+
+template <typename real>
+cudaError_t launch_sibc_batch(const SibcArgs<real>* A, const BatchGrid& G, int blocks, int variant, cudaStream_t s) {
+  if (blocks <= 0) return cudaSuccess;
+  if (variant == 2)
+    sibc_batch_kernel<real, 2, 16><<<blocks, 128, 0, s>>>(A, G);
+  else if (variant == 1)
+    sibc_batch_kernel<real, 1, 16><<<blocks, 128, 0, s>>>(A, G);
+  else if (variant == 4)
+    sibc_batch_kernel<real, 4, 16><<<blocks, 128, 0, s>>>(A, G);
+  else
+    sibc_batch_kernel<real, 0, 16><<<blocks, 128, 0, s>>>(A, G);
+  return cudaGetLastError();
+}
+
+template <typename real>
 cudaError_t launch_sibc(const SibcArgs<real>& a, cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;
   const unsigned blocks = (unsigned)((a.n + 127) / 128);
@@ -194,8 +270,8 @@ cudaError_t launch_sibc(const SibcArgs<real>& a, cudaStream_t s) {
 // Injection (reference.py:223-234) and the Debye update of dispersive edges with injection
 // (reference.py:119-127), in the reference's order after the surface impedance.
 template <typename real>
-__global__ void __launch_bounds__(128) edge_kernel(const __grid_constant__ EdgeArgs<real> a, int off) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void edge_body(const EdgeArgs<real>& a, int off, int block) {
+  const int e = block * blockDim.x + threadIdx.x;
   if (e >= a.n) return;
   const long long step = *a.step_base + off;
   const int c = a.comp[e];
@@ -233,6 +309,21 @@ __global__ void __launch_bounds__(128) edge_kernel(const __grid_constant__ EdgeA
     }
     Ec[f] = val;
   }
+}
+
+template <typename real>
+__global__ void __launch_bounds__(128) edge_kernel(const __grid_constant__ EdgeArgs<real> a, int off) {
+  edge_body(a, off, (int)blockIdx.x);
+}
+
+// Several engines' injection passes in one launch.
+template <typename real>
+__global__ void __launch_bounds__(128) edge_batch_kernel(const EdgeArgs<real>* __restrict__ A, const BatchGrid G,
+                                                         int off) {
+  __shared__ __align__(16) unsigned char args[sizeof(EdgeArgs<real>)];
+  int e;
+  const uint3 bid = G.block(&e);
+  edge_body(stage_args(A + e, args), off, (int)bid.x);
 }
 
 // ----------------------------------------------------------------------------- energy
@@ -283,6 +374,11 @@ __global__ void energy_final_kernel(const double* partial, int nblocks, double* 
 
 __global__ void bump_kernel(long long* step_base, int n) { *step_base += n; }
 
+__global__ void bump_batch_kernel(long long* const* step_base, int n_eng, int n) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n_eng) *step_base[e] += n;
+}
+
 // ----------------------------------------------------------------------------- launchers
 static inline unsigned ceil_div(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
@@ -307,8 +403,44 @@ cudaError_t launch_ghosts(real* const H[3], int pmc_mask, int nx, int ny, int nz
 }
 
 template <typename real>
+int pre_e_blocks(const ProbeArgs<real>& a) {
+  return a.n_kind[1] * a.B + (int)ceil_div(a.n_def, 256);
+}
+
+template <typename real>
+int probe_e_blocks(const ProbeArgs<real>& a) {
+  return a.n_kind[0] * a.B;
+}
+
+template <typename real>
+int edge_blocks(const EdgeArgs<real>& a) {
+  return a.n == 0 ? 0 : (int)ceil_div(a.n, 128);
+}
+
+template <typename real>
+cudaError_t launch_pre_e_batch(const ProbeArgs<real>* A, const BatchGrid& G, int blocks, int off, cudaStream_t s) {
+  if (blocks <= 0) return cudaSuccess;
+  pre_e_batch_kernel<real><<<blocks, 256, 0, s>>>(A, G, off);
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_probe_e_batch(const ProbeArgs<real>* A, const BatchGrid& G, int blocks, int off, cudaStream_t s) {
+  if (blocks <= 0) return cudaSuccess;
+  probe_e_batch_kernel<real><<<blocks, 256, 0, s>>>(A, G, off);
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_edges_batch(const EdgeArgs<real>* A, const BatchGrid& G, int blocks, int off, cudaStream_t s) {
+  if (blocks <= 0) return cudaSuccess;
+  edge_batch_kernel<real><<<blocks, 128, 0, s>>>(A, G, off);
+  return cudaGetLastError();
+}
+
+template <typename real>
 cudaError_t launch_pre_e(const ProbeArgs<real>& a, int off, cudaStream_t s) {
-  const int blocks = a.n_kind[1] * a.B + (int)ceil_div(a.n_def, 256);
+  const int blocks = pre_e_blocks(a);
   if (blocks == 0) return cudaSuccess;
   pre_e_kernel<real><<<blocks, 256, 0, s>>>(a, off);
   return cudaGetLastError();
@@ -344,6 +476,12 @@ cudaError_t launch_bump(long long* step_base, int n, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+cudaError_t launch_bump_batch(long long* const* step_base, int n_eng, int n, cudaStream_t s) {
+  if (n_eng <= 0) return cudaSuccess;
+  bump_batch_kernel<<<(unsigned)ceil_div(n_eng, 128), 128, 0, s>>>(step_base, n_eng, n);
+  return cudaGetLastError();
+}
+
 #define OAFDTD_INSTANTIATE(real)                                                                   \
   template cudaError_t launch_ghosts<real>(real* const[3], int, int, int, int, int, int, int,      \
                                            cudaStream_t);                                           \
@@ -351,6 +489,19 @@ cudaError_t launch_bump(long long* step_base, int n, cudaStream_t s) {
   template cudaError_t launch_probe_e<real>(const ProbeArgs<real>&, int, cudaStream_t);            \
   template cudaError_t launch_edges<real>(const EdgeArgs<real>&, int, cudaStream_t);               \
   template cudaError_t launch_sibc<real>(const SibcArgs<real>&, cudaStream_t);                      \
+  template int pre_e_blocks<real>(const ProbeArgs<real>&);                                          \
+  template int probe_e_blocks<real>(const ProbeArgs<real>&);                                        \
+  template int edge_blocks<real>(const EdgeArgs<real>&);                                            \
+  template int sibc_blocks<real>(const SibcArgs<real>&);                                            \
+  template int sibc_variant<real>(const SibcArgs<real>&);                                           \
+  template cudaError_t launch_pre_e_batch<real>(const ProbeArgs<real>*, const BatchGrid&, int, int, \
+                                                cudaStream_t);                                      \
+  template cudaError_t launch_probe_e_batch<real>(const ProbeArgs<real>*, const BatchGrid&, int, int, \
+                                                  cudaStream_t);                                    \
+  template cudaError_t launch_edges_batch<real>(const EdgeArgs<real>*, const BatchGrid&, int, int,  \
+                                                cudaStream_t);                                      \
+  template cudaError_t launch_sibc_batch<real>(const SibcArgs<real>*, const BatchGrid&, int, int,   \
+                                               cudaStream_t);                                       \
   template cudaError_t preload_kernels<real>();                                                     \
   template cudaError_t launch_energy<real>(const EnergyArgs<real>&, double*, int, double*,         \
                                            cudaStream_t);
@@ -370,6 +521,14 @@ cudaError_t preload_kernels() {
       reinterpret_cast<const void*>(energy_kernel<real>),
       reinterpret_cast<const void*>(energy_final_kernel),
       reinterpret_cast<const void*>(bump_kernel),
+      reinterpret_cast<const void*>(bump_batch_kernel),
+      reinterpret_cast<const void*>(pre_e_batch_kernel<real>),
+      reinterpret_cast<const void*>(probe_e_batch_kernel<real>),
+      reinterpret_cast<const void*>(sibc_batch_kernel<real, 2, 16>),
+      reinterpret_cast<const void*>(sibc_batch_kernel<real, 1, 16>),
+      reinterpret_cast<const void*>(sibc_batch_kernel<real, 4, 16>),
+      reinterpret_cast<const void*>(sibc_batch_kernel<real, 0, 16>),
+      reinterpret_cast<const void*>(edge_batch_kernel<real>),
   };
   for (const void* f : fns) {
     const cudaError_t err = cudaFuncGetAttributes(&fa, f);

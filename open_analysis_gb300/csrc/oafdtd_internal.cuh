@@ -226,6 +226,87 @@ struct EnergyArgs {
   int X, Y, Z, B;
 };
 
+// Launch geometry of the slab kernel: the boxes of one kind with their first block.
+struct SlabLaunch {
+  Span3 box[6];
+  int n;
+  int first[7];  // first block of each box; first[n] = total blocks
+  int cblk[6];   // column blocks per (box, chunk, member)
+  int nch[6];    // z chunks per box
+};
+
+// The blocks of one launch that covers several engines (a batched sweep): block b of the launch
+// is block (x, y, z) = (blk[b].y, blk[b].z, blk[b].w) of engine blk[b].x in that engine's own
+// grid (one 16-byte load per block). The per-engine arguments sit in device arrays indexed by
+// the engine.
+struct BatchGrid {
+  const int4* blk;
+#ifdef __CUDACC__
+  __device__ __forceinline__ uint3 block(int* e) const {
+    const int4 t = __ldg(blk + blockIdx.x);
+    *e = t.x;
+    return make_uint3((unsigned)t.y, (unsigned)t.z, (unsigned)t.w);
+  }
+#endif
+};
+
+#ifdef __CUDACC__
+// A batched kernel's arguments of this block's engine, copied once per block from device memory
+// into shared memory (buf: sizeof(T) bytes, 16-byte aligned), so that the kernel body reads them
+// as cheaply as launch parameters instead of holding them in registers.
+template <typename T>
+__device__ __forceinline__ const T& stage_args(const T* __restrict__ src, unsigned char* buf) {
+  static_assert(sizeof(T) % 4 == 0, "argument blocks are whole words");
+  const int* s = reinterpret_cast<const int*>(src);
+  int* d = reinterpret_cast<int*>(buf);
+  const int tid = (int)(threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z));
+  const int nt = (int)(blockDim.x * blockDim.y * blockDim.z);
+  for (int i = tid; i < (int)(sizeof(T) / 4); i += nt) d[i] = __ldg(s + i);
+  __syncthreads();
+  return *reinterpret_cast<const T*>(buf);
+}
+#endif
+
+// Per-engine launch grids of the step's kernel classes (the single launchers use the same), and
+// the batched launchers: one launch of a class over the blocks of every engine in G, the
+// arguments of engine e at A[e] (and M[e], L[e]) in device memory. A grid with no blocks is empty.
+template <typename real>
+cudaError_t fused_grid(const SweepArgs<real>& a, dim3* grid);
+template <typename real>
+cudaError_t staged_grids(const SweepArgs<real>& a, int kind, dim3* inner, dim3* z);
+template <typename real>
+cudaError_t slab_plan(const SweepArgs<real>& a, int kind, SlabLaunch* L, long long* blocks);
+template <typename real>
+int pre_e_blocks(const ProbeArgs<real>& a);
+template <typename real>
+int probe_e_blocks(const ProbeArgs<real>& a);
+template <typename real>
+int edge_blocks(const EdgeArgs<real>& a);
+template <typename real>
+int sibc_blocks(const SibcArgs<real>& a);
+// the SIBC kernel variant of an engine: 0 generic, else the unrolled batch size (poles 16)
+template <typename real>
+int sibc_variant(const SibcArgs<real>& a);
+template <typename real>
+cudaError_t launch_fused_batch(const SweepArgs<real>* A, const FusedMaps* M, const BatchGrid& G, int blocks,
+                               bool multi_pole, cudaStream_t s);
+template <typename real>
+cudaError_t launch_staged_batch(const SweepArgs<real>* A, const SweepMaps* M, const BatchGrid& G, int blocks, bool h,
+                                bool tma, bool z, bool multi_pole, cudaStream_t s);
+template <typename real>
+cudaError_t launch_slab_batch(const SweepArgs<real>* A, const SlabLaunch* L, const BatchGrid& G, int blocks, int kind,
+                              bool multi_pole, cudaStream_t s);
+template <typename real>
+cudaError_t launch_pre_e_batch(const ProbeArgs<real>* A, const BatchGrid& G, int blocks, int off, cudaStream_t s);
+template <typename real>
+cudaError_t launch_probe_e_batch(const ProbeArgs<real>* A, const BatchGrid& G, int blocks, int off, cudaStream_t s);
+template <typename real>
+cudaError_t launch_edges_batch(const EdgeArgs<real>* A, const BatchGrid& G, int blocks, int off, cudaStream_t s);
+template <typename real>
+cudaError_t launch_sibc_batch(const SibcArgs<real>* A, const BatchGrid& G, int blocks, int variant, cudaStream_t s);
+// step_base[e] += n for the n_eng engines' device step counters (an array of device pointers)
+cudaError_t launch_bump_batch(long long* const* step_base, int n_eng, int n, cudaStream_t s);
+
 // kernel launchers (kernels.cu)
 template <typename real>
 cudaError_t launch_h_sweep(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_t s);

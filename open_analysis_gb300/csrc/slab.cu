@@ -30,14 +30,6 @@ constexpr int kSlabThreads = 256;
 // give the kernel enough independent threads to hide its load latency.
 constexpr int kSlabPlanes = 4;
 
-// Launch geometry: the boxes of one kind with their first block.
-struct SlabLaunch {
-  Span3 box[6];
-  int n;
-  int first[7];  // first block of each box; first[n] = total blocks
-  int cblk[6];   // column blocks per (box, chunk, member)
-  int nch[6];    // z chunks per box
-};
 
 template <typename real>
 __device__ __forceinline__ long long psi_index(const CpmlSide<real>& s, int ax, int b, int k, int j, int i, int X,
@@ -137,8 +129,8 @@ struct SlabWork {
   bool live;
 };
 
-__device__ __forceinline__ SlabWork slab_work(const SlabLaunch& L, int nx) {
-  const int blk = (int)blockIdx.x / 3;
+__device__ __forceinline__ SlabWork slab_work(const SlabLaunch& L, int nx, int block) {
+  const int blk = block / 3;
   int s = 0;
   while (s + 1 < L.n && blk >= L.first[s + 1]) ++s;
   const Span3 bx = L.box[s];
@@ -147,7 +139,7 @@ __device__ __forceinline__ SlabWork slab_work(const SlabLaunch& L, int nx) {
   r /= L.cblk[s];
   const int ch = r % L.nch[s];
   SlabWork w;
-  w.comp = (int)blockIdx.x % 3;
+  w.comp = block % 3;
   w.b = r / L.nch[s];
   const int nq = bx.q1 - bx.q0;
   const int col = cb * kSlabThreads + (int)threadIdx.x;
@@ -292,9 +284,8 @@ __device__ __forceinline__ void slab_e_column(const SweepArgs<real>& a, const Sl
 }
 
 template <typename real, bool kMulti>
-__global__ void __launch_bounds__(kSlabThreads, 3)
-    slab_e_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SlabLaunch L) {
-  const SlabWork w = slab_work(L, a.nx);
+__device__ __forceinline__ void slab_e_body(const SweepArgs<real>& a, const SlabLaunch& L, int block) {
+  const SlabWork w = slab_work(L, a.nx, block);
   if (!w.live || w.k0 >= w.k1) return;
   if (w.comp == 0)
     slab_e_column<real, 0, kMulti>(a, w);
@@ -302,6 +293,24 @@ __global__ void __launch_bounds__(kSlabThreads, 3)
     slab_e_column<real, 1, kMulti>(a, w);
   else
     slab_e_column<real, 2, kMulti>(a, w);
+}
+
+template <typename real, bool kMulti>
+__global__ void __launch_bounds__(kSlabThreads, 3)
+    slab_e_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SlabLaunch L) {
+  slab_e_body<real, kMulti>(a, L, (int)blockIdx.x);
+}
+
+// Several engines' E slab updates in one launch: engine e's arguments at A[e] and L[e].
+template <typename real, bool kMulti>
+__global__ void __launch_bounds__(kSlabThreads, 3)
+    slab_e_batch_kernel(const SweepArgs<real>* __restrict__ A, const SlabLaunch* __restrict__ L, const BatchGrid G) {
+  __shared__ __align__(16) unsigned char args[sizeof(SweepArgs<real>)];
+  __shared__ __align__(16) unsigned char launch[sizeof(SlabLaunch)];
+  int e;
+  const uint3 bid = G.block(&e);
+  const SlabLaunch& l = stage_args(L + e, launch);
+  slab_e_body<real, kMulti>(stage_args(A + e, args), l, (int)bid.x);
 }
 
 // ------------------------------------------------------------------------------------- H
@@ -392,9 +401,8 @@ __device__ __forceinline__ void slab_h_column(const SweepArgs<real>& a, const Sl
 }
 
 template <typename real>
-__global__ void __launch_bounds__(kSlabThreads, 4)
-    slab_h_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SlabLaunch L) {
-  const SlabWork w = slab_work(L, a.nx);
+__device__ __forceinline__ void slab_h_body(const SweepArgs<real>& a, const SlabLaunch& L, int block) {
+  const SlabWork w = slab_work(L, a.nx, block);
   if (!w.live || w.k0 >= w.k1) return;
   if (w.comp == 0)
     slab_h_column<real, 0>(a, w);
@@ -404,32 +412,74 @@ __global__ void __launch_bounds__(kSlabThreads, 4)
     slab_h_column<real, 2>(a, w);
 }
 
+template <typename real>
+__global__ void __launch_bounds__(kSlabThreads, 4)
+    slab_h_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SlabLaunch L) {
+  slab_h_body<real>(a, L, (int)blockIdx.x);
+}
+
+// Several engines' H slab updates in one launch.
+template <typename real>
+__global__ void __launch_bounds__(kSlabThreads, 4)
+    slab_h_batch_kernel(const SweepArgs<real>* __restrict__ A, const SlabLaunch* __restrict__ L, const BatchGrid G) {
+  __shared__ __align__(16) unsigned char args[sizeof(SweepArgs<real>)];
+  __shared__ __align__(16) unsigned char launch[sizeof(SlabLaunch)];
+  int e;
+  const uint3 bid = G.block(&e);
+  const SlabLaunch& l = stage_args(L + e, launch);
+  slab_h_body<real>(stage_args(A + e, args), l, (int)bid.x);
+}
+
 // ------------------------------------------------------------------------------------- launch
 template <typename real>
-cudaError_t launch_slab(const SweepArgs<real>& a, int kind, cudaStream_t s) {
-  SlabLaunch L{};
-  L.n = 0;
+cudaError_t slab_plan(const SweepArgs<real>& a, int kind, SlabLaunch* L, long long* blocks) {
+  *L = SlabLaunch{};
+  L->n = 0;
+  *blocks = 0;
   long long total = 0;
   for (int n = 0; n < a.n_slab[kind]; ++n) {
     const Span3& bx = a.slab[kind][n];
     const long long cols = (long long)(bx.q1 - bx.q0) * (bx.j1 - bx.j0);
     if (cols <= 0 || bx.k1 <= bx.k0) continue;
-    L.box[L.n] = bx;
-    L.first[L.n] = (int)total;
-    L.cblk[L.n] = (int)((cols + kSlabThreads - 1) / kSlabThreads);
-    L.nch[L.n] = (bx.k1 - bx.k0 + kSlabPlanes - 1) / kSlabPlanes;
-    total += (long long)L.cblk[L.n] * L.nch[L.n] * a.B;
-    ++L.n;
+    L->box[L->n] = bx;
+    L->first[L->n] = (int)total;
+    L->cblk[L->n] = (int)((cols + kSlabThreads - 1) / kSlabThreads);
+    L->nch[L->n] = (bx.k1 - bx.k0 + kSlabPlanes - 1) / kSlabPlanes;
+    total += (long long)L->cblk[L->n] * L->nch[L->n] * a.B;
+    ++L->n;
   }
-  if (L.n == 0) return cudaSuccess;
+  if (L->n == 0) return cudaSuccess;
   if (3 * total > 2147483647LL) return cudaErrorInvalidConfiguration;
-  L.first[L.n] = (int)total;
+  L->first[L->n] = (int)total;
+  *blocks = 3 * total;  // one block per component of every column block
+  return cudaSuccess;
+}
+
+template <typename real>
+cudaError_t launch_slab(const SweepArgs<real>& a, int kind, cudaStream_t s) {
+  SlabLaunch L;
+  long long blocks = 0;
+  if (const cudaError_t e = slab_plan(a, kind, &L, &blocks)) return e;
+  if (blocks == 0) return cudaSuccess;
   if (kind == 0 && a.ade_P > 1)
-    slab_e_kernel<real, true><<<(unsigned)(3 * total), kSlabThreads, 0, s>>>(a, L);
+    slab_e_kernel<real, true><<<(unsigned)blocks, kSlabThreads, 0, s>>>(a, L);
   else if (kind == 0)
-    slab_e_kernel<real, false><<<(unsigned)(3 * total), kSlabThreads, 0, s>>>(a, L);
+    slab_e_kernel<real, false><<<(unsigned)blocks, kSlabThreads, 0, s>>>(a, L);
   else
-    slab_h_kernel<real><<<(unsigned)(3 * total), kSlabThreads, 0, s>>>(a, L);
+    slab_h_kernel<real><<<(unsigned)blocks, kSlabThreads, 0, s>>>(a, L);
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_slab_batch(const SweepArgs<real>* A, const SlabLaunch* L, const BatchGrid& G, int blocks, int kind,
+                              bool multi_pole, cudaStream_t s) {
+  if (blocks <= 0) return cudaSuccess;
+  if (kind == 0 && multi_pole)
+    slab_e_batch_kernel<real, true><<<blocks, kSlabThreads, 0, s>>>(A, L, G);
+  else if (kind == 0)
+    slab_e_batch_kernel<real, false><<<blocks, kSlabThreads, 0, s>>>(A, L, G);
+  else
+    slab_h_batch_kernel<real><<<blocks, kSlabThreads, 0, s>>>(A, L, G);
   return cudaGetLastError();
 }
 
@@ -440,6 +490,9 @@ cudaError_t preload_slab() {
       reinterpret_cast<const void*>(slab_e_kernel<real, false>),
       reinterpret_cast<const void*>(slab_e_kernel<real, true>),
       reinterpret_cast<const void*>(slab_h_kernel<real>),
+      reinterpret_cast<const void*>(slab_e_batch_kernel<real, false>),
+      reinterpret_cast<const void*>(slab_e_batch_kernel<real, true>),
+      reinterpret_cast<const void*>(slab_h_batch_kernel<real>),
   };
   for (const void* f : fns) {
     const cudaError_t err = cudaFuncGetAttributes(&fa, f);
@@ -450,6 +503,12 @@ cudaError_t preload_slab() {
 
 template cudaError_t preload_slab<float>();
 template cudaError_t preload_slab<double>();
+template cudaError_t slab_plan<float>(const SweepArgs<float>&, int, SlabLaunch*, long long*);
+template cudaError_t slab_plan<double>(const SweepArgs<double>&, int, SlabLaunch*, long long*);
+template cudaError_t launch_slab_batch<float>(const SweepArgs<float>*, const SlabLaunch*, const BatchGrid&, int, int,
+                                              bool, cudaStream_t);
+template cudaError_t launch_slab_batch<double>(const SweepArgs<double>*, const SlabLaunch*, const BatchGrid&, int, int,
+                                               bool, cudaStream_t);
 template cudaError_t launch_slab<float>(const SweepArgs<float>&, int, cudaStream_t);
 template cudaError_t launch_slab<double>(const SweepArgs<double>&, int, cudaStream_t);
 

@@ -57,11 +57,11 @@ struct BlockSpan {
 };
 
 template <typename real, bool kZ>
-__device__ __forceinline__ BlockSpan block_span(const SweepArgs<real>& a, int kind) {
+__device__ __forceinline__ BlockSpan block_span(const SweepArgs<real>& a, int kind, const uint3 bid) {
   BlockSpan s;
   if (kZ) {
-    s.zr = (int)blockIdx.z & 1;
-    s.b = (int)blockIdx.z >> 1;
+    s.zr = (int)bid.z & 1;
+    s.b = (int)bid.z >> 1;
     s.box = a.zin[kind][s.zr];
     s.k0 = s.box.k0;
     s.k1 = s.box.k1;
@@ -69,13 +69,13 @@ __device__ __forceinline__ BlockSpan block_span(const SweepArgs<real>& a, int ki
     s.zr = 0;
     s.box = a.inner[kind];
     const int nkc = (s.box.k1 - s.box.k0 + a.tile_z - 1) / a.tile_z;
-    s.b = (int)blockIdx.z / nkc;
-    const int kc = (int)blockIdx.z % nkc;
+    s.b = (int)bid.z / nkc;
+    const int kc = (int)bid.z % nkc;
     s.k0 = s.box.k0 + kc * a.tile_z;
     s.k1 = min(s.k0 + a.tile_z, s.box.k1);
   }
-  s.x0 = 4 * (s.box.q0 + (int)blockIdx.x * kTQ);
-  s.y0 = s.box.j0 + (int)blockIdx.y * kTY;
+  s.x0 = 4 * (s.box.q0 + (int)bid.x * kTQ);
+  s.y0 = s.box.j0 + (int)bid.y * kTY;
   s.empty = s.k1 <= s.k0 || s.x0 >= 4 * s.box.q1 || s.y0 >= s.box.j1;
   return s;
 }
@@ -190,8 +190,7 @@ __device__ __forceinline__ void h_issue(const SweepArgs<real>& a, const SweepMap
 }
 
 template <typename real, bool kTma, bool kZ>
-__global__ void __launch_bounds__(256, 2)
-    h_staged_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SweepMaps tm) {
+__device__ __forceinline__ void h_staged_body(const SweepArgs<real>& a, const SweepMaps& tm, const uint3 bid) {
   constexpr int S = stages<false, kZ>();
   extern __shared__ unsigned char smem_raw[];
   __shared__ unsigned long long bar[S];
@@ -199,7 +198,7 @@ __global__ void __launch_bounds__(256, 2)
   const int tx = threadIdx.x, ty = threadIdx.y;
   const bool leader = tx == 0 && ty == 0;
   const int nx = a.nx, ny = a.ny, nz = a.nz, X = a.X, Y = a.Y, Z = nz + 2;
-  const BlockSpan sp = block_span<real, kZ>(a, 1);
+  const BlockSpan sp = block_span<real, kZ>(a, 1, bid);
   if (sp.empty) return;
   const int x0 = sp.x0, y0 = sp.y0, b = sp.b, zr = sp.zr, k0 = sp.k0, k1 = sp.k1;
   const int n_stage = k1 < Z ? k1 - k0 + 1 : k1 - k0;
@@ -313,6 +312,22 @@ __global__ void __launch_bounds__(256, 2)
   if (!kTma) cp_wait<0>();
 }
 
+template <typename real, bool kTma, bool kZ>
+__global__ void __launch_bounds__(256, 2)
+    h_staged_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SweepMaps tm) {
+  h_staged_body<real, kTma, kZ>(a, tm, blockIdx);
+}
+
+// Several engines' H sweeps in one launch: engine e's arguments at A[e] and M[e].
+template <typename real, bool kTma, bool kZ>
+__global__ void __launch_bounds__(256, 2)
+    h_staged_batch_kernel(const SweepArgs<real>* __restrict__ A, const SweepMaps* __restrict__ M, const BatchGrid G) {
+  __shared__ __align__(16) unsigned char args[sizeof(SweepArgs<real>)];
+  int e;
+  const uint3 bid = G.block(&e);
+  h_staged_body<real, kTma, kZ>(stage_args(A + e, args), M[e], bid);
+}
+
 // ------------------------------------------------------------------------------------- E sweep
 // Slot: H[3] rows y0-1..y0+7, x0-4..x0+127; E[3] and mat[3] rows y0..y0+7, x0..x0+127; z sweeps
 // also the psi of Ex and Ey.
@@ -392,8 +407,7 @@ __device__ __forceinline__ void j_prefetch(const SweepArgs<real>& a, Quad<real> 
 }
 
 template <typename real, bool kTma, bool kZ, bool kMulti>
-__global__ void __launch_bounds__(256, 2)
-    e_staged_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SweepMaps tm) {
+__device__ __forceinline__ void e_staged_body(const SweepArgs<real>& a, const SweepMaps& tm, const uint3 bid) {
   constexpr int S = stages<true, kZ>();
   extern __shared__ unsigned char smem_raw[];
   __shared__ unsigned long long bar[S];
@@ -401,7 +415,7 @@ __global__ void __launch_bounds__(256, 2)
   const int tx = threadIdx.x, ty = threadIdx.y;
   const bool leader = tx == 0 && ty == 0;
   const int nx = a.nx, X = a.X, Y = a.Y;
-  const BlockSpan sp = block_span<real, kZ>(a, 0);
+  const BlockSpan sp = block_span<real, kZ>(a, 0, bid);
   if (sp.empty) return;
   const int x0 = sp.x0, y0 = sp.y0, b = sp.b, zr = sp.zr, k0 = sp.k0, k1 = sp.k1;
   const int n_stage = k1 - k0;
@@ -514,6 +528,22 @@ __global__ void __launch_bounds__(256, 2)
   if (!kTma) cp_wait<0>();
 }
 
+template <typename real, bool kTma, bool kZ, bool kMulti>
+__global__ void __launch_bounds__(256, 2)
+    e_staged_kernel(const __grid_constant__ SweepArgs<real> a, const __grid_constant__ SweepMaps tm) {
+  e_staged_body<real, kTma, kZ, kMulti>(a, tm, blockIdx);
+}
+
+// Several engines' E sweeps in one launch: engine e's arguments at A[e] and M[e].
+template <typename real, bool kTma, bool kZ, bool kMulti>
+__global__ void __launch_bounds__(256, 2)
+    e_staged_batch_kernel(const SweepArgs<real>* __restrict__ A, const SweepMaps* __restrict__ M, const BatchGrid G) {
+  __shared__ __align__(16) unsigned char args[sizeof(SweepArgs<real>)];
+  int e;
+  const uint3 bid = G.block(&e);
+  e_staged_body<real, kTma, kZ, kMulti>(stage_args(A + e, args), M[e], bid);
+}
+
 // ------------------------------------------------------------------------------------- launch
 template <typename real, bool kTma, bool kZ>
 cudaError_t launch_one(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_t s, bool h, dim3 grid) {
@@ -536,37 +566,76 @@ cudaError_t launch_one(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_
 }
 
 template <typename real>
-cudaError_t launch_staged_sweep(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_t s, bool h) {
-  const int kind = h ? 1 : 0;
-  const bool tma = a.staged == 2;
+cudaError_t staged_grids(const SweepArgs<real>& a, int kind, dim3* inner, dim3* z) {
   // Every TMA box starts at x = 4 (q0 + 32 n) (the E sweep's halo box 4 cells earlier, which may
   // be -4: a load may start before the grid): a multiple of 8 cells keeps the start 16-byte
   // aligned for the 2-byte index boxes too.
+  *inner = dim3(0, 0, 0);
+  *z = dim3(0, 0, 0);
   const Span3 in = a.inner[kind];
   if (in.q1 > in.q0 && in.j1 > in.j0 && in.k1 > in.k0) {
     if (in.q0 % 2 != 0) return cudaErrorInvalidValue;
     const int nkc = (in.k1 - in.k0 + a.tile_z - 1) / a.tile_z;
-    const dim3 grid((in.q1 - in.q0 + kTQ - 1) / kTQ, (in.j1 - in.j0 + kTY - 1) / kTY, nkc * a.B);
-    const cudaError_t err = tma ? launch_one<real, true, false>(a, m, s, h, grid)
-                                : launch_one<real, false, false>(a, m, s, h, grid);
-    if (err != cudaSuccess) return err;
+    *inner = dim3((in.q1 - in.q0 + kTQ - 1) / kTQ, (in.j1 - in.j0 + kTY - 1) / kTY, nkc * a.B);
   }
   // the z-slab planes over the same x-y extent: one block per tile, member and side
   int nq = 0, nj = 0;
   for (int zr = 0; zr < 2; ++zr) {
-    const Span3& z = a.zin[kind][zr];
-    if (z.k1 <= z.k0 || z.q1 <= z.q0 || z.j1 <= z.j0) continue;
-    if (z.q0 % 2 != 0) return cudaErrorInvalidValue;
-    nq = max(nq, z.q1 - z.q0);
-    nj = max(nj, z.j1 - z.j0);
+    const Span3& zb = a.zin[kind][zr];
+    if (zb.k1 <= zb.k0 || zb.q1 <= zb.q0 || zb.j1 <= zb.j0) continue;
+    if (zb.q0 % 2 != 0) return cudaErrorInvalidValue;
+    nq = max(nq, zb.q1 - zb.q0);
+    nj = max(nj, zb.j1 - zb.j0);
   }
-  if (nq > 0 && nj > 0) {
-    const dim3 grid((nq + kTQ - 1) / kTQ, (nj + kTY - 1) / kTY, 2 * a.B);
-    const cudaError_t err = tma ? launch_one<real, true, true>(a, m, s, h, grid)
-                                : launch_one<real, false, true>(a, m, s, h, grid);
+  if (nq > 0 && nj > 0) *z = dim3((nq + kTQ - 1) / kTQ, (nj + kTY - 1) / kTY, 2 * a.B);
+  return cudaSuccess;
+}
+
+template <typename real>
+cudaError_t launch_staged_sweep(const SweepArgs<real>& a, const SweepMaps& m, cudaStream_t s, bool h) {
+  const bool tma = a.staged == 2;
+  dim3 inner, z;
+  if (const cudaError_t e = staged_grids(a, h ? 1 : 0, &inner, &z)) return e;
+  if (inner.x > 0) {
+    const cudaError_t err = tma ? launch_one<real, true, false>(a, m, s, h, inner)
+                                : launch_one<real, false, false>(a, m, s, h, inner);
+    if (err != cudaSuccess) return err;
+  }
+  if (z.x > 0) {
+    const cudaError_t err = tma ? launch_one<real, true, true>(a, m, s, h, z) : launch_one<real, false, true>(a, m, s, h, z);
     if (err != cudaSuccess) return err;
   }
   return cudaSuccess;
+}
+
+template <typename real, bool kTma, bool kZ>
+cudaError_t launch_batch_one(const SweepArgs<real>* A, const SweepMaps* M, const BatchGrid& G, int blocks, bool h,
+                             bool multi_pole, cudaStream_t s) {
+  const dim3 block(kTQ, kTY);
+  if (h) {
+    const size_t bytes = sizeof(HSlot<real, kZ>) * stages<false, kZ>() + 128;
+    auto kern = h_staged_batch_kernel<real, kTma, kZ>;
+    const cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (err != cudaSuccess) return err;
+    kern<<<blocks, block, bytes, s>>>(A, M, G);
+  } else {
+    const size_t bytes = sizeof(ESlot<real, kZ>) * stages<true, kZ>() + 128;
+    auto kern = multi_pole ? e_staged_batch_kernel<real, kTma, kZ, true> : e_staged_batch_kernel<real, kTma, kZ, false>;
+    const cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (err != cudaSuccess) return err;
+    kern<<<blocks, block, bytes, s>>>(A, M, G);
+  }
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_staged_batch(const SweepArgs<real>* A, const SweepMaps* M, const BatchGrid& G, int blocks, bool h,
+                                bool tma, bool z, bool multi_pole, cudaStream_t s) {
+  if (blocks <= 0) return cudaSuccess;
+  if (tma) return z ? launch_batch_one<real, true, true>(A, M, G, blocks, h, multi_pole, s)
+                    : launch_batch_one<real, true, false>(A, M, G, blocks, h, multi_pole, s);
+  return z ? launch_batch_one<real, false, true>(A, M, G, blocks, h, multi_pole, s)
+           : launch_batch_one<real, false, false>(A, M, G, blocks, h, multi_pole, s);
 }
 
 // ------------------------------------------------------------------------------- descriptors
@@ -667,6 +736,18 @@ cudaError_t preload_staged() {
       reinterpret_cast<const void*>(e_staged_kernel<real, true, true, true>),
       reinterpret_cast<const void*>(e_staged_kernel<real, false, false, true>),
       reinterpret_cast<const void*>(e_staged_kernel<real, false, true, true>),
+      reinterpret_cast<const void*>(h_staged_batch_kernel<real, true, false>),
+      reinterpret_cast<const void*>(h_staged_batch_kernel<real, true, true>),
+      reinterpret_cast<const void*>(h_staged_batch_kernel<real, false, false>),
+      reinterpret_cast<const void*>(h_staged_batch_kernel<real, false, true>),
+      reinterpret_cast<const void*>(e_staged_batch_kernel<real, true, false, false>),
+      reinterpret_cast<const void*>(e_staged_batch_kernel<real, true, true, false>),
+      reinterpret_cast<const void*>(e_staged_batch_kernel<real, false, false, false>),
+      reinterpret_cast<const void*>(e_staged_batch_kernel<real, false, true, false>),
+      reinterpret_cast<const void*>(e_staged_batch_kernel<real, true, false, true>),
+      reinterpret_cast<const void*>(e_staged_batch_kernel<real, true, true, true>),
+      reinterpret_cast<const void*>(e_staged_batch_kernel<real, false, false, true>),
+      reinterpret_cast<const void*>(e_staged_batch_kernel<real, false, true, true>),
   };
   for (const void* f : fns) {
     const cudaError_t err = cudaFuncGetAttributes(&fa, f);
@@ -677,6 +758,12 @@ cudaError_t preload_staged() {
 
 template cudaError_t preload_staged<float>();
 template cudaError_t preload_staged<double>();
+template cudaError_t staged_grids<float>(const SweepArgs<float>&, int, dim3*, dim3*);
+template cudaError_t staged_grids<double>(const SweepArgs<double>&, int, dim3*, dim3*);
+template cudaError_t launch_staged_batch<float>(const SweepArgs<float>*, const SweepMaps*, const BatchGrid&, int, bool,
+                                                bool, bool, bool, cudaStream_t);
+template cudaError_t launch_staged_batch<double>(const SweepArgs<double>*, const SweepMaps*, const BatchGrid&, int,
+                                                 bool, bool, bool, bool, cudaStream_t);
 template cudaError_t launch_staged_sweep<float>(const SweepArgs<float>&, const SweepMaps&, cudaStream_t, bool);
 template cudaError_t launch_staged_sweep<double>(const SweepArgs<double>&, const SweepMaps&, cudaStream_t, bool);
 template bool encode_sweep_maps<float>(const SweepArgs<float>&, SweepMaps*, std::string*);

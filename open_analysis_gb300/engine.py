@@ -387,6 +387,12 @@ class Gb300Engine:
         the interior, 2 staged by TMA, 1 staged by cp.async, 0 register marching, -1 keeps)."""
         native.check(self._lib.oafdtd_set_tuning(self._h, int(tile_z), int(variant)), "set_tuning")
 
+    def get_tuning(self) -> tuple[int, int]:
+        """The current launch shape: (planes per block, sweep variant)."""
+        tz, v = C.c_int32(), C.c_int32()
+        native.check(self._lib.oafdtd_get_tuning(self._h, C.byref(tz), C.byref(v)), "get_tuning")
+        return int(tz.value), int(v.value)
+
     def set_profiling(self, on: bool) -> None:
         native.check(self._lib.oafdtd_set_profiling(self._h, int(bool(on))), "set_profiling")
 

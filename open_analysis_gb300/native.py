@@ -189,6 +189,12 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "oafdtd_peak_bytes": (C.c_int, [C.c_void_p, _pi64]),
     "oafdtd_set_graph": (C.c_int, [C.c_void_p, _i32]),
     "oafdtd_set_tuning": (C.c_int, [C.c_void_p, _i32, _i32]),
+    "oafdtd_get_tuning": (C.c_int, [C.c_void_p, _pi32, _pi32]),
+    "oafdtd_batch_create": (C.c_int, [C.POINTER(C.c_void_p), _i32, C.POINTER(C.c_void_p)]),
+    "oafdtd_batch_step_async": (C.c_int, [C.c_void_p, _i64]),
+    "oafdtd_batch_wait": (C.c_int, [C.c_void_p]),
+    "oafdtd_batch_graph_kernels": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "oafdtd_batch_destroy": (C.c_int, [C.c_void_p]),
     "oafdtd_set_profiling": (C.c_int, [C.c_void_p, _i32]),
     "oafdtd_kernel_times": (C.c_int, [C.c_void_p, _pd, _i32]),
     "oafdtd_model_bytes": (C.c_int, [C.c_void_p, _pd]),

@@ -122,3 +122,98 @@ def test_batched_mode_port_sweep_equals_looped(tmp_path) -> None:  # type: ignor
     for fa, fb in zip(a.extra["wire"], b.extra["wire"], strict=True):
         with np.load(fa["wire"]) as za, np.load(fb["wire"]) as zb:
             assert np.array_equal(za["s"], zb["s"])
+
+
+def _small_instances(n: int, seed: int = 11):  # type: ignore[no-untyped-def]
+    params = sweep_params(n, seed=seed)
+    small = [p.__class__(**{**p.__dict__, "nx": p.nx // 2, "ny": p.ny // 2, "nz": p.nz // 2 + 8}) for p in params]
+    return [line_instance(p, n_freq=16) for p in small]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("steps", [150, 71])
+def test_engine_batch_fields_equal_engines_stepped_alone(steps: int) -> None:
+    """The native batch (one launch per kernel class over all instances) against every engine
+    stepped on its own: all six fields, the probe DFTs and the energy bit for bit. The instances
+    differ in size and in sweep variant (fused, TMA-staged, register marching, one tile height
+    each), so the batch splits into one native batch per variant; 150 steps take two graph
+    chunks and 22 eager steps (an even and an odd count leave the fused variant's buffers
+    swapped differently)."""
+    from open_analysis_gb300.batch import EngineBatch, compile_all
+    from open_analysis_gb300.engine import Gb300Engine
+    from open_analysis_gb300.model import ModelError
+
+    models = _small_instances(5)
+    compiled = compile_all(models, workers=1)
+    shapes = [(16, 3), (8, 3), (8, 2), (4, 2), (16, 0)]
+
+    def make() -> list:  # type: ignore[type-arg]
+        out = []
+        for c, (tz, v) in zip(compiled, shapes, strict=True):
+            e = Gb300Engine(c, "float32", max_steps=steps + 10)
+            try:
+                e.set_tuning(tz, v)
+            except ModelError:  # no fused box in this instance: the TMA-staged sweeps
+                e.set_tuning(tz, 2)
+            out.append(e)
+        return out
+
+    alone, grouped = make(), make()
+    for e in alone:
+        e.step(steps)
+    batch = EngineBatch(grouped)
+    assert len(batch.handles) == len({e.get_tuning()[1] for e in grouped}) >= 2
+    batch.step_async(steps - 7)
+    batch.step(7)
+    assert batch.graph_kernels() > 0
+    for a, b in zip(alone, grouped, strict=True):
+        assert a.step_count == b.step_count == steps
+        for k in range(6):
+            assert np.array_equal(a.field(k), b.field(k)), k
+        ra, rb = a.results(), b.results()
+        assert ra.keys() == rb.keys()
+        for key in ra:
+            assert np.array_equal(ra[key], rb[key]), key
+        assert a.energy() == b.energy()
+    batch.close()
+    for e in alone + grouped:
+        e.close()
+
+
+@pytest.mark.gpu
+def test_engine_batch_refuses_out_of_step_engines() -> None:
+    """Host-side checks: engines at different steps cannot form a batch, and an engine stepped on
+    its own while in a batch stops the batch with FDTD_BAD_INPUT instead of racing it."""
+    from open_analysis_gb300.batch import EngineBatch, compile_all
+    from open_analysis_gb300.engine import Gb300Engine
+    from open_analysis_gb300.model import ModelError
+
+    compiled = compile_all(_small_instances(2), workers=1)
+    e1, e2 = (Gb300Engine(c, "float32", max_steps=200) for c in compiled)
+    e1.set_tuning(8, 2)
+    e2.set_tuning(8, 2)
+    e1.step(3)
+    with pytest.raises(ModelError):
+        EngineBatch([e1, e2])
+    e2.step(3)
+    batch = EngineBatch([e1, e2])
+    batch.step(5)
+    e1.step(1)
+    with pytest.raises(ModelError):
+        batch.step(1)
+    batch.close()
+    e1.close()
+    e2.close()
+
+
+@pytest.mark.gpu
+def test_stream_launches_equal_batched_launches() -> None:
+    from open_analysis_gb300.batch import compile_all, run_batched
+
+    models = _small_instances(4, seed=5)
+    compiled = compile_all(models, workers=1)
+    a = run_batched(models, compiled, 200, launch="batch")
+    b = run_batched(models, compiled, 200, launch="streams")
+    assert a.extra["launch"] == "batch" and a.extra["graph_kernels_per_chunk"] > 0
+    for sa, sb in zip(a.s, b.s, strict=True):
+        assert np.array_equal(sa, sb)
