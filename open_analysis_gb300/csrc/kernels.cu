@@ -136,9 +136,9 @@ __global__ void __launch_bounds__(256) probe_e_batch_kernel(const ProbeArgs<real
 // H samples (reference.py:129-150). One thread per edge handles every batch member; BB and PP
 // unroll the batch and pole loops so all loads of an edge are issued together.
 template <typename real, int BB, int PP>
-__device__ __forceinline__ void sibc_body(const SibcArgs<real>& a, int block) {
-  const int s = block * blockDim.x + threadIdx.x;
-  if (s >= a.n) return;
+__device__ __forceinline__ void sibc_body(const SibcArgs<real>& a, int block, int lo, int hi) {
+  const int s = lo + block * (int)blockDim.x + (int)threadIdx.x;
+  if (s >= hi) return;
   const SibcEdge<real> ed = a.edge[s];
   const real* __restrict__ alpha = a.alpha + (long long)ed.mat * PP;
   const long long n = a.n;
@@ -177,15 +177,15 @@ __device__ __forceinline__ void sibc_body(const SibcArgs<real>& a, int block) {
 }
 
 template <typename real, int BB, int PP>
-__global__ void __launch_bounds__(128) sibc_kernel(const __grid_constant__ SibcArgs<real> a) {
-  sibc_body<real, BB, PP>(a, (int)blockIdx.x);
+__global__ void __launch_bounds__(128) sibc_kernel(const __grid_constant__ SibcArgs<real> a, int lo, int hi) {
+  sibc_body<real, BB, PP>(a, (int)blockIdx.x, lo, hi);
 }
 
 // Any batch size and pole count (loops not unrolled).
 template <typename real>
-__device__ __forceinline__ void sibc_generic_body(const SibcArgs<real>& a, int block) {
-  const int s = block * blockDim.x + threadIdx.x;
-  if (s >= a.n) return;
+__device__ __forceinline__ void sibc_generic_body(const SibcArgs<real>& a, int block, int lo, int hi) {
+  const int s = lo + block * (int)blockDim.x + (int)threadIdx.x;
+  if (s >= hi) return;
   const SibcEdge<real> ed = a.edge[s];
   const int B = a.B, P = a.P;
   const real* __restrict__ alpha = a.alpha + (long long)ed.mat * P;
@@ -210,8 +210,8 @@ __device__ __forceinline__ void sibc_generic_body(const SibcArgs<real>& a, int b
 }
 
 template <typename real>
-__global__ void __launch_bounds__(128) sibc_generic_kernel(const __grid_constant__ SibcArgs<real> a) {
-  sibc_generic_body(a, (int)blockIdx.x);
+__global__ void __launch_bounds__(128) sibc_generic_kernel(const __grid_constant__ SibcArgs<real> a, int lo, int hi) {
+  sibc_generic_body(a, (int)blockIdx.x, lo, hi);
 }
 
 // Several engines' surface-impedance updates in one launch (engines of one kernel variant).
@@ -222,9 +222,9 @@ __global__ void __launch_bounds__(128) sibc_batch_kernel(const SibcArgs<real>* _
   const uint3 bid = G.block(&e);
   const SibcArgs<real>& a = stage_args(A + e, args);
   if constexpr (BB == 0)
-    sibc_generic_body(a, (int)bid.x);
+    sibc_generic_body(a, (int)bid.x, 0, a.n);
   else
-    sibc_body<real, BB, PP>(a, (int)bid.x);
+    sibc_body<real, BB, PP>(a, (int)bid.x, 0, a.n);
 }
 
 template <typename real>
@@ -252,17 +252,18 @@ cudaError_t launch_sibc_batch(const SibcArgs<real>* A, const BatchGrid& G, int b
 }
 
 template <typename real>
-cudaError_t launch_sibc(const SibcArgs<real>& a, cudaStream_t s) {
-  if (a.n == 0) return cudaSuccess;
-  const unsigned blocks = (unsigned)((a.n + 127) / 128);
+cudaError_t launch_sibc(const SibcArgs<real>& a, cudaStream_t s, int lo, int hi) {
+  if (hi < 0) hi = a.n;
+  if (hi <= lo) return cudaSuccess;
+  const unsigned blocks = (unsigned)((hi - lo + 127) / 128);
   if (a.B == 2 && a.P == 16)
-    sibc_kernel<real, 2, 16><<<blocks, 128, 0, s>>>(a);
+    sibc_kernel<real, 2, 16><<<blocks, 128, 0, s>>>(a, lo, hi);
   else if (a.B == 1 && a.P == 16)
-    sibc_kernel<real, 1, 16><<<blocks, 128, 0, s>>>(a);
+    sibc_kernel<real, 1, 16><<<blocks, 128, 0, s>>>(a, lo, hi);
   else if (a.B == 4 && a.P == 16)
-    sibc_kernel<real, 4, 16><<<blocks, 128, 0, s>>>(a);
+    sibc_kernel<real, 4, 16><<<blocks, 128, 0, s>>>(a, lo, hi);
   else
-    sibc_generic_kernel<real><<<blocks, 128, 0, s>>>(a);
+    sibc_generic_kernel<real><<<blocks, 128, 0, s>>>(a, lo, hi);
   return cudaGetLastError();
 }
 
@@ -488,7 +489,7 @@ cudaError_t launch_bump_batch(long long* const* step_base, int n_eng, int n, cud
   template cudaError_t launch_pre_e<real>(const ProbeArgs<real>&, int, cudaStream_t);              \
   template cudaError_t launch_probe_e<real>(const ProbeArgs<real>&, int, cudaStream_t);            \
   template cudaError_t launch_edges<real>(const EdgeArgs<real>&, int, cudaStream_t);               \
-  template cudaError_t launch_sibc<real>(const SibcArgs<real>&, cudaStream_t);                      \
+  template cudaError_t launch_sibc<real>(const SibcArgs<real>&, cudaStream_t, int, int);            \
   template int pre_e_blocks<real>(const ProbeArgs<real>&);                                          \
   template int probe_e_blocks<real>(const ProbeArgs<real>&);                                        \
   template int edge_blocks<real>(const EdgeArgs<real>&);                                            \

@@ -321,8 +321,9 @@ template <typename real>
 cudaError_t launch_pre_e(const ProbeArgs<real>& a, int off, cudaStream_t s);
 template <typename real>
 cudaError_t launch_edges(const EdgeArgs<real>& a, int off, cudaStream_t s);
+// the surface-impedance edges [lo, hi) (hi < 0: to the last)
 template <typename real>
-cudaError_t launch_sibc(const SibcArgs<real>& a, cudaStream_t s);
+cudaError_t launch_sibc(const SibcArgs<real>& a, cudaStream_t s, int lo = 0, int hi = -1);
 template <typename real>
 cudaError_t launch_probe_e(const ProbeArgs<real>& a, int off, cudaStream_t s);
 template <typename real>
