@@ -100,10 +100,6 @@ struct Engine final : EngineBase {
   int cur[2] = {0, 0};
   bool two_buffers = false;
   oafdtd::Span3 fused_box{};              // the fused sweep's box (variant 3)
-  // SIBC records [0, sibc_inside) have their E edge in the fused box: in a fused step nothing but
-  // the fused sweep writes those edges, so they are updated beside the E slab kernel
-  int sibc_inside = 0;
-  std::vector<oafdtd::SibcEdge<real>> sibc_recs;  // host records until the regions are known
   oafdtd::Span3 zin_fused[2][2]{};        // z-slab planes over its x-y extent
   oafdtd::Span3 slab_fused[2][6]{};       // the slab boxes around it
   int n_slab_fused[2] = {0, 0};
@@ -795,8 +791,10 @@ int Engine<real>::build(const oafdtd_problem& p) {
     }
     for (int q = 0; q < SP; ++q) gp[q] = (real)p.sibc_gp[q];
     int rc;
+    oafdtd::SibcEdge<real>* dre = nullptr;
     real* dr = nullptr;
-    sibc_recs = std::move(recs);  // uploaded once the fused box is known
+    if ((rc = upload_vec(&dre, recs))) return rc;
+    sb.edge = dre;
     if ((rc = upload_vec(&dr, r0))) return rc;
     sb.r0 = dr;
     if ((rc = upload_vec(&dr, alpha))) return rc;
@@ -997,26 +995,6 @@ int Engine<real>::build(const oafdtd_problem& p) {
           n_slab_fused[kind] = n;
         }
       }
-    }
-    // SIBC records with their edge in the fused box first (a stable partition: the order within
-    // each part stays the compiled one; every record owns its state slots, all zero here)
-    {
-      const oafdtd::Span3& F = fused_box;
-      sibc_inside = 0;
-      if (F.k1 > F.k0 && sb.n > 0) {
-        const long long XY = (long long)X * Y;
-        auto inside = [&](const oafdtd::SibcEdge<real>& r) {
-          const long long f = r.flat;
-          const int k = (int)(f / XY), j = (int)((f % XY) / X), i = (int)(f % X);
-          return i >= 4 * F.q0 && i < 4 * F.q1 && j >= F.j0 && j < F.j1 && k >= F.k0 && k < F.k1;
-        };
-        auto mid = std::stable_partition(sibc_recs.begin(), sibc_recs.begin() + sb.n, inside);
-        sibc_inside = (int)(mid - sibc_recs.begin());
-      }
-      oafdtd::SibcEdge<real>* dre = nullptr;
-      if (int rc = upload_vec(&dre, sibc_recs)) return rc;
-      sb.edge = dre;
-      std::vector<oafdtd::SibcEdge<real>>().swap(sibc_recs);
     }
     use_regions(staged);
     std::string why;
@@ -1221,23 +1199,8 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing, int part
     if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("pre_e: ") + cudaGetErrorString(err));
   }
   if (parts & 2) {
-    if (fused && !ev && sibc_inside > 0) {
-      // the SIBC edges inside the fused box beside the E slab kernel (they touch no slab cell),
-      // the rest after it
-      OA_CUDA(cudaEventRecord(fork_ev, stream));
-      OA_CUDA(cudaStreamWaitEvent(side, fork_ev, 0));
-      err = oafdtd::launch_slab<real>(sw, 0, side);
-      if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("e_slab: ") + cudaGetErrorString(err));
-      OA_CUDA(cudaEventRecord(join_ev, side));
-      err = oafdtd::launch_staged_sweep<real>(sw, mp, stream, false);
-      if (err == cudaSuccess) err = oafdtd::launch_sibc<real>(sb, stream, 0, sibc_inside);
-      if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("e_sweep: ") + cudaGetErrorString(err));
-      OA_CUDA(cudaStreamWaitEvent(stream, join_ev, 0));
-      err = oafdtd::launch_sibc<real>(sb, stream, sibc_inside, -1);
-    } else {
-      if (int rc = sweep_pair(0, ev, 4, rec, mp)) return rc;
-      err = oafdtd::launch_sibc<real>(sb, stream);
-    }
+    if (int rc = sweep_pair(0, ev, 4, rec, mp)) return rc;
+    err = oafdtd::launch_sibc<real>(sb, stream);
     if (err == cudaSuccess) err = oafdtd::launch_edges<real>(ed, off, stream);
     if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("edges: ") + cudaGetErrorString(err));
     if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[7], stream, rec));

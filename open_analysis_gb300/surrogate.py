@@ -682,23 +682,31 @@ class Mlp:
         self.check_status()
         return losses
 
-    def predict(self, x: npt.ArrayLike, chunk: int = 4096) -> FloatArray:
-        """Outputs for ``x (n, n_in)`` (scaled inputs): ``(n, sizes[-1])`` for one member,
-        ``(members, n, sizes[-1])`` for more; FP32 on the GPU, float64 on return."""
+    def predict_device(self, x: npt.ArrayLike, chunk: int = 4096) -> Any:
+        """Outputs for ``x (n, n_in)`` (scaled inputs) as an FP32 device tensor ``(members, n,
+        sizes[-1])``."""
         torch = self.torch
         x = self.pad(x)
         n, g = x.shape[0], self.members
-        out = np.zeros((g, n, self.sizes[-1]))
+        out = torch.empty((g, n, self.sizes[-1]), dtype=torch.float32, device=self.dev)
         s = self._stream()
         for a in range(0, n, chunk):
             m = min(chunk, n - a)
             x16 = torch.from_numpy(x[a : a + m]).to(self.dev).to(torch.bfloat16).expand(g, m, -1).contiguous()
             acts = [torch.empty((g, m, b), dtype=torch.bfloat16, device=self.dev) for b in self.sizes[1:-1]]
-            y = torch.empty((g, m, self.sizes[-1]), dtype=torch.float32, device=self.dev)
+            y = out[:, a : a + m] if g == 1 or n == m else torch.empty((g, m, self.sizes[-1]), dtype=torch.float32,
+                                                                         device=self.dev)
             self._forward(x16.data_ptr(), acts, y.data_ptr(), m, s)
-            out[:, a : a + m] = y.cpu().numpy()
+            if y.data_ptr() != out[:, a : a + m].data_ptr():
+                out[:, a : a + m].copy_(y)
         self.check_status()
-        return out[0] if g == 1 else out
+        return out
+
+    def predict(self, x: npt.ArrayLike, chunk: int = 4096) -> FloatArray:
+        """Outputs for ``x (n, n_in)`` (scaled inputs): ``(n, sizes[-1])`` for one member,
+        ``(members, n, sizes[-1])`` for more; FP32 on the GPU, float64 on return."""
+        out = self.predict_device(x, chunk).cpu().numpy().astype(np.float64)
+        return out[0] if self.members == 1 else out
 
 
 # ------------------------------------------------------------------------------------ ensemble
@@ -817,15 +825,24 @@ class Ensemble:
         return logs
 
     def raw(self, params: npt.ArrayLike) -> tuple[ComplexArray, FloatArray, float]:
+        """The ensemble mean of S ``(n, 2, F)``, the largest complex standard deviation over the
+        members per instance, and the seconds all of it took. The members' outputs stay on the
+        GPU: scaling, the line factors, mean and spread run there in float64."""
+        torch = self.net.torch
         t0 = time.perf_counter()
-        x = scale_params(params)
-        ys = self.net.predict(x).reshape(self.net.members, len(x), -1) * self.sigma + self.mu
-        sec = time.perf_counter() - t0
-        fac = line_factor(params, self.g)
-        stack = np.stack([rows_to_s(y) / fac for y in ys])  # (members, n, 2, F)
-        mean = stack.mean(axis=0)
-        dev = np.sqrt((np.abs(stack - mean) ** 2).mean(axis=0))  # complex std per (n, 2, F)
-        return mean, dev.reshape(dev.shape[0], -1).max(axis=1), sec
+        params = np.atleast_2d(np.asarray(params, np.float64))
+        n, f = len(params), self.g.n_freq
+        y = self.net.predict_device(scale_params(params)).to(torch.float64)  # (members, n, 4 F)
+        y = y * self.sigma + torch.from_numpy(np.asarray(self.mu, np.float64)).to(y.device)
+        s11 = torch.complex(y[..., :f], y[..., f : 2 * f])
+        s21 = torch.complex(y[..., 2 * f : 3 * f], y[..., 3 * f :])
+        fac = torch.from_numpy(line_factor(params, self.g)).to(y.device)  # (n, 2, F)
+        stack = torch.stack([s11, s21], dim=2) / fac  # (members, n, 2, F)
+        mean = stack.mean(dim=0)
+        dev = torch.sqrt((torch.abs(stack - mean) ** 2).mean(dim=0))  # complex std per (n, 2, F)
+        spread = dev.reshape(n, -1).amax(dim=1)
+        out = mean.cpu().numpy(), spread.cpu().numpy()
+        return out[0], out[1], time.perf_counter() - t0
 
     def save(self, path: str) -> None:
         """Write the trained ensemble (grid, widths, activation, every member's FP32 weights,
