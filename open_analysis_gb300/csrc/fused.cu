@@ -121,6 +121,10 @@ __device__ __forceinline__ void fused_body(const SweepArgs<real>& a, const Fused
   const real ipy_h = a.ip[1][y0 - 1];  // the halo row
   const real ipx_h = a.ip[0][x0 - 1];  // the halo column
   const int cc = 4 + 4 * tx;           // own first cell in the staged E and H rows
+  // the halo row's cells, 128 of them: lanes 0-15 of every warp, cell hc of the tile row
+  const int hc = 16 * ty + tx;
+  const bool halo_live = tx < 16 && x0 + 4 * (hc / 4) < 4 * F.q1;
+  const real ipx_c = halo_live ? a.ip[0][x0 + hc] : (real)0;
   if (leader) {
 #pragma unroll
     for (int s = 0; s < kSE; ++s) mbar_init(&bar_e[s], 1);
@@ -228,30 +232,24 @@ __device__ __forceinline__ void fused_body(const SweepArgs<real>& a, const Fused
         st4(&hs.h[2].v[ty + 1][cc], hz_n);
       }
     }
-    if (inner && live && ty == 0) {  // the halo row y0 - 1: Hx and Hz
-      const int jh = y0 - 1;
-      Quad<real> hx = ld4(&hs.h[0].v[0][cc]), hz = ld4(&hs.h[2].v[0][cc]);
-      const Quad<real> ex = ld4(&ec.e[0].v[0][cc]), ey = ld4(&ec.e[1].v[0][cc]), ez = ld4(&ec.e[2].v[0][cc]);
-      const Quad<real> ezy = ld4(&ec.e[2].v[1][cc]), exy = ld4(&ec.e[0].v[1][cc]);
-      const Quad<real> ey1 = ld4(&en.e[1].v[0][cc]);
-      const real ey_r = ec.e[1].v[0][cc + 4];
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const int i = i0 + e;
-        if (jh <= ny && kin) {
-          const real d0 = (ezy.v[e] - ez.v[e]) * ipy_h;
-          const real d1 = (ey1.v[e] - ey.v[e]) * ipz;
-          if (i >= 1 && i <= nx + 1) hx.v[e] = hx.v[e] + dtmu * ((-d0) + d1);
-        }
-        if (jh <= ny) {
-          const real eyr = e < 3 ? ey.v[e + 1] : ey_r;
-          const real d0 = (eyr - ey.v[e]) * ipx.v[e];
-          const real d1 = (exy.v[e] - ex.v[e]) * ipy_h;
-          if (i >= 1 && i <= nx) hz.v[e] = hz.v[e] + dtmu * ((-d0) + d1);
-        }
+    if (inner && halo_live) {  // the halo row y0 - 1: Hx and Hz, one cell per lane, every warp a share
+      const int jh = y0 - 1, i = x0 + hc, ch = 4 + hc;
+      real hx = hs.h[0].v[0][ch], hz = hs.h[2].v[0][ch];
+      const real ex = ec.e[0].v[0][ch], ey = ec.e[1].v[0][ch], ez = ec.e[2].v[0][ch];
+      const real ezy = ec.e[2].v[1][ch], exy = ec.e[0].v[1][ch];
+      const real ey1 = en.e[1].v[0][ch], eyr = ec.e[1].v[0][ch + 1];
+      if (jh <= ny && kin) {
+        const real d0 = (ezy - ez) * ipy_h;
+        const real d1 = (ey1 - ey) * ipz;
+        if (i >= 1 && i <= nx + 1) hx = hx + dtmu * ((-d0) + d1);
       }
-      st4(&hs.h[0].v[0][cc], hx);
-      st4(&hs.h[2].v[0][cc], hz);
+      if (jh <= ny) {
+        const real d0 = (eyr - ey) * ipx_c;
+        const real d1 = (exy - ex) * ipy_h;
+        if (i >= 1 && i <= nx) hz = hz + dtmu * ((-d0) + d1);
+      }
+      hs.h[0].v[0][ch] = hx;
+      hs.h[2].v[0][ch] = hz;
     }
     if (inner && live && tx == 0) {  // the halo column x0 - 1: Hy and Hz
       const int ih = x0 - 1;
