@@ -26,6 +26,9 @@ advances between energy checks. Gcell-updates/s = interior cells x batch x time 
   ``sweeps.surrogate``: batched + learned surrogate against batched alone and against the plain
   loop, on a three-parameter sweep of small via transitions (``surrogate.experiment``: data from
   the batched engine, the ensemble trained on the GPU, held-out answers judged against FDTD).
+* ``large_board``: the 1600 x 1200 x 160 board region (307 M cells, eight ports as a batch of
+  eight, 512 frequencies) on the same GPU after the sweeps: ``--board-chunks`` timed 64-step
+  chunks, the per-class fractions of the measured copy bandwidth, compile time and device bytes.
 
 ``--impl reference`` times the reference's CPU path (the oracle port; the reference is a Python
 package and is not installed on the GPU host) on the same workload, one time step per bench step.
@@ -297,6 +300,64 @@ def surrogate_measure(n: int) -> dict[str, Any]:
     return out
 
 
+def board_measure(chunks: int, warmup: int = 2) -> dict[str, Any]:
+    """The large board region on one GPU: 1600 x 1200 x 160 cells of 20 um (307 M cells), eight
+    Debye layers, 12 traces and 40 vias of surface-impedance copper at seeded positions, 12-cell
+    CPML, eight ports driven as a batch of eight, 512 frequencies 0.05-40 GHz
+    (``structures.large_board``), the engine's default launch shape. ``chunks`` timed 64-step
+    chunks after ``warmup`` untimed ones, then one profiled chunk for the per-class times."""
+    from open_analysis_gb300.engine import Gb300Engine
+    from open_analysis_gb300.model import compile_model
+    from open_analysis_gb300.structures import large_board
+
+    t0 = time.perf_counter()
+    c = compile_model(large_board(), "float32")
+    compile_s = time.perf_counter() - t0
+    nx, ny, nz = c.grid.n
+    batch = c.batch
+    t0 = time.perf_counter()
+    eng = Gb300Engine(c, "float32", max_steps=(warmup + chunks + 3) * CHUNK)
+    create_s = time.perf_counter() - t0
+    del c
+    for _ in range(warmup):
+        eng.step(CHUNK)
+    sampler = ClockSampler(0)
+    sampler.start()
+    times = [eng.step_timed(CHUNK) for _ in range(chunks)]
+    clocks = sampler.stop()
+    ms_step = sum(times) / (chunks * CHUNK)
+    eng.set_profiling(True)
+    eng.step(CHUNK)  # capture the profiled graph
+    eng.step(CHUNK)
+    kt = eng.kernel_times()
+    eng.set_profiling(False)
+    kb = eng.kernel_bytes()
+    model_bytes = eng.model_bytes()
+    device_bytes = eng.peak_bytes()
+    eng.close()
+    peak, peak_kind = measured_peak()
+    classes = {k: {"ms_per_time_step": kt[k], "algorithmic_gb": kb[k] / 1e9,
+                   "frac": kb[k] / (kt[k] / 1e3) / 1e9 / peak}
+               for k in kb if k != "step" and kb[k] > 0 and kt.get(k, 0.0) > 0}
+    return {
+        "workload": f"large_board_{nx}x{ny}x{nz}",
+        "batch": batch,
+        "value": float(nx) * ny * nz * batch / (ms_step / 1e3) / 1e9,
+        "unit": "Gcell-updates/s",
+        "timed_chunks": chunks,
+        "warmup_chunks": warmup,
+        "ms_per_time_step": ms_step,
+        "step_frac": model_bytes / (ms_step / 1e3) / 1e9 / peak,
+        "peak": peak,
+        "peak_source": peak_kind,
+        "classes": classes,
+        "compile_seconds": compile_s,
+        "create_seconds": create_s,
+        "device_bytes": device_bytes,
+        "clocks": clocks,
+    }
+
+
 def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
     from open_analysis_gb300 import native
     from open_analysis_gb300.engine import Gb300Engine
@@ -392,6 +453,10 @@ def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
         if args.surrogate_instances:
             sweeps["surrogate"] = surrogate_measure(args.surrogate_instances)
 
+    board = None
+    if args.board_chunks > 0 and ranks.world == 1 and args.workload == "via_transition":
+        board = board_measure(args.board_chunks)
+
     if ranks.rank == 0:
         line = {
             "metric": "Gcell-updates/s",
@@ -434,6 +499,7 @@ def run_gb300(args: argparse.Namespace, ranks: Ranks) -> None:
             "clocks": clocks,
             "cpu_baseline": cpu,
             "sweeps": sweeps,
+            "large_board": board,
         }
         print(json.dumps(line), flush=True)
 
@@ -505,6 +571,8 @@ def main() -> None:
     ap.add_argument("--sweep-instances", type=int, default=64, help="batched-sweep instances (0: skip)")
     ap.add_argument("--sweep-steps", type=int, default=8000, help="time steps per sweep instance")
     ap.add_argument("--surrogate-instances", type=int, default=384, help="surrogate sweep instances (0: skip)")
+    ap.add_argument("--board-chunks", type=int, default=3,
+                    help="timed 64-step chunks of the large-board region after the sweeps (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

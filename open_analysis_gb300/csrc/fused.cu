@@ -95,6 +95,7 @@ template <typename real, bool kMulti>
 __device__ __forceinline__ void fused_body(const SweepArgs<real>& a, const FusedMaps& tm, const uint3 bid) {
   extern __shared__ unsigned char smem_raw[];
   __shared__ unsigned long long bar_e[kSE], bar_h[kSH];
+  __shared__ unsigned long long bar_done;  // one arrival per warp when it is done with a plane
   FusedSmem<real>& sm = *reinterpret_cast<FusedSmem<real>*>(align_smem(smem_raw));
   const int tx = threadIdx.x, ty = threadIdx.y;
   const bool leader = tx == 0 && ty == 0;
@@ -130,6 +131,7 @@ __device__ __forceinline__ void fused_body(const SweepArgs<real>& a, const Fused
     for (int s = 0; s < kSE; ++s) mbar_init(&bar_e[s], 1);
 #pragma unroll
     for (int s = 0; s < kSH; ++s) mbar_init(&bar_h[s], 1);
+    mbar_init(&bar_done, kFY);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -173,12 +175,10 @@ __device__ __forceinline__ void fused_body(const SweepArgs<real>& a, const Fused
         if (k + 1 >= a.jk0[c] && k + 1 < a.jk0[c] + a.jnk[c])
           jnext[c] = ld4(a.J[c] + (((long long)b * a.jnk[c] + (k + 1 - a.jk0[c])) * Y + j) * X + i0);
     }
-    ok = mbar_wait(&bar_e[(t + 1) % kSE], (unsigned)(((t + 1) / kSE) & 1), kWaitNs);
+    // each thread acquires the plane's copies itself; whether every wait succeeded is agreed on
+    // at the block's one barrier of the plane, before any global store
+    ok = ok && mbar_wait(&bar_e[(t + 1) % kSE], (unsigned)(((t + 1) / kSE) & 1), kWaitNs);
     if (ok) ok = mbar_wait(&bar_h[t % kSH], (unsigned)((t / kSH) & 1), kWaitNs);
-    if (__syncthreads_or(!ok)) {
-      abort_fused(bar_e, bar_h, t + 1, e_issued, t, h_issued, a.status, leader);
-      return;
-    }
     const EPlane<real>& ec = sm.e[t % kSE];         // E^n of plane k
     const EPlane<real>& en = sm.e[(t + 1) % kSE];   // E^n of plane k + 1
     HPlane<real>& hs = sm.h[t % kSH];               // H^{n-1/2} of plane k, updated in place
@@ -267,7 +267,11 @@ __device__ __forceinline__ void fused_body(const SweepArgs<real>& a, const Fused
       hs.h[1].v[ty + 1][3] = hy;
       hs.h[2].v[ty + 1][3] = hz;
     }
-    __syncthreads();  // the new H of the plane (halo included) is complete
+    // the new H of the plane (halo included) is complete
+    if (__syncthreads_or(!ok)) {
+      abort_fused(bar_e, bar_h, t + 1, e_issued, t, h_issued, a.status, leader);
+      return;
+    }
     // ---- 2. E^{n+1} of the own quad, and the stores
     if (inner && live) {
       const long long p = base + (long long)k * X * Y + (long long)j * X + i0;
@@ -314,15 +318,22 @@ __device__ __forceinline__ void fused_body(const SweepArgs<real>& a, const Fused
 #pragma unroll
       for (int c = 0; c < 3; ++c) jcur[c] = jnext[c];
     }
-    __syncthreads();  // every thread is done with E(k) and the H / index slot of plane k
-    if (leader) {
-      if (e_issued < n_e) {  // E(k + 3) into the slot of E(k)
-        fence_proxy_async();
+    // This warp is done with E(k) and the H / index slot of plane k: its reads and writes of
+    // the slots are ordered before the copies that refill them, and the warp moves on to the
+    // next plane without waiting for the others. The leader refills the slots once every warp
+    // has arrived (phase t of bar_done; phase t + 1 cannot complete before the leader has passed
+    // the next plane's barrier).
+    fence_proxy_async();
+    __syncwarp();
+    if (tx == 0) mbar_arrive(&bar_done);
+    if (leader && ok && (e_issued < n_e || h_issued < n_planes)) {
+      // a wait that gives up is reported at the next plane's barrier; nothing more is issued
+      ok = mbar_wait(&bar_done, (unsigned)(t & 1), kWaitNs);
+      if (ok && e_issued < n_e) {  // E(k + 3) into the slot of E(k)
         issue_e(tm, sm.e[e_issued % kSE], &bar_e[e_issued % kSE], x0, y0, ks + e_issued, b);
         ++e_issued;
       }
-      if (h_issued < n_planes) {  // H and index of plane k + 2 into the slot of plane k
-        fence_proxy_async();
+      if (ok && h_issued < n_planes) {  // H and index of plane k + 2 into the slot of plane k
         issue_h(tm, sm.h[h_issued % kSH], &bar_h[h_issued % kSH], x0, y0, ks + h_issued, b);
         ++h_issued;
       }
