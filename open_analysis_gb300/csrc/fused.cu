@@ -13,7 +13,10 @@
 // A block owns a tile of 32 quads (128 x cells) by 8 rows and a chunk of z planes. Per plane it
 // stages, by TMA tensor copies into shared memory: E^n of the plane above (with a one-quad and
 // one-row halo on every side; the plane itself is still staged from the previous step of the
-// march), H^{n-1/2} of the plane (with a halo on the low sides) and the material index. It then
+// march), H^{n-1/2} of the plane (with a halo on the low sides) and the material index. Each warp
+// waits for the copies itself; one block barrier per plane (after the H update) also agrees on
+// whether every wait succeeded, and the warps release their slots through an mbarrier that the
+// leader waits on before it refills them. It then
 //   1. updates H of its cells (and of the halo column x0 - 1 and row y0 - 1) in shared memory,
 //      with the H sweep's arithmetic (packages/oa-fdtd/src/oa_fdtd/reference.py:152-165);
 //   2. updates E of its cells from the new H (and the carried H of the plane below), with the

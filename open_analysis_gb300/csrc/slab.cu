@@ -21,6 +21,8 @@
 // psi layout, one array per (kind, component, axis, side): (B, Z', Y', X') with the slab width
 // on the derivative axis and the full storage extent on the other two.
 
+#include <algorithm>
+
 #include "device_common.cuh"
 
 namespace oafdtd {
@@ -193,11 +195,11 @@ __device__ __forceinline__ void slab_e_column(const SweepArgs<real>& a, const Sl
       s2 = ld4(Hy + q);
     } else if (C == 1) {
       s0 = ld4(Hz + q);
-      sl = Hz[q - 1];
+      if (i0 > 0) sl = Hz[q - 1];  // cell 0 is never updated: no neighbour from the row before
       s2 = ld4(Hx + q);
     } else {
       s0 = ld4(Hy + q);
-      sl = Hy[q - 1];
+      if (i0 > 0) sl = Hy[q - 1];
       s2 = ld4(Hx + q);
       s1 = ld4(Hx + q - X);
     }
@@ -438,7 +440,8 @@ cudaError_t slab_plan(const SweepArgs<real>& a, int kind, SlabLaunch* L, long lo
   *blocks = 0;
   long long total = 0;
   for (int n = 0; n < a.n_slab[kind]; ++n) {
-    const Span3& bx = a.slab[kind][n];
+    Span3 bx = a.slab[kind][n];
+    bx.q1 = std::min(bx.q1, (a.nx + 1) / 4 + 1);  // quads past the last updated cell hold no work
     const long long cols = (long long)(bx.q1 - bx.q0) * (bx.j1 - bx.j0);
     if (cols <= 0 || bx.k1 <= bx.k0) continue;
     L->box[L->n] = bx;
