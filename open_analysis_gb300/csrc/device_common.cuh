@@ -139,8 +139,10 @@ template <typename real, bool kZ, bool kMulti>
 __device__ __forceinline__ void e_apply(const SweepArgs<real>& a, int c, real* __restrict__ E, long long p,
                                         const Quad<real>& e_old, const uint16_t* m, const real (&d0)[4],
                                         const real (&d1)[4], bool first_plus, const Quad<real>& j4in,
-                                        const ZTerm<real>& zt, int i0, int j, int k, int b) {
+                                        const ZTerm<real>& zt, int i0, int j, int k, int b,
+                                        const Coef<real>* ctab = nullptr) {
   const int X = a.X, Y = a.Y, nx = a.nx;
+  const Coef<real>* tab = ctab != nullptr ? ctab : a.coef;  // the table staged in shared memory, or global
   Quad<real> e4 = e_old;
   Coef<real> cf[4];
   real kf[4];
@@ -149,7 +151,7 @@ __device__ __forceinline__ void e_apply(const SweepArgs<real>& a, int c, real* _
 #pragma unroll
   for (int e = 0; e < 4; ++e) {
     const int i = i0 + e;
-    cf[e] = a.coef[m[e]];
+    cf[e] = tab[m[e]];
     kf[e] = cf[e].cb;
     valid[e] = i >= 1 && i <= nx + 1;
     const real acc = first_plus ? d0[e] + (-d1[e]) : d1[e] + (-d0[e]);

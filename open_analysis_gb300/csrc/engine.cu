@@ -565,6 +565,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
     int rc = upload_vec(&dc, t_coef);
     if (rc) return rc;
     sw.coef = ed.coef = dc;
+    sw.n_coef = (int)t_coef.size();
     sw.ade_lo = ade_lo;
     sw.ade_hi = ade_hi;
     real* d = nullptr;
@@ -1003,7 +1004,8 @@ int Engine<real>::build(const oafdtd_problem& p) {
       staged = 1;
       use_regions(staged);
     }
-    if (tma_ok && fused_box.k1 > fused_box.k0) {
+    // the fused sweep reads the combined table from shared memory (kCoefSmem entries at most)
+    if (tma_ok && fused_box.k1 > fused_box.k0 && sw.n_coef <= oafdtd::kCoefSmem) {
       oafdtd::FusedMaps probe{};
       fused_ok = oafdtd::encode_fused_maps<real>(sw, &probe, &why);
     }

@@ -61,6 +61,7 @@ template <typename real>
 struct FusedSmem {
   EPlane<real> e[kSE];
   HPlane<real> h[kSH];
+  Coef<real> coef[kCoefSmem];  // the combined material table (the E update's 12 gathers per quad)
 };
 
 template <typename real>
@@ -143,6 +144,7 @@ __device__ __forceinline__ void fused_body(const SweepArgs<real>& a, const Fused
       prefetch_map(&tm.mat[c]);
     }
   }
+  for (int e = ty * kFQ + tx; e < a.n_coef; e += kFQ * kFY) sm.coef[e] = a.coef[e];
   __syncthreads();
   int e_issued = 0, h_issued = 0;
   if (leader) {
@@ -292,7 +294,7 @@ __device__ __forceinline__ void fused_body(const SweepArgs<real>& a, const Fused
         d1[e] = (hy_n.v[e] - hy_m.v[e]) * idz;
       }
       e_apply<real, false, kMulti>(a, 0, a.Eo[0] + base, q, ld4(&ec.e[0].v[ty + 1][cc]), &hs.m[0].v[ty][4 * tx], d0,
-                                   d1, true, jcur[0], none, i0, j, k, b);
+                                   d1, true, jcur[0], none, i0, j, k, b, sm.coef);
       // Ey: terms (a = z, +Hx) then (a = x, -Hz)
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
@@ -301,7 +303,7 @@ __device__ __forceinline__ void fused_body(const SweepArgs<real>& a, const Fused
         d1[e] = (hx_n.v[e] - hx_m.v[e]) * idz;
       }
       e_apply<real, false, kMulti>(a, 1, a.Eo[1] + base, q, ld4(&ec.e[1].v[ty + 1][cc]), &hs.m[1].v[ty][4 * tx], d0,
-                                   d1, false, jcur[1], none, i0, j, k, b);
+                                   d1, false, jcur[1], none, i0, j, k, b, sm.coef);
       // Ez: terms (a = x, +Hy) then (a = y, -Hx)
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
@@ -310,7 +312,7 @@ __device__ __forceinline__ void fused_body(const SweepArgs<real>& a, const Fused
         d1[e] = (hx_n.v[e] - hxy.v[e]) * idy;
       }
       e_apply<real, false, kMulti>(a, 2, a.Eo[2] + base, q, ld4(&ec.e[2].v[ty + 1][cc]), &hs.m[2].v[ty][4 * tx], d0,
-                                   d1, true, jcur[2], none, i0, j, k, b);
+                                   d1, true, jcur[2], none, i0, j, k, b, sm.coef);
       if (j <= ny && kin) st4(a.Ho[0] + p, hx_n);
       if (kin) st4(a.Ho[1] + p, hy_n);
       if (j <= ny) st4(a.Ho[2] + p, hz_n);

@@ -27,6 +27,7 @@ namespace oafdtd {
 
 constexpr int kChunk = 64;        // steps per captured graph (the reference's CHUNK)
 constexpr int kMaxAdePoles = 16;  // Debye poles handled by the fused sweep
+constexpr int kCoefSmem = 256;    // table entries the fused sweep keeps in shared memory
 
 template <typename real>
 struct CpmlSide {
@@ -67,6 +68,7 @@ struct SweepArgs {
   real* Ho[3];
   const uint16_t* mat[3];
   const Coef<real>* coef;   // [entry]; entries [ade_lo, ade_hi) are dispersive, then deferred ones
+  int n_coef;               // entries in the table
   int ade_lo, ade_hi;
   const real* ade_beta;     // [entry * P + p]
   const real* ade_kp;       // [p]
