@@ -262,7 +262,8 @@ struct Engine final : EngineBase {
   // read only the other field): forked onto `side` and joined back, inside the graph as well.
   cudaStream_t side = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
-  int sweep_pair(int kind, cudaEvent_t* ev, int slot, unsigned rec, const oafdtd::SweepMaps& mp);
+  int sweep_pair(int kind, cudaEvent_t* ev, int slot, unsigned rec, const oafdtd::SweepMaps& mp,
+                 int pre_e_off = -1);
 };
 
 // Build phase timer: with OAFDTD_TIMING set in the environment, oafdtd_create prints the
@@ -1127,7 +1128,8 @@ int Engine<real>::build(const oafdtd_problem& p) {
 // other between the class events ev[slot], ev[slot + 1], ev[slot + 2]; otherwise the slab kernel
 // is forked onto the side stream and joined back.
 template <typename real>
-int Engine<real>::sweep_pair(int kind, cudaEvent_t* ev, int slot, unsigned rec, const oafdtd::SweepMaps& mp) {
+int Engine<real>::sweep_pair(int kind, cudaEvent_t* ev, int slot, unsigned rec, const oafdtd::SweepMaps& mp,
+                             int pre_e_off) {
   const char* names[2][2] = {{"e_sweep: ", "e_slab: "}, {"h_sweep: ", "h_slab: "}};
   const bool fork = ev == nullptr && sw.staged;
   cudaError_t err;
@@ -1139,6 +1141,10 @@ int Engine<real>::sweep_pair(int kind, cudaEvent_t* ev, int slot, unsigned rec, 
     OA_CUDA(cudaEventRecord(join_ev, side));
     err = oafdtd::launch_staged_sweep<real>(sw, mp, stream, kind == 1);
     if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string(names[kind][0]) + cudaGetErrorString(err));
+    if (pre_e_off >= 0) {  // the fused step's pre_e, after the (shorter) staged sweep, beside the slab kernel
+      err = oafdtd::launch_pre_e<real>(pr, pre_e_off, stream);
+      if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("pre_e: ") + cudaGetErrorString(err));
+    }
     OA_CUDA(cudaStreamWaitEvent(stream, join_ev, 0));
     return OAFDTD_OK;
   }
@@ -1166,6 +1172,11 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing, int part
   const unsigned rec = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
   const int p = cur[0];
   const bool fused = staged == 3 && parts == 3;
+  // In a fused step E^n stays in the current buffers for the whole step, so pre_e (the H probes
+  // at (n + 1/2) dt, E^n of the deferred Debye edges) can wait until the E z-slab sweep is
+  // launched and run beside the E slab kernel; the edge pass, which uses what it saves, comes
+  // after both. In place (the other variants, the halves) it must precede the E sweeps.
+  const bool late_pre_e = fused && ev == nullptr;
   use_regions(fused ? 3 : (staged == 3 ? 2 : staged));
   bind(p, p);
   const oafdtd::SweepMaps& mp = maps_p[p];
@@ -1176,15 +1187,19 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing, int part
       if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("fused: ") + cudaGetErrorString(err));
       if (int rc = sweep_pair(1, ev, 0, rec, mp)) return rc;
     } else {
-      // the H cells outside the fused box read only the current buffers: beside the fused sweep
+      // The H cells outside the fused box read only the current buffers: the H z-slab sweep and
+      // the H slab kernel run beside the fused sweep, on the side stream, launched after it so
+      // its one wave of blocks is placed first (the side kernels take the SMs it leaves and its
+      // tail). Launched before it, or all three on one stream, the step took 0.886 and 0.891 ms
+      // against 0.871 ms (400x400x120, 128 planes per block).
       OA_CUDA(cudaEventRecord(fork_ev, stream));
+      err = oafdtd::launch_fused_sweep<real>(sw, fmaps[p], stream);
+      if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("fused: ") + cudaGetErrorString(err));
       OA_CUDA(cudaStreamWaitEvent(side, fork_ev, 0));
       err = oafdtd::launch_staged_sweep<real>(sw, mp, side, true);
       if (err == cudaSuccess) err = oafdtd::launch_slab<real>(sw, 1, side);
       if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("h_sweep: ") + cudaGetErrorString(err));
       OA_CUDA(cudaEventRecord(join_ev, side));
-      err = oafdtd::launch_fused_sweep<real>(sw, fmaps[p], stream);
-      if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("fused: ") + cudaGetErrorString(err));
       OA_CUDA(cudaStreamWaitEvent(stream, join_ev, 0));
     }
   } else if (parts & 1) {
@@ -1197,11 +1212,13 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing, int part
       if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("ghosts: ") + cudaGetErrorString(err));
     }
     if (ev) OA_CUDA(cudaEventRecordWithFlags(ev[3], stream, rec));
-    err = oafdtd::launch_pre_e<real>(pr, off, stream);
-    if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("pre_e: ") + cudaGetErrorString(err));
+    if (!late_pre_e) {
+      err = oafdtd::launch_pre_e<real>(pr, off, stream);
+      if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("pre_e: ") + cudaGetErrorString(err));
+    }
   }
   if (parts & 2) {
-    if (int rc = sweep_pair(0, ev, 4, rec, mp)) return rc;
+    if (int rc = sweep_pair(0, ev, 4, rec, mp, late_pre_e ? off : -1)) return rc;
     err = oafdtd::launch_sibc<real>(sb, stream);
     if (err == cudaSuccess) err = oafdtd::launch_edges<real>(ed, off, stream);
     if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("edges: ") + cudaGetErrorString(err));
@@ -1857,16 +1874,16 @@ struct Batch final : BatchBase {
   // One time step of every engine, from buffers p (Engine::launch_step with parts 3).
   int launch_step(int off, int p) {
     cudaError_t err = cudaSuccess;
-    if (variant == 3) {
+    if (variant == 3) {  // the fused sweeps first, the H work outside their boxes beside them
       OA_CUDA(cudaEventRecord(fork_ev, stream));
+      for (const Launch& L : fused)
+        if ((err = oafdtd::launch_fused_batch<real>(d_sw[p], d_fm[p], L.g, L.blocks, L.key != 0, stream)) != cudaSuccess)
+          return fail(OAFDTD_E_CUDA, std::string("batched fused sweep: ") + cudaGetErrorString(err));
       OA_CUDA(cudaStreamWaitEvent(side, fork_ev, 0));
       if (int rc = sweep_launches(h_inner, true, false, p, side)) return rc;
       if (int rc = sweep_launches(h_z, true, true, p, side)) return rc;
       if (int rc = slab_launches(1, p, side)) return rc;
       OA_CUDA(cudaEventRecord(join_ev, side));
-      for (const Launch& L : fused)
-        if ((err = oafdtd::launch_fused_batch<real>(d_sw[p], d_fm[p], L.g, L.blocks, L.key != 0, stream)) != cudaSuccess)
-          return fail(OAFDTD_E_CUDA, std::string("batched fused sweep: ") + cudaGetErrorString(err));
       OA_CUDA(cudaStreamWaitEvent(stream, join_ev, 0));
     } else if (int rc = pair(1, p)) {
       return rc;
