@@ -130,7 +130,7 @@ struct Engine final : EngineBase {
     if (t_start) cudaEventDestroy(t_start);
     if (t_stop) cudaEventDestroy(t_stop);
     for (void* p : allocs) cudaFree(p);
-    for (cudaEvent_t e : {fork_ev, join_ev})
+    for (cudaEvent_t e : {fork_ev, join_ev, ejoin_ev})
       if (e) cudaEventDestroy(e);
     if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
@@ -261,7 +261,22 @@ struct Engine final : EngineBase {
   // The slab kernel runs beside the staged sweep of the same kind (they write disjoint cells and
   // read only the other field): forked onto `side` and joined back, inside the graph as well.
   cudaStream_t side = nullptr;
-  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr, ejoin_ev = nullptr;
+  // The E work of a fused step that reads no H the fused sweep writes (early) or the rest: the
+  // slab boxes and z-slab boxes that lie entirely below the fused box on some axis (E at
+  // (i, j, k) reads H at i - 1, j - 1 and k - 1 and at the cell itself).
+  oafdtd::SweepArgs<real> e_part(bool early) const {
+    oafdtd::SweepArgs<real> a = sw;
+    const oafdtd::Span3& F = fused_box;
+    auto below = [&](const oafdtd::Span3& b) { return b.j1 <= F.j0 || b.q1 <= F.q0 || b.k1 <= F.k0; };
+    int n = 0;
+    for (int s = 0; s < sw.n_slab[0]; ++s)
+      if (below(sw.slab[0][s]) == early) a.slab[0][n++] = sw.slab[0][s];
+    a.n_slab[0] = n;
+    for (int zr = 0; zr < 2; ++zr)
+      if (below(sw.zin[0][zr]) != early) a.zin[0][zr] = oafdtd::Span3{0, 0, 0, 0, 0, 0};
+    return a;
+  }
   int sweep_pair(int kind, cudaEvent_t* ev, int slot, unsigned rec, const oafdtd::SweepMaps& mp,
                  int pre_e_off = -1);
 };
@@ -326,6 +341,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
   OA_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
   OA_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
   OA_CUDA(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming));
+  OA_CUDA(cudaEventCreateWithFlags(&ejoin_ev, cudaEventDisableTiming));
 
   auto in_range = [&](long long f) { return f >= 0 && f < bs; };
 
@@ -1177,6 +1193,10 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing, int part
   // launched and run beside the E slab kernel; the edge pass, which uses what it saves, comes
   // after both. In place (the other variants, the halves) it must precede the E sweeps.
   const bool late_pre_e = fused && ev == nullptr;
+  // In a fused step without PMC mirrors, the E work whose stencil reads no H of the fused box (the
+  // slab and z-slab boxes below it on some axis) starts on the side stream as soon as the H work
+  // outside the box is done, beside the rest of the H phase; the rest follows the fused sweep.
+  const bool early_e = late_pre_e && pmc_mask == 0;
   use_regions(fused ? 3 : (staged == 3 ? 2 : staged));
   bind(p, p);
   const oafdtd::SweepMaps& mp = maps_p[p];
@@ -1200,6 +1220,13 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing, int part
       if (err == cudaSuccess) err = oafdtd::launch_slab<real>(sw, 1, side);
       if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("h_sweep: ") + cudaGetErrorString(err));
       OA_CUDA(cudaEventRecord(join_ev, side));
+      if (early_e) {  // the E work that needs only the H just done, on the side stream at once
+        const oafdtd::SweepArgs<real> lo = e_part(true);
+        err = oafdtd::launch_slab<real>(lo, 0, side);
+        if (err == cudaSuccess) err = oafdtd::launch_staged_sweep<real>(lo, mp, side, false);
+        if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("early E: ") + cudaGetErrorString(err));
+        OA_CUDA(cudaEventRecord(ejoin_ev, side));
+      }
       OA_CUDA(cudaStreamWaitEvent(stream, join_ev, 0));
     }
   } else if (parts & 1) {
@@ -1218,7 +1245,16 @@ int Engine<real>::launch_step(int off, cudaEvent_t* ev, bool capturing, int part
     }
   }
   if (parts & 2) {
-    if (int rc = sweep_pair(0, ev, 4, rec, mp, late_pre_e ? off : -1)) return rc;
+    if (early_e) {  // the rest of the E work on the main stream, then pre_e, then both joined
+      const oafdtd::SweepArgs<real> hi = e_part(false);
+      err = oafdtd::launch_slab<real>(hi, 0, stream);
+      if (err == cudaSuccess) err = oafdtd::launch_staged_sweep<real>(hi, mp, stream, false);
+      if (err == cudaSuccess) err = oafdtd::launch_pre_e<real>(pr, off, stream);
+      if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("late E: ") + cudaGetErrorString(err));
+      OA_CUDA(cudaStreamWaitEvent(stream, ejoin_ev, 0));
+    } else if (int rc = sweep_pair(0, ev, 4, rec, mp, late_pre_e ? off : -1)) {
+      return rc;
+    }
     err = oafdtd::launch_sibc<real>(sb, stream);
     if (err == cudaSuccess) err = oafdtd::launch_edges<real>(ed, off, stream);
     if (err != cudaSuccess) return fail(OAFDTD_E_CUDA, std::string("edges: ") + cudaGetErrorString(err));
