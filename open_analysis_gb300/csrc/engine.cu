@@ -928,6 +928,33 @@ int Engine<real>::build(const oafdtd_problem& p) {
         en.w[cc][a] = node ? nodew[a] : cellw[a];
       }
     }
+    if (sizeof(real) == 4) {  // the float-float weights of the float32 energy sum
+      auto split = [](double d) {
+        const float hi = (float)d;
+        return make_float2(hi, (float)(d - (double)hi));
+      };
+      const double wscale = std::ldexp(1.0, oafdtd::kEnergyWShift);
+      for (int cc = 0; cc < 6; ++cc) {
+        const int c = cc % 3;
+        const bool is_e = cc < 3;
+        const double* hw[3];
+        for (int a = 0; a < 3; ++a) hw[a] = (is_e ? (a != c) : (a == c)) ? p.node_w[a] : p.cell_w[a];
+        std::vector<float2> wx((size_t)X), wyz((size_t)Z * Y);
+        for (int i = 0; i < X; ++i) wx[i] = split(hw[0][i]);
+        for (int k = 0; k < Z; ++k)
+          for (int j = 0; j < Y; ++j) wyz[(size_t)k * Y + j] = split(hw[1][j] * hw[2][k] * wscale);
+        float2* d = nullptr;
+        if (int rc = upload_vec(&d, wx)) return rc;
+        en.wxf[cc] = d;
+        if (int rc = upload_vec(&d, wyz)) return rc;
+        en.wyzf[cc] = d;
+      }
+      std::vector<float2> ef(t_eps.size());
+      for (size_t m = 0; m < t_eps.size(); ++m) ef[m] = split(t_eps[m]);
+      float2* d = nullptr;
+      if (int rc = upload_vec(&d, ef)) return rc;
+      en.epsf = d;
+    }
     if (int rc = alloc(&energy_partial, (size_t)6 * oafdtd::kEnergyBlocks)) return rc;
     if (int rc = alloc(&energy_out, 6)) return rc;
   }

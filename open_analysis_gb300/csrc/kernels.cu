@@ -328,6 +328,36 @@ __global__ void __launch_bounds__(128) edge_batch_kernel(const EdgeArgs<real>* _
 }
 
 // ----------------------------------------------------------------------------- energy
+// Float-float arithmetic (a value is hi + lo, two float32 with |lo| <= ulp(hi) / 2): products
+// from the float32 multiply and its exact error (one fused multiply-add, written out: the
+// library is built without contraction), sums by Knuth's two-sum. About 2^-46 relative error
+// per operation.
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
+  const float p = a.x * b.x;
+  float e = __fmaf_rn(a.x, b.x, -p);
+  e = __fmaf_rn(a.x, b.y, e);
+  e = __fmaf_rn(a.y, b.x, e);
+  const float s = p + e;
+  return make_float2(s, e - (s - p));
+}
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+  const float s = a.x + b.x;
+  const float bb = s - a.x;
+  const float err = (a.x - (s - bb)) + (b.x - bb);
+  const float lo = (err + a.y) + b.y;
+  const float h = s + lo;
+  return make_float2(h, lo - (h - s));
+}
+
+// Energy sums 1/2 sum eps E^2 V (and sum H^2 V) per component, in float64 or, for float32
+// fields, in float-float: GB300's float64 rate is a small fraction of its float32 rate, and a
+// float64 product chain per cell made this kernel compute-bound (3.3 ms at 400x400x120, batch
+// 2; the fields are read in 0.15 ms). A float32 field value squares exactly into a float-float
+// pair; the weights come as float-float pairs; the terms of a thread are summed in float-float
+// and the thread's sum converted to float64 once. Each term is then exact to about 1e-13 relative,
+// so the sum is too (every term is positive). The fields are scaled by 2^32 and the weights by
+// 2^40 (exact) so that squares of fields down to 1e-28 and weights down to 1e-30 stay normal;
+// the thread's sum is scaled back by 2^-104. Fields above 4e9 would overflow the square.
 template <typename real>
 __global__ void __launch_bounds__(256) energy_kernel(const __grid_constant__ EnergyArgs<real> a,
                                                      double* partial) {
@@ -340,19 +370,40 @@ __global__ void __launch_bounds__(256) energy_kernel(const __grid_constant__ Ene
   const long long rows = (long long)a.B * a.Z * a.Y;
   const long long bs = (long long)a.Z * a.Y * a.X;
   double acc = 0.0;
-  for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
-    const long long plane = r % ((long long)a.Z * a.Y);
-    const int k = (int)(plane / a.Y), j = (int)(plane % a.Y);
-    const double wyz = wy[j] * wz[k];
-    const long long row = r * a.X;
-    double racc = 0.0;
-    for (int i = threadIdx.x; i < a.X; i += blockDim.x) {
-      const double v = (double)F[row + i];
-      double term = wx[i] * wyz * v * v;
-      if (cc < 3) term *= a.eps[a.mat[cc][(row % bs) + i]];
-      racc += term;
+  if constexpr (sizeof(real) == 4) {
+    const float vscale = ldexpf(1.0f, kEnergyVShift);
+    const float2* wxf = a.wxf[cc];
+    const float2* wyzf = a.wyzf[cc];
+    float2 sum = make_float2(0.0f, 0.0f);
+    for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+      const long long plane = r % ((long long)a.Z * a.Y);
+      const float2 wyz = wyzf[plane];
+      const long long row = r * a.X;
+      for (int i = threadIdx.x; i < a.X; i += blockDim.x) {
+        const float v = F[row + i] * vscale;
+        const float p = v * v;
+        const float2 v2 = make_float2(p, __fmaf_rn(v, v, -p));
+        float2 w = ff_mul(wxf[i], wyz);
+        if (cc < 3) w = ff_mul(w, a.epsf[a.mat[cc][(row % bs) + i]]);
+        sum = ff_add(sum, ff_mul(w, v2));
+      }
     }
-    acc += racc;
+    acc = ldexp((double)sum.x + (double)sum.y, -(kEnergyVShift * 2 + kEnergyWShift));
+  } else {
+    for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+      const long long plane = r % ((long long)a.Z * a.Y);
+      const int k = (int)(plane / a.Y), j = (int)(plane % a.Y);
+      const double wyz = wy[j] * wz[k];
+      const long long row = r * a.X;
+      double racc = 0.0;
+      for (int i = threadIdx.x; i < a.X; i += blockDim.x) {
+        const double v = (double)F[row + i];
+        double term = wx[i] * wyz * v * v;
+        if (cc < 3) term *= a.eps[a.mat[cc][(row % bs) + i]];
+        racc += term;
+      }
+      acc += racc;
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);

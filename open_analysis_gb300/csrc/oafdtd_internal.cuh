@@ -226,7 +226,14 @@ struct EnergyArgs {
   const double* eps;         // [entry] eps_r * eps0
   const double* w[6][3];     // per component, per axis: node or cell weights
   int X, Y, Z, B;
+  // float32 fields: the same weights as float-float pairs (hi, lo), the y-z product per plane and
+  // row pre-multiplied by 2^kEnergyWShift (kept clear of float32 underflow)
+  const float2* wxf[6];      // [i]
+  const float2* wyzf[6];     // [k * Y + j]
+  const float2* epsf;        // [entry]
 };
+constexpr int kEnergyWShift = 40;  // weights scaled by 2^40 ...
+constexpr int kEnergyVShift = 32;  // ... and fields by 2^32 (squares by 2^64) in the float-float sum
 
 // Launch geometry of the slab kernel: the boxes of one kind with their first block.
 struct SlabLaunch {

@@ -39,6 +39,8 @@ def estimate_bytes(c: Any, itemsize: int, max_steps: int = 200_000, record_serie
     * the edge list of injection targets and deferred Debye edges with their saved ``E^n``, the
       sampled wave table ``(channels, max_steps)``, the probe lists, the DFT accumulators
       ``(probes, B, F)`` complex128 and, when recording, the series ``(probes, B, max_steps)``;
+    * the energy sum's float-float weights for float32 fields (per component, the x row and the
+      y-z plane of pairs of float32);
     * the one-dimensional metrics, CPML coefficients, energy weights and partial sums, which are
       small; a fixed 1 MiB covers them and the per-allocation minimums.
     """
@@ -91,6 +93,8 @@ def estimate_bytes(c: Any, itemsize: int, max_steps: int = 200_000, record_serie
     total += n_probe * B * int(c.frequencies.size) * 16
     if record_series:
         total += n_probe * B * max_steps * 8
+    if rb == 4:  # the float-float weights of the float32 energy sum: x row and y-z plane per component
+        total += 6 * (X + Z * Y) * 8
     return int(total + (1 << 20))
 
 
