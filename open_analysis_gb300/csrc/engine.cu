@@ -1084,31 +1084,54 @@ int Engine<real>::build(const oafdtd_problem& p) {
       }
       return out;
     };
-    // Debye current bytes of the dispersive (not deferred) edges inside a box
+    // Debye current bytes of the dispersive (not deferred) edges inside a box. One pass over the
+    // index arrays counts them per storage row (all three components) for each distinct x range
+    // of the boxes asked about; a box then sums its rows.
     const double jv = (double)B * P * 2.0 * rb;
-    auto j_in = [&](const oafdtd::Span3& bx) {
-      double n_in = 0.0;
-      if (ade_hi <= ade_lo || bx.q1 <= bx.q0 || bx.j1 <= bx.j0 || bx.k1 <= bx.k0) return 0.0;
-      for (int c = 0; c < 3; ++c) {
-        std::vector<long long> part(kMaxParts, 0);
-        const int nj = bx.j1 - bx.j0;
-        parallel_parts((long long)(bx.k1 - bx.k0) * nj, [&](long long b0, long long e0, int t) {
-          long long n = 0;
-          for (long long r = b0; r < e0; ++r) {
-            const uint16_t* row = host_mat[c].data() + ((long long)(bx.k0 + r / nj) * Y + bx.j0 + r % nj) * X;
-            for (int i = 4 * bx.q0; i < 4 * bx.q1; ++i) n += row[i] >= ade_lo && row[i] < ade_hi;
+    const oafdtd::Span3* jboxes[6] = {&inner_staged[0], &zin_staged[0][0], &zin_staged[0][1],
+                                      &fused_box,       &zin_fused[0][0],  &zin_fused[0][1]};
+    std::vector<std::pair<int, int>> xr;  // distinct x ranges [x0, x1)
+    for (const oafdtd::Span3* b : jboxes) {
+      const std::pair<int, int> r{4 * b->q0, 4 * b->q1};
+      if (b->q1 > b->q0 && std::find(xr.begin(), xr.end(), r) == xr.end()) xr.push_back(r);
+    }
+    const long long R = (long long)Z * Y;
+    std::vector<long long> rowcnt(xr.size() * (size_t)R, 0);
+    if (ade_hi > ade_lo && !xr.empty())
+      parallel_parts(R, [&](long long b0, long long e0, int) {
+        for (long long r = b0; r < e0; ++r)
+          for (int c = 0; c < 3; ++c) {
+            const uint16_t* row = host_mat[c].data() + r * X;
+            for (size_t x = 0; x < xr.size(); ++x) {
+              long long n = 0;
+              for (int i = xr[x].first; i < xr[x].second; ++i) n += row[i] >= ade_lo && row[i] < ade_hi;
+              rowcnt[x * (size_t)R + r] += n;
+            }
           }
-          part[t] = n;
-        });
-        for (long long n : part) n_in += (double)n;
-      }
+      });
+    auto j_in = [&](const oafdtd::Span3& bx) {
+      if (ade_hi <= ade_lo || bx.q1 <= bx.q0 || bx.j1 <= bx.j0 || bx.k1 <= bx.k0) return 0.0;
+      const size_t x = (size_t)(std::find(xr.begin(), xr.end(), std::pair<int, int>{4 * bx.q0, 4 * bx.q1}) - xr.begin());
+      double n_in = 0.0;
+      for (int k = bx.k0; k < bx.k1; ++k)
+        for (int j = bx.j0; j < bx.j1; ++j) n_in += (double)rowcnt[x * (size_t)R + (size_t)k * Y + j];
       return n_in * jv;
     };
     const oafdtd::Span3 all{0, X / 4, 0, Y, 0, Z};
     const double cells = (double)nx * ny * nz;
     double n_all = 0.0, n_def = 0.0;
-    for (int c = 0; c < 3; ++c)
-      for (const AdeEdge& ae : ade_edges[c]) (ae.defer ? n_def : n_all) += 1.0;
+    for (int c = 0; c < 3; ++c) {
+      std::vector<long long> nd(kMaxParts, 0);
+      parallel_parts((long long)ade_edges[c].size(), [&](long long b0, long long e0, int t) {
+        long long n = 0;
+        for (long long e = b0; e < e0; ++e) n += ade_edges[c][e].defer ? 1 : 0;
+        nd[t] = n;
+      });
+      long long d = 0;
+      for (long long n : nd) d += n;
+      n_def += (double)d;
+      n_all += (double)((long long)ade_edges[c].size() - d);
+    }
     const double j_all = n_all * jv, j_def = n_def * jv;
     const double psi_all[2] = {psi_in(0, all), psi_in(1, all)};
     const double per_h = B * 9.0 * rb, per_e = B * 9.0 * rb + 6.0, per_f = B * 12.0 * rb + 6.0;

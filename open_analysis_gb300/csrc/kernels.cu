@@ -371,20 +371,33 @@ __global__ void __launch_bounds__(256) energy_kernel(const __grid_constant__ Ene
   const long long bs = (long long)a.Z * a.Y * a.X;
   double acc = 0.0;
   if constexpr (sizeof(real) == 4) {
+    // one quad (four cells, 16-byte loads) per thread and iteration, quads of consecutive rows
+    // on consecutive threads: enough loads in flight to stream the fields
     const float vscale = ldexpf(1.0f, kEnergyVShift);
     const float2* wxf = a.wxf[cc];
     const float2* wyzf = a.wyzf[cc];
+    const int Q = a.X / 4;
+    const long long quads = rows * Q;
     float2 sum = make_float2(0.0f, 0.0f);
-    for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < quads;
+         t += (long long)gridDim.x * blockDim.x) {
+      const long long r = t / Q;
+      const int i0 = 4 * (int)(t - r * Q);
       const long long plane = r % ((long long)a.Z * a.Y);
+      const long long q = r * a.X + i0;
+      const float4 f4 = *reinterpret_cast<const float4*>(F + q);
       const float2 wyz = wyzf[plane];
-      const long long row = r * a.X;
-      for (int i = threadIdx.x; i < a.X; i += blockDim.x) {
-        const float v = F[row + i] * vscale;
+      ushort4 m4 = make_ushort4(0, 0, 0, 0);
+      if (cc < 3) m4 = *reinterpret_cast<const ushort4*>(a.mat[cc] + (q % bs));
+      const float fv[4] = {f4.x, f4.y, f4.z, f4.w};
+      const unsigned short mv[4] = {m4.x, m4.y, m4.z, m4.w};
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float v = fv[e] * vscale;
         const float p = v * v;
         const float2 v2 = make_float2(p, __fmaf_rn(v, v, -p));
-        float2 w = ff_mul(wxf[i], wyz);
-        if (cc < 3) w = ff_mul(w, a.epsf[a.mat[cc][(row % bs) + i]]);
+        float2 w = ff_mul(wxf[i0 + e], wyz);
+        if (cc < 3) w = ff_mul(w, a.epsf[mv[e]]);
         sum = ff_add(sum, ff_mul(w, v2));
       }
     }
