@@ -7,7 +7,9 @@
 #include <cstdlib>
 #include <cmath>
 #include <cstdio>
+#include <array>
 #include <cstring>
+#include <future>
 #include <map>
 #include <memory>
 #include <new>
@@ -62,6 +64,8 @@ struct EngineBase {
   virtual int step_timed(int64_t n, double* ms) = 0;
   // Switches the sweep variant (0..3); the fused variant allocates the second field buffers.
   virtual int set_variant(int v) = 0;
+  // Waits until class_bytes / model_bytes are filled in (a host thread computes them after build).
+  virtual void traffic_ready() {}
   int64_t steps = 0;
   int64_t bytes = 0;
   int use_graph = 1;
@@ -279,6 +283,12 @@ struct Engine final : EngineBase {
   }
   int sweep_pair(int kind, cudaEvent_t* ev, int slot, unsigned rec, const oafdtd::SweepMaps& mp,
                  int pre_e_off = -1);
+  // The traffic model, computed on a host thread of its own while the engine is in use (it
+  // scans the index arrays). Declared last: it is destroyed, and so waited for, first.
+  std::future<void> traffic;
+  void traffic_ready() override {
+    if (traffic.valid()) traffic.wait();
+  }
 };
 
 // Build phase timer: with OAFDTD_TIMING set in the environment, oafdtd_create prints the
@@ -1064,6 +1074,27 @@ int Engine<real>::build(const oafdtd_problem& p) {
   // edge. The step's model bytes are those of the separate sweeps (72 + 6 / B bytes per plain
   // cell-update in float32), whatever the variant moves.
   {
+    // the Debye edge counts here; the rest on a host thread of its own, with the index arrays
+    // and the correction list moved or copied into it
+    double n_all = 0.0, n_def = 0.0;
+    for (int c = 0; c < 3; ++c) {
+      std::vector<long long> nd(kMaxParts, 0);
+      parallel_parts((long long)ade_edges[c].size(), [&](long long b0, long long e0, int t) {
+        long long n = 0;
+        for (long long e = b0; e < e0; ++e) n += ade_edges[c][e].defer ? 1 : 0;
+        nd[t] = n;
+      });
+      long long d = 0;
+      for (long long n : nd) d += n;
+      n_def += (double)d;
+      n_all += (double)((long long)ade_edges[c].size() - d);
+    }
+    std::vector<oafdtd_correction> corr(p.corr, p.corr + p.n_corr);
+    std::array<std::vector<uint16_t>, 3> mats{std::move(host_mat[0]), std::move(host_mat[1]), std::move(host_mat[2])};
+    const double sibc_n = (double)p.sibc_n, sibc_poles = (double)p.sibc_poles;
+    traffic = std::async(std::launch::async, [this, corr = std::move(corr), mats = std::move(mats), n_all, n_def,
+                                              sibc_n, sibc_poles, P, ade_lo, ade_hi]() {
+    const std::array<std::vector<uint16_t>, 3>& host_mat = mats;
     const double rb = sizeof(real);
     auto cells_in = [&](const oafdtd::Span3& s) {
       const double x = std::max(0, std::min(4 * s.q1, nx + 1) - std::max(4 * s.q0, 1));
@@ -1074,8 +1105,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
     // psi bytes of one kind's corrections inside a box (all of them for the whole domain)
     auto psi_in = [&](int kind, const oafdtd::Span3& z) {
       double out = 0.0;
-      for (int n = 0; n < p.n_corr; ++n) {
-        const oafdtd_correction& k = p.corr[n];
+      for (const oafdtd_correction& k : corr) {
         if (k.kind != kind) continue;
         const double x = std::max(0, std::min(4 * z.q1, (int)k.hi[0]) - std::max(4 * z.q0, (int)k.lo[0]));
         const double y = std::max(0, std::min(z.j1, (int)k.hi[1]) - std::max(z.j0, (int)k.lo[1]));
@@ -1119,23 +1149,10 @@ int Engine<real>::build(const oafdtd_problem& p) {
     };
     const oafdtd::Span3 all{0, X / 4, 0, Y, 0, Z};
     const double cells = (double)nx * ny * nz;
-    double n_all = 0.0, n_def = 0.0;
-    for (int c = 0; c < 3; ++c) {
-      std::vector<long long> nd(kMaxParts, 0);
-      parallel_parts((long long)ade_edges[c].size(), [&](long long b0, long long e0, int t) {
-        long long n = 0;
-        for (long long e = b0; e < e0; ++e) n += ade_edges[c][e].defer ? 1 : 0;
-        nd[t] = n;
-      });
-      long long d = 0;
-      for (long long n : nd) d += n;
-      n_def += (double)d;
-      n_all += (double)((long long)ade_edges[c].size() - d);
-    }
     const double j_all = n_all * jv, j_def = n_def * jv;
     const double psi_all[2] = {psi_in(0, all), psi_in(1, all)};
     const double per_h = B * 9.0 * rb, per_e = B * 9.0 * rb + 6.0, per_f = B * 12.0 * rb + 6.0;
-    const double edges = (double)p.sibc_n * B * (2.0 * rb * (1 + p.sibc_poles) + 3.0 * rb) + j_def;
+    const double edges = sibc_n * B * (2.0 * rb * (1 + sibc_poles) + 3.0 * rb) + j_def;
     // classes: h_sweep, h_slab, ghosts, pre_e, e_sweep, e_slab, edges, probe_e, fused
     {  // variants 1 and 2: staged interior and z-slab boxes, slab boxes around them
       double* st = class_bytes[1];
@@ -1174,6 +1191,7 @@ int Engine<real>::build(const oafdtd_problem& p) {
       fu[5] = (cells - fc - ez) * per_e + psi_all[0] - ep + (j_all - fj - ej);
       fu[6] = edges;
     }
+    });
   }
   timer.mark("traffic_model");
   // The fused sweep is the default where it applies and the device has room for the second
@@ -2359,6 +2377,7 @@ int oafdtd_graph_kernels(oafdtd_engine* engine, int64_t* out) {
 int oafdtd_kernel_bytes(oafdtd_engine* engine, double* out, int32_t n) {
   if (!engine || !out || n < 0) return fail(OAFDTD_E_INVALID, "null argument");
   EngineBase& e = *engine->impl;
+  e.traffic_ready();
   const double* cls = e.class_bytes[e.staged == 3 ? 2 : (e.staged ? 1 : 0)];
   double total = 0.0;
   for (int k = 0; k < EngineBase::kClasses; ++k) {
@@ -2383,6 +2402,7 @@ int oafdtd_kernel_times(oafdtd_engine* engine, double* out_ms, int32_t n) {
 
 int oafdtd_model_bytes(const oafdtd_engine* engine, double* out) {
   if (!engine || !out) return fail(OAFDTD_E_INVALID, "null argument");
+  engine->impl->traffic_ready();
   *out = engine->impl->model_bytes;
   return OAFDTD_OK;
 }
